@@ -1,0 +1,93 @@
+"""Builds the CUDA extension library in-tree: cpp-pt_gb300/lib/libcpppt_gb300.so.
+
+    python cpp-pt_gb300/build.py            # incremental
+    python cpp-pt_gb300/build.py --force
+
+Three translation units compiled in parallel for sm_103a only:
+  csrc/render.cu  -- all CUDA kernels (nvcc -gencode arch=compute_103a,code=sm_103a)
+  csrc/host.cpp   -- C ABI, render driver, loader, image output
+  csrc/bvh.cpp    -- BVH builders (-ffp-contract=off: the reference-topology
+                     build must round like the reference)
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+OBJ = os.path.join(HERE, "lib", "obj")
+LIB = os.path.join(HERE, "lib", "libcpppt_gb300.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def _nvcc() -> str:
+    for c in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if c and os.path.exists(c):
+            return c
+    raise RuntimeError("nvcc not found")
+
+
+def _deps(src: str) -> list[str]:
+    return [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))] + [
+        os.path.join(HERE, "..", "include", "cpppt_gb300.h"), src]
+
+
+def _stale(out: str, deps: list[str]) -> bool:
+    if not os.path.exists(out):
+        return True
+    t = os.path.getmtime(out)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _commands(extra_cuda: list[str] | None = None):
+    nvcc = _nvcc()
+    common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
+    jobs = []
+    for name in ("render.cu", "host.cpp", "bvh.cpp"):
+        src = os.path.join(CSRC, name)
+        out = os.path.join(OBJ, name + ".o")
+        cmd = [nvcc, "-c", src, "-o", out] + common
+        if name.endswith(".cu"):
+            cmd += ARCH + ["-lineinfo"] + (extra_cuda or [])
+        else:
+            cmd += ["-x", "c++"]
+        jobs.append((src, out, cmd))
+    return nvcc, jobs
+
+
+def build(force: bool = False, verbose: bool = False, extra_cuda: list[str] | None = None) -> str:
+    os.makedirs(OBJ, exist_ok=True)
+    nvcc, jobs = _commands(extra_cuda)
+    todo = [(s, o, c) for s, o, c in jobs if force or _stale(o, _deps(s))]
+
+    def run(job):
+        s, o, c = job
+        r = subprocess.run(c, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"compile failed: {' '.join(c)}\n{r.stdout}\n{r.stderr}")
+        if verbose and (r.stdout or r.stderr):
+            print(r.stdout, r.stderr, file=sys.stderr)
+        return o
+
+    with cf.ThreadPoolExecutor(max_workers=3) as ex:
+        list(ex.map(run, todo))
+    objs = [o for _, o, _ in jobs]
+    if force or todo or _stale(LIB, objs):
+        cmd = [nvcc, "-shared", "-o", LIB] + objs + ARCH
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return LIB
+
+
+if __name__ == "__main__":
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--force", action="store_true")
+    ap.add_argument("--ptxas-v", action="store_true", help="print register / spill usage")
+    a = ap.parse_args()
+    print(build(a.force, verbose=True, extra_cuda=["-Xptxas", "-v"] if a.ptxas_v else None))

@@ -1,0 +1,220 @@
+"""ctypes binding of the C ABI in include/cpppt_gb300.h.
+
+The shared library is built in-tree by cpp-pt_gb300/build.py.  Loading fails
+loudly when it is missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(os.path.dirname(HERE), "lib", "libcpppt_gb300.so")
+
+PT_OK = 0
+STATUS_NAMES = {0: "PT_OK", 1: "PT_ERR_INVALID", 2: "PT_ERR_CUDA", 3: "PT_ERR_MEMORY", 4: "PT_ERR_LIMIT",
+                5: "PT_ERR_IO", 6: "PT_ERR_NO_DEVICE"}
+MODE_MIS, MODE_SDTREE, MODE_NN = 0, 1, 2
+
+# every function the header declares
+EXPORTS = ["pt_scene_create", "pt_scene_load", "pt_scene_destroy", "pt_trace_closest", "pt_trace_any",
+           "pt_trace_closest_device", "pt_trace_any_device", "pt_render", "pt_render_device",
+           "pt_render_stats_get", "pt_image_save", "pt_last_error", "pt_debug_ref_topology"]
+
+
+class PtMaterial(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("rgb", C.c_float * 3), ("roughness", C.c_float), ("ior", C.c_float),
+                ("intensity", C.c_float), ("reserved", C.c_float)]
+
+
+class PtCamera(C.Structure):
+    _fields_ = [("origin", C.c_float * 3), ("at", C.c_float * 3), ("up", C.c_float * 3), ("tan_fovy", C.c_float),
+                ("width", C.c_int32), ("height", C.c_int32)]
+
+
+class PtSceneDesc(C.Structure):
+    _fields_ = [("n_vertices", C.c_int32), ("vertices", C.c_void_p), ("normals", C.c_void_p),
+                ("tangents", C.c_void_p), ("n_triangles", C.c_int32), ("triangles", C.c_void_p),
+                ("tri_material", C.c_void_p), ("n_materials", C.c_int32), ("materials", C.c_void_p),
+                ("camera", PtCamera)]
+
+
+class PtRenderDesc(C.Structure):
+    _fields_ = [("spp", C.c_int32), ("max_depth", C.c_int32), ("rr_start", C.c_int32), ("seed", C.c_uint32),
+                ("mode", C.c_int32), ("flags", C.c_int32)]
+
+
+class PtRenderStats(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("paths", "closest_rays", "shadow_rays", "render_ms", "trace_closest_ms",
+                                           "trace_shadow_ms", "iterations", "kernel_launches")]
+
+
+class PtError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Loads the library (no CUDA call is made)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise FileNotFoundError(f"{path} is missing: build it with cpp-pt_gb300/build.py")
+    lib = C.CDLL(path)
+    P = C.c_void_p
+    lib.pt_scene_create.argtypes = [C.POINTER(PtSceneDesc), C.POINTER(P)]
+    lib.pt_scene_load.argtypes = [C.c_char_p, C.POINTER(P), C.POINTER(PtRenderDesc), C.c_char_p, C.c_int32]
+    lib.pt_scene_destroy.argtypes = [P]
+    lib.pt_scene_destroy.restype = None
+    lib.pt_trace_closest.argtypes = [P, P, C.c_int32, P]
+    lib.pt_trace_any.argtypes = [P, P, C.c_int32, P]
+    lib.pt_trace_closest_device.argtypes = [P, P, C.c_int32, P, P]
+    lib.pt_trace_any_device.argtypes = [P, P, C.c_int32, P, P]
+    lib.pt_render.argtypes = [P, C.POINTER(PtRenderDesc), P]
+    lib.pt_render_device.argtypes = [P, C.POINTER(PtRenderDesc), P]
+    lib.pt_render_stats_get.argtypes = [P, C.POINTER(PtRenderStats)]
+    lib.pt_image_save.argtypes = [C.c_char_p, P, C.c_int32, C.c_int32]
+    lib.pt_last_error.restype = C.c_char_p
+    lib.pt_last_error.argtypes = []
+    lib.pt_debug_ref_topology.argtypes = [P, C.c_int32, P, P, P, C.c_int32, P]
+    for name in EXPORTS:
+        getattr(lib, name).restype = C.c_int32 if name not in ("pt_scene_destroy", "pt_last_error") else \
+            getattr(lib, name).restype
+    _lib = lib
+    return lib
+
+
+def _check(status: int):
+    if status != PT_OK:
+        raise PtError(status, _lib.pt_last_error().decode())
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+class GpuScene:
+    """A scene on the GPU (pt_scene)."""
+
+    def __init__(self, sc=None, settings_file: str | None = None):
+        lib = load()
+        self.h = C.c_void_p()
+        self.render_settings = None
+        self.output_name = None
+        if settings_file is not None:
+            rs = PtRenderDesc()
+            out = C.create_string_buffer(4096)
+            _check(lib.pt_scene_load(settings_file.encode(), C.byref(self.h), C.byref(rs), out, 4096))
+            self.render_settings = rs
+            self.output_name = out.value.decode()
+            self.width = self.height = None
+            return
+        self.sc = sc
+        self._keep = [np.ascontiguousarray(sc.vertices, np.float32), np.ascontiguousarray(sc.normals, np.float32),
+                      np.ascontiguousarray(sc.tangents, np.float32), np.ascontiguousarray(sc.triangles, np.int32),
+                      np.ascontiguousarray(sc.tri_material, np.int32)]
+        mats = (PtMaterial * max(1, len(sc.mat_kind)))()
+        for i, (k, p) in enumerate(zip(sc.mat_kind, sc.mat_params)):
+            mats[i].kind = int(k)
+            mats[i].rgb[:] = [float(p[0]), float(p[1]), float(p[2])]
+            mats[i].roughness, mats[i].ior, mats[i].intensity = float(p[3]), float(p[4]), float(p[5])
+        self._mats = mats
+        d = PtSceneDesc()
+        d.n_vertices = len(sc.vertices)
+        d.vertices, d.normals, d.tangents = _ptr(self._keep[0]), _ptr(self._keep[1]), _ptr(self._keep[2])
+        d.n_triangles = sc.n_triangles
+        d.triangles, d.tri_material = _ptr(self._keep[3]), _ptr(self._keep[4])
+        d.n_materials = len(sc.mat_kind)
+        d.materials = C.cast(mats, C.c_void_p)
+        cam = sc.camera
+        d.camera.origin[:] = [float(x) for x in cam[0:3]]
+        d.camera.at[:] = [float(x) for x in cam[3:6]]
+        d.camera.up[:] = [float(x) for x in cam[6:9]]
+        d.camera.tan_fovy = float(cam[9])
+        d.camera.width, d.camera.height = sc.width, sc.height
+        _check(lib.pt_scene_create(C.byref(d), C.byref(self.h)))
+        self.width, self.height = sc.width, sc.height
+
+    def close(self):
+        if self.h:
+            _lib.pt_scene_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # --- ray batches (host buffers) ---
+    def trace_closest(self, rays: np.ndarray):
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 7)
+        hits = np.zeros((len(rays), 4), np.float32)
+        _check(_lib.pt_trace_closest(self.h, _ptr(rays), len(rays), _ptr(hits)))
+        return hits[:, 1].view(np.int32).copy(), hits[:, 0].copy(), hits[:, 2].copy(), hits[:, 3].copy()
+
+    def trace_any(self, rays: np.ndarray):
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 7)
+        occ = np.zeros(len(rays), np.uint8)
+        _check(_lib.pt_trace_any(self.h, _ptr(rays), len(rays), _ptr(occ)))
+        return occ
+
+    # --- ray batches (device pointers, e.g. torch tensors) ---
+    def trace_closest_device(self, d_rays: int, n: int, d_hits: int, stream: int = 0):
+        _check(_lib.pt_trace_closest_device(self.h, d_rays, n, d_hits, stream or None))
+
+    def trace_any_device(self, d_rays: int, n: int, d_occ: int, stream: int = 0):
+        _check(_lib.pt_trace_any_device(self.h, d_rays, n, d_occ, stream or None))
+
+    # --- rendering ---
+    @staticmethod
+    def desc(spp: int, max_depth: int = 32, rr_start: int = 3, seed: int = 0, mode: int = MODE_MIS,
+             flags: int = 0) -> PtRenderDesc:
+        d = PtRenderDesc()
+        d.spp, d.max_depth, d.rr_start, d.seed, d.mode, d.flags = spp, max_depth, rr_start, seed, mode, flags
+        return d
+
+    def render(self, spp: int, max_depth: int = 32, rr_start: int = 3, seed: int = 0, mode: int = MODE_MIS,
+               flags: int = 0, out: np.ndarray | None = None) -> np.ndarray:
+        d = self.desc(spp, max_depth, rr_start, seed, mode, flags)
+        if out is None:
+            out = np.zeros((self.height, self.width, 3), np.float32)
+        _check(_lib.pt_render(self.h, C.byref(d), _ptr(out)))
+        return out
+
+    def render_device(self, d_out: int, spp: int, max_depth: int = 32, rr_start: int = 3, seed: int = 0,
+                      mode: int = MODE_MIS, flags: int = 0):
+        d = self.desc(spp, max_depth, rr_start, seed, mode, flags)
+        _check(_lib.pt_render_device(self.h, C.byref(d), d_out))
+
+    def stats(self) -> dict:
+        s = PtRenderStats()
+        _check(_lib.pt_render_stats_get(self.h, C.byref(s)))
+        return {n: getattr(s, n) for n, _ in PtRenderStats._fields_}
+
+
+def save_image(prefix: str, rgb: np.ndarray):
+    load()
+    rgb = np.ascontiguousarray(rgb, np.float32)
+    _check(_lib.pt_image_save(prefix.encode(), _ptr(rgb), rgb.shape[1], rgb.shape[0]))
+
+
+def ref_topology(sc):
+    """The reference BVH topology derived by the library (host only)."""
+    lib = load()
+    tv = np.ascontiguousarray(sc.vertices[sc.triangles].reshape(-1), np.float32)
+    n = sc.n_triangles
+    cap = max(2 * n, 16)
+    order = np.zeros(n, np.int32)
+    pparent = np.zeros(n, np.int32)
+    boxes = np.zeros(6 * cap, np.float32)
+    nn = C.c_int32()
+    _check(lib.pt_debug_ref_topology(_ptr(tv), n, _ptr(order), _ptr(pparent), _ptr(boxes), cap, C.byref(nn)))
+    return order, boxes[:6 * nn.value].reshape(-1, 6), pparent

@@ -1,0 +1,61 @@
+// Types shared by the host code and the CUDA kernels.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace cpppt_gb300 {
+
+// Device material; for emitters rgb holds rgb * intensity (EmissiveMaterial::get_bxdf,
+// src/bxdf/emissive_material.h:28-30).
+struct DevMaterial {
+    int32_t kind;     // PT_MAT_*
+    float r, g, b;
+    float alpha;      // GGX: max(roughness^2, 0.01) (glossy_bxdf.h:77-79)
+    int32_t delta;    // GGX: roughness < 0.01 (glossy_bxdf.h:23)
+    float ior;
+    float pad;
+};
+
+// CameraPerspective (src/camera/camera_perspective.h:19-39): origin and the
+// column basis (x, y, z) of `coords`, stored row-major like Mat3.
+struct DevCamera {
+    float o[3];
+    float m[9];
+    float tan_fovy, aspect;
+    int32_t width, height;
+};
+
+struct DevScene {
+    // traversal
+    const uint4* nodes;      // 4 per wide node
+    int32_t n_nodes;
+    int32_t n_tris;
+    const float4* tris;      // 3 per triangle in leaf order: {a, rank}, {b-a, parent box}, {c-a, prim}
+    const float4* ref_box;   // 2 per reference internal node: lo, hi
+    // shading, in insertion order
+    const int4* tri_vidx;    // v0, v1, v2, material
+    const float4* v_pos;
+    const float4* v_nrm;
+    const float4* v_btan;    // cross(normal, tangent) (loader.h:237)
+    const DevMaterial* mats;
+    const int32_t* light_prim;  // emissive triangles in insertion order
+    const float* light_area;    // Triangle::area (triangle.h:197-207)
+    int32_t n_lights;
+    DevCamera cam;
+};
+
+// Ray-batch status word bits (kernel-side bounded loops report here).
+constexpr uint32_t kStatusIterLimit = 1u;
+constexpr uint32_t kStatusStackOverflow = 2u;
+constexpr uint32_t kStatusQueueOverflow = 4u;
+
+// Wavefront counters, one block of device memory per scene.
+struct WaveCounters {
+    int32_t n_cur, n_next, n_shadow, pad0;
+    int32_t fetch_ext, fetch_sh, pad1, pad2;
+    uint32_t status, pad3, pad4, pad5;
+    unsigned long long work_next, work_total;
+    unsigned long long stat_closest, stat_shadow, stat_paths, stat_iters;
+};
+
+}  // namespace cpppt_gb300

@@ -1,0 +1,908 @@
+// C ABI of the GB300 path tracer (declared in include/cpppt_gb300.h).
+//
+// Owns the device copy of a scene, the wavefront buffers and the CUDA graph
+// that replays wavefront iterations.  No call throws across the ABI; errors
+// are status codes plus a thread-local message.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/cpppt_gb300.h"
+#include "bvh.h"
+#include "dev_types.h"
+#include "kernels.h"
+
+using namespace cpppt_gb300;
+
+namespace {
+thread_local std::string g_error;
+
+struct Fail : std::runtime_error {
+    pt_status code;
+    Fail(pt_status c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+void ck(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        throw Fail(e == cudaErrorMemoryAllocation ? PT_ERR_MEMORY : PT_ERR_CUDA,
+                   std::string(what) + ": " + cudaGetErrorString(e));
+    }
+}
+
+template <class F>
+pt_status guarded(F&& f) {
+    try {
+        f();
+        g_error.clear();
+        return PT_OK;
+    } catch (const Fail& e) {
+        g_error = e.what();
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        g_error = "host allocation failed";
+        return PT_ERR_MEMORY;
+    } catch (const std::exception& e) {
+        g_error = e.what();
+        return PT_ERR_INVALID;
+    }
+}
+
+template <class T>
+T* dalloc(std::vector<void*>& owned, size_t count) {
+    void* p = nullptr;
+    if (count == 0) count = 1;
+    ck(cudaMalloc(&p, sizeof(T) * count), "cudaMalloc");
+    owned.push_back(p);
+    return static_cast<T*>(p);
+}
+
+template <class T>
+T* dupload(std::vector<void*>& owned, const std::vector<T>& v, cudaStream_t st) {
+    T* p = dalloc<T>(owned, v.size());
+    if (!v.empty()) ck(cudaMemcpyAsync(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, st), "upload");
+    return p;
+}
+
+float fnorm3(float* v) {
+    float l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    float inv = 1.0f / l;
+    v[0] *= inv; v[1] *= inv; v[2] *= inv;
+    return l;
+}
+void fcross(const float* a, const float* b, float* o) {
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = a[2] * b[0] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+}  // namespace
+
+struct pt_scene {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<void*> owned;  // scene data
+    DevScene dev{};
+    int n_tris = 0, width = 0, height = 0;
+    double build_ref_ms = 0, build_wide_ms = 0;
+    int wide_depth = 0;
+
+    // ray-batch scratch
+    int* d_counter = nullptr;
+    uint32_t* d_status = nullptr;
+    void* d_io = nullptr;
+    size_t d_io_bytes = 0;
+
+    // wavefront state
+    PathBuffers pb{};
+    std::vector<void*> pb_owned;
+    float* film32 = nullptr;
+    double* film64 = nullptr;
+    float* d_out = nullptr;
+    int film_n = 0;
+    WaveCounters* d_ctr = nullptr;
+    WaveCounters* h_ctr = nullptr;  // pinned
+    cudaGraphExec_t graph = nullptr;
+    RenderParams graph_params{};
+    int graph_iters = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    pt_render_stats stats{};
+
+    ~pt_scene() {
+        if (graph) cudaGraphExecDestroy(graph);
+        for (void* p : owned) cudaFree(p);
+        for (void* p : pb_owned) cudaFree(p);
+        if (film32) cudaFree(film32);
+        if (film64) cudaFree(film64);
+        if (d_out) cudaFree(d_out);
+        if (d_io) cudaFree(d_io);
+        if (h_ctr) cudaFreeHost(h_ctr);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+void check_device(pt_scene* s) {
+    int dev = 0;
+    ck(cudaGetDevice(&dev), "cudaGetDevice");
+    cudaDeviceProp prop;
+    ck(cudaGetDeviceProperties(&prop, dev), "cudaGetDeviceProperties");
+    if (prop.major * 10 + prop.minor != 103)
+        throw Fail(PT_ERR_NO_DEVICE, "device " + std::string(prop.name) + " is not compute capability 10.3 (sm_103a)");
+    s->device = dev;
+    s->num_sms = prop.multiProcessorCount;
+}
+
+void create_scene(const pt_scene_desc* d, pt_scene* s) {
+    if (!d) throw std::invalid_argument("null scene description");
+    const int nv = d->n_vertices, nt = d->n_triangles, nm = d->n_materials;
+    if (nv < 0 || nt < 0 || nm < 0) throw std::invalid_argument("negative count");
+    if (nt > 0 && (!d->vertices || !d->normals || !d->triangles || !d->tri_material))
+        throw std::invalid_argument("missing vertex or triangle arrays");
+    if (nt > (1 << 27) - 1) throw std::invalid_argument("too many triangles (max 2^27-1)");
+    if (nm > 0 && !d->materials) throw std::invalid_argument("missing materials");
+    if (d->camera.width <= 0 || d->camera.height <= 0) throw std::invalid_argument("camera resolution must be positive");
+    for (int i = 0; i < 3 * nt; i++)
+        if (d->triangles[i] < 0 || d->triangles[i] >= nv) throw std::invalid_argument("triangle vertex index out of range");
+    for (int i = 0; i < nt; i++)
+        if (d->tri_material[i] < 0 || d->tri_material[i] >= nm) throw std::invalid_argument("triangle material out of range");
+    for (int i = 0; i < nm; i++)
+        if (d->materials[i].kind < 0 || d->materials[i].kind > 3) throw std::invalid_argument("unknown material kind");
+
+    check_device(s);
+    ck(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    s->n_tris = nt;
+    s->width = d->camera.width;
+    s->height = d->camera.height;
+
+    // per-triangle vertex positions (a, b, c)
+    std::vector<float> tv(9 * (size_t)nt);
+    for (int t = 0; t < nt; t++)
+        for (int k = 0; k < 3; k++)
+            std::memcpy(&tv[9 * (size_t)t + 3 * k], d->vertices + 3 * (size_t)d->triangles[3 * t + k], 12);
+
+    auto t0 = std::chrono::steady_clock::now();
+    RefTopology ref = build_ref_topology(tv.data(), nt);
+    auto t1 = std::chrono::steady_clock::now();
+    WideBVH wide = build_wide_bvh(tv.data(), nt, 4);
+    auto t2 = std::chrono::steady_clock::now();
+    s->build_ref_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    s->build_wide_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();
+    s->wide_depth = wide.max_depth;
+    if (3 * wide.max_depth + 4 > 64) throw Fail(PT_ERR_LIMIT, "wide BVH too deep for the traversal stack");
+
+    // traversal triangles in leaf order: {a, rank}, {b - a, parent}, {c - a, prim}
+    std::vector<float4> tris(3 * (size_t)nt);
+    for (int k = 0; k < nt; k++) {
+        const int p = wide.tri_order[k];
+        const float* v = &tv[9 * (size_t)p];
+        float a[3] = {v[0], v[1], v[2]};
+        float e1[3] = {v[3] - v[0], v[4] - v[1], v[5] - v[2]};  // triangle.h:40 (b - a)
+        float e2[3] = {v[6] - v[0], v[7] - v[1], v[8] - v[2]};  // triangle.h:41 (c - a)
+        int32_t rank = ref.rank[p], parent = ref.prim_parent[p];
+        float rf, pf, idf;
+        std::memcpy(&rf, &rank, 4);
+        std::memcpy(&pf, &parent, 4);
+        std::memcpy(&idf, &p, 4);
+        tris[3 * (size_t)k] = make_float4(a[0], a[1], a[2], rf);
+        tris[3 * (size_t)k + 1] = make_float4(e1[0], e1[1], e1[2], pf);
+        tris[3 * (size_t)k + 2] = make_float4(e2[0], e2[1], e2[2], idf);
+    }
+    std::vector<float4> rbox(2 * ref.node_box.size());
+    for (size_t i = 0; i < ref.node_box.size(); i++) {
+        const Box3& b = ref.node_box[i];
+        rbox[2 * i] = make_float4(b.lo[0], b.lo[1], b.lo[2], 0.f);
+        rbox[2 * i + 1] = make_float4(b.hi[0], b.hi[1], b.hi[2], 0.f);
+    }
+    // shading data
+    std::vector<int4> vidx(nt);
+    for (int t = 0; t < nt; t++)
+        vidx[t] = make_int4(d->triangles[3 * t], d->triangles[3 * t + 1], d->triangles[3 * t + 2], d->tri_material[t]);
+    std::vector<float4> vpos(nv), vnrm(nv), vbt(nv);
+    for (int v = 0; v < nv; v++) {
+        const float* p = d->vertices + 3 * (size_t)v;
+        const float* n = d->normals + 3 * (size_t)v;
+        float tg[3];
+        if (d->tangents) {
+            std::memcpy(tg, d->tangents + 3 * (size_t)v, 12);
+        } else {  // any vector perpendicular to the normal
+            float ax[3] = {std::fabs(n[1]) < 0.9f ? 0.f : 1.f, std::fabs(n[1]) < 0.9f ? 1.f : 0.f, 0.f};
+            fcross(ax, n, tg);
+            fnorm3(tg);
+        }
+        float bt[3];
+        fcross(n, tg, bt);  // loader.h:237
+        vpos[v] = make_float4(p[0], p[1], p[2], 0.f);
+        vnrm[v] = make_float4(n[0], n[1], n[2], 0.f);
+        vbt[v] = make_float4(bt[0], bt[1], bt[2], 0.f);
+    }
+    std::vector<DevMaterial> mats(nm);
+    for (int i = 0; i < nm; i++) {
+        const pt_material& m = d->materials[i];
+        DevMaterial dm{};
+        dm.kind = m.kind;
+        dm.r = m.rgb[0]; dm.g = m.rgb[1]; dm.b = m.rgb[2];
+        if (m.kind == PT_MAT_EMISSIVE) { dm.r *= m.intensity; dm.g *= m.intensity; dm.b *= m.intensity; }
+        float r2 = m.roughness * m.roughness;
+        dm.alpha = std::max(r2, 0.01f);
+        dm.delta = (double)m.roughness < 0.01 ? 1 : 0;
+        dm.ior = m.ior;
+        mats[i] = dm;
+    }
+    std::vector<int32_t> lprim;
+    std::vector<float> larea;
+    for (int t = 0; t < nt; t++) {
+        if (d->materials[d->tri_material[t]].kind != PT_MAT_EMISSIVE) continue;
+        lprim.push_back(t);
+        const float* v = &tv[9 * (size_t)t];
+        float e1[3] = {v[3] - v[0], v[4] - v[1], v[5] - v[2]}, e2[3] = {v[6] - v[0], v[7] - v[1], v[8] - v[2]}, c[3];
+        fcross(e1, e2, c);
+        larea.push_back(std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]) * 0.5f);
+    }
+    std::vector<uint4> nodes(4 * wide.nodes.size());
+    std::memcpy(nodes.data(), wide.nodes.data(), sizeof(WideNode) * wide.nodes.size());
+
+    DevScene& S = s->dev;
+    S.nodes = dupload(s->owned, nodes, s->stream);
+    S.n_nodes = (int)wide.nodes.size();
+    S.n_tris = nt;
+    S.tris = dupload(s->owned, tris, s->stream);
+    S.ref_box = dupload(s->owned, rbox, s->stream);
+    S.tri_vidx = dupload(s->owned, vidx, s->stream);
+    S.v_pos = dupload(s->owned, vpos, s->stream);
+    S.v_nrm = dupload(s->owned, vnrm, s->stream);
+    S.v_btan = dupload(s->owned, vbt, s->stream);
+    S.mats = dupload(s->owned, mats, s->stream);
+    S.light_prim = dupload(s->owned, lprim, s->stream);
+    S.light_area = dupload(s->owned, larea, s->stream);
+    S.n_lights = (int)lprim.size();
+    // camera: CameraPerspective(res, tan_fovy, origin, normalized(at - origin), up)
+    const pt_camera& c = d->camera;
+    float fwd[3] = {c.at[0] - c.origin[0], c.at[1] - c.origin[1], c.at[2] - c.origin[2]};
+    fnorm3(fwd);
+    float z[3] = {-fwd[0], -fwd[1], -fwd[2]}, x[3], y[3];
+    fnorm3(z);
+    fcross(c.up, z, x);
+    fnorm3(x);
+    fcross(z, x, y);
+    fnorm3(y);
+    DevCamera& C = S.cam;
+    for (int k = 0; k < 3; k++) C.o[k] = c.origin[k];
+    float m9[9] = {x[0], y[0], z[0], x[1], y[1], z[1], x[2], y[2], z[2]};
+    std::memcpy(C.m, m9, sizeof(m9));
+    C.tan_fovy = c.tan_fovy;
+    C.aspect = (float)c.width / (float)c.height;
+    C.width = c.width;
+    C.height = c.height;
+
+    s->d_counter = dalloc<int>(s->owned, 4);
+    s->d_status = reinterpret_cast<uint32_t*>(s->d_counter + 1);
+    s->d_ctr = dalloc<WaveCounters>(s->owned, 1);
+    ck(cudaMallocHost(&s->h_ctr, sizeof(WaveCounters)), "cudaMallocHost");
+    ck(cudaEventCreate(&s->ev0), "cudaEventCreate");
+    ck(cudaEventCreate(&s->ev1), "cudaEventCreate");
+    ck(cudaStreamSynchronize(s->stream), "scene upload");
+}
+
+void ensure_io(pt_scene* s, size_t bytes) {
+    if (s->d_io_bytes >= bytes) return;
+    if (s->d_io) cudaFree(s->d_io);
+    s->d_io = nullptr;
+    s->d_io_bytes = 0;
+    ck(cudaMalloc(&s->d_io, bytes), "cudaMalloc");
+    s->d_io_bytes = bytes;
+}
+
+void check_status(pt_scene* s, uint32_t status) {
+    if (status & kStatusIterLimit) throw Fail(PT_ERR_LIMIT, "traversal step limit reached");
+    if (status & kStatusStackOverflow) throw Fail(PT_ERR_LIMIT, "traversal stack overflow");
+    if (status & kStatusQueueOverflow) throw Fail(PT_ERR_LIMIT, "wavefront queue overflow");
+}
+
+void trace_device(pt_scene* s, const pt_ray* rays, int n, void* out, bool any, cudaStream_t st) {
+    if (n < 0) throw std::invalid_argument("negative ray count");
+    if (n == 0) return;
+    if (!rays || !out) throw std::invalid_argument("null buffer");
+    ck(cudaMemsetAsync(s->d_counter, 0, 2 * sizeof(int), st), "memset");
+    if (any)
+        launch_trace_any(s->dev, reinterpret_cast<const float*>(rays), n, static_cast<uint8_t*>(out), s->d_counter,
+                         s->d_status, s->num_sms, st);
+    else
+        launch_trace_closest(s->dev, reinterpret_cast<const float*>(rays), n, static_cast<float4*>(out), s->d_counter,
+                             s->d_status, s->num_sms, st);
+    ck(cudaGetLastError(), "trace launch");
+}
+
+void trace_host(pt_scene* s, const pt_ray* rays, int n, void* out, bool any) {
+    if (n < 0) throw std::invalid_argument("negative ray count");
+    if (n == 0) return;
+    if (!rays || !out) throw std::invalid_argument("null buffer");
+    const size_t in_bytes = sizeof(pt_ray) * (size_t)n;
+    const size_t out_bytes = any ? (size_t)n : sizeof(pt_hit) * (size_t)n;
+    const size_t out_off = (in_bytes + 255) & ~(size_t)255;
+    ensure_io(s, out_off + out_bytes);
+    char* base = static_cast<char*>(s->d_io);
+    ck(cudaMemcpyAsync(base, rays, in_bytes, cudaMemcpyHostToDevice, s->stream), "copy rays");
+    trace_device(s, reinterpret_cast<const pt_ray*>(base), n, base + out_off, any, s->stream);
+    ck(cudaMemcpyAsync(out, base + out_off, out_bytes, cudaMemcpyDeviceToHost, s->stream), "copy hits");
+    uint32_t status = 0;
+    ck(cudaMemcpyAsync(&status, s->d_status, 4, cudaMemcpyDeviceToHost, s->stream), "copy status");
+    ck(cudaStreamSynchronize(s->stream), "trace");
+    check_status(s, status);
+}
+
+constexpr int kMaxCapacity = 1 << 21;
+constexpr int kItersPerGraph = 16;  // even: buffers alternate
+
+void ensure_wave(pt_scene* s, int capacity, int film_n) {
+    if (s->pb.capacity < capacity) {
+        for (void* p : s->pb_owned) cudaFree(p);
+        s->pb_owned.clear();
+        PathBuffers& B = s->pb;
+        for (int k = 0; k < 2; k++) {
+            B.o[k] = dalloc<float4>(s->pb_owned, capacity);
+            B.d[k] = dalloc<float4>(s->pb_owned, capacity);
+            B.thr[k] = dalloc<float4>(s->pb_owned, capacity);
+            B.info[k] = dalloc<int4>(s->pb_owned, capacity);
+        }
+        B.hit = dalloc<float4>(s->pb_owned, capacity);
+        B.sh_o = dalloc<float4>(s->pb_owned, capacity);
+        B.sh_d = dalloc<float4>(s->pb_owned, capacity);
+        B.sh_c = dalloc<float4>(s->pb_owned, capacity);
+        B.capacity = capacity;
+        if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
+    }
+    if (s->film_n != film_n) {
+        if (s->film32) cudaFree(s->film32);
+        if (s->film64) cudaFree(s->film64);
+        if (s->d_out) cudaFree(s->d_out);
+        s->film32 = nullptr; s->film64 = nullptr; s->d_out = nullptr;
+        ck(cudaMalloc(&s->film32, sizeof(float) * film_n), "cudaMalloc film");
+        ck(cudaMalloc(&s->film64, sizeof(double) * film_n), "cudaMalloc film");
+        ck(cudaMalloc(&s->d_out, sizeof(float) * film_n), "cudaMalloc film");
+        s->film_n = film_n;
+        if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
+    }
+}
+
+bool same_params(const RenderParams& a, const RenderParams& b) { return std::memcmp(&a, &b, sizeof(a)) == 0; }
+
+void enqueue_iterations(pt_scene* s, const RenderParams& P, int iters) {
+    for (int k = 0; k < iters; k++) {
+        const int cur = k & 1;
+        launch_extend(s->dev, s->pb, cur, s->d_ctr, s->num_sms, s->stream);
+        launch_shade(s->dev, s->pb, cur, P, s->d_ctr, s->film32, s->stream);
+        launch_shadow(s->dev, s->pb, s->d_ctr, s->film32, s->num_sms, s->stream);
+        launch_generate(s->dev, s->pb, cur, P, s->d_ctr, s->stream);
+    }
+    launch_film_fold(s->film32, s->film64, s->film_n, s->stream);
+}
+
+void render_impl(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
+    if (!desc) throw std::invalid_argument("null render description");
+    if (desc->spp < 1) throw std::invalid_argument("spp must be >= 1");
+    if (desc->max_depth < 1 || desc->max_depth > 0xffff) throw std::invalid_argument("max_depth must be in [1, 65535]");
+    if (desc->mode != PT_MODE_MIS) throw Fail(PT_ERR_INVALID, "render mode not available in this build");
+    RenderParams P{};
+    P.spp = desc->spp;
+    int ax = (int)std::lround(std::sqrt((double)desc->spp));
+    P.spp_axis = (ax * ax == desc->spp) ? ax : 0;
+    P.max_depth = desc->max_depth;
+    P.rr_start = desc->rr_start;
+    P.seed = desc->seed;
+    P.width = s->width;
+    P.height = s->height;
+    const unsigned long long total = (unsigned long long)s->width * s->height * (unsigned long long)desc->spp;
+    int capacity = (int)std::min<unsigned long long>(kMaxCapacity, (total + 1023) / 1024 * 1024);
+    const int film_n = 3 * s->width * s->height;
+    ensure_wave(s, capacity, film_n);
+    cudaStream_t st = s->stream;
+    ck(cudaMemsetAsync(s->film32, 0, sizeof(float) * film_n, st), "memset film");
+    ck(cudaMemsetAsync(s->film64, 0, sizeof(double) * film_n, st), "memset film");
+    WaveCounters init{};
+    init.work_total = total;
+    *s->h_ctr = init;
+    ck(cudaMemcpyAsync(s->d_ctr, s->h_ctr, sizeof(WaveCounters), cudaMemcpyHostToDevice, st), "init counters");
+    ck(cudaStreamSynchronize(st), "init");
+    const bool timed = (desc->flags & 1) != 0;
+    if (!timed && (!s->graph || !same_params(s->graph_params, P))) {
+        if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
+        cudaGraph_t g;
+        ck(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
+        enqueue_iterations(s, P, kItersPerGraph);
+        ck(cudaStreamEndCapture(st, &g), "end capture");
+        ck(cudaGraphInstantiate(&s->graph, g, 0), "graph instantiate");
+        cudaGraphDestroy(g);
+        s->graph_params = P;
+    }
+    ck(cudaEventRecord(s->ev0, st), "event");
+    launch_generate(s->dev, s->pb, 1, P, s->d_ctr, st);  // fills buffer 0
+    double launches = 2;
+    const unsigned long long max_rounds = 64 + (total / (unsigned long long)capacity + 2) *
+                                                   (unsigned long long)(desc->max_depth + 2) * 4 / kItersPerGraph;
+    std::vector<cudaEvent_t> tev;
+    unsigned long long rounds = 0;
+    while (true) {
+        if (timed) {
+            // same work, launched directly with events around the traversal kernels
+            for (int k = 0; k < kItersPerGraph; k++) {
+                const int cur = k & 1;
+                cudaEvent_t e[4];
+                for (int q = 0; q < 4; q++) { ck(cudaEventCreate(&e[q]), "event"); tev.push_back(e[q]); }
+                ck(cudaEventRecord(e[0], st), "event");
+                launch_extend(s->dev, s->pb, cur, s->d_ctr, s->num_sms, st);
+                ck(cudaEventRecord(e[1], st), "event");
+                launch_shade(s->dev, s->pb, cur, P, s->d_ctr, s->film32, st);
+                ck(cudaEventRecord(e[2], st), "event");
+                launch_shadow(s->dev, s->pb, s->d_ctr, s->film32, s->num_sms, st);
+                ck(cudaEventRecord(e[3], st), "event");
+                launch_generate(s->dev, s->pb, cur, P, s->d_ctr, st);
+            }
+            launch_film_fold(s->film32, s->film64, s->film_n, st);
+        } else {
+            ck(cudaGraphLaunch(s->graph, st), "graph launch");
+        }
+        launches += kKernelsPerIteration * kItersPerGraph + 1;
+        ck(cudaMemcpyAsync(s->h_ctr, s->d_ctr, sizeof(WaveCounters), cudaMemcpyDeviceToHost, st), "read counters");
+        ck(cudaStreamSynchronize(st), "render");
+        check_status(s, s->h_ctr->status);
+        rounds++;
+        if (s->h_ctr->n_cur == 0 && s->h_ctr->work_next >= s->h_ctr->work_total) break;
+        if (rounds > max_rounds) throw Fail(PT_ERR_LIMIT, "render did not converge within the iteration bound");
+    }
+    launch_film_resolve(s->film64, d_dst ? d_dst : s->d_out, film_n, 1.0 / (double)desc->spp, st);
+    ck(cudaEventRecord(s->ev1, st), "event");
+    ck(cudaStreamSynchronize(st), "render");
+    ck(cudaGetLastError(), "render kernels");
+    float ms = 0;
+    ck(cudaEventElapsedTime(&ms, s->ev0, s->ev1), "elapsed");
+    pt_render_stats& R = s->stats;
+    R = pt_render_stats{};
+    R.paths = (double)s->h_ctr->stat_paths;
+    R.closest_rays = (double)s->h_ctr->stat_closest;
+    R.shadow_rays = (double)s->h_ctr->stat_shadow;
+    R.iterations = (double)s->h_ctr->stat_iters;
+    R.render_ms = ms;
+    R.kernel_launches = launches + 1;
+    if (timed) {
+        double ext = 0, sh = 0;
+        for (size_t q = 0; q + 3 < tev.size(); q += 4) {
+            float a = 0, b = 0;
+            cudaEventElapsedTime(&a, tev[q], tev[q + 1]);
+            cudaEventElapsedTime(&b, tev[q + 2], tev[q + 3]);
+            ext += a;
+            sh += b;
+        }
+        for (cudaEvent_t e : tev) cudaEventDestroy(e);
+        R.trace_closest_ms = ext;
+        R.trace_shadow_ms = sh;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Reference file formats (Loader, src/loader/loader.h:20-374)
+// ---------------------------------------------------------------------------
+std::string trim(const std::string& s) {
+    size_t i = s.find_first_not_of(" \n\t\r");
+    if (i == std::string::npos) return "";
+    size_t j = s.find_last_not_of(" \n\t\r");
+    return s.substr(i, j - i + 1);
+}
+
+float srgb2linear(float a) {  // rgb_image.h:122-128
+    return a > 0.04045f ? std::pow((a + 0.055f) / 1.055f, 2.4f) : a / 12.92f;
+}
+
+// texture string -> rgb (ConstantTexture); bw: keep the first channel only
+void parse_tex(const std::string& tex, bool bw, bool srgb, float out[3]) {
+    if (tex.rfind("rgb", 0) == 0) {  // loader.h:47-61: rgb(...) is never sRGB-converted
+        size_t c1 = tex.find(',');
+        size_t c2 = tex.find(',', c1 + 1);
+        if (tex.size() < 5 || c1 == std::string::npos || c2 == std::string::npos)
+            throw Fail(PT_ERR_IO, "bad texture: " + tex);
+        out[0] = (float)std::atof(tex.substr(4, c1 - 4).c_str());
+        out[1] = (float)std::atof(tex.substr(c1 + 1, c2 - c1 - 1).c_str());
+        out[2] = (float)std::atof(tex.substr(c2 + 1, tex.size() - c2 - 2).c_str());
+        if (bw) out[1] = out[2] = out[0];
+        return;
+    }
+    if (tex.rfind("float", 0) == 0) {  // loader.h:62-77
+        if (tex.size() < 7) throw Fail(PT_ERR_IO, "bad texture: " + tex);
+        float r = (float)std::atof(tex.substr(6, tex.size() - 7).c_str());
+        if (srgb) r = srgb2linear(r);
+        out[0] = out[1] = out[2] = r;
+        return;
+    }
+    if (tex.rfind("image", 0) == 0) throw Fail(PT_ERR_IO, "image textures are not supported: " + tex);
+    throw Fail(PT_ERR_IO, "Unknown type of tex: " + tex);
+}
+
+struct LoadedScene {
+    std::vector<float> v, n, t;
+    std::vector<int32_t> tri, tri_mat;
+    std::vector<pt_material> mats;
+    pt_camera cam{};
+    bool has_camera = false;
+};
+
+std::string dir_of(const std::string& f) {
+    size_t i = f.find_last_of("/\\");
+    return i == std::string::npos ? std::string("./") : f.substr(0, i) + "/";
+}
+
+void parse_ptobj(const std::string& path, LoadedScene& L, int mat) {  // loader.h:209-251
+    std::ifstream f(path);
+    if (!f) throw Fail(PT_ERR_IO, "cannot open " + path);
+    std::string line, type;
+    if (!std::getline(f, line)) throw Fail(PT_ERR_IO, "Insuficient number of lines when reading file");
+    std::istringstream h(line);
+    int nv = 0, nf = 0;
+    h >> nv >> nf >> type;
+    if (type != "TRIANGLE_MESH") throw Fail(PT_ERR_IO, "Unknown mesh type: " + type);
+    const int base = (int)(L.v.size() / 3);
+    for (int i = 0; i < nv; i++) {
+        if (!std::getline(f, line)) throw Fail(PT_ERR_IO, "Insuficient number of lines when reading verts");
+        std::istringstream s(line);
+        float p[3], uv[2], nn[3], tg[3];
+        s >> p[0] >> p[1] >> p[2] >> uv[0] >> uv[1] >> nn[0] >> nn[1] >> nn[2] >> tg[0] >> tg[1] >> tg[2];
+        L.v.insert(L.v.end(), p, p + 3);
+        L.n.insert(L.n.end(), nn, nn + 3);
+        L.t.insert(L.t.end(), tg, tg + 3);
+    }
+    for (int i = 0; i < nf; i++) {
+        if (!std::getline(f, line)) throw Fail(PT_ERR_IO, "Insuficient number of lines when reading faces");
+        std::istringstream s(line);
+        int a, b, c;
+        s >> a >> b >> c;
+        if (a < 0 || b < 0 || c < 0 || a >= nv || b >= nv || c >= nv) throw Fail(PT_ERR_IO, "face index out of range in " + path);
+        L.tri.push_back(base + a);
+        L.tri.push_back(base + b);
+        L.tri.push_back(base + c);
+        L.tri_mat.push_back(mat);
+    }
+}
+
+int parse_ptmat(const std::string& path, LoadedScene& L, std::unordered_map<std::string, int>& cache) {
+    auto it = cache.find(path);  // loader.h:147-150: materials are shared by file name
+    if (it != cache.end()) return it->second;
+    std::ifstream f(path);
+    if (!f) throw Fail(PT_ERR_IO, "cannot open " + path);
+    std::string word;
+    f >> word;
+    pt_material m{};
+    if (word == "DISNEY") {  // loader.h:154-180
+        std::string albedo, spec, rough, metal, transp, ior, normal, alpha;
+        f >> albedo >> spec >> rough >> metal >> transp >> ior >> normal >> alpha;
+        float a[3], r[3], me[3], io[3];
+        parse_tex(albedo, false, true, a);
+        parse_tex(rough, true, false, r);
+        parse_tex(metal, true, false, me);
+        parse_tex(ior, true, true, io);
+        // standard_material.h:46-61: Diffuse when metal < 0.1, else Glossy(roughness)
+        m.kind = (double)me[0] < 0.1 ? PT_MAT_DIFFUSE : PT_MAT_GGX;
+        std::memcpy(m.rgb, a, 12);
+        m.roughness = r[0];
+        m.ior = io[0];
+    } else if (word == "EMISSION") {  // loader.h:181-201
+        std::string col, inten;
+        f >> col >> inten;
+        float c[3];
+        parse_tex(col, false, true, c);
+        m.kind = PT_MAT_EMISSIVE;
+        std::memcpy(m.rgb, c, 12);
+        m.intensity = (float)std::atof(inten.substr(6, inten.size() - 7).c_str());
+    } else if (word == "DIELECTRIC") {  // extension: RefractionBxDF(ior)
+        std::string ior;
+        f >> ior;
+        float io[3];
+        parse_tex(ior, true, false, io);
+        m.kind = PT_MAT_DIELECTRIC;
+        m.ior = io[0];
+        m.rgb[0] = m.rgb[1] = m.rgb[2] = 1.0f;
+    } else {
+        throw Fail(PT_ERR_IO, "Wrong bsdf type: " + word);
+    }
+    L.mats.push_back(m);
+    int id = (int)L.mats.size() - 1;
+    cache[path] = id;
+    return id;
+}
+
+void load_files(const std::string& settings_file, LoadedScene& L, pt_render_desc* rs, std::string& output) {
+    std::ifstream f(settings_file);
+    if (!f) throw Fail(PT_ERR_IO, "cannot open " + settings_file);
+    std::string line, scene_name;
+    int spp = 1, rx = 256, ry = 256;  // RenderSettings defaults (renderer.h:19-22)
+    while (std::getline(f, line)) {  // loader.h:256-311
+        line = line.substr(0, line.find('#'));
+        std::istringstream s(line);
+        std::string type;
+        s >> type;
+        if (type == "renderer") {
+            std::string r;
+            s >> r;
+            if (r != "pathtracer_mis" && r != "pathtracer" && r != "pure_pt" && r != "ppg" && r != "debug" &&
+                r != "lighttracer" && r != "pathtracer_mlt" && r != "lighttracer_mlt" && r != "photonmapping" &&
+                r != "validation")
+                throw Fail(PT_ERR_IO, "Unknown renderer type: " + r);
+        } else if (type == "spp") {
+            s >> spp;
+        } else if (type == "resolution") {
+            s >> rx >> ry;
+        } else if (type == "scene") {
+            s >> scene_name;
+        } else if (type == "output") {
+            s >> output;
+        } else if (!type.empty()) {
+            throw Fail(PT_ERR_IO, "Unknown render setting: " + type);
+        }
+    }
+    std::ifstream sf(scene_name);
+    if (!sf) throw Fail(PT_ERR_IO, "cannot open scene " + scene_name);
+    const std::string dir = dir_of(scene_name);
+    std::unordered_map<std::string, int> cache;
+    while (std::getline(sf, line)) {  // loader.h:330-351
+        line = trim(line.substr(0, line.find('#')));
+        std::istringstream s(line);
+        std::string type;
+        s >> type;
+        if (type == "camera") {
+            pt_camera& c = L.cam;
+            s >> c.origin[0] >> c.origin[1] >> c.origin[2] >> c.at[0] >> c.at[1] >> c.at[2] >> c.up[0] >> c.up[1] >>
+                c.up[2] >> c.tan_fovy;
+            L.has_camera = true;
+        } else if (type == "obj") {
+            std::string obj, mat;
+            s >> obj >> mat;
+            const size_t first = L.tri_mat.size();
+            parse_ptobj(dir + obj, L, 0);
+            int m = parse_ptmat(dir + mat, L, cache);
+            for (size_t i = first; i < L.tri_mat.size(); i++) L.tri_mat[i] = m;
+        } else if (type == "light") {
+            throw Fail(PT_ERR_IO, "point lights are not supported");
+        } else if (!type.empty()) {
+            throw Fail(PT_ERR_IO, "Unknown scene obj: " + type);
+        }
+    }
+    if (!L.has_camera) throw Fail(PT_ERR_IO, "scene has no camera");
+    L.cam.width = rx;
+    L.cam.height = ry;
+    rs->spp = spp * spp;  // pathtracerMIS.h:148-149: spp x spp samples per pixel
+    rs->max_depth = 32;
+    rs->rr_start = 3;
+    rs->seed = 0;
+    rs->mode = PT_MODE_MIS;
+    rs->flags = 0;
+}
+
+// ---------------------------------------------------------------------------
+// Image output (Image::save, rgb_image.h:300-318): 8-bit sRGB PNG and RGBE.
+// PNG is written with stored (uncompressed) deflate blocks.
+// ---------------------------------------------------------------------------
+uint32_t crc32_update(uint32_t crc, const unsigned char* p, size_t n) {
+    static uint32_t table[256];
+    static bool init = false;
+    if (!init) {
+        for (uint32_t i = 0; i < 256; i++) {
+            uint32_t c = i;
+            for (int k = 0; k < 8; k++) c = (c & 1) ? 0xedb88320u ^ (c >> 1) : c >> 1;
+            table[i] = c;
+        }
+        init = true;
+    }
+    crc = ~crc;
+    for (size_t i = 0; i < n; i++) crc = table[(crc ^ p[i]) & 0xff] ^ (crc >> 8);
+    return ~crc;
+}
+
+void put_be32(std::vector<unsigned char>& v, uint32_t x) {
+    v.push_back((unsigned char)(x >> 24)); v.push_back((unsigned char)(x >> 16));
+    v.push_back((unsigned char)(x >> 8)); v.push_back((unsigned char)x);
+}
+
+void png_chunk(FILE* f, const char* type, const std::vector<unsigned char>& data) {
+    std::vector<unsigned char> b;
+    put_be32(b, (uint32_t)data.size());
+    b.insert(b.end(), type, type + 4);
+    b.insert(b.end(), data.begin(), data.end());
+    uint32_t crc = crc32_update(0, b.data() + 4, b.size() - 4);
+    put_be32(b, crc);
+    fwrite(b.data(), 1, b.size(), f);
+}
+
+float linear2srgb(float a) { return a > 0.0031308f ? 1.055f * std::pow(a, 1.0f / 2.4f) - 0.055f : 12.92f * a; }
+
+void save_png(const std::string& path, const float* rgb, int W, int H) {
+    std::vector<unsigned char> raw;
+    raw.reserve((size_t)H * (3 * W + 1));
+    for (int j = 0; j < H; j++) {
+        raw.push_back(0);
+        for (int i = 0; i < 3 * W; i++) {
+            float a = linear2srgb(rgb[(size_t)j * 3 * W + i]);
+            if (!(a > 0.0f)) a = 0.0f;  // put2char1 (rgb_image.h:23-35)
+            if (a >= 0.99999f) a = 0.99999f;
+            raw.push_back((unsigned char)(unsigned int)(a * 255.0f));
+        }
+    }
+    std::vector<unsigned char> z = {0x78, 0x01};
+    uint32_t s1 = 1, s2 = 0;
+    for (unsigned char c : raw) { s1 = (s1 + c) % 65521; s2 = (s2 + s1) % 65521; }
+    size_t pos = 0;
+    do {
+        size_t len = std::min<size_t>(65535, raw.size() - pos);
+        z.push_back(pos + len == raw.size() ? 1 : 0);
+        z.push_back((unsigned char)(len & 0xff)); z.push_back((unsigned char)(len >> 8));
+        z.push_back((unsigned char)(~len & 0xff)); z.push_back((unsigned char)((~len >> 8) & 0xff));
+        z.insert(z.end(), raw.begin() + pos, raw.begin() + pos + len);
+        pos += len;
+    } while (pos < raw.size());
+    put_be32(z, (s2 << 16) | s1);
+    FILE* f = std::fopen(path.c_str(), "wb");
+    if (!f) throw Fail(PT_ERR_IO, "cannot write " + path);
+    const unsigned char sig[8] = {137, 80, 78, 71, 13, 10, 26, 10};
+    fwrite(sig, 1, 8, f);
+    std::vector<unsigned char> ihdr;
+    put_be32(ihdr, (uint32_t)W);
+    put_be32(ihdr, (uint32_t)H);
+    ihdr.insert(ihdr.end(), {8, 2, 0, 0, 0});
+    png_chunk(f, "IHDR", ihdr);
+    png_chunk(f, "IDAT", z);
+    png_chunk(f, "IEND", {});
+    std::fclose(f);
+}
+
+void save_hdr(const std::string& path, const float* rgb, int W, int H) {
+    FILE* f = std::fopen(path.c_str(), "wb");
+    if (!f) throw Fail(PT_ERR_IO, "cannot write " + path);
+    std::fprintf(f, "#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n-Y %d +X %d\n", H, W);
+    std::vector<unsigned char> row(4 * (size_t)W);
+    for (int j = 0; j < H; j++) {
+        for (int i = 0; i < W; i++) {
+            const float* p = rgb + 3 * ((size_t)j * W + i);
+            float m = std::max(p[0], std::max(p[1], p[2]));
+            unsigned char* o = &row[4 * (size_t)i];
+            if (!(m >= 1e-32f)) { o[0] = o[1] = o[2] = o[3] = 0; continue; }
+            int e;
+            float scale = std::frexp(m, &e) * 256.0f / m;
+            o[0] = (unsigned char)std::max(0.0f, p[0] * scale);
+            o[1] = (unsigned char)std::max(0.0f, p[1] * scale);
+            o[2] = (unsigned char)std::max(0.0f, p[2] * scale);
+            o[3] = (unsigned char)(e + 128);
+        }
+        fwrite(row.data(), 1, row.size(), f);
+    }
+    std::fclose(f);
+}
+
+}  // namespace
+
+extern "C" {
+
+pt_status pt_scene_create(const pt_scene_desc* desc, pt_scene** out) {
+    if (!out) { g_error = "null output pointer"; return PT_ERR_INVALID; }
+    *out = nullptr;
+    pt_scene* s = new (std::nothrow) pt_scene();
+    if (!s) { g_error = "host allocation failed"; return PT_ERR_MEMORY; }
+    pt_status st = guarded([&] { create_scene(desc, s); });
+    if (st != PT_OK) { delete s; return st; }
+    *out = s;
+    return PT_OK;
+}
+
+pt_status pt_scene_load(const char* settings_file, pt_scene** out, pt_render_desc* settings, char* output_name,
+                        int32_t output_name_len) {
+    if (!out || !settings_file) { g_error = "null argument"; return PT_ERR_INVALID; }
+    *out = nullptr;
+    LoadedScene L;
+    pt_render_desc rs{};
+    std::string output;
+    pt_status st = guarded([&] { load_files(settings_file, L, &rs, output); });
+    if (st != PT_OK) return st;
+    pt_scene_desc d{};
+    d.n_vertices = (int32_t)(L.v.size() / 3);
+    d.vertices = L.v.data();
+    d.normals = L.n.data();
+    d.tangents = L.t.data();
+    d.n_triangles = (int32_t)L.tri_mat.size();
+    d.triangles = L.tri.data();
+    d.tri_material = L.tri_mat.data();
+    d.n_materials = (int32_t)L.mats.size();
+    d.materials = L.mats.data();
+    d.camera = L.cam;
+    st = pt_scene_create(&d, out);
+    if (st != PT_OK) return st;
+    if (settings) *settings = rs;
+    if (output_name && output_name_len > 0) {
+        std::snprintf(output_name, (size_t)output_name_len, "%s", output.c_str());
+    }
+    return PT_OK;
+}
+
+void pt_scene_destroy(pt_scene* s) { delete s; }
+
+pt_status pt_trace_closest(pt_scene* s, const pt_ray* rays, int32_t n, pt_hit* hits) {
+    if (!s) { g_error = "null scene"; return PT_ERR_INVALID; }
+    return guarded([&] { trace_host(s, rays, n, hits, false); });
+}
+
+pt_status pt_trace_any(pt_scene* s, const pt_ray* rays, int32_t n, uint8_t* occluded) {
+    if (!s) { g_error = "null scene"; return PT_ERR_INVALID; }
+    return guarded([&] { trace_host(s, rays, n, occluded, true); });
+}
+
+pt_status pt_trace_closest_device(pt_scene* s, const pt_ray* d_rays, int32_t n, pt_hit* d_hits, void* stream) {
+    if (!s) { g_error = "null scene"; return PT_ERR_INVALID; }
+    return guarded([&] { trace_device(s, d_rays, n, d_hits, false, static_cast<cudaStream_t>(stream)); });
+}
+
+pt_status pt_trace_any_device(pt_scene* s, const pt_ray* d_rays, int32_t n, uint8_t* d_occ, void* stream) {
+    if (!s) { g_error = "null scene"; return PT_ERR_INVALID; }
+    return guarded([&] { trace_device(s, d_rays, n, d_occ, true, static_cast<cudaStream_t>(stream)); });
+}
+
+pt_status pt_render(pt_scene* s, const pt_render_desc* desc, float* rgb_out) {
+    if (!s || !rgb_out) { g_error = "null argument"; return PT_ERR_INVALID; }
+    return guarded([&] {
+        render_impl(s, desc, nullptr);
+        ck(cudaMemcpyAsync(rgb_out, s->d_out, sizeof(float) * s->film_n, cudaMemcpyDeviceToHost, s->stream), "copy image");
+        ck(cudaStreamSynchronize(s->stream), "copy image");
+    });
+}
+
+pt_status pt_render_device(pt_scene* s, const pt_render_desc* desc, float* d_rgb_out) {
+    if (!s || !d_rgb_out) { g_error = "null argument"; return PT_ERR_INVALID; }
+    return guarded([&] { render_impl(s, desc, d_rgb_out); });
+}
+
+pt_status pt_render_stats_get(pt_scene* s, pt_render_stats* out) {
+    if (!s || !out) { g_error = "null argument"; return PT_ERR_INVALID; }
+    *out = s->stats;
+    return PT_OK;
+}
+
+pt_status pt_image_save(const char* prefix, const float* rgb, int32_t w, int32_t h) {
+    if (!prefix || !rgb || w <= 0 || h <= 0) { g_error = "bad argument"; return PT_ERR_INVALID; }
+    return guarded([&] {
+        save_png(std::string(prefix) + ".png", rgb, w, h);
+        save_hdr(std::string(prefix) + ".hdr", rgb, w, h);
+    });
+}
+
+const char* pt_last_error(void) { return g_error.c_str(); }
+
+pt_status pt_debug_ref_topology(const float* tri_v, int32_t n, int32_t* leaf_order, int32_t* prim_parent,
+                                float* node_boxes, int32_t max_nodes, int32_t* n_nodes) {
+    if (n < 0 || (n > 0 && (!tri_v || !leaf_order || !prim_parent)) || !n_nodes) {
+        g_error = "bad argument";
+        return PT_ERR_INVALID;
+    }
+    return guarded([&] {
+        RefTopology t = build_ref_topology(tri_v, n);
+        *n_nodes = (int32_t)t.node_box.size();
+        if ((int32_t)t.node_box.size() > max_nodes) throw Fail(PT_ERR_LIMIT, "node buffer too small");
+        for (int i = 0; i < n; i++) {
+            leaf_order[i] = t.leaf_order[i];
+            prim_parent[i] = t.prim_parent[i];
+        }
+        for (size_t i = 0; i < t.node_box.size(); i++) {
+            std::memcpy(node_boxes + 6 * i, t.node_box[i].lo, 12);
+            std::memcpy(node_boxes + 6 * i + 3, t.node_box[i].hi, 12);
+        }
+    });
+}
+
+}  // extern "C"

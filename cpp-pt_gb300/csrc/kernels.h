@@ -1,0 +1,54 @@
+// Host-side launchers of the CUDA kernels (implemented in render.cu).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "dev_types.h"
+
+namespace cpppt_gb300 {
+
+// Persistent-warp ray-batch kernels.  `rays` are 7 packed floats per ray;
+// `counter` is one zeroed int in device memory (work queue head);
+// `status` collects kStatus* bits.
+void launch_trace_closest(const DevScene& S, const float* rays, int n, float4* hits, int* counter,
+                          uint32_t* status, int num_sms, cudaStream_t st);
+void launch_trace_any(const DevScene& S, const float* rays, int n, uint8_t* occluded, int* counter,
+                      uint32_t* status, int num_sms, cudaStream_t st);
+
+// Wavefront path state: capacity paths, structure of arrays, two copies.
+struct PathBuffers {
+    float4* o[2];    // origin.xyz, p (pdf of the last BSDF sample, RR scaled)
+    float4* d[2];    // direction.xyz, unused
+    float4* thr[2];  // throughput rgb, unused
+    int4* info[2];   // pixel, sample, bounce | sampled_delta << 16, unused
+    float4* hit;     // t, prim, beta, gamma of the current buffer
+    float4* sh_o;    // shadow ray origin.xyz, max_t
+    float4* sh_d;    // direction.xyz, pixel
+    float4* sh_c;    // contribution rgb
+    int capacity;
+};
+
+struct RenderParams {
+    int spp;
+    int spp_axis;        // >0: spp = spp_axis^2, stratified as pathtracerMIS.h:148-153
+    int max_depth;
+    int rr_start;
+    uint32_t seed;
+    int width, height;
+};
+
+// The stages of one wavefront iteration reading path buffer `cur` (writing
+// 1 - cur): extend (closest hit), shade (BSDF, NEE, MIS, RR, compaction),
+// shadow (any hit + film), generate (new camera paths) + advance (counters).
+void launch_extend(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, int num_sms, cudaStream_t st);
+void launch_shade(const DevScene& S, const PathBuffers& B, int cur, const RenderParams& P, WaveCounters* ctr,
+                  float* film32, cudaStream_t st);
+void launch_shadow(const DevScene& S, const PathBuffers& B, WaveCounters* ctr, float* film32, int num_sms,
+                   cudaStream_t st);
+void launch_generate(const DevScene& S, const PathBuffers& B, int cur, const RenderParams& P, WaveCounters* ctr,
+                     cudaStream_t st);
+constexpr int kKernelsPerIteration = 5;
+void launch_film_fold(float* film32, double* film64, int n, cudaStream_t st);
+void launch_film_resolve(const double* film64, float* out, int n, double scale, cudaStream_t st);
+
+}  // namespace cpppt_gb300

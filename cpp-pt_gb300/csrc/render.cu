@@ -1,0 +1,344 @@
+// CUDA kernels: ray-batch traversal and the wavefront PT+NEE+MIS integrator
+// (PathtracerMIS::integrate/render, src/renderer/pathtracerMIS.h:29-167).
+//
+// Wavefront layout: path state lives in HBM as structure-of-arrays, two
+// copies (current / next).  One iteration = extend (closest hit for every
+// live path) -> shade (emission + MIS, BSDF sample, NEE shadow ray, Russian
+// roulette; survivors are appended compactly to the next buffer with
+// warp-aggregated atomics) -> shadow (any hit; unoccluded NEE contributions
+// go to the film) -> generate (new camera paths fill the next buffer up to
+// capacity from a global work counter) -> advance (one thread swaps counts).
+// All sizes are read from device counters, so an iteration needs no host
+// round trip and a chain of iterations is captured once in a CUDA graph.
+#include <cuda_runtime.h>
+
+#include "kernels.h"
+#include "shade.cuh"
+#include "trace.cuh"
+
+namespace cpppt_gb300 {
+
+constexpr int kTraceThreads = 256;
+constexpr int kTraceBlocksPerSM = 4;
+
+__device__ __forceinline__ void stage_top_nodes(const DevScene& S, uint4* snodes) {
+    const int n = min(S.n_nodes, kSmemNodes) * 4;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) snodes[i] = __ldg(S.nodes + i);
+    __syncthreads();
+}
+
+// Each warp takes 32 consecutive work items at a time from a global counter
+// (persistent threads); returns the first index, or >= n when done.
+__device__ __forceinline__ int warp_fetch(int* counter, int n) {
+    int base = 0;
+    if ((threadIdx.x & 31) == 0) base = atomicAdd(counter, 32);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    return base;
+}
+
+// Appends from every lane with pred set; all 32 lanes must call it.
+__device__ __forceinline__ int warp_append(int* counter, bool pred) {
+    const unsigned mask = __ballot_sync(0xffffffffu, pred);
+    if (mask == 0) return -1;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(counter, __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    return pred ? base + __popc(mask & ((1u << lane) - 1u)) : -1;
+}
+
+// ---------------------------------------------------------------------------
+// Ray batches (BVH::intersect / intersect_any on arrays of rays)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kTraceThreads) k_trace_closest(DevScene S, const float* __restrict__ rays, int n,
+                                                                 float4* __restrict__ hits, int* counter,
+                                                                 uint32_t* status) {
+    __shared__ uint4 snodes[kSmemNodes * 4];
+    stage_top_nodes(S, snodes);
+    while (true) {
+        const int base = warp_fetch(counter, n);
+        if (base >= n) break;
+        const int i = base + (threadIdx.x & 31);
+        if (i < n) {
+            const float* r = rays + 7 * (size_t)i;
+            const float3 o = make_float3(r[0], r[1], r[2]), d = make_float3(r[3], r[4], r[5]);
+            HitRec h;
+            traverse<false>(S, snodes, o, d, r[6], h, status);
+            hits[i] = make_float4(h.t, __int_as_float(h.prim), h.beta, h.gamma);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kTraceThreads) k_trace_any(DevScene S, const float* __restrict__ rays, int n,
+                                                             uint8_t* __restrict__ occ, int* counter,
+                                                             uint32_t* status) {
+    __shared__ uint4 snodes[kSmemNodes * 4];
+    stage_top_nodes(S, snodes);
+    while (true) {
+        const int base = warp_fetch(counter, n);
+        if (base >= n) break;
+        const int i = base + (threadIdx.x & 31);
+        if (i < n) {
+            const float* r = rays + 7 * (size_t)i;
+            const float3 o = make_float3(r[0], r[1], r[2]), d = make_float3(r[3], r[4], r[5]);
+            HitRec h;
+            occ[i] = traverse<true>(S, snodes, o, d, r[6], h, status) ? 1 : 0;
+        }
+    }
+}
+
+void launch_trace_closest(const DevScene& S, const float* rays, int n, float4* hits, int* counter, uint32_t* status,
+                          int num_sms, cudaStream_t st) {
+    if (n <= 0) return;
+    const int blocks = min(num_sms * kTraceBlocksPerSM, (n + kTraceThreads - 1) / kTraceThreads);
+    k_trace_closest<<<blocks, kTraceThreads, 0, st>>>(S, rays, n, hits, counter, status);
+}
+
+void launch_trace_any(const DevScene& S, const float* rays, int n, uint8_t* occ, int* counter, uint32_t* status,
+                      int num_sms, cudaStream_t st) {
+    if (n <= 0) return;
+    const int blocks = min(num_sms * kTraceBlocksPerSM, (n + kTraceThreads - 1) / kTraceThreads);
+    k_trace_any<<<blocks, kTraceThreads, 0, st>>>(S, rays, n, occ, counter, status);
+}
+
+// ---------------------------------------------------------------------------
+// Wavefront integrator
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kTraceThreads) k_extend(DevScene S, PathBuffers B, int cur, WaveCounters* ctr) {
+    __shared__ uint4 snodes[kSmemNodes * 4];
+    stage_top_nodes(S, snodes);
+    const int n = ctr->n_cur;
+    const float4* __restrict__ O = B.o[cur];
+    const float4* __restrict__ D = B.d[cur];
+    while (true) {
+        const int base = warp_fetch(&ctr->fetch_ext, n);
+        if (base >= n) break;
+        const int i = base + (threadIdx.x & 31);
+        if (i < n) {
+            const float4 o = O[i], d = D[i];
+            HitRec h;
+            traverse<false>(S, snodes, make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z),
+                            __int_as_float(0x7f800000), h, &ctr->status);
+            B.hit[i] = make_float4(h.t, __int_as_float(h.prim), h.beta, h.gamma);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kTraceThreads) k_shadow(DevScene S, PathBuffers B, WaveCounters* ctr,
+                                                          float* __restrict__ film) {
+    __shared__ uint4 snodes[kSmemNodes * 4];
+    stage_top_nodes(S, snodes);
+    const int n = ctr->n_shadow;
+    while (true) {
+        const int base = warp_fetch(&ctr->fetch_sh, n);
+        if (base >= n) break;
+        const int i = base + (threadIdx.x & 31);
+        if (i < n) {
+            const float4 o = B.sh_o[i], d = B.sh_d[i];
+            HitRec h;
+            const bool occluded = traverse<true>(S, snodes, make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z),
+                                                 o.w, h, &ctr->status);
+            if (!occluded) {
+                const float4 c = B.sh_c[i];
+                const int pix = __float_as_int(d.w);
+                atomicAdd(film + 3 * pix, c.x);
+                atomicAdd(film + 3 * pix + 1, c.y);
+                atomicAdd(film + 3 * pix + 2, c.z);
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_shade(DevScene S, PathBuffers B, int cur, RenderParams P, WaveCounters* ctr,
+                                               float* __restrict__ film) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = ctr->n_cur;
+    bool push_sh = false, push_cont = false;
+    float4 sh_o, sh_d, sh_c, no, nd, nt;
+    int4 ninfo;
+    if (i < n) {
+        const float4 O = B.o[cur][i], D = B.d[cur][i], T = B.thr[cur][i];
+        const int4 I = B.info[cur][i];
+        const float4 H = B.hit[i];
+        const int prim = __float_as_int(H.y);
+        const int pixel = I.x, sample = I.y, bounce = I.z & 0xffff;
+        const bool sdelta = (I.z >> 16) & 1;
+        float p = O.w;
+        f3 mul = mk(T.x, T.y, T.z);
+        const f3 ro = mk(O.x, O.y, O.z), rd = mk(D.x, D.y, D.z);
+        if (prim >= 0) {  // a miss adds render_sky = 0 (pathtracerMIS.h:38-41)
+            int kind;
+            DevMaterial m;
+            const Surf s = make_surf(S, prim, ro, rd, H.x, H.z, H.w, bounce == 0, &kind, &m);
+            const f3 wo = -rd;
+            if (kind == PT_MAT_EMISSIVE_) {  // pathtracerMIS.h:43-67: emitters end the path
+                float w = 1.0f;
+                if (!sdelta) {
+                    const int4 vi = __ldg(S.tri_vidx + prim);
+                    const f3 a = f3of(__ldg(S.v_pos + vi.x)), b = f3of(__ldg(S.v_pos + vi.y)),
+                             c = f3of(__ldg(S.v_pos + vi.z));
+                    const float area = length(cross(b - a, c - a)) * 0.5f;
+                    const float pdf_l = (1.0f / (float)S.n_lights) * (1.0f / area);
+                    const float r = H.x;
+                    const float cos_theta = fabsf(dot(s.n, rd)) + kEps;
+                    const float p_nee = pdf_l * r * r / cos_theta;
+                    w = p / (p + p_nee);
+                }
+                atomicAdd(film + 3 * pixel, mul.x * m.r * w);
+                atomicAdd(film + 3 * pixel + 1, mul.y * m.g * w);
+                atomicAdd(film + 3 * pixel + 2, mul.z * m.b * w);
+            } else {
+                const Rng4 r0 = rng4(P.seed, sample, pixel, bounce, 0);
+                const Rng4 r1 = rng4(P.seed, sample, pixel, bounce, 1);
+                const BSample bs = bsdf_sample(m, s, wo, r0.v[0], r0.v[1]);
+                p = bs.pdf;
+                if (!bs.delta && S.n_lights > 0) {  // NEE, pathtracerMIS.h:79-106
+                    const LSample ls = sample_light(S, s.p, r0.v[2], r0.v[3], r1.v[0]);
+                    f3 sd = ls.pos - s.p;
+                    const float len = length(sd);
+                    sd = sd * (1.0f / len);
+                    if (same_hemisphere(s, wo, sd)) {
+                        const float pb = bsdf_pdf(m, s, wo, sd);
+                        const float cosl = fabsf(dot(ls.n, sd)) + kEps;
+                        const float pn = ls.pdf * len * len / cosl;
+                        const float w = pn / (pb + pn);
+                        const f3 f = bsdf_eval(m, s, wo, sd);
+                        const f3 c = mul * f * ls.le * (1.0f / (ls.pdf * len * len)) * w;
+                        if (c.x != 0.f || c.y != 0.f || c.z != 0.f) {
+                            push_sh = true;
+                            const f3 so = s.p + sd * kEps;
+                            sh_o = make_float4(so.x, so.y, so.z, len - 2.0f * kEps);
+                            sh_d = make_float4(sd.x, sd.y, sd.z, __int_as_float(pixel));
+                            sh_c = make_float4(c.x, c.y, c.z, 0.f);
+                        }
+                    }
+                }
+                if (same_hemisphere(s, wo, bs.wi)) {  // pathtracerMIS.h:112-126
+                    const f3 f = bsdf_eval(m, s, wo, bs.wi);
+                    bool alive = true;
+                    if (bounce >= P.rr_start) {
+                        const float rr = russian_roulette(f);
+                        if (r1.v[1] > rr) alive = false;
+                        else p = p * rr;
+                    }
+                    if (alive && bounce + 1 < P.max_depth) {
+                        mul = mul * f * (1.0f / p);
+                        const f3 oo = s.p + bs.wi * kEps;
+                        push_cont = true;
+                        no = make_float4(oo.x, oo.y, oo.z, p);
+                        nd = make_float4(bs.wi.x, bs.wi.y, bs.wi.z, 0.f);
+                        nt = make_float4(mul.x, mul.y, mul.z, 0.f);
+                        ninfo = make_int4(pixel, sample, (bounce + 1) | ((bs.delta ? 1 : 0) << 16), 0);
+                    }
+                }
+            }
+        }
+    }
+    const int js = warp_append(&ctr->n_shadow, push_sh);
+    if (push_sh) {
+        B.sh_o[js] = sh_o;
+        B.sh_d[js] = sh_d;
+        B.sh_c[js] = sh_c;
+    }
+    const int jc = warp_append(&ctr->n_next, push_cont);
+    if (push_cont) {
+        const int nx = 1 - cur;
+        B.o[nx][jc] = no;
+        B.d[nx][jc] = nd;
+        B.thr[nx][jc] = nt;
+        B.info[nx][jc] = ninfo;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_generate(DevScene S, PathBuffers B, int cur, RenderParams P,
+                                                  WaveCounters* ctr) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n_next = ctr->n_next;
+    const int avail = B.capacity - n_next;
+    const unsigned long long w = ctr->work_next + (unsigned long long)t;
+    if (t >= avail || w >= ctr->work_total) return;
+    const unsigned long long npix = (unsigned long long)P.width * P.height;
+    const int sample = (int)(w / npix);
+    const int pixel = (int)(w - (unsigned long long)sample * npix);
+    const int px = pixel % P.width, py = pixel / P.width;
+    const Rng4 r = rng4(P.seed, sample, pixel, 0xffffu, 2);
+    float cx, cy;
+    if (P.spp_axis > 0) {  // pathtracerMIS.h:148-153: spp x spp strata
+        const int k = sample / P.spp_axis, l = sample - (sample / P.spp_axis) * P.spp_axis;
+        cx = (((float)px + ((float)k + r.v[0]) / (float)P.spp_axis) / (float)P.width) * 2.0f - 1.0f;
+        cy = -((((float)py + ((float)l + r.v[1]) / (float)P.spp_axis) / (float)P.height) * 2.0f - 1.0f);
+    } else {
+        cx = (((float)px + r.v[0]) / (float)P.width) * 2.0f - 1.0f;
+        cy = -((((float)py + r.v[1]) / (float)P.height) * 2.0f - 1.0f);
+    }
+    // CameraPerspective::get_ray (camera_perspective.h:30-39)
+    const DevCamera& C = S.cam;
+    const float dx = cx * C.tan_fovy * C.aspect, dy = cy * C.tan_fovy, dz = -1.0f;
+    const f3 d = normalized(mk(C.m[0] * dx + C.m[1] * dy + C.m[2] * dz, C.m[3] * dx + C.m[4] * dy + C.m[5] * dz,
+                               C.m[6] * dx + C.m[7] * dy + C.m[8] * dz));
+    const int nx = 1 - cur;
+    const int j = n_next + t;
+    B.o[nx][j] = make_float4(C.o[0], C.o[1], C.o[2], 1.0f);
+    B.d[nx][j] = make_float4(d.x, d.y, d.z, 0.f);
+    B.thr[nx][j] = make_float4(1.f, 1.f, 1.f, 0.f);
+    B.info[nx][j] = make_int4(pixel, sample, 0 | (1 << 16), 0);  // sampled_delta starts true (:34)
+}
+
+__global__ void k_advance(WaveCounters* ctr, int capacity) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int n_next = ctr->n_next;
+    const unsigned long long left = ctr->work_total - ctr->work_next;
+    const unsigned long long room = (unsigned long long)(capacity - n_next);
+    const unsigned long long added = left < room ? left : room;
+    ctr->work_next += added;
+    ctr->stat_paths += added;
+    ctr->stat_shadow += (unsigned long long)ctr->n_shadow;
+    ctr->n_cur = n_next + (int)added;
+    ctr->stat_closest += (unsigned long long)ctr->n_cur;
+    ctr->n_next = 0;
+    ctr->n_shadow = 0;
+    ctr->fetch_ext = 0;
+    ctr->fetch_sh = 0;
+    ctr->stat_iters += 1;
+}
+
+__global__ void k_fold(float* __restrict__ f32, double* __restrict__ f64, int n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float v = f32[i];
+        if (v != 0.f) {
+            f64[i] += (double)v;
+            f32[i] = 0.f;
+        }
+    }
+}
+
+__global__ void k_resolve(const double* __restrict__ f64, float* __restrict__ out, int n, double scale) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[i] = (float)(f64[i] * scale);
+}
+
+void launch_extend(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, int num_sms, cudaStream_t st) {
+    k_extend<<<num_sms * kTraceBlocksPerSM, kTraceThreads, 0, st>>>(S, B, cur, ctr);
+}
+void launch_shade(const DevScene& S, const PathBuffers& B, int cur, const RenderParams& P, WaveCounters* ctr,
+                  float* film32, cudaStream_t st) {
+    k_shade<<<(B.capacity + 255) / 256, 256, 0, st>>>(S, B, cur, P, ctr, film32);
+}
+void launch_shadow(const DevScene& S, const PathBuffers& B, WaveCounters* ctr, float* film32, int num_sms,
+                   cudaStream_t st) {
+    k_shadow<<<num_sms * kTraceBlocksPerSM, kTraceThreads, 0, st>>>(S, B, ctr, film32);
+}
+void launch_generate(const DevScene& S, const PathBuffers& B, int cur, const RenderParams& P, WaveCounters* ctr,
+                     cudaStream_t st) {
+    k_generate<<<(B.capacity + 255) / 256, 256, 0, st>>>(S, B, cur, P, ctr);
+    k_advance<<<1, 32, 0, st>>>(ctr, B.capacity);
+}
+void launch_film_fold(float* film32, double* film64, int n, cudaStream_t st) {
+    k_fold<<<min((n + 255) / 256, 4096), 256, 0, st>>>(film32, film64, n);
+}
+void launch_film_resolve(const double* film64, float* out, int n, double scale, cudaStream_t st) {
+    k_resolve<<<min((n + 255) / 256, 4096), 256, 0, st>>>(film64, out, n, scale);
+}
+
+}  // namespace cpppt_gb300

@@ -1,0 +1,232 @@
+// Device traversal of the compressed 4-wide BVH with the reference's exact
+// closest-hit semantics (see bvh.h for why this reproduces BVH::intersect).
+#pragma once
+#include "dev_types.h"
+
+namespace cpppt_gb300 {
+
+constexpr int kSmemNodes = 256;       // top of the wide BVH staged in shared memory (16 KB)
+constexpr int kStackSize = 64;
+constexpr int kMaxTraversalSteps = 1 << 22;
+// Nodes whose entry distance exceeds best_t * (1 + 2^-8) are skipped.  The
+// margin covers the rounding of the reference's Cramer-rule t (triangle.h:41-57)
+// for every hit that is not within ~1e-4 rad of grazing the triangle.
+constexpr float kCullScale = 1.00390625f;
+
+// float(t) < 1e-4 (double) <=> t < kTriEps (triangle.h:55 compares with the double EPS)
+__device__ __forceinline__ float tri_eps() { return __int_as_float(0x38d1b718); }  // nextafterf(1e-4f, inf)
+
+struct HitRec {
+    float t;
+    int32_t prim;
+    float beta, gamma;
+    int32_t rank;
+};
+
+__device__ __forceinline__ float m3r(float a, float b, float c) { return __fmul_rn(__fmul_rn(a, b), c); }
+
+// Triangle::intersect up to acceptance (triangle.h:18-80): Cramer's rule with
+// the reference's product and sum order, no fused multiply-add, IEEE
+// reciprocal for 1.0/den (1.0 / float in double rounded to float is the
+// correctly rounded float reciprocal).
+__device__ __forceinline__ bool tri_exact(float4 A, float4 E1, float4 E2, float3 o, float3 d, float max_t,
+                                          float& t, float& beta, float& gamma) {
+    const float v1x = E1.x, v1y = E1.y, v1z = E1.z;
+    const float v2x = E2.x, v2y = E2.y, v2z = E2.z;
+    const float v3x = -d.x, v3y = -d.y, v3z = -d.z;
+    const float vsx = __fsub_rn(o.x, A.x), vsy = __fsub_rn(o.y, A.y), vsz = __fsub_rn(o.z, A.z);
+    float den = m3r(v1x, v2y, v3z);
+    den = __fadd_rn(den, m3r(v2x, v3y, v1z));
+    den = __fadd_rn(den, m3r(v3x, v1y, v2z));
+    den = __fsub_rn(den, m3r(v3x, v2y, v1z));
+    den = __fsub_rn(den, m3r(v3y, v2z, v1x));
+    den = __fsub_rn(den, m3r(v3z, v2x, v1y));
+    const float inv = __frcp_rn(den);
+    float nt = m3r(v1x, v2y, vsz);
+    nt = __fadd_rn(nt, m3r(v2x, vsy, v1z));
+    nt = __fadd_rn(nt, m3r(vsx, v1y, v2z));
+    nt = __fsub_rn(nt, m3r(vsx, v2y, v1z));
+    nt = __fsub_rn(nt, m3r(vsy, v2z, v1x));
+    nt = __fsub_rn(nt, m3r(vsz, v2x, v1y));
+    t = __fmul_rn(nt, inv);
+    if (t < tri_eps() || t > max_t) return false;
+    float nb = m3r(vsx, v2y, v3z);
+    nb = __fadd_rn(nb, m3r(v2x, v3y, vsz));
+    nb = __fadd_rn(nb, m3r(v3x, vsy, v2z));
+    nb = __fsub_rn(nb, m3r(v3x, v2y, vsz));
+    nb = __fsub_rn(nb, m3r(v3y, v2z, vsx));
+    nb = __fsub_rn(nb, m3r(v3z, v2x, vsy));
+    beta = __fmul_rn(nb, inv);
+    float ng = m3r(v1x, vsy, v3z);
+    ng = __fadd_rn(ng, m3r(vsx, v3y, v1z));
+    ng = __fadd_rn(ng, m3r(v3x, v1y, vsz));
+    ng = __fsub_rn(ng, m3r(v3x, vsy, v1z));
+    ng = __fsub_rn(ng, m3r(v3y, vsz, v1x));
+    ng = __fsub_rn(ng, m3r(v3z, vsx, v1y));
+    gamma = __fmul_rn(ng, inv);
+    const float alpha = __fsub_rn(1.0f, __fadd_rn(gamma, beta));
+    if (alpha < 0.f || alpha > 1.f || beta < 0.f || beta > 1.f || gamma < 0.f || gamma > 1.f) return false;
+    // NaN t passes the reference's checks (it then accepts a NaN hit); such
+    // rays lie exactly in the triangle's plane.  They are rejected here.
+    return t == t;
+}
+
+// AABB::intersect_any (aabb.h:19-61) with the reference's division, order2
+// swaps and comparison sequence.  `cand_t` stands in for the ray's running
+// max_t, which only matters when tmax is NaN (a -0.0 direction component
+// with the origin on the box's lower x plane).
+__device__ __forceinline__ bool ref_box_exact(float4 lo, float4 hi, float3 o, float3 d, float cand_t) {
+    float nminx = __fdiv_rn(__fsub_rn(lo.x, o.x), d.x);
+    float nminy = __fdiv_rn(__fsub_rn(lo.y, o.y), d.y);
+    float nminz = __fdiv_rn(__fsub_rn(lo.z, o.z), d.z);
+    float nmaxx = __fdiv_rn(__fsub_rn(hi.x, o.x), d.x);
+    float nmaxy = __fdiv_rn(__fsub_rn(hi.y, o.y), d.y);
+    float nmaxz = __fdiv_rn(__fsub_rn(hi.z, o.z), d.z);
+    float s;
+    if (!(nmaxx >= nminx)) { s = nminx; nminx = nmaxx; nmaxx = s; }
+    if (!(nmaxy >= nminy)) { s = nminy; nminy = nmaxy; nmaxy = s; }
+    if (!(nmaxz >= nminz)) { s = nminz; nminz = nmaxz; nmaxz = s; }
+    float tmin = nminx;
+    if (tmin < nminy) tmin = nminy;
+    if (tmin < nminz && nminz > nminy) tmin = nminz;
+    float tmax = nmaxx;
+    if (tmax > nmaxy) tmax = nmaxy;
+    if (tmax > nmaxz && nmaxz < nmaxy) tmax = nmaxz;
+    if (tmax < tmin) return false;
+    if (tmin > 0.f && (double)tmin < (double)cand_t + 1e-4) return true;
+    return tmax > 0.f;
+}
+
+__device__ __forceinline__ float byte_to_float(uint32_t w, int c) {
+    // exact: 2^23 + b, minus 2^23
+    return __uint_as_float(0x4b000000u | ((w >> (8 * c)) & 0xffu)) - 8388608.0f;
+}
+
+// Traverses the wide BVH.  ANY=false: closest hit into `best` (best.t starts
+// at the ray's max_t).  ANY=true: returns true at the first hit the
+// reference would also report.
+template <bool ANY>
+__device__ __forceinline__ bool traverse(const DevScene& S, const uint4* __restrict__ snodes, float3 o, float3 d,
+                                         float tmax0, HitRec& best, uint32_t* status) {
+    best.t = tmax0;
+    best.prim = -1;
+    best.rank = -1;
+    best.beta = best.gamma = 0.f;
+    if (S.n_tris == 0) return false;
+    const float tiny = 7.888609052210118e-31f;  // 2^-100
+    const float dx = d.x == 0.f ? copysignf(tiny, d.x) : d.x;
+    const float dy = d.y == 0.f ? copysignf(tiny, d.y) : d.y;
+    const float dz = d.z == 0.f ? copysignf(tiny, d.z) : d.z;
+    const float idx = 1.0f / dx, idy = 1.0f / dy, idz = 1.0f / dz;
+    const float oix = o.x * idx, oiy = o.y * idy, oiz = o.z * idz;
+    const bool negx = idx < 0.f, negy = idy < 0.f, negz = idz < 0.f;
+
+    uint32_t stack_ref[kStackSize];
+    float stack_t[kStackSize];
+    int sp = 0;
+    uint32_t cur = 0;  // root
+    int steps = 0;
+    while (true) {
+        if (++steps > kMaxTraversalSteps) {
+            atomicOr(status, kStatusIterLimit);
+            return false;
+        }
+        const float cull = best.t * kCullScale + 1e-6f;
+        if (!(cur & 0x80000000u)) {
+            uint4 w0, w1, w2, w3;
+            if (cur < (uint32_t)kSmemNodes) {
+                w0 = snodes[4 * cur]; w1 = snodes[4 * cur + 1]; w2 = snodes[4 * cur + 2]; w3 = snodes[4 * cur + 3];
+            } else {
+                const uint4* np = S.nodes + 4 * (size_t)cur;
+                w0 = __ldg(np); w1 = __ldg(np + 1); w2 = __ldg(np + 2); w3 = __ldg(np + 3);
+            }
+            const float ax = fmaf(__uint_as_float(w0.x), idx, -oix);
+            const float ay = fmaf(__uint_as_float(w0.y), idy, -oiy);
+            const float az = fmaf(__uint_as_float(w0.z), idz, -oiz);
+            const float bx = __uint_as_float((w0.w & 0xffu) << 23) * idx;
+            const float by = __uint_as_float(((w0.w >> 8) & 0xffu) << 23) * idy;
+            const float bz = __uint_as_float(((w0.w >> 16) & 0xffu) << 23) * idz;
+            // lo_x lo_y lo_z hi_x | hi_y hi_z ref0 ref1 | ref2 ref3
+            const uint32_t nx = negx ? w1.w : w1.x, fx = negx ? w1.x : w1.w;
+            const uint32_t ny = negy ? w2.x : w1.y, fy = negy ? w1.y : w2.x;
+            const uint32_t nz = negz ? w2.y : w1.z, fz = negz ? w1.z : w2.y;
+            uint32_t key[4];
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                const float tnx = fmaf(byte_to_float(nx, c), bx, ax);
+                const float tny = fmaf(byte_to_float(ny, c), by, ay);
+                const float tnz = fmaf(byte_to_float(nz, c), bz, az);
+                const float tfx = fmaf(byte_to_float(fx, c), bx, ax);
+                const float tfy = fmaf(byte_to_float(fy, c), by, ay);
+                const float tfz = fmaf(byte_to_float(fz, c), bz, az);
+                const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.0f));
+                const float tf = fminf(fminf(tfx, tfy), fminf(tfz, cull));
+                const bool hit = tn <= tf * 1.0000005f;
+                key[c] = hit ? ((__float_as_uint(tn) & ~3u) | (uint32_t)c) : 0xffffffffu;
+            }
+            // sort ascending (5 compare-exchanges)
+#define CSWAP(a, b) { uint32_t lo_ = min(key[a], key[b]), hi_ = max(key[a], key[b]); key[a] = lo_; key[b] = hi_; }
+            CSWAP(0, 1) CSWAP(2, 3) CSWAP(0, 2) CSWAP(1, 3) CSWAP(1, 2)
+#undef CSWAP
+            const uint32_t refs[4] = {w2.z, w2.w, w3.x, w3.y};
+            if (key[0] != 0xffffffffu) {
+#pragma unroll
+                for (int k = 3; k >= 1; k--) {
+                    if (key[k] != 0xffffffffu) {
+                        if (sp >= kStackSize) {
+                            atomicOr(status, kStatusStackOverflow);
+                            return false;
+                        }
+                        stack_ref[sp] = refs[key[k] & 3u];
+                        stack_t[sp] = __uint_as_float(key[k] & ~3u);
+                        sp++;
+                    }
+                }
+                cur = refs[key[0] & 3u];
+                continue;
+            }
+        } else {
+            const uint32_t start = cur & 0x7ffffffu;
+            const uint32_t count = ((cur >> 27) & 15u) + 1u;
+            for (uint32_t k = 0; k < count; k++) {
+                const float4* tp = S.tris + 3 * (size_t)(start + k);
+                const float4 A = __ldg(tp), E1 = __ldg(tp + 1), E2 = __ldg(tp + 2);
+                float t, beta, gamma;
+                // ANY: the reference tests against the ray's own max_t
+                if (!tri_exact(A, E1, E2, o, d, ANY ? tmax0 : best.t, t, beta, gamma)) continue;
+                const int32_t rank = __float_as_int(A.w);
+                if (!ANY && !(t < best.t || rank > best.rank)) continue;  // t == best.t here otherwise
+                const int32_t parent = __float_as_int(E1.w);
+                if (parent >= 0) {
+                    const float4 lo = __ldg(S.ref_box + 2 * parent), hi = __ldg(S.ref_box + 2 * parent + 1);
+                    if (!ref_box_exact(lo, hi, o, d, t)) continue;
+                }
+                if (ANY) {
+                    best.t = t;
+                    best.prim = __float_as_int(E2.w);
+                    return true;
+                }
+                best.t = t;
+                best.rank = rank;
+                best.prim = __float_as_int(E2.w);
+                best.beta = beta;
+                best.gamma = gamma;
+            }
+        }
+        // pop the next node that is still in front of the best hit
+        const float cull2 = best.t * kCullScale + 1e-6f;
+        bool found = false;
+        while (sp > 0) {
+            sp--;
+            if (stack_t[sp] <= cull2) {
+                cur = stack_ref[sp];
+                found = true;
+                break;
+            }
+        }
+        if (!found) break;
+    }
+    return best.prim >= 0;
+}
+
+}  // namespace cpppt_gb300

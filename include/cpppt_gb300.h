@@ -1,0 +1,187 @@
+/*
+ * cpppt_gb300.h -- C ABI of the GB300 path tracer (PT + NEE + MIS and its BVH).
+ *
+ * Drop-in for the reference's path-tracing path (drcd1/cpp-pt):
+ *   - the renderer behind `class Renderer { virtual void render(Scene&,
+ *     std::string) = 0; }` (src/renderer/renderer.h:30-33), selected by the
+ *     settings key `renderer pathtracer_mis` (src/loader/loader.h:280-281) and
+ *     implemented by PathtracerMIS (src/renderer/pathtracerMIS.h:17-168);
+ *   - the geometry queries Primitive::intersect / intersect_any
+ *     (src/primitive/primitive.h:10-15) of its BVH (src/primitive/bvh.h:50-229).
+ *
+ * Conventions: plain pointers and sizes, no C++ types.  Every call returns a
+ * pt_status and never throws; pt_last_error() describes the last failure on
+ * the calling thread.  The caller owns host buffers; the library owns device
+ * buffers.  A pt_scene is not safe for concurrent use from several threads.
+ */
+#ifndef CPPPT_GB300_H
+#define CPPPT_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t pt_status;
+typedef struct pt_scene pt_scene; /* opaque */
+#define PT_OK 0
+#define PT_ERR_INVALID 1   /* bad argument or scene description */
+#define PT_ERR_CUDA 2      /* CUDA runtime error (message in pt_last_error) */
+#define PT_ERR_MEMORY 3    /* device allocation failed */
+#define PT_ERR_LIMIT 4     /* a bounded loop or queue ran out (kernel status word) */
+#define PT_ERR_IO 5        /* scene / settings file could not be read or parsed */
+#define PT_ERR_NO_DEVICE 6 /* no CUDA device of compute capability 10.3 */
+
+/* Material kinds of the reference scene model:
+ *  DIFFUSE   StandardMaterial with metal < 0.1 -> DiffuseBxDF (diffuse_bxdf.h:25-49)
+ *  GGX       StandardMaterial with metal >= 0.1 -> GlossyBxDF(roughness) (glossy_bxdf.h:23-79)
+ *  DIELECTRIC RefractionBxDF(ior) (refraction_bxdf.h:17-61)
+ *  EMISSIVE  EmissiveMaterial rgb * intensity (emissive_material.h:28-34) */
+#define PT_MAT_DIFFUSE 0
+#define PT_MAT_GGX 1
+#define PT_MAT_DIELECTRIC 2
+#define PT_MAT_EMISSIVE 3
+
+typedef struct {
+    int32_t kind;
+    float rgb[3];     /* albedo, or emission colour */
+    float roughness;  /* GGX */
+    float ior;        /* dielectric */
+    float intensity;  /* emissive: radiance = rgb * intensity */
+    float reserved;
+} pt_material;        /* 32 bytes */
+
+/* CameraPerspective(res, tan_fovy, origin, normalize(at - origin), up)
+ * as Loader::parse_camera builds it (loader.h:117-128). */
+typedef struct {
+    float origin[3];
+    float at[3];
+    float up[3];
+    float tan_fovy;
+    int32_t width, height;
+} pt_camera;
+
+/* Flat scene in the reference's insertion order (loader.h:353-367): the
+ * global primitive index of a triangle is its position in `triangles`, and
+ * emissive triangles become lights in that order. */
+typedef struct {
+    int32_t n_vertices;
+    const float* vertices;     /* 3 per vertex */
+    const float* normals;      /* 3 per vertex (the .ptobj normal) */
+    const float* tangents;     /* 3 per vertex (the .ptobj tangent); NULL: any perpendicular */
+    int32_t n_triangles;
+    const int32_t* triangles;  /* 3 vertex indices per triangle */
+    const int32_t* tri_material;
+    int32_t n_materials;
+    const pt_material* materials;
+    pt_camera camera;
+} pt_scene_desc;
+
+/* Ray as the reference's Ray (src/primitive/ray.h:8-20): origin, direction,
+ * max_t; 7 packed floats. */
+typedef struct {
+    float o[3];
+    float d[3];
+    float max_t;
+} pt_ray;
+
+/* Closest hit: prim = insertion index of the triangle BVH::intersect reports
+ * (-1: none); t = the ray's max_t after the query (triangle.h:106);
+ * beta/gamma = barycentrics of the hit (triangle.h:63-74). */
+typedef struct {
+    float t;
+    int32_t prim;
+    float beta, gamma;
+} pt_hit;
+
+/* Integrator modes. */
+#define PT_MODE_MIS 0       /* PathtracerMIS, reference estimator (default) */
+#define PT_MODE_SDTREE 1    /* SD-tree guided (practical path guiding) */
+#define PT_MODE_NN 2        /* learned (MLP, vMF mixture) guiding */
+
+typedef struct {
+    int32_t spp;        /* samples per pixel (the reference settings value `spp N` means N*N) */
+    int32_t max_depth;  /* maximum path segments; reference: 32 (pathtracerMIS.h:36) */
+    int32_t rr_start;   /* Russian roulette from this bounce index; reference: 3 (i > 2, :118) */
+    uint32_t seed;      /* random stream of this render */
+    int32_t mode;       /* PT_MODE_* */
+    int32_t flags;      /* reserved, 0 */
+} pt_render_desc;
+
+/* Counters of the last render on a scene. */
+typedef struct {
+    double paths;            /* camera paths traced */
+    double closest_rays;     /* closest-hit queries (extension rays) */
+    double shadow_rays;      /* any-hit queries (NEE shadow rays) */
+    double render_ms;        /* device time of the render loop (CUDA events) */
+    double trace_closest_ms; /* device time inside the closest-hit kernel */
+    double trace_shadow_ms;  /* device time inside the any-hit kernel */
+    double iterations;       /* wavefront iterations */
+    double kernel_launches;  /* kernels launched by the render */
+} pt_render_stats;
+
+/* Replaces: Loader::load_scene + BVH::add/build (loader.h:314-374,
+ * bvh.h:205-216) for a scene given as flat arrays.  Builds the
+ * reference-topology BVH (for tie-breaks) and the wide traversal BVH, and
+ * uploads the scene to the current CUDA device. */
+pt_status pt_scene_create(const pt_scene_desc* desc, pt_scene** scene);
+
+/* Replaces: Loader::load_render_settings + Loader::load_scene
+ * (loader.h:256-374) -- reads a render-settings file and the .ptscene /
+ * .ptobj / .ptmat files it names.  `settings` receives spp (= N*N for
+ * `spp N`), max_depth 32, rr_start 3.  width/height come from `resolution`. */
+pt_status pt_scene_load(const char* settings_file, pt_scene** scene, pt_render_desc* settings,
+                        char* output_name, int32_t output_name_len);
+
+void pt_scene_destroy(pt_scene* scene);
+
+/* Replaces: BVH::intersect(Ray&, Intersection*) (bvh.h:219-221) on a batch of
+ * rays in host memory.  Same hit and same tie-break as the reference: the
+ * smallest t among the triangles the reference tests; on equal t the one it
+ * visits last. */
+pt_status pt_trace_closest(pt_scene* scene, const pt_ray* rays, int32_t n, pt_hit* hits);
+
+/* Replaces: BVH::intersect_any(Ray&) (bvh.h:222-224) on a host batch;
+ * occluded[i] = 1 when the reference reports a hit. */
+pt_status pt_trace_any(pt_scene* scene, const pt_ray* rays, int32_t n, uint8_t* occluded);
+
+/* Device-pointer variants: rays/hits in device memory, enqueued on `stream`
+ * (a cudaStream_t, NULL for the legacy default stream); asynchronous. */
+pt_status pt_trace_closest_device(pt_scene* scene, const pt_ray* d_rays, int32_t n, pt_hit* d_hits, void* stream);
+pt_status pt_trace_any_device(pt_scene* scene, const pt_ray* d_rays, int32_t n, uint8_t* d_occluded, void* stream);
+
+/* Replaces: PathtracerMIS::render(Scene&, filename) (pathtracerMIS.h:135-167)
+ * without the file writes: renders desc->spp samples per pixel and writes
+ * width*height*3 floats (row-major from the top row, as Image::put_pixel,
+ * rgb_image.h:208-210) to the host buffer rgb_out. */
+pt_status pt_render(pt_scene* scene, const pt_render_desc* desc, float* rgb_out);
+
+/* Device variant: leaves the average in a device buffer of width*height*3
+ * floats; enqueued on the scene's stream and synchronised before return. */
+pt_status pt_render_device(pt_scene* scene, const pt_render_desc* desc, float* d_rgb_out);
+
+pt_status pt_render_stats_get(pt_scene* scene, pt_render_stats* stats);
+
+/* Writes <prefix>.png (sRGB, 8-bit, clipped as pixel_ops::put2char1) and
+ * <prefix>.hdr (Radiance RGBE), as Image::save (rgb_image.h:300-318). */
+pt_status pt_image_save(const char* prefix, const float* rgb, int32_t width, int32_t height);
+
+/* Message of the last failed call on this thread ("" when none). */
+const char* pt_last_error(void);
+
+/* Diagnostic, host only (no CUDA call): the reference BVH topology the
+ * library derives for a triangle list -- BVH::build (bvh.h:151-216) --
+ * as used for the tie-break.  tri_v: 9 floats per triangle (a, b, c).
+ * Outputs: leaf_order[n] (insertion indices in the order BVHNode::intersect
+ * visits leaves), prim_parent[n] (innermost internal node above each
+ * triangle, -1 when the root is a leaf), node_boxes[6 * max_nodes]
+ * (min xyz, max xyz per internal node, pre-order); *n_nodes receives the
+ * internal-node count (PT_ERR_LIMIT when it exceeds max_nodes). */
+pt_status pt_debug_ref_topology(const float* tri_v, int32_t n, int32_t* leaf_order, int32_t* prim_parent,
+                                float* node_boxes, int32_t max_nodes, int32_t* n_nodes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CPPPT_GB300_H */

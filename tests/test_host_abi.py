@@ -1,0 +1,57 @@
+"""Host-only checks of the C ABI library (no CUDA call)."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from tests.golden.make_golden import SMALL_SCENES
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    src = open(os.path.join(ROOT, "include", "cpppt_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(pt_[a-z_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_function():
+    from cpppt import lib
+    L = lib.load()
+    names = header_functions()
+    assert len(names) >= 12
+    for n in names:
+        assert hasattr(L, n), n
+    assert sorted(lib.EXPORTS) == names
+
+
+@pytest.mark.parametrize("name", sorted(SMALL_SCENES))
+def test_product_ref_topology_matches_reference(golden, name):
+    """The library's own rebuild of BVH::build equals the reference's tree."""
+    from cpppt import lib
+    g = golden(f"{name}_ref.npz")
+    order, boxes, pparent = lib.ref_topology(SMALL_SCENES[name]())
+    assert np.array_equal(order, g["leaf_order"])
+    assert np.array_equal(boxes.view(np.uint32), g["node_boxes"].view(np.uint32))
+    assert np.array_equal(pparent, g["prim_parent"])
+
+
+def test_product_ref_topology_large_matches_oracle():
+    from cpppt import lib, scenes
+    from oracle.oracle import Oracle
+    sc = scenes.soup(seed=5, n_spheres=300, freq=4, width=8, height=8)
+    order, boxes, pparent = lib.ref_topology(sc)
+    o_order, o_boxes, _, o_pparent = Oracle("port").scene(sc).bvh_dump()
+    assert np.array_equal(order, o_order)
+    assert np.array_equal(boxes.view(np.uint32), o_boxes.view(np.uint32))
+    assert np.array_equal(pparent, o_pparent)
+
+
+def test_errors_are_status_codes():
+    from cpppt import lib
+    L = lib.load()
+    import ctypes as C
+    nn = C.c_int32()
+    assert L.pt_debug_ref_topology(None, -1, None, None, None, 0, C.byref(nn)) == 1
+    assert b"bad argument" in L.pt_last_error()
