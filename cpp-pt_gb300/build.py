@@ -81,6 +81,16 @@ def build(force: bool = False, verbose: bool = False, extra_cuda: list[str] | No
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    # command-line renderer with the reference's main() interface
+    cli_src = os.path.join(CSRC, "cpppt_render.cpp")
+    cli = os.path.join(HERE, "lib", "cpppt_render")
+    if force or _stale(cli, [cli_src, LIB, os.path.join(CSRC, "gpu_pathtracer.h")]):
+        cxx = os.environ.get("CXX", "g++")
+        cmd = [cxx, "-O2", "-std=c++17", cli_src, "-o", cli, "-L" + os.path.dirname(LIB), "-lcpppt_gb300",
+               "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"CLI build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     return LIB
 
 

@@ -17,9 +17,10 @@ PT_OK = 0
 STATUS_NAMES = {0: "PT_OK", 1: "PT_ERR_INVALID", 2: "PT_ERR_CUDA", 3: "PT_ERR_MEMORY", 4: "PT_ERR_LIMIT",
                 5: "PT_ERR_IO", 6: "PT_ERR_NO_DEVICE"}
 MODE_MIS, MODE_SDTREE, MODE_NN = 0, 1, 2
+FLAG_TIME_KERNELS, FLAG_COUNT = 1, 2
 
 # every function the header declares
-EXPORTS = ["pt_scene_create", "pt_scene_load", "pt_scene_destroy", "pt_trace_closest", "pt_trace_any",
+EXPORTS = ["pt_scene_create", "pt_scene_load", "pt_scene_destroy", "pt_scene_info", "pt_trace_closest", "pt_trace_any",
            "pt_trace_closest_device", "pt_trace_any_device", "pt_render", "pt_render_device",
            "pt_render_stats_get", "pt_image_save", "pt_last_error", "pt_debug_ref_topology"]
 
@@ -48,7 +49,8 @@ class PtRenderDesc(C.Structure):
 
 class PtRenderStats(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("paths", "closest_rays", "shadow_rays", "render_ms", "trace_closest_ms",
-                                           "trace_shadow_ms", "iterations", "kernel_launches")]
+                                           "trace_shadow_ms", "iterations", "kernel_launches", "extend_nodes",
+                                           "extend_tris", "h2d_bytes", "d2h_bytes")]
 
 
 class PtError(RuntimeError):
@@ -73,6 +75,7 @@ def load(path: str = LIB_PATH):
     lib.pt_scene_load.argtypes = [C.c_char_p, C.POINTER(P), C.POINTER(PtRenderDesc), C.c_char_p, C.c_int32]
     lib.pt_scene_destroy.argtypes = [P]
     lib.pt_scene_destroy.restype = None
+    lib.pt_scene_info.argtypes = [P, P, P, P, P]
     lib.pt_trace_closest.argtypes = [P, P, C.c_int32, P]
     lib.pt_trace_any.argtypes = [P, P, C.c_int32, P]
     lib.pt_trace_closest_device.argtypes = [P, P, C.c_int32, P, P]
@@ -114,7 +117,7 @@ class GpuScene:
             _check(lib.pt_scene_load(settings_file.encode(), C.byref(self.h), C.byref(rs), out, 4096))
             self.render_settings = rs
             self.output_name = out.value.decode()
-            self.width = self.height = None
+            self.width, self.height, self.n_triangles, self.n_lights = self.info()
             return
         self.sc = sc
         self._keep = [np.ascontiguousarray(sc.vertices, np.float32), np.ascontiguousarray(sc.normals, np.float32),
@@ -152,6 +155,11 @@ class GpuScene:
             self.close()
         except Exception:
             pass
+
+    def info(self):
+        v = [C.c_int32() for _ in range(4)]
+        _check(_lib.pt_scene_info(self.h, *[C.byref(x) for x in v]))
+        return tuple(x.value for x in v)
 
     # --- ray batches (host buffers) ---
     def trace_closest(self, rays: np.ndarray):

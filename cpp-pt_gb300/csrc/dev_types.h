@@ -56,6 +56,7 @@ struct WaveCounters {
     uint32_t status, pad3, pad4, pad5;
     unsigned long long work_next, work_total;
     unsigned long long stat_closest, stat_shadow, stat_paths, stat_iters;
+    unsigned long long stat_nodes, stat_tris;  // counting build of the extend kernel only
 };
 
 }  // namespace cpppt_gb300

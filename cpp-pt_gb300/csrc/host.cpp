@@ -411,15 +411,10 @@ void render_impl(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
     const int film_n = 3 * s->width * s->height;
     ensure_wave(s, capacity, film_n);
     cudaStream_t st = s->stream;
-    ck(cudaMemsetAsync(s->film32, 0, sizeof(float) * film_n, st), "memset film");
-    ck(cudaMemsetAsync(s->film64, 0, sizeof(double) * film_n, st), "memset film");
-    WaveCounters init{};
-    init.work_total = total;
-    *s->h_ctr = init;
-    ck(cudaMemcpyAsync(s->d_ctr, s->h_ctr, sizeof(WaveCounters), cudaMemcpyHostToDevice, st), "init counters");
-    ck(cudaStreamSynchronize(st), "init");
-    const bool timed = (desc->flags & 1) != 0;
-    if (!timed && (!s->graph || !same_params(s->graph_params, P))) {
+    const bool timed = (desc->flags & PT_FLAG_TIME_KERNELS) != 0;
+    const bool count = (desc->flags & PT_FLAG_COUNT) != 0;
+    const bool direct = timed || count;
+    if (!direct && (!s->graph || !same_params(s->graph_params, P))) {
         if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
         cudaGraph_t g;
         ck(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
@@ -430,6 +425,12 @@ void render_impl(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
         s->graph_params = P;
     }
     ck(cudaEventRecord(s->ev0, st), "event");
+    ck(cudaMemsetAsync(s->film32, 0, sizeof(float) * film_n, st), "memset film");
+    ck(cudaMemsetAsync(s->film64, 0, sizeof(double) * film_n, st), "memset film");
+    WaveCounters init{};
+    init.work_total = total;
+    *s->h_ctr = init;
+    ck(cudaMemcpyAsync(s->d_ctr, s->h_ctr, sizeof(WaveCounters), cudaMemcpyHostToDevice, st), "init counters");
     launch_generate(s->dev, s->pb, 1, P, s->d_ctr, st);  // fills buffer 0
     double launches = 2;
     const unsigned long long max_rounds = 64 + (total / (unsigned long long)capacity + 2) *
@@ -437,19 +438,20 @@ void render_impl(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
     std::vector<cudaEvent_t> tev;
     unsigned long long rounds = 0;
     while (true) {
-        if (timed) {
-            // same work, launched directly with events around the traversal kernels
+        if (direct) {
+            // the graph's work, launched one kernel at a time
             for (int k = 0; k < kItersPerGraph; k++) {
                 const int cur = k & 1;
-                cudaEvent_t e[4];
-                for (int q = 0; q < 4; q++) { ck(cudaEventCreate(&e[q]), "event"); tev.push_back(e[q]); }
-                ck(cudaEventRecord(e[0], st), "event");
-                launch_extend(s->dev, s->pb, cur, s->d_ctr, s->num_sms, st);
-                ck(cudaEventRecord(e[1], st), "event");
+                cudaEvent_t e[4] = {nullptr, nullptr, nullptr, nullptr};
+                if (timed)
+                    for (int q = 0; q < 4; q++) { ck(cudaEventCreate(&e[q]), "event"); tev.push_back(e[q]); }
+                if (timed) ck(cudaEventRecord(e[0], st), "event");
+                launch_extend(s->dev, s->pb, cur, s->d_ctr, s->num_sms, st, count);
+                if (timed) ck(cudaEventRecord(e[1], st), "event");
                 launch_shade(s->dev, s->pb, cur, P, s->d_ctr, s->film32, st);
-                ck(cudaEventRecord(e[2], st), "event");
+                if (timed) ck(cudaEventRecord(e[2], st), "event");
                 launch_shadow(s->dev, s->pb, s->d_ctr, s->film32, s->num_sms, st);
-                ck(cudaEventRecord(e[3], st), "event");
+                if (timed) ck(cudaEventRecord(e[3], st), "event");
                 launch_generate(s->dev, s->pb, cur, P, s->d_ctr, st);
             }
             launch_film_fold(s->film32, s->film64, s->film_n, st);
@@ -478,6 +480,10 @@ void render_impl(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
     R.iterations = (double)s->h_ctr->stat_iters;
     R.render_ms = ms;
     R.kernel_launches = launches + 1;
+    R.extend_nodes = (double)s->h_ctr->stat_nodes;
+    R.extend_tris = (double)s->h_ctr->stat_tris;
+    R.h2d_bytes = (double)sizeof(WaveCounters);
+    R.d2h_bytes = (double)(rounds * sizeof(WaveCounters));
     if (timed) {
         double ext = 0, sh = 0;
         for (size_t q = 0; q + 3 < tev.size(); q += 4) {
@@ -834,6 +840,15 @@ pt_status pt_scene_load(const char* settings_file, pt_scene** out, pt_render_des
 
 void pt_scene_destroy(pt_scene* s) { delete s; }
 
+pt_status pt_scene_info(pt_scene* s, int32_t* width, int32_t* height, int32_t* n_triangles, int32_t* n_lights) {
+    if (!s) { g_error = "null scene"; return PT_ERR_INVALID; }
+    if (width) *width = s->width;
+    if (height) *height = s->height;
+    if (n_triangles) *n_triangles = s->n_tris;
+    if (n_lights) *n_lights = s->dev.n_lights;
+    return PT_OK;
+}
+
 pt_status pt_trace_closest(pt_scene* s, const pt_ray* rays, int32_t n, pt_hit* hits) {
     if (!s) { g_error = "null scene"; return PT_ERR_INVALID; }
     return guarded([&] { trace_host(s, rays, n, hits, false); });
@@ -860,6 +875,7 @@ pt_status pt_render(pt_scene* s, const pt_render_desc* desc, float* rgb_out) {
         render_impl(s, desc, nullptr);
         ck(cudaMemcpyAsync(rgb_out, s->d_out, sizeof(float) * s->film_n, cudaMemcpyDeviceToHost, s->stream), "copy image");
         ck(cudaStreamSynchronize(s->stream), "copy image");
+        s->stats.d2h_bytes += (double)(sizeof(float) * s->film_n);
     });
 }
 

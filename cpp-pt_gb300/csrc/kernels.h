@@ -40,7 +40,8 @@ struct RenderParams {
 // The stages of one wavefront iteration reading path buffer `cur` (writing
 // 1 - cur): extend (closest hit), shade (BSDF, NEE, MIS, RR, compaction),
 // shadow (any hit + film), generate (new camera paths) + advance (counters).
-void launch_extend(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, int num_sms, cudaStream_t st);
+void launch_extend(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, int num_sms, cudaStream_t st,
+                   bool count = false);
 void launch_shade(const DevScene& S, const PathBuffers& B, int cur, const RenderParams& P, WaveCounters* ctr,
                   float* film32, cudaStream_t st);
 void launch_shadow(const DevScene& S, const PathBuffers& B, WaveCounters* ctr, float* film32, int num_sms,

@@ -105,12 +105,14 @@ void launch_trace_any(const DevScene& S, const float* rays, int n, uint8_t* occ,
 // ---------------------------------------------------------------------------
 // Wavefront integrator
 // ---------------------------------------------------------------------------
+template <bool COUNT>
 __global__ void __launch_bounds__(kTraceThreads) k_extend(DevScene S, PathBuffers B, int cur, WaveCounters* ctr) {
     __shared__ uint4 snodes[kSmemNodes * 4];
     stage_top_nodes(S, snodes);
     const int n = ctr->n_cur;
     const float4* __restrict__ O = B.o[cur];
     const float4* __restrict__ D = B.d[cur];
+    TraceCount cnt{0u, 0u};
     while (true) {
         const int base = warp_fetch(&ctr->fetch_ext, n);
         if (base >= n) break;
@@ -118,9 +120,17 @@ __global__ void __launch_bounds__(kTraceThreads) k_extend(DevScene S, PathBuffer
         if (i < n) {
             const float4 o = O[i], d = D[i];
             HitRec h;
-            traverse<false>(S, snodes, make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z),
-                            __int_as_float(0x7f800000), h, &ctr->status);
+            traverse<false, COUNT>(S, snodes, make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z),
+                                   __int_as_float(0x7f800000), h, &ctr->status, &cnt);
             B.hit[i] = make_float4(h.t, __int_as_float(h.prim), h.beta, h.gamma);
+        }
+    }
+    if (COUNT) {
+        const unsigned nodes = __reduce_add_sync(0xffffffffu, cnt.nodes);
+        const unsigned tris = __reduce_add_sync(0xffffffffu, cnt.tris);
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(&ctr->stat_nodes, (unsigned long long)nodes);
+            atomicAdd(&ctr->stat_tris, (unsigned long long)tris);
         }
     }
 }
@@ -318,8 +328,10 @@ __global__ void k_resolve(const double* __restrict__ f64, float* __restrict__ ou
         out[i] = (float)(f64[i] * scale);
 }
 
-void launch_extend(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, int num_sms, cudaStream_t st) {
-    k_extend<<<num_sms * kTraceBlocksPerSM, kTraceThreads, 0, st>>>(S, B, cur, ctr);
+void launch_extend(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, int num_sms, cudaStream_t st,
+                   bool count) {
+    if (count) k_extend<true><<<num_sms * kTraceBlocksPerSM, kTraceThreads, 0, st>>>(S, B, cur, ctr);
+    else k_extend<false><<<num_sms * kTraceBlocksPerSM, kTraceThreads, 0, st>>>(S, B, cur, ctr);
 }
 void launch_shade(const DevScene& S, const PathBuffers& B, int cur, const RenderParams& P, WaveCounters* ctr,
                   float* film32, cudaStream_t st) {

@@ -105,9 +105,15 @@ __device__ __forceinline__ float byte_to_float(uint32_t w, int c) {
 // Traverses the wide BVH.  ANY=false: closest hit into `best` (best.t starts
 // at the ray's max_t).  ANY=true: returns true at the first hit the
 // reference would also report.
-template <bool ANY>
+// COUNT: also tallies visited wide nodes and tested triangles (algorithmic
+// bytes of the roofline; the counting build is never the timed one).
+struct TraceCount {
+    uint32_t nodes, tris;
+};
+
+template <bool ANY, bool COUNT = false>
 __device__ __forceinline__ bool traverse(const DevScene& S, const uint4* __restrict__ snodes, float3 o, float3 d,
-                                         float tmax0, HitRec& best, uint32_t* status) {
+                                         float tmax0, HitRec& best, uint32_t* status, TraceCount* cnt = nullptr) {
     best.t = tmax0;
     best.prim = -1;
     best.rank = -1;
@@ -133,6 +139,7 @@ __device__ __forceinline__ bool traverse(const DevScene& S, const uint4* __restr
         }
         const float cull = best.t * kCullScale + 1e-6f;
         if (!(cur & 0x80000000u)) {
+            if (COUNT) cnt->nodes++;
             uint4 w0, w1, w2, w3;
             if (cur < (uint32_t)kSmemNodes) {
                 w0 = snodes[4 * cur]; w1 = snodes[4 * cur + 1]; w2 = snodes[4 * cur + 2]; w3 = snodes[4 * cur + 3];
@@ -188,6 +195,7 @@ __device__ __forceinline__ bool traverse(const DevScene& S, const uint4* __restr
         } else {
             const uint32_t start = cur & 0x7ffffffu;
             const uint32_t count = ((cur >> 27) & 15u) + 1u;
+            if (COUNT) cnt->tris += count;
             for (uint32_t k = 0; k < count; k++) {
                 const float4* tp = S.tris + 3 * (size_t)(start + k);
                 const float4 A = __ldg(tp), E1 = __ldg(tp + 1), E2 = __ldg(tp + 2);

@@ -119,7 +119,15 @@ typedef struct {
     double trace_shadow_ms;  /* device time inside the any-hit kernel */
     double iterations;       /* wavefront iterations */
     double kernel_launches;  /* kernels launched by the render */
+    double extend_nodes;     /* wide-BVH nodes visited by extension rays (PT_FLAG_COUNT renders) */
+    double extend_tris;      /* triangles tested by extension rays (PT_FLAG_COUNT renders) */
+    double h2d_bytes;        /* host-to-device bytes copied by the call */
+    double d2h_bytes;        /* device-to-host bytes copied by the call */
 } pt_render_stats;
+
+/* pt_render_desc.flags */
+#define PT_FLAG_TIME_KERNELS 1 /* launch iterations directly with CUDA events around the traversal kernels */
+#define PT_FLAG_COUNT 2        /* counting build of the extension kernel (visited nodes / tested triangles) */
 
 /* Replaces: Loader::load_scene + BVH::add/build (loader.h:314-374,
  * bvh.h:205-216) for a scene given as flat arrays.  Builds the
@@ -135,6 +143,9 @@ pt_status pt_scene_load(const char* settings_file, pt_scene** scene, pt_render_d
                         char* output_name, int32_t output_name_len);
 
 void pt_scene_destroy(pt_scene* scene);
+
+/* Image resolution of the scene's camera, its triangle and light counts. */
+pt_status pt_scene_info(pt_scene* scene, int32_t* width, int32_t* height, int32_t* n_triangles, int32_t* n_lights);
 
 /* Replaces: BVH::intersect(Ray&, Intersection*) (bvh.h:219-221) on a batch of
  * rays in host memory.  Same hit and same tie-break as the reference: the

@@ -97,12 +97,28 @@ class Oracle:
                 lib.ref_scene_error.restype = C.c_char_p
                 lib.ref_scene_error.argtypes = [_P]
                 lib.ref_max_threads.restype = C.c_int
+                lib.ref_scene_load.restype = _P
+                lib.ref_scene_load.argtypes = [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                               C.POINTER(C.c_int)]
             Oracle._libs[kind] = lib
         self.lib = Oracle._libs[kind]
         self.p = "or_" if kind == "port" else "ref_"
 
     def scene(self, sc) -> "OracleScene":
         return OracleScene(self, sc)
+
+    def load_files(self, settings_file: str) -> "OracleScene":
+        """The reference's own Loader (loader.h:256-374) on scene files."""
+        assert self.kind == "reference"
+        w, h, spp = C.c_int(), C.c_int(), C.c_int()
+        hnd = self.lib.ref_scene_load(settings_file.encode(), C.byref(w), C.byref(h), C.byref(spp))
+        err = self.lib.ref_scene_error(hnd)
+        s = OracleScene.__new__(OracleScene)
+        s.o, s.sc, s.h, s._keep = self, None, hnd, []
+        s.width, s.height, s.spp_axis = w.value, h.value, spp.value
+        if err:
+            raise RuntimeError("reference loader: " + err.decode())
+        return s
 
 
 class OracleScene:

@@ -1,0 +1,107 @@
+"""Image parity of the GPU PT+NEE+MIS with the reference's PathtracerMIS.
+
+The GPU draws its own (counter-based) random numbers, so parity is
+statistical:
+
+* Cornell box 256x256, 16384 spp, depth 8 against the reference's own
+  16k-spp render (tests/golden/cornell256_16k_ref.npz: 16 replicas x 1024
+  spp): relMSE < 1e-3 with relMSE = mean (x - ref)^2 / (ref^2 + 1e-2), and a
+  per-tile z-test on the means (16x16-pixel tiles, standard errors from the
+  replicas of both sides).
+* Scenes with GGX, dielectric and occluded light against the oracle port
+  (pinned to the reference bit for bit) at small size: per-tile z-test.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from cpppt import scenes
+from tests.golden.make_golden import SMALL_SCENES
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_mse(x, ref):
+    return float(np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2)))
+
+
+def tile_means(imgs, tile):
+    R, H, W, _ = imgs.shape
+    return imgs.reshape(R, H // tile, tile, W // tile, tile, 3).mean(axis=(2, 4))
+
+
+def ztest(tiles_a, tiles_b):
+    """z per tile and channel from replica means (R_a x T x T x 3, R_b x ...)."""
+    ma, mb = tiles_a.mean(0), tiles_b.mean(0)
+    va = tiles_a.var(0, ddof=1) / tiles_a.shape[0]
+    vb = tiles_b.var(0, ddof=1) / tiles_b.shape[0]
+    return (ma - mb) / np.sqrt(va + vb + 1e-20)
+
+
+def check_z(z, max_abs=5.5, frac3=0.02):
+    z = z.reshape(-1)
+    assert np.isfinite(z).all()
+    assert np.abs(z).max() < max_abs, f"max |z| {np.abs(z).max():.2f}"
+    assert (np.abs(z) > 3).mean() <= frac3, f"{(np.abs(z) > 3).mean():.3f} of tiles beyond 3 sigma"
+
+
+def test_cornell_16k_matches_reference(gpu_lib, golden):
+    from cpppt.lib import GpuScene
+    path = os.path.join(os.path.dirname(__file__), "golden", "cornell256_16k_ref.npz")
+    if not os.path.exists(path):
+        pytest.fail("missing golden fixture cornell256_16k_ref.npz")
+    g = golden("cornell256_16k_ref.npz")
+    R = int(g["replicas"])
+    spp = int(g["spp_per_replica"])
+    tile = int(g["tile"])
+    gs = GpuScene(scenes.cornell(256, 256))
+    imgs = np.stack([gs.render(spp, max_depth=int(g["depth"]), seed=77 + r) for r in range(R)])
+    mean = imgs.mean(0)
+    rel = rel_mse(mean, g["mean"])
+    assert rel < 1e-3, f"relMSE {rel:.3e}"
+    check_z(ztest(tile_means(imgs, tile), g["tile_means"]))
+
+
+@pytest.mark.parametrize("name", ["soup", "slitroom", "cornell"])
+def test_small_scenes_match_oracle(gpu_lib, name):
+    from cpppt.lib import GpuScene
+    from oracle.oracle import Oracle
+    sc = SMALL_SCENES[name]()
+    R, tile = 8, 8
+    sc = sc.with_resolution(32, 32) if name == "cornell" else sc.with_resolution(32, 16)
+    ors = Oracle("port").scene(sc)
+    o_imgs = np.stack([ors.render_mis(16, 10, 5000 * (r + 1))[0] for r in range(R)])  # 256 spp each
+    gs = GpuScene(sc)
+    g_imgs = np.stack([gs.render(1024, max_depth=10, seed=300 + r) for r in range(R)])
+    check_z(ztest(tile_means(g_imgs, tile), tile_means(o_imgs, tile)))
+    assert rel_mse(g_imgs.mean(0), o_imgs.mean(0)) < 0.05
+
+
+def test_render_is_deterministic_and_seeded(gpu_lib):
+    from cpppt.lib import GpuScene
+    gs = GpuScene(scenes.cornell(32, 32))
+    a = gs.render(16, max_depth=8, seed=5)
+    b = gs.render(16, max_depth=8, seed=5)
+    c = gs.render(16, max_depth=8, seed=6)
+    assert np.array_equal(a, b)
+    assert not np.array_equal(a, c)
+
+
+def test_render_stats_account_for_every_path(gpu_lib):
+    from cpppt.lib import GpuScene
+    gs = GpuScene(scenes.cornell(48, 40))
+    gs.render(9, max_depth=8, seed=1)
+    st = gs.stats()
+    assert st["paths"] == 48 * 40 * 9
+    assert st["closest_rays"] >= st["paths"]
+    assert st["iterations"] >= 8
+
+
+def test_render_argument_errors(gpu_lib):
+    from cpppt.lib import GpuScene, PtError
+    gs = GpuScene(scenes.cornell(8, 8))
+    with pytest.raises(PtError):
+        gs.render(0)
+    with pytest.raises(PtError):
+        gs.render(4, max_depth=0)
