@@ -50,7 +50,7 @@ class PtRenderDesc(C.Structure):
 class PtRenderStats(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("paths", "closest_rays", "shadow_rays", "render_ms", "trace_closest_ms",
                                            "trace_shadow_ms", "iterations", "kernel_launches", "extend_nodes",
-                                           "extend_tris", "h2d_bytes", "d2h_bytes")]
+                                           "extend_tris", "h2d_bytes", "d2h_bytes", "nonfinite")]
 
 
 class PtError(RuntimeError):

@@ -57,6 +57,7 @@ struct WaveCounters {
     unsigned long long work_next, work_total;
     unsigned long long stat_closest, stat_shadow, stat_paths, stat_iters;
     unsigned long long stat_nodes, stat_tris;  // counting build of the extend kernel only
+    unsigned long long stat_nonfinite;         // contributions dropped because they were inf/NaN
 };
 
 }  // namespace cpppt_gb300

@@ -107,8 +107,7 @@ struct pt_scene {
     // wavefront state
     PathBuffers pb{};
     std::vector<void*> pb_owned;
-    float* film32 = nullptr;
-    double* film64 = nullptr;
+    unsigned long long* film = nullptr;  // 32.32 fixed point
     float* d_out = nullptr;
     int film_n = 0;
     WaveCounters* d_ctr = nullptr;
@@ -123,8 +122,7 @@ struct pt_scene {
         if (graph) cudaGraphExecDestroy(graph);
         for (void* p : owned) cudaFree(p);
         for (void* p : pb_owned) cudaFree(p);
-        if (film32) cudaFree(film32);
-        if (film64) cudaFree(film64);
+        if (film) cudaFree(film);
         if (d_out) cudaFree(d_out);
         if (d_io) cudaFree(d_io);
         if (h_ctr) cudaFreeHost(h_ctr);
@@ -367,12 +365,10 @@ void ensure_wave(pt_scene* s, int capacity, int film_n) {
         if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
     }
     if (s->film_n != film_n) {
-        if (s->film32) cudaFree(s->film32);
-        if (s->film64) cudaFree(s->film64);
+        if (s->film) cudaFree(s->film);
         if (s->d_out) cudaFree(s->d_out);
-        s->film32 = nullptr; s->film64 = nullptr; s->d_out = nullptr;
-        ck(cudaMalloc(&s->film32, sizeof(float) * film_n), "cudaMalloc film");
-        ck(cudaMalloc(&s->film64, sizeof(double) * film_n), "cudaMalloc film");
+        s->film = nullptr; s->d_out = nullptr;
+        ck(cudaMalloc(&s->film, sizeof(unsigned long long) * film_n), "cudaMalloc film");
         ck(cudaMalloc(&s->d_out, sizeof(float) * film_n), "cudaMalloc film");
         s->film_n = film_n;
         if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
@@ -385,11 +381,10 @@ void enqueue_iterations(pt_scene* s, const RenderParams& P, int iters) {
     for (int k = 0; k < iters; k++) {
         const int cur = k & 1;
         launch_extend(s->dev, s->pb, cur, s->d_ctr, s->num_sms, s->stream);
-        launch_shade(s->dev, s->pb, cur, P, s->d_ctr, s->film32, s->stream);
-        launch_shadow(s->dev, s->pb, s->d_ctr, s->film32, s->num_sms, s->stream);
+        launch_shade(s->dev, s->pb, cur, P, s->d_ctr, s->film, s->stream);
+        launch_shadow(s->dev, s->pb, s->d_ctr, s->film, s->num_sms, s->stream);
         launch_generate(s->dev, s->pb, cur, P, s->d_ctr, s->stream);
     }
-    launch_film_fold(s->film32, s->film64, s->film_n, s->stream);
 }
 
 void render_impl(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
@@ -425,8 +420,7 @@ void render_impl(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
         s->graph_params = P;
     }
     ck(cudaEventRecord(s->ev0, st), "event");
-    ck(cudaMemsetAsync(s->film32, 0, sizeof(float) * film_n, st), "memset film");
-    ck(cudaMemsetAsync(s->film64, 0, sizeof(double) * film_n, st), "memset film");
+    ck(cudaMemsetAsync(s->film, 0, sizeof(unsigned long long) * film_n, st), "memset film");
     WaveCounters init{};
     init.work_total = total;
     *s->h_ctr = init;
@@ -448,17 +442,16 @@ void render_impl(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
                 if (timed) ck(cudaEventRecord(e[0], st), "event");
                 launch_extend(s->dev, s->pb, cur, s->d_ctr, s->num_sms, st, count);
                 if (timed) ck(cudaEventRecord(e[1], st), "event");
-                launch_shade(s->dev, s->pb, cur, P, s->d_ctr, s->film32, st);
+                launch_shade(s->dev, s->pb, cur, P, s->d_ctr, s->film, st);
                 if (timed) ck(cudaEventRecord(e[2], st), "event");
-                launch_shadow(s->dev, s->pb, s->d_ctr, s->film32, s->num_sms, st);
+                launch_shadow(s->dev, s->pb, s->d_ctr, s->film, s->num_sms, st);
                 if (timed) ck(cudaEventRecord(e[3], st), "event");
                 launch_generate(s->dev, s->pb, cur, P, s->d_ctr, st);
             }
-            launch_film_fold(s->film32, s->film64, s->film_n, st);
         } else {
             ck(cudaGraphLaunch(s->graph, st), "graph launch");
         }
-        launches += kKernelsPerIteration * kItersPerGraph + 1;
+        launches += kKernelsPerIteration * kItersPerGraph;
         ck(cudaMemcpyAsync(s->h_ctr, s->d_ctr, sizeof(WaveCounters), cudaMemcpyDeviceToHost, st), "read counters");
         ck(cudaStreamSynchronize(st), "render");
         check_status(s, s->h_ctr->status);
@@ -466,7 +459,7 @@ void render_impl(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
         if (s->h_ctr->n_cur == 0 && s->h_ctr->work_next >= s->h_ctr->work_total) break;
         if (rounds > max_rounds) throw Fail(PT_ERR_LIMIT, "render did not converge within the iteration bound");
     }
-    launch_film_resolve(s->film64, d_dst ? d_dst : s->d_out, film_n, 1.0 / (double)desc->spp, st);
+    launch_film_resolve(s->film, d_dst ? d_dst : s->d_out, film_n, 1.0 / (double)desc->spp, st);
     ck(cudaEventRecord(s->ev1, st), "event");
     ck(cudaStreamSynchronize(st), "render");
     ck(cudaGetLastError(), "render kernels");
@@ -482,6 +475,7 @@ void render_impl(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
     R.kernel_launches = launches + 1;
     R.extend_nodes = (double)s->h_ctr->stat_nodes;
     R.extend_tris = (double)s->h_ctr->stat_tris;
+    R.nonfinite = (double)s->h_ctr->stat_nonfinite;
     R.h2d_bytes = (double)sizeof(WaveCounters);
     R.d2h_bytes = (double)(rounds * sizeof(WaveCounters));
     if (timed) {

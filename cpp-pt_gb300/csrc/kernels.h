@@ -43,13 +43,13 @@ struct RenderParams {
 void launch_extend(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, int num_sms, cudaStream_t st,
                    bool count = false);
 void launch_shade(const DevScene& S, const PathBuffers& B, int cur, const RenderParams& P, WaveCounters* ctr,
-                  float* film32, cudaStream_t st);
-void launch_shadow(const DevScene& S, const PathBuffers& B, WaveCounters* ctr, float* film32, int num_sms,
+                  unsigned long long* film, cudaStream_t st);
+void launch_shadow(const DevScene& S, const PathBuffers& B, WaveCounters* ctr, unsigned long long* film, int num_sms,
                    cudaStream_t st);
 void launch_generate(const DevScene& S, const PathBuffers& B, int cur, const RenderParams& P, WaveCounters* ctr,
                      cudaStream_t st);
 constexpr int kKernelsPerIteration = 5;
-void launch_film_fold(float* film32, double* film64, int n, cudaStream_t st);
-void launch_film_resolve(const double* film64, float* out, int n, double scale, cudaStream_t st);
+// film: 32.32 fixed point per pixel and channel; out = film * scale / 2^32
+void launch_film_resolve(const unsigned long long* film, float* out, int n, double scale, cudaStream_t st);
 
 }  // namespace cpppt_gb300

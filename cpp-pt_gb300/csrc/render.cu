@@ -56,18 +56,16 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_closest(DevScene S, con
                                                                  uint32_t* status) {
     __shared__ uint4 snodes[kSmemNodes * 4];
     stage_top_nodes(S, snodes);
-    while (true) {
-        const int base = warp_fetch(counter, n);
-        if (base >= n) break;
-        const int i = base + (threadIdx.x & 31);
-        if (i < n) {
+    TraceCount cnt{0u, 0u};
+    persistent_trace<false, false>(
+        S, snodes, n, counter, status, cnt,
+        [&](int i, float3& o, float3& d, float& tmax) {
             const float* r = rays + 7 * (size_t)i;
-            const float3 o = make_float3(r[0], r[1], r[2]), d = make_float3(r[3], r[4], r[5]);
-            HitRec h;
-            traverse<false>(S, snodes, o, d, r[6], h, status);
-            hits[i] = make_float4(h.t, __int_as_float(h.prim), h.beta, h.gamma);
-        }
-    }
+            o = make_float3(r[0], r[1], r[2]);
+            d = make_float3(r[3], r[4], r[5]);
+            tmax = r[6];
+        },
+        [&](int i, const HitRec& h) { hits[i] = make_float4(h.t, __int_as_float(h.prim), h.beta, h.gamma); });
 }
 
 __global__ void __launch_bounds__(kTraceThreads) k_trace_any(DevScene S, const float* __restrict__ rays, int n,
@@ -75,17 +73,16 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_any(DevScene S, const f
                                                              uint32_t* status) {
     __shared__ uint4 snodes[kSmemNodes * 4];
     stage_top_nodes(S, snodes);
-    while (true) {
-        const int base = warp_fetch(counter, n);
-        if (base >= n) break;
-        const int i = base + (threadIdx.x & 31);
-        if (i < n) {
+    TraceCount cnt{0u, 0u};
+    persistent_trace<true, false>(
+        S, snodes, n, counter, status, cnt,
+        [&](int i, float3& o, float3& d, float& tmax) {
             const float* r = rays + 7 * (size_t)i;
-            const float3 o = make_float3(r[0], r[1], r[2]), d = make_float3(r[3], r[4], r[5]);
-            HitRec h;
-            occ[i] = traverse<true>(S, snodes, o, d, r[6], h, status) ? 1 : 0;
-        }
-    }
+            o = make_float3(r[0], r[1], r[2]);
+            d = make_float3(r[3], r[4], r[5]);
+            tmax = r[6];
+        },
+        [&](int i, const HitRec& h) { occ[i] = h.prim >= 0 ? 1 : 0; });
 }
 
 void launch_trace_closest(const DevScene& S, const float* rays, int n, float4* hits, int* counter, uint32_t* status,
@@ -105,6 +102,22 @@ void launch_trace_any(const DevScene& S, const float* rays, int n, uint8_t* occ,
 // ---------------------------------------------------------------------------
 // Wavefront integrator
 // ---------------------------------------------------------------------------
+// Film: signed 32.32 fixed point, one 64-bit integer per pixel and channel.
+// Integer addition is associative, so a render's image does not depend on
+// the order in which contributions arrive (bit-identical across schedules,
+// batch sizes and launch shapes).  The final division by spp happens in FP64.
+__device__ __forceinline__ void film_add(unsigned long long* film, int pix, float r, float g, float b,
+                                         WaveCounters* ctr) {
+    if (!isfinite(r) || !isfinite(g) || !isfinite(b)) {
+        atomicAdd(&ctr->stat_nonfinite, 1ull);
+        return;
+    }
+    const float s = 4294967296.0f;
+    if (r != 0.f) atomicAdd(film + 3 * pix, (unsigned long long)__float2ll_rn(r * s));
+    if (g != 0.f) atomicAdd(film + 3 * pix + 1, (unsigned long long)__float2ll_rn(g * s));
+    if (b != 0.f) atomicAdd(film + 3 * pix + 2, (unsigned long long)__float2ll_rn(b * s));
+}
+
 template <bool COUNT>
 __global__ void __launch_bounds__(kTraceThreads) k_extend(DevScene S, PathBuffers B, int cur, WaveCounters* ctr) {
     __shared__ uint4 snodes[kSmemNodes * 4];
@@ -112,19 +125,17 @@ __global__ void __launch_bounds__(kTraceThreads) k_extend(DevScene S, PathBuffer
     const int n = ctr->n_cur;
     const float4* __restrict__ O = B.o[cur];
     const float4* __restrict__ D = B.d[cur];
+    float4* __restrict__ Hout = B.hit;
     TraceCount cnt{0u, 0u};
-    while (true) {
-        const int base = warp_fetch(&ctr->fetch_ext, n);
-        if (base >= n) break;
-        const int i = base + (threadIdx.x & 31);
-        if (i < n) {
-            const float4 o = O[i], d = D[i];
-            HitRec h;
-            traverse<false, COUNT>(S, snodes, make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z),
-                                   __int_as_float(0x7f800000), h, &ctr->status, &cnt);
-            B.hit[i] = make_float4(h.t, __int_as_float(h.prim), h.beta, h.gamma);
-        }
-    }
+    persistent_trace<false, COUNT>(
+        S, snodes, n, &ctr->fetch_ext, &ctr->status, cnt,
+        [&](int i, float3& o, float3& d, float& tmax) {
+            const float4 a = O[i], b = D[i];
+            o = make_float3(a.x, a.y, a.z);
+            d = make_float3(b.x, b.y, b.z);
+            tmax = __int_as_float(0x7f800000);
+        },
+        [&](int i, const HitRec& h) { Hout[i] = make_float4(h.t, __int_as_float(h.prim), h.beta, h.gamma); });
     if (COUNT) {
         const unsigned nodes = __reduce_add_sync(0xffffffffu, cnt.nodes);
         const unsigned tris = __reduce_add_sync(0xffffffffu, cnt.tris);
@@ -136,32 +147,29 @@ __global__ void __launch_bounds__(kTraceThreads) k_extend(DevScene S, PathBuffer
 }
 
 __global__ void __launch_bounds__(kTraceThreads) k_shadow(DevScene S, PathBuffers B, WaveCounters* ctr,
-                                                          float* __restrict__ film) {
+                                                          unsigned long long* __restrict__ film) {
     __shared__ uint4 snodes[kSmemNodes * 4];
     stage_top_nodes(S, snodes);
     const int n = ctr->n_shadow;
-    while (true) {
-        const int base = warp_fetch(&ctr->fetch_sh, n);
-        if (base >= n) break;
-        const int i = base + (threadIdx.x & 31);
-        if (i < n) {
-            const float4 o = B.sh_o[i], d = B.sh_d[i];
-            HitRec h;
-            const bool occluded = traverse<true>(S, snodes, make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z),
-                                                 o.w, h, &ctr->status);
-            if (!occluded) {
+    TraceCount cnt{0u, 0u};
+    persistent_trace<true, false>(
+        S, snodes, n, &ctr->fetch_sh, &ctr->status, cnt,
+        [&](int i, float3& o, float3& d, float& tmax) {
+            const float4 a = B.sh_o[i], b = B.sh_d[i];
+            o = make_float3(a.x, a.y, a.z);
+            d = make_float3(b.x, b.y, b.z);
+            tmax = a.w;
+        },
+        [&](int i, const HitRec& h) {
+            if (h.prim < 0) {  // unoccluded: the NEE contribution reaches the film
                 const float4 c = B.sh_c[i];
-                const int pix = __float_as_int(d.w);
-                atomicAdd(film + 3 * pix, c.x);
-                atomicAdd(film + 3 * pix + 1, c.y);
-                atomicAdd(film + 3 * pix + 2, c.z);
+                film_add(film, __float_as_int(B.sh_d[i].w), c.x, c.y, c.z, ctr);
             }
-        }
-    }
+        });
 }
 
 __global__ void __launch_bounds__(256) k_shade(DevScene S, PathBuffers B, int cur, RenderParams P, WaveCounters* ctr,
-                                               float* __restrict__ film) {
+                                               unsigned long long* __restrict__ film) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = ctr->n_cur;
     bool push_sh = false, push_cont = false;
@@ -195,9 +203,7 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, PathBuffers B, int cu
                     const float p_nee = pdf_l * r * r / cos_theta;
                     w = p / (p + p_nee);
                 }
-                atomicAdd(film + 3 * pixel, mul.x * m.r * w);
-                atomicAdd(film + 3 * pixel + 1, mul.y * m.g * w);
-                atomicAdd(film + 3 * pixel + 2, mul.z * m.b * w);
+                film_add(film, pixel, mul.x * m.r * w, mul.y * m.g * w, mul.z * m.b * w, ctr);
             } else {
                 const Rng4 r0 = rng4(P.seed, sample, pixel, bounce, 0);
                 const Rng4 r1 = rng4(P.seed, sample, pixel, bounce, 1);
@@ -313,19 +319,9 @@ __global__ void k_advance(WaveCounters* ctr, int capacity) {
     ctr->stat_iters += 1;
 }
 
-__global__ void k_fold(float* __restrict__ f32, double* __restrict__ f64, int n) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float v = f32[i];
-        if (v != 0.f) {
-            f64[i] += (double)v;
-            f32[i] = 0.f;
-        }
-    }
-}
-
-__global__ void k_resolve(const double* __restrict__ f64, float* __restrict__ out, int n, double scale) {
+__global__ void k_resolve(const unsigned long long* __restrict__ film, float* __restrict__ out, int n, double scale) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        out[i] = (float)(f64[i] * scale);
+        out[i] = (float)((double)(long long)film[i] * scale);
 }
 
 void launch_extend(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, int num_sms, cudaStream_t st,
@@ -334,23 +330,20 @@ void launch_extend(const DevScene& S, const PathBuffers& B, int cur, WaveCounter
     else k_extend<false><<<num_sms * kTraceBlocksPerSM, kTraceThreads, 0, st>>>(S, B, cur, ctr);
 }
 void launch_shade(const DevScene& S, const PathBuffers& B, int cur, const RenderParams& P, WaveCounters* ctr,
-                  float* film32, cudaStream_t st) {
-    k_shade<<<(B.capacity + 255) / 256, 256, 0, st>>>(S, B, cur, P, ctr, film32);
+                  unsigned long long* film, cudaStream_t st) {
+    k_shade<<<(B.capacity + 255) / 256, 256, 0, st>>>(S, B, cur, P, ctr, film);
 }
-void launch_shadow(const DevScene& S, const PathBuffers& B, WaveCounters* ctr, float* film32, int num_sms,
+void launch_shadow(const DevScene& S, const PathBuffers& B, WaveCounters* ctr, unsigned long long* film, int num_sms,
                    cudaStream_t st) {
-    k_shadow<<<num_sms * kTraceBlocksPerSM, kTraceThreads, 0, st>>>(S, B, ctr, film32);
+    k_shadow<<<num_sms * kTraceBlocksPerSM, kTraceThreads, 0, st>>>(S, B, ctr, film);
 }
 void launch_generate(const DevScene& S, const PathBuffers& B, int cur, const RenderParams& P, WaveCounters* ctr,
                      cudaStream_t st) {
     k_generate<<<(B.capacity + 255) / 256, 256, 0, st>>>(S, B, cur, P, ctr);
     k_advance<<<1, 32, 0, st>>>(ctr, B.capacity);
 }
-void launch_film_fold(float* film32, double* film64, int n, cudaStream_t st) {
-    k_fold<<<min((n + 255) / 256, 4096), 256, 0, st>>>(film32, film64, n);
-}
-void launch_film_resolve(const double* film64, float* out, int n, double scale, cudaStream_t st) {
-    k_resolve<<<min((n + 255) / 256, 4096), 256, 0, st>>>(film64, out, n, scale);
+void launch_film_resolve(const unsigned long long* film, float* out, int n, double scale, cudaStream_t st) {
+    k_resolve<<<min((n + 255) / 256, 4096), 256, 0, st>>>(film, out, n, scale * (1.0 / 4294967296.0));
 }
 
 }  // namespace cpppt_gb300

@@ -102,138 +102,224 @@ __device__ __forceinline__ float byte_to_float(uint32_t w, int c) {
     return __uint_as_float(0x4b000000u | ((w >> (8 * c)) & 0xffu)) - 8388608.0f;
 }
 
-// Traverses the wide BVH.  ANY=false: closest hit into `best` (best.t starts
-// at the ray's max_t).  ANY=true: returns true at the first hit the
-// reference would also report.
-// COUNT: also tallies visited wide nodes and tested triangles (algorithmic
-// bytes of the roofline; the counting build is never the timed one).
+// Per-lane traversal state (one ray in flight).  ANY=false: closest hit in
+// `best` (best.t starts at the ray's max_t).  ANY=true: finishes at the first
+// hit the reference would also report.
 struct TraceCount {
-    uint32_t nodes, tris;
+    uint32_t nodes, tris;  // visited wide nodes, tested triangles (counting build only)
 };
 
-template <bool ANY, bool COUNT = false>
-__device__ __forceinline__ bool traverse(const DevScene& S, const uint4* __restrict__ snodes, float3 o, float3 d,
-                                         float tmax0, HitRec& best, uint32_t* status, TraceCount* cnt = nullptr) {
-    best.t = tmax0;
-    best.prim = -1;
-    best.rank = -1;
-    best.beta = best.gamma = 0.f;
-    if (S.n_tris == 0) return false;
-    const float tiny = 7.888609052210118e-31f;  // 2^-100
+constexpr uint32_t kTravDone = 0xffffffffu;  // never a valid node or leaf reference
+
+struct Trav {
+    float3 o, d;
+    float idx, idy, idz, oix, oiy, oiz;
+    float tmax0;
+    uint32_t neg;  // bit k: direction component k is negative
+    uint32_t cur;
+    int sp, steps;
+    HitRec best;
+};
+
+// Traversal stack of one lane: node references and their entry distances.
+struct TravStack {
+    uint32_t ref[kStackSize];
+    float t[kStackSize];
+};
+
+__device__ __forceinline__ void trav_init(Trav& T, const DevScene& S, float3 o, float3 d, float tmax0) {
+    T.o = o;
+    T.d = d;
+    T.tmax0 = tmax0;
+    T.best.t = tmax0;
+    T.best.prim = -1;
+    T.best.rank = -1;
+    T.best.beta = T.best.gamma = 0.f;
+    const float tiny = 7.888609052210118e-31f;  // 2^-100 stands in for a zero component
     const float dx = d.x == 0.f ? copysignf(tiny, d.x) : d.x;
     const float dy = d.y == 0.f ? copysignf(tiny, d.y) : d.y;
     const float dz = d.z == 0.f ? copysignf(tiny, d.z) : d.z;
-    const float idx = 1.0f / dx, idy = 1.0f / dy, idz = 1.0f / dz;
-    const float oix = o.x * idx, oiy = o.y * idy, oiz = o.z * idz;
-    const bool negx = idx < 0.f, negy = idy < 0.f, negz = idz < 0.f;
+    T.idx = 1.0f / dx;
+    T.idy = 1.0f / dy;
+    T.idz = 1.0f / dz;
+    T.oix = o.x * T.idx;
+    T.oiy = o.y * T.idy;
+    T.oiz = o.z * T.idz;
+    T.neg = (T.idx < 0.f ? 1u : 0u) | (T.idy < 0.f ? 2u : 0u) | (T.idz < 0.f ? 4u : 0u);
+    T.cur = S.n_tris > 0 ? 0u : kTravDone;
+    T.sp = 0;
+    T.steps = 0;
+}
 
-    uint32_t stack_ref[kStackSize];
-    float stack_t[kStackSize];
-    int sp = 0;
-    uint32_t cur = 0;  // root
-    int steps = 0;
-    while (true) {
-        if (++steps > kMaxTraversalSteps) {
-            atomicOr(status, kStatusIterLimit);
+// Advances the ray by one wide node or one leaf.  Returns true when the
+// traversal is finished (result in T.best).
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ bool trav_step(Trav& T, TravStack& K, const DevScene& S, const uint4* __restrict__ snodes,
+                                          uint32_t* status, TraceCount& cnt) {
+    if (T.cur == kTravDone) return true;
+    if (++T.steps > kMaxTraversalSteps) {
+        atomicOr(status, kStatusIterLimit);
+        T.cur = kTravDone;
+        return true;
+    }
+    if (!(T.cur & 0x80000000u)) {
+        if (COUNT) cnt.nodes++;
+        const uint32_t cur = T.cur;
+        uint4 w0, w1, w2, w3;
+        if (cur < (uint32_t)kSmemNodes) {
+            w0 = snodes[4 * cur]; w1 = snodes[4 * cur + 1]; w2 = snodes[4 * cur + 2]; w3 = snodes[4 * cur + 3];
+        } else {
+            const uint4* np = S.nodes + 4 * (size_t)cur;
+            w0 = __ldg(np); w1 = __ldg(np + 1); w2 = __ldg(np + 2); w3 = __ldg(np + 3);
+        }
+        const float cull = T.best.t * kCullScale + 1e-6f;
+        const float ax = fmaf(__uint_as_float(w0.x), T.idx, -T.oix);
+        const float ay = fmaf(__uint_as_float(w0.y), T.idy, -T.oiy);
+        const float az = fmaf(__uint_as_float(w0.z), T.idz, -T.oiz);
+        const float bx = __uint_as_float((w0.w & 0xffu) << 23) * T.idx;
+        const float by = __uint_as_float(((w0.w >> 8) & 0xffu) << 23) * T.idy;
+        const float bz = __uint_as_float(((w0.w >> 16) & 0xffu) << 23) * T.idz;
+        // words: lo_x lo_y lo_z hi_x | hi_y hi_z ref0 ref1 | ref2 ref3
+        const bool nxs = T.neg & 1u, nys = T.neg & 2u, nzs = T.neg & 4u;
+        const uint32_t nx = nxs ? w1.w : w1.x, fx = nxs ? w1.x : w1.w;
+        const uint32_t ny = nys ? w2.x : w1.y, fy = nys ? w1.y : w2.x;
+        const uint32_t nz = nzs ? w2.y : w1.z, fz = nzs ? w1.z : w2.y;
+        uint32_t key[4];
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            const float tnx = fmaf(byte_to_float(nx, c), bx, ax);
+            const float tny = fmaf(byte_to_float(ny, c), by, ay);
+            const float tnz = fmaf(byte_to_float(nz, c), bz, az);
+            const float tfx = fmaf(byte_to_float(fx, c), bx, ax);
+            const float tfy = fmaf(byte_to_float(fy, c), by, ay);
+            const float tfz = fmaf(byte_to_float(fz, c), bz, az);
+            const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.0f));
+            const float tf = fminf(fminf(tfx, tfy), fminf(tfz, cull));
+            const bool hit = tn <= tf * 1.0000005f;
+            key[c] = hit ? ((__float_as_uint(tn) & ~3u) | (uint32_t)c) : 0xffffffffu;
+        }
+#define CSWAP(a, b) { uint32_t lo_ = min(key[a], key[b]), hi_ = max(key[a], key[b]); key[a] = lo_; key[b] = hi_; }
+        CSWAP(0, 1) CSWAP(2, 3) CSWAP(0, 2) CSWAP(1, 3) CSWAP(1, 2)
+#undef CSWAP
+        if (key[0] != 0xffffffffu) {
+            const uint32_t refs[4] = {w2.z, w2.w, w3.x, w3.y};
+#pragma unroll
+            for (int k = 3; k >= 1; k--) {
+                if (key[k] != 0xffffffffu) {
+                    if (T.sp >= kStackSize) {
+                        atomicOr(status, kStatusStackOverflow);
+                        T.cur = kTravDone;
+                        return true;
+                    }
+                    K.ref[T.sp] = refs[key[k] & 3u];
+                    K.t[T.sp] = __uint_as_float(key[k] & ~3u);
+                    T.sp++;
+                }
+            }
+            T.cur = refs[key[0] & 3u];
             return false;
         }
-        const float cull = best.t * kCullScale + 1e-6f;
-        if (!(cur & 0x80000000u)) {
-            if (COUNT) cnt->nodes++;
-            uint4 w0, w1, w2, w3;
-            if (cur < (uint32_t)kSmemNodes) {
-                w0 = snodes[4 * cur]; w1 = snodes[4 * cur + 1]; w2 = snodes[4 * cur + 2]; w3 = snodes[4 * cur + 3];
-            } else {
-                const uint4* np = S.nodes + 4 * (size_t)cur;
-                w0 = __ldg(np); w1 = __ldg(np + 1); w2 = __ldg(np + 2); w3 = __ldg(np + 3);
+    } else {
+        const uint32_t start = T.cur & 0x7ffffffu;
+        const uint32_t count = ((T.cur >> 27) & 15u) + 1u;
+        if (COUNT) cnt.tris += count;
+        for (uint32_t k = 0; k < count; k++) {
+            const float4* tp = S.tris + 3 * (size_t)(start + k);
+            const float4 A = __ldg(tp), E1 = __ldg(tp + 1), E2 = __ldg(tp + 2);
+            float t, beta, gamma;
+            // ANY: the reference tests against the ray's own max_t
+            if (!tri_exact(A, E1, E2, T.o, T.d, ANY ? T.tmax0 : T.best.t, t, beta, gamma)) continue;
+            const int32_t rank = __float_as_int(A.w);
+            if (!ANY && !(t < T.best.t || rank > T.best.rank)) continue;  // equal t: the later-visited wins
+            const int32_t parent = __float_as_int(E1.w);
+            if (parent >= 0) {
+                const float4 lo = __ldg(S.ref_box + 2 * parent), hi = __ldg(S.ref_box + 2 * parent + 1);
+                if (!ref_box_exact(lo, hi, T.o, T.d, t)) continue;
             }
-            const float ax = fmaf(__uint_as_float(w0.x), idx, -oix);
-            const float ay = fmaf(__uint_as_float(w0.y), idy, -oiy);
-            const float az = fmaf(__uint_as_float(w0.z), idz, -oiz);
-            const float bx = __uint_as_float((w0.w & 0xffu) << 23) * idx;
-            const float by = __uint_as_float(((w0.w >> 8) & 0xffu) << 23) * idy;
-            const float bz = __uint_as_float(((w0.w >> 16) & 0xffu) << 23) * idz;
-            // lo_x lo_y lo_z hi_x | hi_y hi_z ref0 ref1 | ref2 ref3
-            const uint32_t nx = negx ? w1.w : w1.x, fx = negx ? w1.x : w1.w;
-            const uint32_t ny = negy ? w2.x : w1.y, fy = negy ? w1.y : w2.x;
-            const uint32_t nz = negz ? w2.y : w1.z, fz = negz ? w1.z : w2.y;
-            uint32_t key[4];
-#pragma unroll
-            for (int c = 0; c < 4; c++) {
-                const float tnx = fmaf(byte_to_float(nx, c), bx, ax);
-                const float tny = fmaf(byte_to_float(ny, c), by, ay);
-                const float tnz = fmaf(byte_to_float(nz, c), bz, az);
-                const float tfx = fmaf(byte_to_float(fx, c), bx, ax);
-                const float tfy = fmaf(byte_to_float(fy, c), by, ay);
-                const float tfz = fmaf(byte_to_float(fz, c), bz, az);
-                const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.0f));
-                const float tf = fminf(fminf(tfx, tfy), fminf(tfz, cull));
-                const bool hit = tn <= tf * 1.0000005f;
-                key[c] = hit ? ((__float_as_uint(tn) & ~3u) | (uint32_t)c) : 0xffffffffu;
-            }
-            // sort ascending (5 compare-exchanges)
-#define CSWAP(a, b) { uint32_t lo_ = min(key[a], key[b]), hi_ = max(key[a], key[b]); key[a] = lo_; key[b] = hi_; }
-            CSWAP(0, 1) CSWAP(2, 3) CSWAP(0, 2) CSWAP(1, 3) CSWAP(1, 2)
-#undef CSWAP
-            const uint32_t refs[4] = {w2.z, w2.w, w3.x, w3.y};
-            if (key[0] != 0xffffffffu) {
-#pragma unroll
-                for (int k = 3; k >= 1; k--) {
-                    if (key[k] != 0xffffffffu) {
-                        if (sp >= kStackSize) {
-                            atomicOr(status, kStatusStackOverflow);
-                            return false;
-                        }
-                        stack_ref[sp] = refs[key[k] & 3u];
-                        stack_t[sp] = __uint_as_float(key[k] & ~3u);
-                        sp++;
-                    }
-                }
-                cur = refs[key[0] & 3u];
-                continue;
-            }
-        } else {
-            const uint32_t start = cur & 0x7ffffffu;
-            const uint32_t count = ((cur >> 27) & 15u) + 1u;
-            if (COUNT) cnt->tris += count;
-            for (uint32_t k = 0; k < count; k++) {
-                const float4* tp = S.tris + 3 * (size_t)(start + k);
-                const float4 A = __ldg(tp), E1 = __ldg(tp + 1), E2 = __ldg(tp + 2);
-                float t, beta, gamma;
-                // ANY: the reference tests against the ray's own max_t
-                if (!tri_exact(A, E1, E2, o, d, ANY ? tmax0 : best.t, t, beta, gamma)) continue;
-                const int32_t rank = __float_as_int(A.w);
-                if (!ANY && !(t < best.t || rank > best.rank)) continue;  // t == best.t here otherwise
-                const int32_t parent = __float_as_int(E1.w);
-                if (parent >= 0) {
-                    const float4 lo = __ldg(S.ref_box + 2 * parent), hi = __ldg(S.ref_box + 2 * parent + 1);
-                    if (!ref_box_exact(lo, hi, o, d, t)) continue;
-                }
-                if (ANY) {
-                    best.t = t;
-                    best.prim = __float_as_int(E2.w);
-                    return true;
-                }
-                best.t = t;
-                best.rank = rank;
-                best.prim = __float_as_int(E2.w);
-                best.beta = beta;
-                best.gamma = gamma;
+            T.best.t = t;
+            T.best.rank = rank;
+            T.best.prim = __float_as_int(E2.w);
+            T.best.beta = beta;
+            T.best.gamma = gamma;
+            if (ANY) {
+                T.cur = kTravDone;
+                return true;
             }
         }
-        // pop the next node that is still in front of the best hit
-        const float cull2 = best.t * kCullScale + 1e-6f;
-        bool found = false;
-        while (sp > 0) {
-            sp--;
-            if (stack_t[sp] <= cull2) {
-                cur = stack_ref[sp];
-                found = true;
-                break;
-            }
-        }
-        if (!found) break;
     }
+    // pop the next node that is still in front of the best hit
+    const float cull2 = T.best.t * kCullScale + 1e-6f;
+    while (T.sp > 0) {
+        T.sp--;
+        if (K.t[T.sp] <= cull2) {
+            T.cur = K.ref[T.sp];
+            return false;
+        }
+    }
+    T.cur = kTravDone;
+    return true;
+}
+
+// Persistent ray loop.  Each warp takes chunks of kChunk consecutive rays
+// from a global counter into a warp-private range; a lane whose ray finishes
+// takes the next ray of the range at once (no waiting for the other lanes),
+// and the warp runs one traversal step per iteration.
+constexpr int kChunk = 64;
+
+template <bool ANY, bool COUNT, class Load, class Store>
+__device__ __forceinline__ void persistent_trace(const DevScene& S, const uint4* __restrict__ snodes, int n,
+                                                 int* counter, uint32_t* status, TraceCount& cnt, Load load,
+                                                 Store store) {
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    Trav T;
+    TravStack K;
+    int ray = -1;
+    int pool_next = 0, pool_end = 0;  // warp-uniform
+    bool exhausted = false;
+    while (true) {
+        const unsigned idle = __ballot_sync(0xffffffffu, ray < 0);
+        if (idle) {
+            if (pool_next >= pool_end && !exhausted) {
+                int base = 0;
+                if (lane == 0) base = atomicAdd(counter, kChunk);
+                base = __shfl_sync(0xffffffffu, base, 0);
+                pool_next = base;
+                pool_end = min(base + kChunk, n);
+                if (base + kChunk >= n) exhausted = true;
+            }
+            const int avail = max(0, pool_end - pool_next);
+            if (avail > 0) {
+                const int r = __popc(idle & lt_mask);
+                if (ray < 0 && r < avail) {
+                    ray = pool_next + r;
+                    float3 o, d;
+                    float tmax;
+                    load(ray, o, d, tmax);
+                    trav_init(T, S, o, d, tmax);
+                }
+                pool_next += min(avail, __popc(idle));
+            }
+        }
+        if (__ballot_sync(0xffffffffu, ray >= 0) == 0) break;
+        if (ray >= 0 && trav_step<ANY, COUNT>(T, K, S, snodes, status, cnt)) {
+            store(ray, T.best);
+            ray = -1;
+        }
+    }
+}
+
+// One ray, start to finish (used where rays are not batched).
+template <bool ANY>
+__device__ __forceinline__ bool traverse(const DevScene& S, const uint4* __restrict__ snodes, float3 o, float3 d,
+                                         float tmax0, HitRec& best, uint32_t* status) {
+    Trav T;
+    TravStack K;
+    TraceCount cnt{0u, 0u};
+    trav_init(T, S, o, d, tmax0);
+    while (!trav_step<ANY, false>(T, K, S, snodes, status, cnt)) {
+    }
+    best = T.best;
     return best.prim >= 0;
 }
 

@@ -123,6 +123,7 @@ typedef struct {
     double extend_tris;      /* triangles tested by extension rays (PT_FLAG_COUNT renders) */
     double h2d_bytes;        /* host-to-device bytes copied by the call */
     double d2h_bytes;        /* device-to-host bytes copied by the call */
+    double nonfinite;        /* contributions dropped because they were inf or NaN */
 } pt_render_stats;
 
 /* pt_render_desc.flags */
