@@ -121,8 +121,9 @@ __device__ __forceinline__ void film_add(unsigned long long* film, int pix, floa
 template <bool COUNT>
 __global__ void __launch_bounds__(kTraceThreads) k_extend(DevScene S, PathBuffers B, int cur, WaveCounters* ctr) {
     __shared__ uint4 snodes[kSmemNodes * 4];
-    stage_top_nodes(S, snodes);
     const int n = ctr->n_cur;
+    if (n == 0) return;  // drained wavefront: skip staging
+    stage_top_nodes(S, snodes);
     const float4* __restrict__ O = B.o[cur];
     const float4* __restrict__ D = B.d[cur];
     float4* __restrict__ Hout = B.hit;
@@ -149,8 +150,9 @@ __global__ void __launch_bounds__(kTraceThreads) k_extend(DevScene S, PathBuffer
 __global__ void __launch_bounds__(kTraceThreads) k_shadow(DevScene S, PathBuffers B, WaveCounters* ctr,
                                                           unsigned long long* __restrict__ film) {
     __shared__ uint4 snodes[kSmemNodes * 4];
-    stage_top_nodes(S, snodes);
     const int n = ctr->n_shadow;
+    if (n == 0) return;
+    stage_top_nodes(S, snodes);
     TraceCount cnt{0u, 0u};
     persistent_trace<true, false>(
         S, snodes, n, &ctr->fetch_sh, &ctr->status, cnt,
