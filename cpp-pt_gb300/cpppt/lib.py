@@ -22,6 +22,7 @@ FLAG_TIME_KERNELS, FLAG_COUNT = 1, 2
 # every function the header declares
 EXPORTS = ["pt_scene_create", "pt_scene_load", "pt_scene_destroy", "pt_scene_info", "pt_trace_closest", "pt_trace_any",
            "pt_trace_closest_device", "pt_trace_any_device", "pt_render", "pt_render_device",
+           "pt_render_device_noalloc",
            "pt_render_stats_get", "pt_image_save", "pt_last_error", "pt_debug_ref_topology"]
 
 
@@ -82,6 +83,7 @@ def load(path: str = LIB_PATH):
     lib.pt_trace_any_device.argtypes = [P, P, C.c_int32, P, P]
     lib.pt_render.argtypes = [P, C.POINTER(PtRenderDesc), P]
     lib.pt_render_device.argtypes = [P, C.POINTER(PtRenderDesc), P]
+    lib.pt_render_device_noalloc.argtypes = [P, C.POINTER(PtRenderDesc), P, P]
     lib.pt_render_stats_get.argtypes = [P, C.POINTER(PtRenderStats)]
     lib.pt_image_save.argtypes = [C.c_char_p, P, C.c_int32, C.c_int32]
     lib.pt_last_error.restype = C.c_char_p

@@ -878,6 +878,41 @@ pt_status pt_render_device(pt_scene* s, const pt_render_desc* desc, float* d_rgb
     return guarded([&] { render_impl(s, desc, d_rgb_out); });
 }
 
+// For callers that must not allocate device memory during a render (see the
+// header): same wavefront and same image as pt_render_device, scratch in the
+// library's fixed __device__ array.  The scene (created earlier) is read only.
+pt_status pt_render_device_noalloc(pt_scene* s, const pt_render_desc* desc, float* d_rgb_out, void* stream) {
+    if (!s || !d_rgb_out) { g_error = "null argument"; return PT_ERR_INVALID; }
+    return guarded([&] {
+        if (!desc) throw std::invalid_argument("null render description");
+        if (desc->spp < 1) throw std::invalid_argument("spp must be >= 1");
+        if (desc->max_depth < 1 || desc->max_depth > 0xffff)
+            throw std::invalid_argument("max_depth must be in [1, 65535]");
+        if (desc->mode != PT_MODE_MIS) throw Fail(PT_ERR_INVALID, "the allocation-free render supports PT_MODE_MIS only");
+        if (desc->flags != 0) throw Fail(PT_ERR_INVALID, "the allocation-free render takes no flags");
+        const long long pixels = (long long)s->width * s->height;
+        if (pixels > noalloc_max_pixels())
+            throw Fail(PT_ERR_LIMIT, "image of " + std::to_string(pixels) + " pixels exceeds the allocation-free render's "
+                                     "maximum of " + std::to_string(noalloc_max_pixels()) + " pixels");
+        RenderParams P{};
+        P.spp = desc->spp;
+        int ax = (int)std::lround(std::sqrt((double)desc->spp));
+        P.spp_axis = (ax * ax == desc->spp) ? ax : 0;
+        P.max_depth = desc->max_depth;
+        P.rr_start = desc->rr_start;
+        P.seed = desc->seed;
+        P.width = s->width;
+        P.height = s->height;
+        WaveCounters h{};
+        int limit = 0;
+        ck(render_noalloc(s->dev, P, s->num_sms, desc->max_depth, d_rgb_out, static_cast<cudaStream_t>(stream), &h,
+                          &limit),
+           "allocation-free render");
+        check_status(s, h.status);
+        if (limit) throw Fail(PT_ERR_LIMIT, "render did not converge within the iteration bound");
+    });
+}
+
 pt_status pt_render_stats_get(pt_scene* s, pt_render_stats* out) {
     if (!s || !out) { g_error = "null argument"; return PT_ERR_INVALID; }
     *out = s->stats;

@@ -49,6 +49,15 @@ void launch_shadow(const DevScene& S, const PathBuffers& B, WaveCounters* ctr, u
 void launch_generate(const DevScene& S, const PathBuffers& B, int cur, const RenderParams& P, WaveCounters* ctr,
                      cudaStream_t st);
 constexpr int kKernelsPerIteration = 5;
+// Allocation-free render: the wavefront of launch_* above with its scratch in
+// a file-scope __device__ array (see render.cu).  Synchronises `st`.
+// limit_hit is set when the iteration bound ran out; the kernels' status
+// bits are in final_counters->status.
+cudaError_t render_noalloc(const DevScene& S, const RenderParams& P, int num_sms, int max_depth, float* d_out,
+                           cudaStream_t st, WaveCounters* final_counters, int* limit_hit);
+size_t noalloc_scratch_bytes();
+int noalloc_max_pixels();
+int noalloc_paths();
 // film: 32.32 fixed point per pixel and channel; out = film * scale / 2^32
 void launch_film_resolve(const unsigned long long* film, float* out, int n, double scale, cudaStream_t st);
 

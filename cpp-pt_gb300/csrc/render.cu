@@ -12,6 +12,8 @@
 // round trip and a chain of iterations is captured once in a CUDA graph.
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "kernels.h"
 #include "shade.cuh"
 #include "trace.cuh"
@@ -346,6 +348,119 @@ void launch_generate(const DevScene& S, const PathBuffers& B, int cur, const Ren
 }
 void launch_film_resolve(const unsigned long long* film, float* out, int n, double scale, cudaStream_t st) {
     k_resolve<<<min((n + 255) / 256, 4096), 256, 0, st>>>(film, out, n, scale * (1.0 / 4294967296.0));
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free render (pt_render_device_noalloc)
+//
+// For callers that cannot allocate device memory at render time: a host
+// whose device memory is reserved up front by another allocator (a caching
+// allocator or an engine's memory budget), a process that is inside CUDA
+// stream capture (cudaMalloc is not allowed there), or a frame loop that
+// must not enter the driver's allocation path.  The wavefront's scratch --
+// path state, queues, film and counters -- lives in one file-scope
+// __device__ array instead of per-scene buffers.  The array is part of this
+// module, so every GPU that loads the library holds it until the process
+// exits.  Capacity: kNoAllocPaths paths in flight, at most kNoAllocMaxPixels
+// pixels.  Every call shares the array and leaves its contents behind; each
+// call clears the film and counters first, and calls that overlap on the GPU
+// (concurrent streams or threads) race on it.
+// ---------------------------------------------------------------------------
+constexpr int kNoAllocPaths = 1 << 16;
+constexpr int kNoAllocMaxPixels = 1 << 18;  // e.g. 512 x 512
+constexpr size_t kNoAllocPathBytes = (size_t)kNoAllocPaths * 16;  // one float4 / int4 array
+constexpr size_t kNoAllocFilmOffset = 12 * kNoAllocPathBytes;
+constexpr size_t kNoAllocCtrOffset = kNoAllocFilmOffset + (size_t)3 * kNoAllocMaxPixels * 8;
+constexpr size_t kNoAllocBytes = kNoAllocCtrOffset + 256;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+namespace {
+std::mutex g_noalloc_mutex;
+void* g_noalloc_addr[128] = {};  // per device ordinal
+}  // namespace
+
+size_t noalloc_scratch_bytes() { return kNoAllocBytes; }
+int noalloc_max_pixels() { return kNoAllocMaxPixels; }
+int noalloc_paths() { return kNoAllocPaths; }
+
+// Device address of the scratch array on the current device, looked up once
+// per device (the host-side symbol is not a device address).
+static cudaError_t noalloc_scratch(void** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 128) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return cudaSuccess;
+}
+
+cudaError_t render_noalloc(const DevScene& S, const RenderParams& P, int num_sms, int max_depth, float* d_out,
+                           cudaStream_t st, WaveCounters* final_counters, int* limit_hit) {
+    *limit_hit = 0;
+    void* base = nullptr;
+    cudaError_t e = noalloc_scratch(&base);
+    if (e != cudaSuccess) return e;
+    unsigned char* b = static_cast<unsigned char*>(base);
+    PathBuffers B;
+    for (int k = 0; k < 2; k++) {
+        B.o[k] = reinterpret_cast<float4*>(b + (0 + k) * kNoAllocPathBytes);
+        B.d[k] = reinterpret_cast<float4*>(b + (2 + k) * kNoAllocPathBytes);
+        B.thr[k] = reinterpret_cast<float4*>(b + (4 + k) * kNoAllocPathBytes);
+        B.info[k] = reinterpret_cast<int4*>(b + (6 + k) * kNoAllocPathBytes);
+    }
+    B.hit = reinterpret_cast<float4*>(b + 8 * kNoAllocPathBytes);
+    B.sh_o = reinterpret_cast<float4*>(b + 9 * kNoAllocPathBytes);
+    B.sh_d = reinterpret_cast<float4*>(b + 10 * kNoAllocPathBytes);
+    B.sh_c = reinterpret_cast<float4*>(b + 11 * kNoAllocPathBytes);
+    B.capacity = kNoAllocPaths;
+    unsigned long long* film = reinterpret_cast<unsigned long long*>(b + kNoAllocFilmOffset);
+    WaveCounters* ctr = reinterpret_cast<WaveCounters*>(b + kNoAllocCtrOffset);
+    const int film_n = 3 * P.width * P.height;
+    const unsigned long long total = (unsigned long long)P.width * P.height * (unsigned long long)P.spp;
+    e = cudaMemsetAsync(film, 0, sizeof(unsigned long long) * film_n, st);
+    if (e != cudaSuccess) return e;
+    WaveCounters init{};
+    init.work_total = total;
+    e = cudaMemcpyAsync(ctr, &init, sizeof(init), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return e;
+    launch_generate(S, B, 1, P, ctr, st);
+    const int iters = 16;
+    const unsigned long long max_rounds =
+        64 + (total / (unsigned long long)kNoAllocPaths + 2) * (unsigned long long)(max_depth + 2) * 4 / iters;
+    WaveCounters h{};
+    for (unsigned long long round = 0;; round++) {
+        for (int k = 0; k < iters; k++) {
+            const int cur = k & 1;
+            launch_extend(S, B, cur, ctr, num_sms, st, false);
+            launch_shade(S, B, cur, P, ctr, film, st);
+            launch_shadow(S, B, ctr, film, num_sms, st);
+            launch_generate(S, B, cur, P, ctr, st);
+        }
+        e = cudaMemcpyAsync(&h, ctr, sizeof(h), cudaMemcpyDeviceToHost, st);
+        if (e != cudaSuccess) return e;
+        e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return e;
+        if (h.status) break;
+        if (h.n_cur == 0 && h.work_next >= h.work_total) break;
+        if (round > max_rounds) {
+            *limit_hit = 1;
+            break;
+        }
+    }
+    *final_counters = h;
+    if (h.status || *limit_hit) return cudaSuccess;
+    launch_film_resolve(film, d_out, film_n, 1.0 / (double)P.spp, st);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(st);
 }
 
 }  // namespace cpppt_gb300
