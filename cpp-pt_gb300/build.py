@@ -3,11 +3,14 @@
     python cpp-pt_gb300/build.py            # incremental
     python cpp-pt_gb300/build.py --force
 
-Three translation units compiled in parallel for sm_103a only:
-  csrc/render.cu  -- all CUDA kernels (nvcc -gencode arch=compute_103a,code=sm_103a)
-  csrc/host.cpp   -- C ABI, render driver, loader, image output
-  csrc/bvh.cpp    -- BVH builders (-ffp-contract=off: the reference-topology
-                     build must round like the reference)
+Translation units, compiled in parallel, CUDA for sm_103a only:
+  csrc/render.cu  -- traversal and PT+NEE+MIS wavefront kernels (nvcc -gencode arch=compute_103a,code=sm_103a)
+  csrc/guide.cu   -- SD-tree guided (PPG) wavefront kernels
+  csrc/host.cpp   -- C ABI, render drivers, loader, image output
+  csrc/bvh.cpp    -- BVH builders
+  csrc/sdtree.cpp -- SD-tree structure and update
+Host files use -ffp-contract=off: the reference-topology BVH and the SD-tree
+update must round like the reference.
 """
 from __future__ import annotations
 
@@ -47,7 +50,7 @@ def _commands(extra_cuda: list[str] | None = None):
     nvcc = _nvcc()
     common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
     jobs = []
-    for name in ("render.cu", "host.cpp", "bvh.cpp"):
+    for name in ("render.cu", "guide.cu", "host.cpp", "bvh.cpp", "sdtree.cpp"):
         src = os.path.join(CSRC, name)
         out = os.path.join(OBJ, name + ".o")
         cmd = [nvcc, "-c", src, "-o", out] + common
@@ -73,7 +76,7 @@ def build(force: bool = False, verbose: bool = False, extra_cuda: list[str] | No
             print(r.stdout, r.stderr, file=sys.stderr)
         return o
 
-    with cf.ThreadPoolExecutor(max_workers=3) as ex:
+    with cf.ThreadPoolExecutor(max_workers=5) as ex:
         list(ex.map(run, todo))
     objs = [o for _, o, _ in jobs]
     if force or todo or _stale(LIB, objs):

@@ -23,7 +23,8 @@ FLAG_TIME_KERNELS, FLAG_COUNT = 1, 2
 EXPORTS = ["pt_scene_create", "pt_scene_load", "pt_scene_destroy", "pt_scene_info", "pt_trace_closest", "pt_trace_any",
            "pt_trace_closest_device", "pt_trace_any_device", "pt_render", "pt_render_device",
            "pt_render_device_noalloc",
-           "pt_render_stats_get", "pt_image_save", "pt_last_error", "pt_debug_ref_topology"]
+           "pt_render_stats_get", "pt_image_save", "pt_last_error", "pt_debug_ref_topology",
+           "pt_debug_sdtree_run"]
 
 
 class PtMaterial(C.Structure):
@@ -89,6 +90,7 @@ def load(path: str = LIB_PATH):
     lib.pt_last_error.restype = C.c_char_p
     lib.pt_last_error.argtypes = []
     lib.pt_debug_ref_topology.argtypes = [P, C.c_int32, P, P, P, C.c_int32, P]
+    lib.pt_debug_sdtree_run.argtypes = [P, P, C.c_int32, P, P, C.c_int32, P, P, P, P, C.c_int32, P, P, P]
     for name in EXPORTS:
         getattr(lib, name).restype = C.c_int32 if name not in ("pt_scene_destroy", "pt_last_error") else \
             getattr(lib, name).restype
@@ -228,3 +230,35 @@ def ref_topology(sc):
     nn = C.c_int32()
     _check(lib.pt_debug_ref_topology(_ptr(tv), n, _ptr(order), _ptr(pparent), _ptr(boxes), cap, C.byref(nn)))
     return order, boxes[:6 * nn.value].reshape(-1, 6), pparent
+
+
+def sdtree_run(lo, hi, rounds, queries, max_leaves=1 << 20, fn=None, lib=None):
+    """Runs an SD-tree through rounds of splats + update (host only).
+    rounds: list of (n,7) arrays {radiance, pos, dir}.  Returns dict with the
+    sampling leaves, per-spatial-leaf leaf counts, splat counts, flux and the
+    pdf of each query (n,6).  `fn` selects another implementation with the
+    same signature (e.g. the reference harness)."""
+    L = lib or load()
+    f = fn or L.pt_debug_sdtree_run
+    lo = np.ascontiguousarray(lo, np.float32)
+    hi = np.ascontiguousarray(hi, np.float32)
+    ns = np.array([len(r) for r in rounds], np.int32)
+    sp = np.ascontiguousarray(np.concatenate(rounds) if rounds else np.zeros((0, 7)), np.float32)
+    q = np.ascontiguousarray(queries, np.float32)
+    leaves = np.zeros(4 * max_leaves, np.float32)
+    cap = 1 << 16
+    lc = np.zeros(cap, np.int32)
+    cnt = np.zeros(cap, np.int32)
+    flux = np.zeros(cap, np.float32)
+    pdf = np.zeros(len(q), np.float32)
+    nsp = C.c_int32()
+    r = f(_ptr(lo), _ptr(hi), len(rounds), _ptr(ns), _ptr(sp), max_leaves, _ptr(leaves), _ptr(lc), _ptr(cnt),
+          _ptr(flux), len(q), _ptr(q), _ptr(pdf), C.byref(nsp))
+    if fn is None:
+        _check(r)
+        n = nsp.value
+    else:
+        n = r
+    total = int(lc[:n].sum())
+    return {"leaves": leaves[:4 * total].reshape(-1, 4), "leaf_counts": lc[:n], "counts": cnt[:n],
+            "flux": flux[:n], "pdf": pdf}

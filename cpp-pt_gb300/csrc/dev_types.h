@@ -52,7 +52,7 @@ constexpr uint32_t kStatusQueueOverflow = 4u;
 // Wavefront counters, one block of device memory per scene.
 struct WaveCounters {
     int32_t n_cur, n_next, n_shadow, pad0;
-    int32_t fetch_ext, fetch_sh, pad1, pad2;
+    int32_t fetch_ext, fetch_sh, free_top, pad2;  // free_top: PPG vertex-slot free list
     uint32_t status, pad3, pad4, pad5;
     unsigned long long work_next, work_total;
     unsigned long long stat_closest, stat_shadow, stat_paths, stat_iters;

@@ -20,7 +20,9 @@
 #include "../../include/cpppt_gb300.h"
 #include "bvh.h"
 #include "dev_types.h"
+#include "guide.h"
 #include "kernels.h"
+#include "sdtree.h"
 
 using namespace cpppt_gb300;
 
@@ -96,6 +98,7 @@ struct pt_scene {
     DevScene dev{};
     int n_tris = 0, width = 0, height = 0;
     double build_ref_ms = 0, build_wide_ms = 0;
+    float bounds_lo[3] = {0, 0, 0}, bounds_hi[3] = {0, 0, 0};  // union of the triangles' boxes
     int wide_depth = 0;
 
     // ray-batch scratch
@@ -181,6 +184,12 @@ void create_scene(const pt_scene_desc* d, pt_scene* s) {
     s->build_ref_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
     s->build_wide_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();
     s->wide_depth = wide.max_depth;
+    for (int k = 0; k < 3; k++) { s->bounds_lo[k] = INFINITY; s->bounds_hi[k] = -INFINITY; }
+    for (size_t i = 0; i < tv.size(); i += 3)
+        for (int k = 0; k < 3; k++) {
+            s->bounds_lo[k] = std::min(s->bounds_lo[k], tv[i + k]);
+            s->bounds_hi[k] = std::max(s->bounds_hi[k], tv[i + k]);
+        }
     if (3 * wide.max_depth + 4 > 64) throw Fail(PT_ERR_LIMIT, "wide BVH too deep for the traversal stack");
 
     // traversal triangles in leaf order: {a, rank}, {b - a, parent}, {c - a, prim}
@@ -387,10 +396,129 @@ void enqueue_iterations(pt_scene* s, const RenderParams& P, int iters) {
     }
 }
 
+// PPG::render (src/renderer/ppg.h:149-215): passes of 1, 2, 4, ... spp while
+// below spp in total; the SD-tree learns from every pass (splats on the GPU,
+// SDTree::update on the host) and only the last pass's image is kept.
+void render_ppg(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
+    cudaStream_t st = s->stream;
+    std::vector<int> passes;
+    for (int spp = 1;; spp *= 2) {
+        passes.push_back(spp);
+        if (spp * 2 >= desc->spp) break;
+    }
+    const int film_n = 3 * s->width * s->height;
+    const int D = desc->max_depth;
+    const unsigned long long max_pass = (unsigned long long)s->width * s->height * (unsigned long long)passes.back();
+    const int capacity = (int)std::min<unsigned long long>(1 << 20, (max_pass + 1023) / 1024 * 1024);
+    ensure_wave(s, capacity, film_n);
+    std::vector<void*> tmp;  // per-render buffers
+    struct Free {
+        std::vector<void*>& v;
+        ~Free() { for (void* p : v) cudaFree(p); }
+    } free_guard{tmp};
+    PPGVerts V;
+    V.vp = dalloc<float4>(tmp, (size_t)capacity * D);
+    V.vd = dalloc<float4>(tmp, (size_t)capacity * D);
+    V.vr = dalloc<float>(tmp, (size_t)capacity * D);
+    int* slots = dalloc<int>(tmp, capacity);
+    SDTreeHost tree(s->bounds_lo, s->bounds_hi);
+    RenderParams P{};
+    P.max_depth = desc->max_depth;
+    P.rr_start = desc->rr_start;
+    P.width = s->width;
+    P.height = s->height;
+    P.spp_axis = 0;  // ppg.h:181-184: one jittered sample per pixel per pass
+    pt_render_stats total{};
+    ck(cudaEventRecord(s->ev0, st), "event");
+    double launches = 0;
+    for (size_t l = 0; l < passes.size(); l++) {
+        const SDTreeFlat f = tree.flatten();
+        std::vector<void*> tt;
+        Free tguard{tt};
+        DevSDTree T;
+        for (int k = 0; k < 3; k++) { T.lo[k] = f.lo[k]; T.hi[k] = f.hi[k]; }
+        std::vector<int2> sn(f.snode.size() / 2);
+        for (size_t i = 0; i < sn.size(); i++) sn[i] = make_int2(f.snode[2 * i], f.snode[2 * i + 1]);
+        T.snode = dupload(tt, sn, st);
+        T.dnode = dupload(tt, f.dnode, st);
+        T.dtree_root = dupload(tt, f.dtree_root, st);
+        T.leaf_off = dupload(tt, f.dtree_leaf_off, st);
+        T.leaf_cnt = dupload(tt, f.dtree_leaf_cnt, st);
+        std::vector<float4> lv(f.leaves.size() / 4);
+        for (size_t i = 0; i < lv.size(); i++)
+            lv[i] = make_float4(f.leaves[4 * i], f.leaves[4 * i + 1], f.leaves[4 * i + 2], f.leaves[4 * i + 3]);
+        T.leaves = dupload(tt, lv, st);
+        const int n_dtree = (int)f.dtree_root.size();
+        T.slot_value = dalloc<float>(tt, f.n_value_slots);
+        T.dtree_count = dalloc<int>(tt, n_dtree);
+        T.dtree_rad = dalloc<float>(tt, n_dtree);
+        ck(cudaMemsetAsync(T.slot_value, 0, sizeof(float) * std::max(1, f.n_value_slots), st), "memset");
+        ck(cudaMemsetAsync(T.dtree_count, 0, sizeof(int) * std::max(1, n_dtree), st), "memset");
+        ck(cudaMemsetAsync(T.dtree_rad, 0, sizeof(float) * std::max(1, n_dtree), st), "memset");
+        ck(cudaMemsetAsync(s->film, 0, sizeof(unsigned long long) * film_n, st), "memset film");
+        launch_init_slots(slots, capacity, st);
+        P.spp = passes[l];
+        P.seed = desc->seed * 7919u + (uint32_t)l;
+        const unsigned long long work = (unsigned long long)s->width * s->height * (unsigned long long)passes[l];
+        WaveCounters init{};
+        init.work_total = work;
+        init.free_top = capacity;
+        *s->h_ctr = init;
+        ck(cudaMemcpyAsync(s->d_ctr, s->h_ctr, sizeof(WaveCounters), cudaMemcpyHostToDevice, st), "init counters");
+        launch_generate_ppg(s->dev, s->pb, 1, P, s->d_ctr, slots, st);
+        launches += 4;
+        const unsigned long long max_rounds =
+            64 + (work / (unsigned long long)capacity + 2) * (unsigned long long)(D + 2) * 4 / kItersPerGraph;
+        for (unsigned long long round = 0;; round++) {
+            for (int k = 0; k < kItersPerGraph; k++) {
+                const int cur = k & 1;
+                launch_extend(s->dev, s->pb, cur, s->d_ctr, s->num_sms, st);
+                launch_shade_ppg(s->dev, s->pb, cur, P, s->d_ctr, s->film, T, V, slots, st);
+                launch_generate_ppg(s->dev, s->pb, cur, P, s->d_ctr, slots, st);
+            }
+            launches += 4 * kItersPerGraph;
+            ck(cudaMemcpyAsync(s->h_ctr, s->d_ctr, sizeof(WaveCounters), cudaMemcpyDeviceToHost, st), "read counters");
+            ck(cudaStreamSynchronize(st), "render");
+            check_status(s, s->h_ctr->status);
+            if (s->h_ctr->n_cur == 0 && s->h_ctr->work_next >= s->h_ctr->work_total) break;
+            if (round > max_rounds) throw Fail(PT_ERR_LIMIT, "guided render did not converge within the iteration bound");
+        }
+        total.paths += (double)s->h_ctr->stat_paths;
+        total.closest_rays += (double)s->h_ctr->stat_closest;
+        total.iterations += (double)s->h_ctr->stat_iters;
+        total.nonfinite += (double)s->h_ctr->stat_nonfinite;
+        if (l + 1 == passes.size()) {
+            launch_film_resolve(s->film, d_dst ? d_dst : s->d_out, film_n, 1.0 / (double)passes[l], st);
+            launches += 1;
+        }
+        std::vector<float> hv(std::max(1, f.n_value_slots)), hr(std::max(1, n_dtree));
+        std::vector<int32_t> hc(std::max(1, n_dtree));
+        ck(cudaMemcpyAsync(hv.data(), T.slot_value, sizeof(float) * hv.size(), cudaMemcpyDeviceToHost, st), "copy");
+        ck(cudaMemcpyAsync(hc.data(), T.dtree_count, sizeof(int) * hc.size(), cudaMemcpyDeviceToHost, st), "copy");
+        ck(cudaMemcpyAsync(hr.data(), T.dtree_rad, sizeof(float) * hr.size(), cudaMemcpyDeviceToHost, st), "copy");
+        ck(cudaStreamSynchronize(st), "copy tree");
+        tree.accumulate(hv.data(), hc.data(), hr.data());
+        tree.update();
+    }
+    ck(cudaEventRecord(s->ev1, st), "event");
+    ck(cudaStreamSynchronize(st), "render");
+    ck(cudaGetLastError(), "render kernels");
+    float ms = 0;
+    ck(cudaEventElapsedTime(&ms, s->ev0, s->ev1), "elapsed");
+    total.render_ms = ms;
+    total.kernel_launches = launches;
+    s->stats = total;
+}
+
 void render_impl(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
     if (!desc) throw std::invalid_argument("null render description");
     if (desc->spp < 1) throw std::invalid_argument("spp must be >= 1");
     if (desc->max_depth < 1 || desc->max_depth > 0xffff) throw std::invalid_argument("max_depth must be in [1, 65535]");
+    if (desc->mode == PT_MODE_SDTREE) {
+        if (desc->flags != 0) throw Fail(PT_ERR_INVALID, "flags are not supported by the SD-tree guided render");
+        render_ppg(s, desc, d_dst);
+        return;
+    }
     if (desc->mode != PT_MODE_MIS) throw Fail(PT_ERR_INVALID, "render mode not available in this build");
     RenderParams P{};
     P.spp = desc->spp;
@@ -928,6 +1056,45 @@ pt_status pt_image_save(const char* prefix, const float* rgb, int32_t w, int32_t
 }
 
 const char* pt_last_error(void) { return g_error.c_str(); }
+
+pt_status pt_debug_sdtree_run(const float* lo, const float* hi, int32_t n_iters, const int32_t* n_splats,
+                              const float* splats, int32_t max_leaves, float* out_leaves, int32_t* out_leaf_counts,
+                              int32_t* out_counts, float* out_flux, int32_t n_queries, const float* queries,
+                              float* out_pdf, int32_t* n_spatial) {
+    if (!lo || !hi || n_iters < 0 || (n_iters > 0 && (!n_splats || !splats)) || !n_spatial ||
+        (n_queries > 0 && (!queries || !out_pdf))) {
+        g_error = "bad argument";
+        return PT_ERR_INVALID;
+    }
+    return guarded([&] {
+        SDTreeHost t(lo, hi);
+        size_t off = 0;
+        for (int it = 0; it < n_iters; it++) {
+            for (int k = 0; k < n_splats[it]; k++, off++) {
+                const float* sp = splats + 7 * off;
+                t.splat(sp[0], sp + 1, sp + 4);
+            }
+            t.update();
+        }
+        for (int q = 0; q < n_queries; q++) out_pdf[q] = t.pdf(queries + 6 * q, queries + 6 * q + 3);
+        std::vector<DLeafRegion> leaves;
+        std::vector<int> lc, cnt;
+        std::vector<float> flux;
+        t.dump(&leaves, &lc, &cnt, &flux);
+        *n_spatial = (int32_t)lc.size();
+        for (size_t i = 0; i < leaves.size() && (int32_t)i < max_leaves; i++) {
+            out_leaves[4 * i] = leaves[i].bx;
+            out_leaves[4 * i + 1] = leaves[i].by;
+            out_leaves[4 * i + 2] = leaves[i].sx;
+            out_leaves[4 * i + 3] = leaves[i].sy;
+        }
+        for (size_t i = 0; i < lc.size(); i++) {
+            if (out_leaf_counts) out_leaf_counts[i] = lc[i];
+            if (out_counts) out_counts[i] = cnt[i];
+            if (out_flux) out_flux[i] = flux[i];
+        }
+    });
+}
 
 pt_status pt_debug_ref_topology(const float* tri_v, int32_t n, int32_t* leaf_order, int32_t* prim_parent,
                                 float* node_boxes, int32_t max_nodes, int32_t* n_nodes) {

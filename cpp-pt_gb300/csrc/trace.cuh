@@ -97,9 +97,22 @@ __device__ __forceinline__ bool ref_box_exact(float4 lo, float4 hi, float3 o, fl
     return tmax > 0.f;
 }
 
+// byte c of w as a float: one byte permute builds 2^23 + b, one exact
+// subtraction removes 2^23 (keeps the integer pipe free for the min/max)
 __device__ __forceinline__ float byte_to_float(uint32_t w, int c) {
-    // exact: 2^23 + b, minus 2^23
-    return __uint_as_float(0x4b000000u | ((w >> (8 * c)) & 0xffu)) - 8388608.0f;
+    return __uint_as_float(__byte_perm(w, 0x4b000000u, 0x7540u | (uint32_t)c)) - 8388608.0f;
+}
+
+// three-operand min / max (one instruction on sm_100 and later)
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
 }
 
 // Per-lane traversal state (one ray in flight).  ANY=false: closest hit in
@@ -173,6 +186,8 @@ __device__ __forceinline__ bool trav_step(Trav& T, TravStack& K, const DevScene&
             w0 = __ldg(np); w1 = __ldg(np + 1); w2 = __ldg(np + 2); w3 = __ldg(np + 3);
         }
         const float cull = T.best.t * kCullScale + 1e-6f;
+        // slab distance of quantised coordinate q on axis k:
+        //   (p + q s - o) / d = q (s/d) + (p - o)/d = q B + A
         const float ax = fmaf(__uint_as_float(w0.x), T.idx, -T.oix);
         const float ay = fmaf(__uint_as_float(w0.y), T.idy, -T.oiy);
         const float az = fmaf(__uint_as_float(w0.z), T.idz, -T.oiz);
@@ -193,8 +208,8 @@ __device__ __forceinline__ bool trav_step(Trav& T, TravStack& K, const DevScene&
             const float tfx = fmaf(byte_to_float(fx, c), bx, ax);
             const float tfy = fmaf(byte_to_float(fy, c), by, ay);
             const float tfz = fmaf(byte_to_float(fz, c), bz, az);
-            const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.0f));
-            const float tf = fminf(fminf(tfx, tfy), fminf(tfz, cull));
+            const float tn = fmax3(tnx, tny, fmaxf(tnz, 0.0f));
+            const float tf = fmin3(tfx, tfy, fminf(tfz, cull));
             const bool hit = tn <= tf * 1.0000005f;
             key[c] = hit ? ((__float_as_uint(tn) & ~3u) | (uint32_t)c) : 0xffffffffu;
         }
@@ -203,18 +218,17 @@ __device__ __forceinline__ bool trav_step(Trav& T, TravStack& K, const DevScene&
 #undef CSWAP
         if (key[0] != 0xffffffffu) {
             const uint32_t refs[4] = {w2.z, w2.w, w3.x, w3.y};
+            if (T.sp + 3 > kStackSize) {
+                atomicOr(status, kStatusStackOverflow);
+                T.cur = kTravDone;
+                return true;
+            }
+            // far children first; an invalid key is written but not counted
 #pragma unroll
             for (int k = 3; k >= 1; k--) {
-                if (key[k] != 0xffffffffu) {
-                    if (T.sp >= kStackSize) {
-                        atomicOr(status, kStatusStackOverflow);
-                        T.cur = kTravDone;
-                        return true;
-                    }
-                    K.ref[T.sp] = refs[key[k] & 3u];
-                    K.t[T.sp] = __uint_as_float(key[k] & ~3u);
-                    T.sp++;
-                }
+                K.ref[T.sp] = refs[key[k] & 3u];
+                K.t[T.sp] = __uint_as_float(key[k] & ~3u);
+                T.sp += (key[k] != 0xffffffffu) ? 1 : 0;
             }
             T.cur = refs[key[0] & 3u];
             return false;

@@ -207,6 +207,19 @@ const char* pt_last_error(void);
  * triangle, -1 when the root is a leaf), node_boxes[6 * max_nodes]
  * (min xyz, max xyz per internal node, pre-order); *n_nodes receives the
  * internal-node count (PT_ERR_LIMIT when it exceeds max_nodes). */
+/* Diagnostic, host only (no CUDA call): the library's SD-tree update
+ * (SDTree::splat / update / pdf, src/algorithms/sdtree.h:445-537) run for
+ * n_iters rounds of {splat that round's records, update}.  splats: 7 floats
+ * each {radiance, pos xyz, dir xyz}.  Outputs per spatial leaf (depth
+ * first, child 0 first): its sampling leaves (4 floats: begin phi, begin
+ * cos theta, size phi, size cos theta, into out_leaves up to max_leaves),
+ * their number, the splat count and flux; and the pdf of each query
+ * (6 floats: pos, dir).  *n_spatial receives the spatial-leaf count. */
+pt_status pt_debug_sdtree_run(const float* lo, const float* hi, int32_t n_iters, const int32_t* n_splats,
+                              const float* splats, int32_t max_leaves, float* out_leaves, int32_t* out_leaf_counts,
+                              int32_t* out_counts, float* out_flux, int32_t n_queries, const float* queries,
+                              float* out_pdf, int32_t* n_spatial);
+
 pt_status pt_debug_ref_topology(const float* tri_v, int32_t n, int32_t* leaf_order, int32_t* prim_parent,
                                 float* node_boxes, int32_t max_nodes, int32_t* n_nodes);
 

@@ -97,6 +97,9 @@ class Oracle:
                 lib.ref_scene_error.restype = C.c_char_p
                 lib.ref_scene_error.argtypes = [_P]
                 lib.ref_max_threads.restype = C.c_int
+                lib.ref_sdtree_run.restype = C.c_int
+                lib.ref_sdtree_run.argtypes = [C.c_void_p] * 2 + [C.c_int] + [C.c_void_p] * 2 + [C.c_int] + \
+                    [C.c_void_p] * 4 + [C.c_int] + [C.c_void_p] * 3
                 lib.ref_scene_load.restype = _P
                 lib.ref_scene_load.argtypes = [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                                C.POINTER(C.c_int)]

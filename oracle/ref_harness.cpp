@@ -48,6 +48,11 @@ int cpppt_harness_verbose = 0;
 #include <camera/camera_perspective.h>
 #include <light/point_light.h>
 #include <renderer/pathtracerMIS.h>
+// SDTree's tree sits in the default-private part of a `class`; read it as a
+// struct (its dependencies are already included above).
+#define class struct
+#include <algorithms/sdtree.h>
+#undef class
 #include <renderer/ppg.h>
 #include <primitive/bvh.h>
 #include <shape/triangle.h>
@@ -357,5 +362,58 @@ double ref_render_ppg(void* h, int spp_axis, int seed_offset, int threads, const
 }
 
 int ref_max_threads(void) { return omp_get_max_threads(); }
+
+// Runs the reference's SDTree (src/algorithms/sdtree.h:268-674) through
+// n_iters rounds of {splat the round's records, update()}.  splats: 7 floats
+// each {radiance, pos xyz, dir xyz}.  Then dumps, for every spatial leaf in
+// depth-first order (child 0 first), its sampling leaves (4 floats each:
+// begin phi, begin cos, size phi, size cos), count and flux, and answers pdf
+// queries (6 floats each: pos, dir).  Returns the number of spatial leaves.
+int ref_sdtree_run(const float* lo, const float* hi, int n_iters, const int* n_splats, const float* splats,
+                   int max_leaves, float* out_leaves, int* out_leaf_counts, int* out_counts, float* out_flux,
+                   int n_queries, const float* queries, float* out_pdf) {
+    SDTree st({Vec3(lo[0], lo[1], lo[2]), Vec3(hi[0], hi[1], hi[2])});
+    {
+        Quiet q;
+        size_t off = 0;
+        for (int it = 0; it < n_iters; it++) {
+            for (int k = 0; k < n_splats[it]; k++, off++) {
+                const float* s = splats + 7 * off;
+                st.splat(s[0], Vec3(s[1], s[2], s[3]), Vec3(s[4], s[5], s[6]));
+            }
+            st.update();
+        }
+    }
+    for (int k = 0; k < n_queries; k++) {
+        const float* qv = queries + 6 * k;
+        out_pdf[k] = st.pdf(Vec3(qv[0], qv[1], qv[2]), Vec3(qv[3], qv[4], qv[5]));
+    }
+    int n_sleaf = 0, n_out = 0;
+    std::vector<const SNode*> stack{&st.root};
+    while (!stack.empty()) {
+        const SNode* n = stack.back();
+        stack.pop_back();
+        if (n->isLeaf) {
+            const DTree& d = *n->leaf.pt;
+            out_leaf_counts[n_sleaf] = (int)d.leaves.size();
+            out_counts[n_sleaf] = d.count;
+            out_flux[n_sleaf] = d.radiance;
+            for (auto& l : d.leaves) {
+                if (n_out < max_leaves) {
+                    out_leaves[4 * n_out] = l.begin.x;
+                    out_leaves[4 * n_out + 1] = l.begin.y;
+                    out_leaves[4 * n_out + 2] = l.size.x;
+                    out_leaves[4 * n_out + 3] = l.size.y;
+                }
+                n_out++;
+            }
+            n_sleaf++;
+        } else {
+            stack.push_back(&n->children->at(1));
+            stack.push_back(&n->children->at(0));
+        }
+    }
+    return n_sleaf;
+}
 
 }  // extern "C"
