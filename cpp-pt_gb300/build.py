@@ -6,6 +6,7 @@
 Translation units, compiled in parallel, CUDA for sm_103a only:
   csrc/render.cu  -- traversal and PT+NEE+MIS wavefront kernels (nvcc -gencode arch=compute_103a,code=sm_103a)
   csrc/guide.cu   -- SD-tree guided (PPG) wavefront kernels
+  csrc/nn.cu      -- learned guide: MLP on the tensor cores, training, guided wavefront
   csrc/host.cpp   -- C ABI, render drivers, loader, image output
   csrc/bvh.cpp    -- BVH builders
   csrc/sdtree.cpp -- SD-tree structure and update
@@ -50,7 +51,7 @@ def _commands(extra_cuda: list[str] | None = None):
     nvcc = _nvcc()
     common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
     jobs = []
-    for name in ("render.cu", "guide.cu", "host.cpp", "bvh.cpp", "sdtree.cpp"):
+    for name in ("render.cu", "guide.cu", "nn.cu", "host.cpp", "bvh.cpp", "sdtree.cpp"):
         src = os.path.join(CSRC, name)
         out = os.path.join(OBJ, name + ".o")
         cmd = [nvcc, "-c", src, "-o", out] + common
@@ -76,7 +77,7 @@ def build(force: bool = False, verbose: bool = False, extra_cuda: list[str] | No
             print(r.stdout, r.stderr, file=sys.stderr)
         return o
 
-    with cf.ThreadPoolExecutor(max_workers=5) as ex:
+    with cf.ThreadPoolExecutor(max_workers=6) as ex:
         list(ex.map(run, todo))
     objs = [o for _, o, _ in jobs]
     if force or todo or _stale(LIB, objs):

@@ -17,14 +17,16 @@ PT_OK = 0
 STATUS_NAMES = {0: "PT_OK", 1: "PT_ERR_INVALID", 2: "PT_ERR_CUDA", 3: "PT_ERR_MEMORY", 4: "PT_ERR_LIMIT",
                 5: "PT_ERR_IO", 6: "PT_ERR_NO_DEVICE"}
 MODE_MIS, MODE_SDTREE, MODE_NN = 0, 1, 2
-FLAG_TIME_KERNELS, FLAG_COUNT = 1, 2
+FLAG_TIME_KERNELS, FLAG_COUNT, FLAG_UNBIASED_MIS, FLAG_NN_FREEZE = 1, 2, 4, 8
+NN_WEIGHTS = 15360
 
 # every function the header declares
 EXPORTS = ["pt_scene_create", "pt_scene_load", "pt_scene_destroy", "pt_scene_info", "pt_trace_closest", "pt_trace_any",
            "pt_trace_closest_device", "pt_trace_any_device", "pt_render", "pt_render_device",
            "pt_render_device_noalloc",
            "pt_render_stats_get", "pt_image_save", "pt_last_error", "pt_debug_ref_topology",
-           "pt_debug_sdtree_run"]
+           "pt_debug_sdtree_run", "pt_nn_get_weights", "pt_nn_set_weights", "pt_nn_reset", "pt_nn_stats",
+           "pt_debug_nn_forward", "pt_debug_nn_grad", "pt_nn_configure", "pt_nn_config_get"]
 
 
 class PtMaterial(C.Structure):
@@ -53,6 +55,11 @@ class PtRenderStats(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("paths", "closest_rays", "shadow_rays", "render_ms", "trace_closest_ms",
                                            "trace_shadow_ms", "iterations", "kernel_launches", "extend_nodes",
                                            "extend_tris", "h2d_bytes", "d2h_bytes", "nonfinite")]
+
+
+class PtNNConfig(C.Structure):
+    _fields_ = [("learning_rate", C.c_float), ("bsdf_frac_min", C.c_float), ("bsdf_frac_max", C.c_float),
+                ("batch", C.c_int32)]
 
 
 class PtError(RuntimeError):
@@ -90,6 +97,14 @@ def load(path: str = LIB_PATH):
     lib.pt_last_error.restype = C.c_char_p
     lib.pt_last_error.argtypes = []
     lib.pt_debug_ref_topology.argtypes = [P, C.c_int32, P, P, P, C.c_int32, P]
+    lib.pt_nn_get_weights.argtypes = [P, P]
+    lib.pt_nn_set_weights.argtypes = [P, P]
+    lib.pt_nn_reset.argtypes = [P, C.c_uint32]
+    lib.pt_nn_stats.argtypes = [P, P, P, P]
+    lib.pt_debug_nn_forward.argtypes = [P, P, P, P, C.c_int32, P]
+    lib.pt_debug_nn_grad.argtypes = [P, P, P, P, C.c_int32, P, P]
+    lib.pt_nn_configure.argtypes = [P, P]
+    lib.pt_nn_config_get.argtypes = [P, P]
     lib.pt_debug_sdtree_run.argtypes = [P, P, C.c_int32, P, P, C.c_int32, P, P, P, P, C.c_int32, P, P, P]
     for name in EXPORTS:
         getattr(lib, name).restype = C.c_int32 if name not in ("pt_scene_destroy", "pt_last_error") else \
@@ -206,6 +221,41 @@ class GpuScene:
         d = self.desc(spp, max_depth, rr_start, seed, mode, flags)
         _check(_lib.pt_render_device(self.h, C.byref(d), d_out))
 
+    # --- learned guide ---
+    def nn_weights(self) -> np.ndarray:
+        w = np.zeros(NN_WEIGHTS, np.float32)
+        _check(_lib.pt_nn_get_weights(self.h, _ptr(w)))
+        return w
+
+    def nn_set_weights(self, w: np.ndarray):
+        w = np.ascontiguousarray(w, np.float32)
+        _check(_lib.pt_nn_set_weights(self.h, _ptr(w)))
+
+    def nn_reset(self, seed: int = 12345):
+        _check(_lib.pt_nn_reset(self.h, seed))
+
+    def nn_configure(self, **kw):
+        """Updates the learned guide's settings (learning_rate, bsdf_frac_min,
+        bsdf_frac_max, batch); returns the new settings."""
+        c = PtNNConfig()
+        _check(_lib.pt_nn_config_get(self.h, C.byref(c)))
+        for k, v in kw.items():
+            if k not in dict(PtNNConfig._fields_):
+                raise KeyError(k)
+            setattr(c, k, v)
+        _check(_lib.pt_nn_configure(self.h, C.byref(c)))
+        return self.nn_config()
+
+    def nn_config(self) -> dict:
+        c = PtNNConfig()
+        _check(_lib.pt_nn_config_get(self.h, C.byref(c)))
+        return {k: getattr(c, k) for k, _ in PtNNConfig._fields_}
+
+    def nn_stats(self) -> dict:
+        v = [C.c_double() for _ in range(3)]
+        _check(_lib.pt_nn_stats(self.h, *[C.byref(x) for x in v]))
+        return {"steps": v[0].value, "last_loss": v[1].value, "records": v[2].value}
+
     def stats(self) -> dict:
         s = PtRenderStats()
         _check(_lib.pt_render_stats_get(self.h, C.byref(s)))
@@ -262,3 +312,28 @@ def sdtree_run(lo, hi, rounds, queries, max_leaves=1 << 20, fn=None, lib=None):
     total = int(lc[:n].sum())
     return {"leaves": leaves[:4 * total].reshape(-1, 4), "leaf_counts": lc[:n], "counts": cnt[:n],
             "flux": flux[:n], "pdf": pdf}
+
+
+def nn_forward(weights, lo, hi, inputs):
+    """Debug forward pass of the learned guide on the GPU: (n,9) -> (n,41)."""
+    L = load()
+    w = np.ascontiguousarray(weights, np.float32)
+    x = np.ascontiguousarray(inputs, np.float32)
+    out = np.zeros((len(x), 41), np.float32)
+    lo = np.ascontiguousarray(lo, np.float32)
+    hi = np.ascontiguousarray(hi, np.float32)
+    _check(L.pt_debug_nn_forward(_ptr(w), _ptr(lo), _ptr(hi), _ptr(x), len(x), _ptr(out)))
+    return out
+
+
+def nn_grad(weights, lo, hi, records):
+    """Debug gradient of the training loss on the GPU: returns (loss, dL/dW)."""
+    L = load()
+    w = np.ascontiguousarray(weights, np.float32)
+    r = np.ascontiguousarray(records, np.float32)
+    g = np.zeros(NN_WEIGHTS, np.float32)
+    loss = C.c_float()
+    lo = np.ascontiguousarray(lo, np.float32)
+    hi = np.ascontiguousarray(hi, np.float32)
+    _check(L.pt_debug_nn_grad(_ptr(w), _ptr(lo), _ptr(hi), _ptr(r), len(r), _ptr(g), C.byref(loss)))
+    return loss.value, g

@@ -44,6 +44,19 @@ struct DevScene {
     DevCamera cam;
 };
 
+// One render job of a multi-scene batch (the scenes' geometry is merged into
+// one device arena; each job renders one scene of it at its own resolution,
+// spp and seed into its own range of the merged film).
+struct DevBatchJob {
+    DevCamera cam;
+    unsigned long long work_begin;  // first global work index (pixel x sample) of the job
+    unsigned long long film_off;    // first pixel of the job in the merged film
+    uint32_t root;                  // wide-node index of the scene's root in the arena
+    int32_t light_off, n_lights;    // the scene's emissive triangles in the arena's light list
+    int32_t spp, spp_axis, max_depth, rr_start;
+    uint32_t seed;
+};
+
 // Ray-batch status word bits (kernel-side bounded loops report here).
 constexpr uint32_t kStatusIterLimit = 1u;
 constexpr uint32_t kStatusStackOverflow = 2u;
@@ -51,8 +64,8 @@ constexpr uint32_t kStatusQueueOverflow = 4u;
 
 // Wavefront counters, one block of device memory per scene.
 struct WaveCounters {
-    int32_t n_cur, n_next, n_shadow, pad0;
-    int32_t fetch_ext, fetch_sh, free_top, pad2;  // free_top: PPG vertex-slot free list
+    int32_t n_cur, n_next, n_shadow, n_fin;  // n_fin: finished paths of the learned-guide integrator
+    int32_t fetch_ext, fetch_sh, free_top, n_rec;  // free_top: vertex-slot free list; n_rec: training records
     uint32_t status, pad3, pad4, pad5;
     unsigned long long work_next, work_total;
     unsigned long long stat_closest, stat_shadow, stat_paths, stat_iters;

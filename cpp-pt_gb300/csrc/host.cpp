@@ -3,137 +3,12 @@
 // Owns the device copy of a scene, the wavefront buffers and the CUDA graph
 // that replays wavefront iterations.  No call throws across the ABI; errors
 // are status codes plus a thread-local message.
-#include <algorithm>
-#include <chrono>
-#include <cmath>
-#include <cstdio>
-#include <cstring>
-#include <fstream>
-#include <sstream>
-#include <stdexcept>
-#include <string>
-#include <unordered_map>
-#include <vector>
-
-#include <cuda_runtime.h>
-
-#include "../../include/cpppt_gb300.h"
-#include "bvh.h"
-#include "dev_types.h"
-#include "guide.h"
-#include "kernels.h"
-#include "sdtree.h"
+#include "host_internal.h"
 
 using namespace cpppt_gb300;
+using namespace cpppt_gb300::hostimpl;
 
-namespace {
-thread_local std::string g_error;
-
-struct Fail : std::runtime_error {
-    pt_status code;
-    Fail(pt_status c, const std::string& m) : std::runtime_error(m), code(c) {}
-};
-
-void ck(cudaError_t e, const char* what) {
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        throw Fail(e == cudaErrorMemoryAllocation ? PT_ERR_MEMORY : PT_ERR_CUDA,
-                   std::string(what) + ": " + cudaGetErrorString(e));
-    }
-}
-
-template <class F>
-pt_status guarded(F&& f) {
-    try {
-        f();
-        g_error.clear();
-        return PT_OK;
-    } catch (const Fail& e) {
-        g_error = e.what();
-        return e.code;
-    } catch (const std::bad_alloc&) {
-        g_error = "host allocation failed";
-        return PT_ERR_MEMORY;
-    } catch (const std::exception& e) {
-        g_error = e.what();
-        return PT_ERR_INVALID;
-    }
-}
-
-template <class T>
-T* dalloc(std::vector<void*>& owned, size_t count) {
-    void* p = nullptr;
-    if (count == 0) count = 1;
-    ck(cudaMalloc(&p, sizeof(T) * count), "cudaMalloc");
-    owned.push_back(p);
-    return static_cast<T*>(p);
-}
-
-template <class T>
-T* dupload(std::vector<void*>& owned, const std::vector<T>& v, cudaStream_t st) {
-    T* p = dalloc<T>(owned, v.size());
-    if (!v.empty()) ck(cudaMemcpyAsync(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, st), "upload");
-    return p;
-}
-
-float fnorm3(float* v) {
-    float l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
-    float inv = 1.0f / l;
-    v[0] *= inv; v[1] *= inv; v[2] *= inv;
-    return l;
-}
-void fcross(const float* a, const float* b, float* o) {
-    o[0] = a[1] * b[2] - a[2] * b[1];
-    o[1] = a[2] * b[0] - a[0] * b[2];
-    o[2] = a[0] * b[1] - a[1] * b[0];
-}
-
-}  // namespace
-
-struct pt_scene {
-    int device = 0;
-    int num_sms = 0;
-    cudaStream_t stream = nullptr;
-    std::vector<void*> owned;  // scene data
-    DevScene dev{};
-    int n_tris = 0, width = 0, height = 0;
-    double build_ref_ms = 0, build_wide_ms = 0;
-    float bounds_lo[3] = {0, 0, 0}, bounds_hi[3] = {0, 0, 0};  // union of the triangles' boxes
-    int wide_depth = 0;
-
-    // ray-batch scratch
-    int* d_counter = nullptr;
-    uint32_t* d_status = nullptr;
-    void* d_io = nullptr;
-    size_t d_io_bytes = 0;
-
-    // wavefront state
-    PathBuffers pb{};
-    std::vector<void*> pb_owned;
-    unsigned long long* film = nullptr;  // 32.32 fixed point
-    float* d_out = nullptr;
-    int film_n = 0;
-    WaveCounters* d_ctr = nullptr;
-    WaveCounters* h_ctr = nullptr;  // pinned
-    cudaGraphExec_t graph = nullptr;
-    RenderParams graph_params{};
-    int graph_iters = 0;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    pt_render_stats stats{};
-
-    ~pt_scene() {
-        if (graph) cudaGraphExecDestroy(graph);
-        for (void* p : owned) cudaFree(p);
-        for (void* p : pb_owned) cudaFree(p);
-        if (film) cudaFree(film);
-        if (d_out) cudaFree(d_out);
-        if (d_io) cudaFree(d_io);
-        if (h_ctr) cudaFreeHost(h_ctr);
-        if (ev0) cudaEventDestroy(ev0);
-        if (ev1) cudaEventDestroy(ev1);
-        if (stream) cudaStreamDestroy(stream);
-    }
-};
+thread_local std::string cpppt_gb300::hostimpl::g_error;
 
 namespace {
 
@@ -263,6 +138,9 @@ void create_scene(const pt_scene_desc* d, pt_scene* s) {
     std::vector<uint4> nodes(4 * wide.nodes.size());
     std::memcpy(nodes.data(), wide.nodes.data(), sizeof(WideNode) * wide.nodes.size());
 
+    s->n_verts = nv;
+    s->n_mats = nm;
+    s->n_rbox = (int)ref.node_box.size();
     DevScene& S = s->dev;
     S.nodes = dupload(s->owned, nodes, s->stream);
     S.n_nodes = (int)wide.nodes.size();
@@ -510,10 +388,196 @@ void render_ppg(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
     s->stats = total;
 }
 
+// ---------------------------------------------------------------------------
+// Learned guide: network state and the NN / unbiased-MIS render driver
+// ---------------------------------------------------------------------------
+constexpr int kNNBatch = 1 << 18;  // training records per step
+constexpr int kNNWeightCount = 3 * 64 * 64 + 64 * 48;
+static_assert(kNNWeightCount == PT_NN_WEIGHTS, "weight count");
+
+std::vector<float> nn_random_weights(uint32_t seed) {
+    // He initialisation for the ReLU layers, a smaller output layer
+    std::mt19937 g(seed);
+    std::vector<float> w(kNNWeightCount);
+    for (int l = 0; l < 4; l++) {
+        const int nout = l == 3 ? 48 : 64;
+        const float sd = l == 3 ? 0.05f : std::sqrt(2.0f / 64.0f);
+        std::normal_distribution<float> nd(0.0f, sd);
+        for (int k = 0; k < 64 * nout; k++) w[l * 64 * 64 + k] = nd(g);
+    }
+    return w;
+}
+
+void nn_alloc(std::vector<void*>& owned, NNWeights* W, NNTrainBuf* TB, float** grad, float** scalars, int cap) {
+    W->master = dalloc<float>(owned, kNNWeightCount);
+    W->m = dalloc<float>(owned, kNNWeightCount);
+    W->v = dalloc<float>(owned, kNNWeightCount);
+    W->wt = dalloc<__nv_bfloat16>(owned, nn_wcopy_elems());
+    W->w = dalloc<__nv_bfloat16>(owned, nn_wcopy_elems());
+    if (TB) {
+        TB->cap = cap;
+        TB->act = dalloc<__nv_bfloat16>(owned, (size_t)4 * cap * 64);
+        TB->grad = dalloc<__nv_bfloat16>(owned, (size_t)4 * cap * 64);
+    }
+    *grad = dalloc<float>(owned, kNNWeightCount);
+    *scalars = dalloc<float>(owned, 4);
+    ck(nn_set_smem_limits(), "nn shared memory limits");
+}
+
+void nn_upload(const NNWeights& W, const float* host, cudaStream_t st) {
+    ck(cudaMemcpyAsync(W.master, host, sizeof(float) * kNNWeightCount, cudaMemcpyHostToDevice, st), "nn upload");
+    ck(cudaMemsetAsync(W.m, 0, sizeof(float) * kNNWeightCount, st), "memset");
+    ck(cudaMemsetAsync(W.v, 0, sizeof(float) * kNNWeightCount, st), "memset");
+    ck(cudaMemsetAsync(W.wt, 0, sizeof(__nv_bfloat16) * nn_wcopy_elems(), st), "memset");
+    ck(cudaMemsetAsync(W.w, 0, sizeof(__nv_bfloat16) * nn_wcopy_elems(), st), "memset");
+    launch_nn_pack(W, st);
+}
+
+void nn_ensure(pt_scene* s) {
+    if (s->nn_ready) return;
+    nn_alloc(s->nn_owned, &s->nnw, &s->nn_tb, &s->nn_grad, &s->nn_scalars, kNNBatch);
+    s->nn_rec = dalloc<float4>(s->nn_owned, (size_t)kNNBatch * 4);
+    s->nn_rec_count = 0;
+    std::vector<float> w = nn_random_weights(12345u);
+    nn_upload(s->nnw, w.data(), s->stream);
+    ck(cudaStreamSynchronize(s->stream), "nn init");
+    s->nn_ready = true;
+    s->nn_steps = 0;
+}
+
+NNNorm scene_norm(const pt_scene* s) {
+    NNNorm N;
+    for (int k = 0; k < 3; k++) {
+        const float ext = std::max(s->bounds_hi[k] - s->bounds_lo[k], 1e-6f);
+        N.lo[k] = s->bounds_lo[k];
+        N.inv_ext[k] = 1.0f / ext;
+    }
+    N.c_lo = s->nn_cfg.bsdf_frac_min;
+    N.c_hi = s->nn_cfg.bsdf_frac_max;
+    return N;
+}
+
+// PT + NEE + MIS on the slot-based wavefront (nn.cu).  guided: the learned
+// mixture is sampled and trained online; otherwise the same estimator with
+// the BSDF alone (PT_FLAG_UNBIASED_MIS).
+void render_nn(pt_scene* s, const pt_render_desc* desc, float* d_dst, bool guided) {
+    cudaStream_t st = s->stream;
+    const bool train = guided && !(desc->flags & PT_FLAG_NN_FREEZE);
+    if (guided) nn_ensure(s);
+    RenderParams P{};
+    P.spp = desc->spp;
+    int ax = (int)std::lround(std::sqrt((double)desc->spp));
+    P.spp_axis = (ax * ax == desc->spp) ? ax : 0;
+    P.max_depth = desc->max_depth;
+    P.rr_start = desc->rr_start;
+    P.seed = desc->seed;
+    P.width = s->width;
+    P.height = s->height;
+    const unsigned long long total = (unsigned long long)s->width * s->height * (unsigned long long)desc->spp;
+    const int capacity = (int)std::min<unsigned long long>(1 << 20, (total + 1023) / 1024 * 1024);
+    const int film_n = 3 * s->width * s->height;
+    ensure_wave(s, capacity, film_n);
+    std::vector<void*> tmp;
+    struct Free {
+        std::vector<void*>& v;
+        ~Free() { for (void* p : v) cudaFree(p); }
+    } guard{tmp};
+    NNPathData PD;
+    PD.vert = dalloc<float4>(tmp, (size_t)capacity * P.max_depth * 5);
+    PD.acc = dalloc<float4>(tmp, capacity);
+    PD.slot_stack = dalloc<int>(tmp, capacity);
+    PD.fin = dalloc<int2>(tmp, capacity);
+    const int batch = s->nn_cfg.batch;
+    PD.rec_cap = train ? batch : 0;
+    PD.rec = train ? s->nn_rec : nullptr;
+    float4* params = guided ? dalloc<float4>(tmp, (size_t)capacity * 11) : nullptr;
+    const NNNorm N = scene_norm(s);
+    ck(cudaEventRecord(s->ev0, st), "event");
+    ck(cudaMemsetAsync(s->film, 0, sizeof(unsigned long long) * film_n, st), "memset film");
+    launch_init_slots(PD.slot_stack, capacity, st);
+    WaveCounters init{};
+    init.work_total = total;
+    init.free_top = capacity;
+    init.n_rec = train ? s->nn_rec_count : 0;
+    *s->h_ctr = init;
+    ck(cudaMemcpyAsync(s->d_ctr, s->h_ctr, sizeof(WaveCounters), cudaMemcpyHostToDevice, st), "init counters");
+    launch_nn_generate(s->dev, s->pb, 1, P, s->d_ctr, PD, st);
+    double launches = 3;
+    const unsigned long long max_rounds =
+        64 + (total / (unsigned long long)capacity + 2) * (unsigned long long)(desc->max_depth + 2) * 4 / kItersPerGraph;
+    double records = 0;
+    for (unsigned long long round = 0;; round++) {
+        for (int k = 0; k < kItersPerGraph; k++) {
+            const int cur = k & 1;
+            launch_extend(s->dev, s->pb, cur, s->d_ctr, s->num_sms, st);
+            if (guided) launch_nn_infer(s->dev, s->pb, cur, s->d_ctr, s->nnw, N, params, s->num_sms, st);
+            launch_nn_shade(s->dev, s->pb, cur, P, s->d_ctr, s->film, params, PD, guided, st);
+            launch_nn_shadow(s->dev, s->pb, s->d_ctr, s->film, PD, s->num_sms, st);
+            launch_nn_finish(PD, s->d_ctr, P.max_depth, capacity, st);
+            launch_nn_generate(s->dev, s->pb, cur, P, s->d_ctr, PD, st);
+            launches += guided ? 7 : 6;
+        }
+        ck(cudaMemcpyAsync(s->h_ctr, s->d_ctr, sizeof(WaveCounters), cudaMemcpyDeviceToHost, st), "read counters");
+        ck(cudaStreamSynchronize(st), "render");
+        check_status(s, s->h_ctr->status);
+        if (train && s->h_ctr->n_rec >= batch) {
+            // one Adam step on the batch of records, then start a new batch
+            ck(cudaMemsetAsync(s->nn_scalars, 0, sizeof(float) * 4, st), "memset");
+            launch_sum_T(PD.rec, batch, s->nn_scalars + 1, st);
+            float tsum = 0.f;
+            ck(cudaMemcpyAsync(&tsum, s->nn_scalars + 1, sizeof(float), cudaMemcpyDeviceToHost, st), "copy");
+            ck(cudaStreamSynchronize(st), "tsum");
+            NNAdam opt;
+            opt.lr = s->nn_cfg.learning_rate;
+            launch_nn_train_step(s->nnw, N, PD.rec, batch, tsum, s->nn_tb, s->nn_grad, s->nn_scalars, opt,
+                                 ++s->nn_steps, s->num_sms, st, true);
+            launches += 5;
+            float loss = 0.f;
+            ck(cudaMemcpyAsync(&loss, s->nn_scalars, sizeof(float), cudaMemcpyDeviceToHost, st), "copy");
+            ck(cudaMemsetAsync(&s->d_ctr->n_rec, 0, sizeof(int), st), "reset records");
+            ck(cudaStreamSynchronize(st), "train");
+            s->nn_last_loss = loss;
+            records += batch;
+            s->nn_records += batch;
+        }
+        if (s->h_ctr->n_cur == 0 && s->h_ctr->work_next >= s->h_ctr->work_total) break;
+        if (round > max_rounds) throw Fail(PT_ERR_LIMIT, "render did not converge within the iteration bound");
+    }
+    if (train) s->nn_rec_count = std::min(s->h_ctr->n_rec, batch);
+    launch_film_resolve(s->film, d_dst ? d_dst : s->d_out, film_n, 1.0 / (double)desc->spp, st);
+    ck(cudaEventRecord(s->ev1, st), "event");
+    ck(cudaStreamSynchronize(st), "render");
+    ck(cudaGetLastError(), "render kernels");
+    float ms = 0;
+    ck(cudaEventElapsedTime(&ms, s->ev0, s->ev1), "elapsed");
+    pt_render_stats& R = s->stats;
+    R = pt_render_stats{};
+    R.paths = (double)s->h_ctr->stat_paths;
+    R.closest_rays = (double)s->h_ctr->stat_closest;
+    R.shadow_rays = (double)s->h_ctr->stat_shadow;
+    R.iterations = (double)s->h_ctr->stat_iters;
+    R.render_ms = ms;
+    R.kernel_launches = launches + 1;
+    R.nonfinite = (double)s->h_ctr->stat_nonfinite;
+    (void)records;
+}
+
 void render_impl(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
     if (!desc) throw std::invalid_argument("null render description");
     if (desc->spp < 1) throw std::invalid_argument("spp must be >= 1");
     if (desc->max_depth < 1 || desc->max_depth > 0xffff) throw std::invalid_argument("max_depth must be in [1, 65535]");
+    if (desc->mode == PT_MODE_NN) {
+        if (desc->flags & ~(PT_FLAG_NN_FREEZE | PT_FLAG_UNBIASED_MIS))
+            throw Fail(PT_ERR_INVALID, "unsupported flags for the learned-guide render");
+        render_nn(s, desc, d_dst, true);
+        return;
+    }
+    if (desc->mode == PT_MODE_MIS && (desc->flags & PT_FLAG_UNBIASED_MIS)) {
+        if (desc->flags & ~PT_FLAG_UNBIASED_MIS)
+            throw Fail(PT_ERR_INVALID, "PT_FLAG_UNBIASED_MIS does not combine with other flags");
+        render_nn(s, desc, d_dst, false);
+        return;
+    }
     if (desc->mode == PT_MODE_SDTREE) {
         if (desc->flags != 0) throw Fail(PT_ERR_INVALID, "flags are not supported by the SD-tree guided render");
         render_ppg(s, desc, d_dst);
@@ -1038,6 +1102,149 @@ pt_status pt_render_device_noalloc(pt_scene* s, const pt_render_desc* desc, floa
            "allocation-free render");
         check_status(s, h.status);
         if (limit) throw Fail(PT_ERR_LIMIT, "render did not converge within the iteration bound");
+    });
+}
+
+pt_status pt_nn_get_weights(pt_scene* s, float* w) {
+    if (!s || !w) { g_error = "null argument"; return PT_ERR_INVALID; }
+    return guarded([&] {
+        nn_ensure(s);
+        ck(cudaMemcpyAsync(w, s->nnw.master, sizeof(float) * kNNWeightCount, cudaMemcpyDeviceToHost, s->stream), "copy");
+        ck(cudaStreamSynchronize(s->stream), "copy");
+    });
+}
+
+pt_status pt_nn_set_weights(pt_scene* s, const float* w) {
+    if (!s || !w) { g_error = "null argument"; return PT_ERR_INVALID; }
+    return guarded([&] {
+        nn_ensure(s);
+        nn_upload(s->nnw, w, s->stream);
+        ck(cudaStreamSynchronize(s->stream), "upload");
+        s->nn_steps = 0;
+    });
+}
+
+pt_status pt_nn_reset(pt_scene* s, uint32_t seed) {
+    if (!s) { g_error = "null argument"; return PT_ERR_INVALID; }
+    return guarded([&] {
+        nn_ensure(s);
+        std::vector<float> w = nn_random_weights(seed);
+        nn_upload(s->nnw, w.data(), s->stream);
+        ck(cudaStreamSynchronize(s->stream), "upload");
+        s->nn_steps = 0;
+        s->nn_last_loss = 0;
+        s->nn_records = 0;
+        s->nn_rec_count = 0;
+    });
+}
+
+pt_status pt_nn_configure(pt_scene* s, const pt_nn_config* c) {
+    if (!s || !c) { g_error = "null argument"; return PT_ERR_INVALID; }
+    if (!(c->learning_rate > 0.f) || !(c->learning_rate < 1.f)) {
+        g_error = "learning_rate must be in (0, 1)";
+        return PT_ERR_INVALID;
+    }
+    if (!(c->bsdf_frac_min >= 0.1f) || !(c->bsdf_frac_max >= c->bsdf_frac_min) || !(c->bsdf_frac_max <= 1.f)) {
+        g_error = "need 0.1 <= bsdf_frac_min <= bsdf_frac_max <= 1";
+        return PT_ERR_INVALID;
+    }
+    if (c->batch < 1024 || c->batch > kNNBatch) {
+        g_error = "batch must be in [1024, 262144]";
+        return PT_ERR_INVALID;
+    }
+    s->nn_cfg = *c;
+    s->nn_rec_count = 0;  // records of the previous batch size are dropped
+    return PT_OK;
+}
+
+pt_status pt_nn_config_get(pt_scene* s, pt_nn_config* c) {
+    if (!s || !c) { g_error = "null argument"; return PT_ERR_INVALID; }
+    *c = s->nn_cfg;
+    return PT_OK;
+}
+
+pt_status pt_nn_stats(pt_scene* s, double* steps, double* last_loss, double* records_used) {
+    if (!s) { g_error = "null argument"; return PT_ERR_INVALID; }
+    if (steps) *steps = s->nn_steps;
+    if (last_loss) *last_loss = s->nn_last_loss;
+    if (records_used) *records_used = s->nn_records;
+    return PT_OK;
+}
+
+namespace {
+struct DebugCtx {
+    cudaStream_t st = nullptr;
+    std::vector<void*> owned;
+    int sms = 0;
+    DebugCtx() {
+        int dev = 0;
+        ck(cudaGetDevice(&dev), "cudaGetDevice");
+        cudaDeviceProp prop;
+        ck(cudaGetDeviceProperties(&prop, dev), "cudaGetDeviceProperties");
+        if (prop.major * 10 + prop.minor != 103) throw Fail(PT_ERR_NO_DEVICE, "not a compute capability 10.3 device");
+        sms = prop.multiProcessorCount;
+        ck(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream");
+    }
+    ~DebugCtx() {
+        if (st) cudaStreamSynchronize(st);
+        for (void* p : owned) cudaFree(p);
+        if (st) cudaStreamDestroy(st);
+    }
+};
+NNNorm norm_from(const float* lo, const float* hi) {
+    NNNorm N;
+    for (int k = 0; k < 3; k++) {
+        N.lo[k] = lo[k];
+        N.inv_ext[k] = 1.0f / std::max(hi[k] - lo[k], 1e-6f);
+    }
+    return N;
+}
+}  // namespace
+
+pt_status pt_debug_nn_forward(const float* weights, const float* lo, const float* hi, const float* inputs, int32_t n,
+                              float* out) {
+    if (!weights || !lo || !hi || n < 0 || (n > 0 && (!inputs || !out))) { g_error = "bad argument"; return PT_ERR_INVALID; }
+    return guarded([&] {
+        if (n == 0) return;
+        DebugCtx c;
+        NNWeights W;
+        NNTrainBuf* none = nullptr;
+        float *grad, *scal;
+        nn_alloc(c.owned, &W, none, &grad, &scal, 0);
+        nn_upload(W, weights, c.st);
+        float* din = dalloc<float>(c.owned, (size_t)9 * n);
+        float* dout = dalloc<float>(c.owned, (size_t)41 * n);
+        ck(cudaMemcpyAsync(din, inputs, sizeof(float) * 9 * n, cudaMemcpyHostToDevice, c.st), "copy");
+        launch_nn_forward_debug(W, norm_from(lo, hi), din, n, dout, c.sms, c.st);
+        ck(cudaMemcpyAsync(out, dout, sizeof(float) * 41 * n, cudaMemcpyDeviceToHost, c.st), "copy");
+        ck(cudaStreamSynchronize(c.st), "forward");
+        ck(cudaGetLastError(), "forward");
+    });
+}
+
+pt_status pt_debug_nn_grad(const float* weights, const float* lo, const float* hi, const float* records, int32_t n,
+                           float* out_grad, float* out_loss) {
+    if (!weights || !lo || !hi || n <= 0 || !records || !out_grad) { g_error = "bad argument"; return PT_ERR_INVALID; }
+    return guarded([&] {
+        DebugCtx c;
+        NNWeights W;
+        NNTrainBuf TB;
+        float *grad, *scal;
+        nn_alloc(c.owned, &W, &TB, &grad, &scal, n);
+        nn_upload(W, weights, c.st);
+        float4* drec = dalloc<float4>(c.owned, (size_t)4 * n);
+        ck(cudaMemcpyAsync(drec, records, sizeof(float) * 16 * n, cudaMemcpyHostToDevice, c.st), "copy");
+        double tsum = 0;
+        for (int i = 0; i < n; i++) tsum += records[16 * i + 13];
+        ck(cudaMemsetAsync(scal, 0, sizeof(float) * 4, c.st), "memset");
+        NNAdam opt;
+        launch_nn_train_step(W, norm_from(lo, hi), drec, n, (float)tsum, TB, grad, scal, opt, 1, c.sms, c.st, false);
+        ck(cudaMemcpyAsync(out_grad, grad, sizeof(float) * kNNWeightCount, cudaMemcpyDeviceToHost, c.st), "copy");
+        float loss = 0;
+        ck(cudaMemcpyAsync(&loss, scal, sizeof(float), cudaMemcpyDeviceToHost, c.st), "copy");
+        ck(cudaStreamSynchronize(c.st), "grad");
+        ck(cudaGetLastError(), "grad");
+        if (out_loss) *out_loss = loss;
     });
 }
 

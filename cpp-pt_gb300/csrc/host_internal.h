@@ -1,0 +1,154 @@
+// Internal declarations shared by the C ABI's translation units (host.cpp,
+// batch.cpp): error plumbing, device allocation helpers and the scene object.
+#pragma once
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/cpppt_gb300.h"
+#include "bvh.h"
+#include "dev_types.h"
+#include "guide.h"
+#include "kernels.h"
+#include "nn.h"
+#include "sdtree.h"
+#include <random>
+
+namespace cpppt_gb300 {
+namespace hostimpl {
+extern thread_local std::string g_error;
+
+struct Fail : std::runtime_error {
+    pt_status code;
+    Fail(pt_status c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+inline void ck(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        throw Fail(e == cudaErrorMemoryAllocation ? PT_ERR_MEMORY : PT_ERR_CUDA,
+                   std::string(what) + ": " + cudaGetErrorString(e));
+    }
+}
+
+template <class F>
+pt_status guarded(F&& f) {
+    try {
+        f();
+        g_error.clear();
+        return PT_OK;
+    } catch (const Fail& e) {
+        g_error = e.what();
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        g_error = "host allocation failed";
+        return PT_ERR_MEMORY;
+    } catch (const std::exception& e) {
+        g_error = e.what();
+        return PT_ERR_INVALID;
+    }
+}
+
+template <class T>
+T* dalloc(std::vector<void*>& owned, size_t count) {
+    void* p = nullptr;
+    if (count == 0) count = 1;
+    ck(cudaMalloc(&p, sizeof(T) * count), "cudaMalloc");
+    owned.push_back(p);
+    return static_cast<T*>(p);
+}
+
+template <class T>
+T* dupload(std::vector<void*>& owned, const std::vector<T>& v, cudaStream_t st) {
+    T* p = dalloc<T>(owned, v.size());
+    if (!v.empty()) ck(cudaMemcpyAsync(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, st), "upload");
+    return p;
+}
+
+inline float fnorm3(float* v) {
+    float l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    float inv = 1.0f / l;
+    v[0] *= inv; v[1] *= inv; v[2] *= inv;
+    return l;
+}
+inline void fcross(const float* a, const float* b, float* o) {
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = a[2] * b[0] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+}  // namespace hostimpl
+}  // namespace cpppt_gb300
+
+using namespace cpppt_gb300;  // internal header of the ABI's own translation units
+
+struct pt_scene {
+    // counts of the device arrays (a multi-scene batch copies them)
+    int n_verts = 0, n_mats = 0, n_rbox = 0;
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<void*> owned;  // scene data
+    DevScene dev{};
+    int n_tris = 0, width = 0, height = 0;
+    double build_ref_ms = 0, build_wide_ms = 0;
+    float bounds_lo[3] = {0, 0, 0}, bounds_hi[3] = {0, 0, 0};  // union of the triangles' boxes
+    int wide_depth = 0;
+
+    // ray-batch scratch
+    int* d_counter = nullptr;
+    uint32_t* d_status = nullptr;
+    void* d_io = nullptr;
+    size_t d_io_bytes = 0;
+
+    // wavefront state
+    PathBuffers pb{};
+    std::vector<void*> pb_owned;
+    unsigned long long* film = nullptr;  // 32.32 fixed point
+    float* d_out = nullptr;
+    int film_n = 0;
+    WaveCounters* d_ctr = nullptr;
+    WaveCounters* h_ctr = nullptr;  // pinned
+    cudaGraphExec_t graph = nullptr;
+    RenderParams graph_params{};
+    int graph_iters = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    pt_render_stats stats{};
+
+    // learned guide
+    bool nn_ready = false;
+    std::vector<void*> nn_owned;
+    NNWeights nnw{};
+    NNTrainBuf nn_tb{};
+    float* nn_grad = nullptr;
+    float* nn_scalars = nullptr;  // [0] loss, [1] sum of T
+    int nn_steps = 0;
+    double nn_last_loss = 0, nn_records = 0;
+    float4* nn_rec = nullptr;  // training records carried across renders
+    int nn_rec_count = 0;
+    pt_nn_config nn_cfg{1e-3f, 0.1f, 0.9f, 1 << 18};
+
+    ~pt_scene() {
+        for (void* p : nn_owned) cudaFree(p);
+        if (graph) cudaGraphExecDestroy(graph);
+        for (void* p : owned) cudaFree(p);
+        for (void* p : pb_owned) cudaFree(p);
+        if (film) cudaFree(film);
+        if (d_out) cudaFree(d_out);
+        if (d_io) cudaFree(d_io);
+        if (h_ctr) cudaFreeHost(h_ctr);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};

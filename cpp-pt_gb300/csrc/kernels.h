@@ -42,12 +42,13 @@ struct RenderParams {
 // shadow (any hit + film), generate (new camera paths) + advance (counters).
 void launch_extend(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, int num_sms, cudaStream_t st,
                    bool count = false);
+// jobs != nullptr: a multi-scene batch over a merged arena (DevBatchJob).
 void launch_shade(const DevScene& S, const PathBuffers& B, int cur, const RenderParams& P, WaveCounters* ctr,
-                  unsigned long long* film, cudaStream_t st);
+                  unsigned long long* film, cudaStream_t st, const DevBatchJob* jobs = nullptr);
 void launch_shadow(const DevScene& S, const PathBuffers& B, WaveCounters* ctr, unsigned long long* film, int num_sms,
                    cudaStream_t st);
 void launch_generate(const DevScene& S, const PathBuffers& B, int cur, const RenderParams& P, WaveCounters* ctr,
-                     cudaStream_t st);
+                     cudaStream_t st, const DevBatchJob* jobs = nullptr, int n_jobs = 0);
 constexpr int kKernelsPerIteration = 5;
 // Allocation-free render: the wavefront of launch_* above with its scratch in
 // a file-scope __device__ array (see render.cu).  Synchronises `st`.

@@ -1,0 +1,912 @@
+// Learned path guide on the tensor cores: fused MLP inference and training.
+//
+// Layout of the weights in device memory (one contiguous block per copy):
+//   master  float  [kNNWeights]          layer l at nn_layer_offset(l), row-major [in][out]
+//   wt      bf16   [4 layers][64][72]    transposed [out][in], rows padded to 72 (bank-conflict free)
+//   w       bf16   [4 layers][64][72]    row-major  [in][out] padded (backward data pass)
+// A warp runs 32 samples as two 16-row tiles through all layers with the
+// activations held in mma fragments: the accumulator fragment of one layer
+// is, after ReLU and packing, exactly the A fragment of the next.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "nn.h"
+#include "nn.cuh"
+#include "trace.cuh"
+
+namespace cpppt_gb300 {
+
+constexpr int kWStride = 72;  // padded row of 64 bf16
+constexpr int kWLayer = 64 * kWStride;
+
+// B fragment of W (k = input, n = output) from the transposed copy wt[out][in].
+__device__ __forceinline__ void load_b_fwd(const __nv_bfloat16* wt_l, int nt, int kt, int lane, uint32_t b[2]) {
+    const int g = lane >> 2, t = lane & 3;
+    const __nv_bfloat16* p = wt_l + (nt * 8 + g) * kWStride + kt * 16 + 2 * t;
+    b[0] = *reinterpret_cast<const uint32_t*>(p);
+    b[1] = *reinterpret_cast<const uint32_t*>(p + 8);
+}
+// B fragment of W^T (k = output, n = input) from the row-major copy w[in][out].
+__device__ __forceinline__ void load_b_bwd(const __nv_bfloat16* w_l, int nt, int kt, int lane, uint32_t b[2]) {
+    const int g = lane >> 2, t = lane & 3;
+    const __nv_bfloat16* p = w_l + (nt * 8 + g) * kWStride + kt * 16 + 2 * t;
+    b[0] = *reinterpret_cast<const uint32_t*>(p);
+    b[1] = *reinterpret_cast<const uint32_t*>(p + 8);
+}
+
+// Sample inputs of one lane's sample, gathered by the lanes that need them.
+struct NNIn {
+    f3 pn, n, wo;
+};
+
+__device__ __forceinline__ NNIn shfl_in(const NNIn& v, int src) {
+    NNIn r;
+    r.pn = mk(__shfl_sync(0xffffffffu, v.pn.x, src), __shfl_sync(0xffffffffu, v.pn.y, src),
+              __shfl_sync(0xffffffffu, v.pn.z, src));
+    r.n = mk(__shfl_sync(0xffffffffu, v.n.x, src), __shfl_sync(0xffffffffu, v.n.y, src),
+             __shfl_sync(0xffffffffu, v.n.z, src));
+    r.wo = mk(__shfl_sync(0xffffffffu, v.wo.x, src), __shfl_sync(0xffffffffu, v.wo.y, src),
+              __shfl_sync(0xffffffffu, v.wo.z, src));
+    return r;
+}
+
+// A fragments of the input layer for 16-row tile `mt` (rows mt*16 .. +15 of
+// the warp's 32 samples, sample r owned by lane r).
+__device__ __forceinline__ void input_frags(const NNIn& mine, int mt, int lane, uint32_t a[4][4]) {
+    const int g = lane >> 2, t = lane & 3;
+    const NNIn r0 = shfl_in(mine, mt * 16 + g), r1 = shfl_in(mine, mt * 16 + g + 8);
+#pragma unroll
+    for (int kt = 0; kt < 4; kt++) {
+        const int c = kt * 16 + 2 * t;
+        a[kt][0] = pack_bf16(nn_feature(c, r0.pn, r0.n, r0.wo), nn_feature(c + 1, r0.pn, r0.n, r0.wo));
+        a[kt][1] = pack_bf16(nn_feature(c, r1.pn, r1.n, r1.wo), nn_feature(c + 1, r1.pn, r1.n, r1.wo));
+        a[kt][2] = pack_bf16(nn_feature(c + 8, r0.pn, r0.n, r0.wo), nn_feature(c + 9, r0.pn, r0.n, r0.wo));
+        a[kt][3] = pack_bf16(nn_feature(c + 8, r1.pn, r1.n, r1.wo), nn_feature(c + 9, r1.pn, r1.n, r1.wo));
+    }
+}
+
+// One hidden layer: acc = A W; then A <- bf16(relu(acc)).
+__device__ __forceinline__ void hidden_layer(const __nv_bfloat16* wt_l, int lane, uint32_t a[4][4], float acc[8][4]) {
+#pragma unroll
+    for (int nt = 0; nt < 8; nt++) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
+#pragma unroll
+    for (int kt = 0; kt < 4; kt++)
+#pragma unroll
+        for (int nt = 0; nt < 8; nt++) {
+            uint32_t b[2];
+            load_b_fwd(wt_l, nt, kt, lane, b);
+            mma_bf16(acc[nt], a[kt], b);
+        }
+#pragma unroll
+    for (int kt = 0; kt < 4; kt++) {
+        a[kt][0] = pack_bf16(fmaxf(acc[2 * kt][0], 0.f), fmaxf(acc[2 * kt][1], 0.f));
+        a[kt][1] = pack_bf16(fmaxf(acc[2 * kt][2], 0.f), fmaxf(acc[2 * kt][3], 0.f));
+        a[kt][2] = pack_bf16(fmaxf(acc[2 * kt + 1][0], 0.f), fmaxf(acc[2 * kt + 1][1], 0.f));
+        a[kt][3] = pack_bf16(fmaxf(acc[2 * kt + 1][2], 0.f), fmaxf(acc[2 * kt + 1][3], 0.f));
+    }
+}
+
+__device__ __forceinline__ void output_layer(const __nv_bfloat16* wt_l, int lane, const uint32_t a[4][4],
+                                             float out[6][4]) {
+#pragma unroll
+    for (int nt = 0; nt < 6; nt++) out[nt][0] = out[nt][1] = out[nt][2] = out[nt][3] = 0.f;
+#pragma unroll
+    for (int kt = 0; kt < 4; kt++)
+#pragma unroll
+        for (int nt = 0; nt < 6; nt++) {
+            uint32_t b[2];
+            load_b_fwd(wt_l, nt, kt, lane, b);
+            mma_bf16(out[nt], a[kt], b);
+        }
+}
+
+// Writes a 16 x 48 output tile's fragments to a row-major smem tile.
+__device__ __forceinline__ void store_out_tile(float* tile /*16 x 48*/, const float out[6][4], int lane) {
+    const int g = lane >> 2, t = lane & 3;
+#pragma unroll
+    for (int nt = 0; nt < 6; nt++) {
+        tile[g * kNNOut + nt * 8 + 2 * t] = out[nt][0];
+        tile[g * kNNOut + nt * 8 + 2 * t + 1] = out[nt][1];
+        tile[(g + 8) * kNNOut + nt * 8 + 2 * t] = out[nt][2];
+        tile[(g + 8) * kNNOut + nt * 8 + 2 * t + 1] = out[nt][3];
+    }
+}
+
+__device__ __forceinline__ void stage_weights(const NNWeights& W, __nv_bfloat16* s_wt, __nv_bfloat16* s_w,
+                                              bool with_w) {
+    const uint4* src = reinterpret_cast<const uint4*>(W.wt);
+    uint4* dst = reinterpret_cast<uint4*>(s_wt);
+    const int n16 = kNNLayers * kWLayer * 2 / 16;
+    for (int i = threadIdx.x; i < n16; i += blockDim.x) dst[i] = src[i];
+    if (with_w) {
+        const uint4* s2 = reinterpret_cast<const uint4*>(W.w);
+        uint4* d2 = reinterpret_cast<uint4*>(s_w);
+        for (int i = threadIdx.x; i < n16; i += blockDim.x) d2[i] = s2[i];
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// Inference: raw outputs -> 41 mixture parameters per sample.
+// ---------------------------------------------------------------------------
+template <class GetIn, class Put>
+__device__ __forceinline__ void infer_loop(int n, const __nv_bfloat16* s_wt, float* s_tile /*per warp 32x48*/,
+                                           float c_lo, float c_hi, GetIn get_in, Put put) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int base = warp * 32; base < n; base += nwarps * 32) {
+        const int i = base + lane;
+        NNIn mine;
+        bool valid = false;
+        if (i < n) valid = get_in(i, mine);
+        if (!valid) { mine.pn = mk(0.f, 0.f, 0.f); mine.n = mine.pn; mine.wo = mine.pn; }
+#pragma unroll
+        for (int mt = 0; mt < 2; mt++) {
+            uint32_t a[4][4];
+            float acc[8][4];
+            input_frags(mine, mt, lane, a);
+            for (int l = 0; l < kNNLayers - 1; l++) hidden_layer(s_wt + l * kWLayer, lane, a, acc);
+            float out[6][4];
+            output_layer(s_wt + (kNNLayers - 1) * kWLayer, lane, a, out);
+            store_out_tile(s_tile + mt * 16 * kNNOut, out, lane);
+        }
+        __syncwarp();
+        if (i < n && valid) {
+            float raw[kNNOut];
+#pragma unroll
+            for (int k = 0; k < kNNOut; k++) raw[k] = s_tile[lane * kNNOut + k];
+            float prm[kNNParams];
+            nn_postprocess(raw, prm, c_lo, c_hi);
+            put(i, prm);
+        }
+        __syncwarp();
+    }
+}
+
+constexpr int kNNThreads = 128;
+
+__global__ void __launch_bounds__(kNNThreads) k_nn_forward_debug(NNWeights W, NNNorm N, const float* __restrict__ in,
+                                                                 int n, float* __restrict__ out) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __nv_bfloat16* s_wt = reinterpret_cast<__nv_bfloat16*>(smem);
+    float* s_tile = reinterpret_cast<float*>(smem + kNNLayers * kWLayer * 2) + (threadIdx.x >> 5) * 32 * kNNOut;
+    stage_weights(W, s_wt, nullptr, false);
+    infer_loop(
+        n, s_wt, s_tile, N.c_lo, N.c_hi,
+        [&](int i, NNIn& v) {
+            const float* p = in + 9 * (size_t)i;
+            v.pn = mk((p[0] - N.lo[0]) * N.inv_ext[0], (p[1] - N.lo[1]) * N.inv_ext[1], (p[2] - N.lo[2]) * N.inv_ext[2]);
+            v.n = mk(p[3], p[4], p[5]);
+            v.wo = mk(p[6], p[7], p[8]);
+            return true;
+        },
+        [&](int i, const float* prm) {
+            for (int k = 0; k < kNNParams; k++) out[kNNParams * (size_t)i + k] = prm[k];
+        });
+}
+
+// Guide parameters for every live path's hit (run between extend and shade).
+__global__ void __launch_bounds__(kNNThreads) k_nn_infer(DevScene S, PathBuffers B, int cur, WaveCounters* ctr,
+                                                         NNWeights W, NNNorm N, float4* __restrict__ params) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int n = ctr->n_cur;
+    if (n == 0) return;
+    __nv_bfloat16* s_wt = reinterpret_cast<__nv_bfloat16*>(smem);
+    float* s_tile = reinterpret_cast<float*>(smem + kNNLayers * kWLayer * 2) + (threadIdx.x >> 5) * 32 * kNNOut;
+    stage_weights(W, s_wt, nullptr, false);
+    infer_loop(
+        n, s_wt, s_tile, N.c_lo, N.c_hi,
+        [&](int i, NNIn& v) {
+            const float4 H = B.hit[i];
+            const int prim = __float_as_int(H.y);
+            if (prim < 0) return false;
+            const int4 vi = __ldg(S.tri_vidx + prim);
+            if (S.mats[vi.w].kind == PT_MAT_EMISSIVE_) return false;
+            const float4 O = B.o[cur][i], D = B.d[cur][i];
+            const f3 d = mk(D.x, D.y, D.z);
+            const f3 p = mk(O.x, O.y, O.z) + d * H.x;
+            const float beta = H.z, gamma = H.w, alpha = 1.0f - (gamma + beta);
+            const f3 nn = normalized(f3of(__ldg(S.v_nrm + vi.x)) * alpha + f3of(__ldg(S.v_nrm + vi.y)) * beta +
+                                     f3of(__ldg(S.v_nrm + vi.z)) * gamma);
+            v.pn = mk((p.x - N.lo[0]) * N.inv_ext[0], (p.y - N.lo[1]) * N.inv_ext[1], (p.z - N.lo[2]) * N.inv_ext[2]);
+            v.n = nn;
+            v.wo = -d;
+            return true;
+        },
+        [&](int i, const float* prm) {
+            float4* o = params + 11 * (size_t)i;
+            for (int k = 0; k < 10; k++) o[k] = make_float4(prm[4 * k], prm[4 * k + 1], prm[4 * k + 2], prm[4 * k + 3]);
+            o[10] = make_float4(prm[40], 0.f, 0.f, 0.f);
+        });
+}
+
+// ---------------------------------------------------------------------------
+// Training.  Records (16 floats): pos xyz, normal xyz, wo xyz, wi xyz,
+// p_bsdf(wi), target weight T (>= 0), 0, 0.  Loss over a batch:
+//   L = -sum_r T_r log m_r(wi_r) / sum_r T_r,  m = c p_bsdf + (1 - c) q.
+// ---------------------------------------------------------------------------
+
+// d loss / d raw outputs for one record (raw: 48 floats; returns loss term)
+__device__ __forceinline__ float nn_loss_grad(const float* raw, f3 wi, float p_bsdf, float T, float c_lo, float c_hi,
+                                             float* g /*48*/) {
+    for (int k = 0; k < kNNOut; k++) g[k] = 0.f;
+    if (!(T > 0.f)) return 0.f;
+    float prm[kNNParams];
+    nn_postprocess(raw, prm, c_lo, c_hi);
+    float v[kNNLobes], q = 0.f;
+    for (int j = 0; j < kNNLobes; j++) {
+        v[j] = vmf_pdf(mk(prm[5 * j], prm[5 * j + 1], prm[5 * j + 2]), prm[5 * j + 3], wi);
+        q += prm[5 * j + 4] * v[j];
+    }
+    const float c = prm[40];
+    const float m = fmaxf(c * p_bsdf + (1.0f - c) * q, 1e-20f);
+    const float dL_dm = -T / m;
+    // selection: c = c_lo + (c_hi - c_lo) sigmoid(x)
+    const float sg = 1.0f / (1.0f + __expf(-raw[40]));
+    g[40] = dL_dm * (p_bsdf - q) * (c_hi - c_lo) * sg * (1.0f - sg);
+    const float dL_dq = dL_dm * (1.0f - c);
+    float gw[kNNLobes], wg = 0.f;
+    for (int j = 0; j < kNNLobes; j++) {
+        gw[j] = dL_dq * v[j];
+        wg += prm[5 * j + 4] * gw[j];
+    }
+    for (int j = 0; j < kNNLobes; j++) {
+        const float wj = prm[5 * j + 4];
+        g[32 + j] = wj * (gw[j] - wg);  // softmax
+        const float kappa = prm[5 * j + 3];
+        const f3 mu = mk(prm[5 * j], prm[5 * j + 1], prm[5 * j + 2]);
+        const float dv = dL_dq * wj * v[j];  // dL/d log v_j
+        // kappa = softplus(x) + 0.1 (clamped at 5000)
+        const float dlogv_dk = 1.0f / kappa - 2.0f / expm1f(2.0f * kappa) + (dot(mu, wi) - 1.0f);
+        const float x = raw[24 + j];
+        const float dk_dx = kappa >= 5000.0f ? 0.0f : 1.0f / (1.0f + __expf(-x));
+        g[24 + j] = dv * dlogv_dk * dk_dx;
+        // mu = r / |r|: dL/dr = (I - mu mu^T) (dL/dmu) / |r|,  dlogv/dmu = kappa wi
+        const f3 r = mk(raw[3 * j], raw[3 * j + 1], raw[3 * j + 2]);
+        const float len = sqrtf(dot(r, r));
+        if (len > 1e-20f) {
+            const f3 gm = wi * (dv * kappa);
+            const f3 gr = (gm - mu * dot(mu, gm)) * (1.0f / len);
+            g[3 * j] = gr.x;
+            g[3 * j + 1] = gr.y;
+            g[3 * j + 2] = gr.z;
+        }
+    }
+    return -T * __logf(m);
+}
+
+// Forward + loss gradient + backward through the data, 16 records at a time
+// per warp.  Stores every layer's bf16 input activation A_l (B x 64) and the
+// gradient of its output dZ_l (B x out_l, bf16) for the weight-gradient pass;
+// the backward pass reads A_l back (each thread its own fragment elements)
+// for the ReLU mask.
+__device__ __forceinline__ void store_frag_rows(__nv_bfloat16* M, const uint32_t f[4][4], int row0, int row1, int n,
+                                                int ncols, int t) {
+#pragma unroll
+    for (int kt = 0; kt < 4; kt++) {
+        const int c = kt * 16 + 2 * t;
+        if (c >= ncols) continue;
+        if (row0 < n) {
+            *reinterpret_cast<uint32_t*>(M + (size_t)row0 * 64 + c) = f[kt][0];
+            *reinterpret_cast<uint32_t*>(M + (size_t)row0 * 64 + c + 8) = f[kt][2];
+        }
+        if (row1 < n) {
+            *reinterpret_cast<uint32_t*>(M + (size_t)row1 * 64 + c) = f[kt][1];
+            *reinterpret_cast<uint32_t*>(M + (size_t)row1 * 64 + c + 8) = f[kt][3];
+        }
+    }
+}
+
+__device__ __forceinline__ void load_frag_rows(const __nv_bfloat16* M, uint32_t f[4][4], int row0, int row1, int n,
+                                               int t) {
+#pragma unroll
+    for (int kt = 0; kt < 4; kt++) {
+        const int c = kt * 16 + 2 * t;
+        f[kt][0] = row0 < n ? *reinterpret_cast<const uint32_t*>(M + (size_t)row0 * 64 + c) : 0u;
+        f[kt][2] = row0 < n ? *reinterpret_cast<const uint32_t*>(M + (size_t)row0 * 64 + c + 8) : 0u;
+        f[kt][1] = row1 < n ? *reinterpret_cast<const uint32_t*>(M + (size_t)row1 * 64 + c) : 0u;
+        f[kt][3] = row1 < n ? *reinterpret_cast<const uint32_t*>(M + (size_t)row1 * 64 + c + 8) : 0u;
+    }
+}
+
+__device__ __forceinline__ uint32_t relu_mask(uint32_t act, float lo, float hi) {
+    const __nv_bfloat162 h = *reinterpret_cast<const __nv_bfloat162*>(&act);
+    return pack_bf16(__low2float(h) > 0.f ? lo : 0.f, __high2float(h) > 0.f ? hi : 0.f);
+}
+
+__global__ void __launch_bounds__(kNNThreads) k_nn_train_fb(NNWeights W, NNNorm N, const float4* __restrict__ rec,
+                                                            int n, float inv_tsum, NNTrainBuf TB,
+                                                            float* __restrict__ loss_out) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __nv_bfloat16* s_wt = reinterpret_cast<__nv_bfloat16*>(smem);
+    __nv_bfloat16* s_w = s_wt + kNNLayers * kWLayer;
+    float* s_tile = reinterpret_cast<float*>(smem + 2 * kNNLayers * kWLayer * 2) + (threadIdx.x >> 5) * 32 * kNNOut;
+    stage_weights(W, s_wt, s_w, true);
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    float loss_acc = 0.f;
+    for (int base = warp * 32; base < n; base += nwarps * 32) {
+        const int i = base + lane;
+        NNIn mine;
+        f3 wi = mk(0.f, 0.f, 1.f);
+        float pb = 0.f, T = 0.f;
+        if (i < n) {
+            const float4 r0 = rec[4 * (size_t)i], r1 = rec[4 * (size_t)i + 1], r2 = rec[4 * (size_t)i + 2],
+                         r3 = rec[4 * (size_t)i + 3];
+            mine.pn = mk((r0.x - N.lo[0]) * N.inv_ext[0], (r0.y - N.lo[1]) * N.inv_ext[1],
+                         (r0.z - N.lo[2]) * N.inv_ext[2]);
+            mine.n = mk(r0.w, r1.x, r1.y);
+            mine.wo = mk(r1.z, r1.w, r2.x);
+            wi = mk(r2.y, r2.z, r2.w);
+            pb = r3.x;
+            T = r3.y * inv_tsum;
+        } else {
+            mine.pn = mine.n = mine.wo = mk(0.f, 0.f, 0.f);
+        }
+        for (int mt = 0; mt < 2; mt++) {
+            const int row0 = base + mt * 16 + g, row1 = row0 + 8;
+            // forward; the input of every layer goes to TB.act
+            uint32_t a[4][4];
+            float acc[8][4];
+            input_frags(mine, mt, lane, a);
+            for (int l = 0; l < kNNLayers - 1; l++) {
+                store_frag_rows(TB.act + (size_t)l * TB.cap * 64, a, row0, row1, n, 64, t);
+                hidden_layer(s_wt + l * kWLayer, lane, a, acc);
+            }
+            store_frag_rows(TB.act + (size_t)(kNNLayers - 1) * TB.cap * 64, a, row0, row1, n, 64, t);
+            {
+                float out[6][4];
+                output_layer(s_wt + (kNNLayers - 1) * kWLayer, lane, a, out);
+                store_out_tile(s_tile, out, lane);
+            }
+            __syncwarp();
+            // loss gradient of the tile's 16 records: lane mt*16 + r owns row r
+            if ((lane >> 4) == mt) {
+                const int r = lane & 15;
+                float raw[kNNOut], gr[kNNOut];
+#pragma unroll
+                for (int k = 0; k < kNNOut; k++) raw[k] = s_tile[r * kNNOut + k];
+                loss_acc += (i < n) ? nn_loss_grad(raw, wi, pb, T, N.c_lo, N.c_hi, gr) : 0.f;
+#pragma unroll
+                for (int k = 0; k < kNNOut; k++) s_tile[r * kNNOut + k] = (i < n) ? gr[k] : 0.f;
+            }
+            __syncwarp();
+            // dZ of the output layer as A fragments (k = 48 outputs, 3 k-tiles)
+            uint32_t dz[4][4];
+#pragma unroll
+            for (int kt = 0; kt < 4; kt++) {
+                const float* q0 = s_tile + g * kNNOut;
+                const float* q1 = s_tile + (g + 8) * kNNOut;
+                const int c = kt * 16 + 2 * t;
+                if (kt < 3) {
+                    dz[kt][0] = pack_bf16(q0[c], q0[c + 1]);
+                    dz[kt][1] = pack_bf16(q1[c], q1[c + 1]);
+                    dz[kt][2] = pack_bf16(q0[c + 8], q0[c + 9]);
+                    dz[kt][3] = pack_bf16(q1[c + 8], q1[c + 9]);
+                } else {
+                    dz[kt][0] = dz[kt][1] = dz[kt][2] = dz[kt][3] = 0u;
+                }
+            }
+            __syncwarp();
+            for (int l = kNNLayers - 1; l >= 0; l--) {
+                const int nout = nn_layer_out(l);
+                store_frag_rows(TB.grad + (size_t)l * TB.cap * 64, dz, row0, row1, n, nout, t);
+                if (l == 0) break;
+                // dH = dZ_l W_l^T (16 x 64); dZ_{l-1} = dH where A_l > 0
+#pragma unroll
+                for (int nt = 0; nt < 8; nt++) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
+                const int kts = (nout + 15) / 16;
+                for (int kt = 0; kt < kts; kt++)
+#pragma unroll
+                    for (int nt = 0; nt < 8; nt++) {
+                        uint32_t b[2];
+                        load_b_bwd(s_w + l * kWLayer, nt, kt, lane, b);
+                        mma_bf16(acc[nt], dz[kt], b);
+                    }
+                uint32_t al[4][4];
+                load_frag_rows(TB.act + (size_t)l * TB.cap * 64, al, row0, row1, n, t);
+#pragma unroll
+                for (int kt = 0; kt < 4; kt++) {
+                    dz[kt][0] = relu_mask(al[kt][0], acc[2 * kt][0], acc[2 * kt][1]);
+                    dz[kt][1] = relu_mask(al[kt][1], acc[2 * kt][2], acc[2 * kt][3]);
+                    dz[kt][2] = relu_mask(al[kt][2], acc[2 * kt + 1][0], acc[2 * kt + 1][1]);
+                    dz[kt][3] = relu_mask(al[kt][3], acc[2 * kt + 1][2], acc[2 * kt + 1][3]);
+                }
+            }
+        }
+    }
+    float ls = loss_acc;
+    for (int o = 16; o > 0; o >>= 1) ls += __shfl_xor_sync(0xffffffffu, ls, o);
+    if (loss_out && lane == 0) atomicAdd(loss_out, ls);
+}
+
+// dW_l = A_l^T dZ_l over the batch: one CTA reduces a slice of rows into a
+// 64 x out_l tile with mma (A^T fragments read transposed from smem), then
+// adds it to the FP32 gradient.  blockIdx.y = layer.
+constexpr int kWGRows = 64;
+__global__ void __launch_bounds__(kNNThreads) k_nn_wgrad(NNTrainBuf TB, int n, float* __restrict__ grad) {
+    __shared__ __align__(16) __nv_bfloat16 sA[kWGRows][72];
+    __shared__ __align__(16) __nv_bfloat16 sG[kWGRows][72];
+    const int l = blockIdx.y;
+    const int nout = nn_layer_out(l);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, g = lane >> 2, t = lane & 3;
+    // warp w computes rows (inputs) 16w .. 16w+15 of dW, all outputs
+    float acc[8][4];
+#pragma unroll
+    for (int nt = 0; nt < 8; nt++) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
+    const __nv_bfloat16* A = TB.act + (size_t)l * TB.cap * 64;
+    const __nv_bfloat16* G = TB.grad + (size_t)l * TB.cap * 64;
+    for (int r0 = blockIdx.x * kWGRows; r0 < n; r0 += gridDim.x * kWGRows) {
+        __syncthreads();
+        for (int e = threadIdx.x; e < kWGRows * 8; e += blockDim.x) {
+            const int r = e >> 3, c8 = (e & 7) * 8;
+            uint4 va = make_uint4(0u, 0u, 0u, 0u), vg = make_uint4(0u, 0u, 0u, 0u);
+            if (r0 + r < n) {
+                va = *reinterpret_cast<const uint4*>(A + (size_t)(r0 + r) * 64 + c8);
+                if (c8 < nout) vg = *reinterpret_cast<const uint4*>(G + (size_t)(r0 + r) * 64 + c8);
+            }
+            *reinterpret_cast<uint4*>(&sA[r][c8]) = va;
+            *reinterpret_cast<uint4*>(&sG[r][c8]) = vg;
+        }
+        __syncthreads();
+        // K = rows of the slice, 4 k-tiles of 16
+#pragma unroll
+        for (int kt = 0; kt < kWGRows / 16; kt++) {
+            // A^T fragment: element (m = input 16w+g(+8), k = row 16kt+2t(+1,+8,+9))
+            const int m0 = 16 * warp + g, k0 = 16 * kt + 2 * t;
+            uint32_t a[4];
+            a[0] = pack_bf16(__bfloat162float(sA[k0][m0]), __bfloat162float(sA[k0 + 1][m0]));
+            a[1] = pack_bf16(__bfloat162float(sA[k0][m0 + 8]), __bfloat162float(sA[k0 + 1][m0 + 8]));
+            a[2] = pack_bf16(__bfloat162float(sA[k0 + 8][m0]), __bfloat162float(sA[k0 + 9][m0]));
+            a[3] = pack_bf16(__bfloat162float(sA[k0 + 8][m0 + 8]), __bfloat162float(sA[k0 + 9][m0 + 8]));
+#pragma unroll
+            for (int nt = 0; nt < 8; nt++) {
+                if (nt * 8 >= nout) break;
+                // B fragment: element (k = row 16kt+2t(+1), n = output 8nt+g) from sG[row][out]
+                uint32_t b[2];
+                b[0] = pack_bf16(__bfloat162float(sG[k0][nt * 8 + g]), __bfloat162float(sG[k0 + 1][nt * 8 + g]));
+                b[1] = pack_bf16(__bfloat162float(sG[k0 + 8][nt * 8 + g]), __bfloat162float(sG[k0 + 9][nt * 8 + g]));
+                mma_bf16(acc[nt], a, b);
+            }
+        }
+    }
+    float* dst = grad + nn_layer_offset(l);
+#pragma unroll
+    for (int nt = 0; nt < 8; nt++) {
+        if (nt * 8 >= nout) break;
+        const int m0 = 16 * warp + g, c = nt * 8 + 2 * t;
+        atomicAdd(dst + m0 * nout + c, acc[nt][0]);
+        atomicAdd(dst + m0 * nout + c + 1, acc[nt][1]);
+        atomicAdd(dst + (m0 + 8) * nout + c, acc[nt][2]);
+        atomicAdd(dst + (m0 + 8) * nout + c + 1, acc[nt][3]);
+    }
+}
+
+// Adam (Kingma & Ba 2015) on the FP32 master weights; refreshes the two
+// BF16 copies the kernels read.
+__global__ void k_nn_adam(NNWeights W, const float* __restrict__ grad, float lr, float b1, float b2, float eps,
+                          float bc1, float bc2, float clip) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kNNWeights) return;
+    float gi = grad[i];
+    gi = fminf(fmaxf(gi, -clip), clip);
+    const float m = b1 * W.m[i] + (1.0f - b1) * gi;
+    const float v = b2 * W.v[i] + (1.0f - b2) * gi * gi;
+    W.m[i] = m;
+    W.v[i] = v;
+    const float w = W.master[i] - lr * (m / bc1) / (sqrtf(v / bc2) + eps);
+    W.master[i] = w;
+    // locate (layer, in, out)
+    int l = i / (64 * 64);
+    if (l > kNNLayers - 1) l = kNNLayers - 1;
+    const int off = i - nn_layer_offset(l), nout = nn_layer_out(l);
+    const int in = off / nout, out = off - in * nout;
+    W.wt[l * kWLayer + out * kWStride + in] = __float2bfloat16_rn(w);
+    W.w[l * kWLayer + in * kWStride + out] = __float2bfloat16_rn(w);
+}
+
+__global__ void k_nn_pack(NNWeights W) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kNNWeights) return;
+    int l = i / (64 * 64);
+    if (l > kNNLayers - 1) l = kNNLayers - 1;
+    const int off = i - nn_layer_offset(l), nout = nn_layer_out(l);
+    const int in = off / nout, out = off - in * nout;
+    const __nv_bfloat16 b = __float2bfloat16_rn(W.master[i]);
+    W.wt[l * kWLayer + out * kWStride + in] = b;
+    W.w[l * kWLayer + in * kWStride + out] = b;
+}
+
+size_t nn_smem_infer() { return (size_t)kNNLayers * kWLayer * 2 + (kNNThreads / 32) * 32 * kNNOut * 4; }
+size_t nn_smem_train() { return (size_t)2 * kNNLayers * kWLayer * 2 + (kNNThreads / 32) * 32 * kNNOut * 4; }
+size_t nn_wcopy_elems() { return (size_t)kNNLayers * kWLayer; }
+
+cudaError_t nn_set_smem_limits() {
+    cudaError_t e = cudaFuncSetAttribute(k_nn_forward_debug, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)nn_smem_infer());
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_nn_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nn_smem_infer());
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_nn_train_fb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nn_smem_train());
+}
+
+void launch_nn_pack(const NNWeights& W, cudaStream_t st) {
+    k_nn_pack<<<(kNNWeights + 255) / 256, 256, 0, st>>>(W);
+}
+void launch_nn_forward_debug(const NNWeights& W, const NNNorm& N, const float* in, int n, float* out, int num_sms,
+                             cudaStream_t st) {
+    const int blocks = std::max(1, std::min(num_sms * 4, (n + kNNThreads - 1) / kNNThreads));
+    k_nn_forward_debug<<<blocks, kNNThreads, nn_smem_infer(), st>>>(W, N, in, n, out);
+}
+void launch_nn_infer(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, const NNWeights& W,
+                     const NNNorm& N, float4* params, int num_sms, cudaStream_t st) {
+    k_nn_infer<<<num_sms * 4, kNNThreads, nn_smem_infer(), st>>>(S, B, cur, ctr, W, N, params);
+}
+void launch_nn_train_step(const NNWeights& W, const NNNorm& N, const float4* rec, int n, float tsum,
+                          const NNTrainBuf& TB, float* grad, float* loss, const NNAdam& opt, int step, int num_sms,
+                          cudaStream_t st, bool apply) {
+    cudaMemsetAsync(grad, 0, sizeof(float) * kNNWeights, st);
+    const int blocks = std::max(1, std::min(num_sms * 4, (n + kNNThreads - 1) / kNNThreads));
+    k_nn_train_fb<<<blocks, kNNThreads, nn_smem_train(), st>>>(W, N, rec, n, tsum > 0.f ? 1.0f / tsum : 0.f, TB,
+                                                               loss);
+    dim3 gw(std::max(1, std::min(num_sms, (n + kWGRows - 1) / kWGRows)), kNNLayers);
+    k_nn_wgrad<<<gw, kNNThreads, 0, st>>>(TB, n, grad);
+    if (apply) {
+        const float bc1 = 1.0f - powf(opt.b1, (float)step), bc2 = 1.0f - powf(opt.b2, (float)step);
+        k_nn_adam<<<(kNNWeights + 255) / 256, 256, 0, st>>>(W, grad, opt.lr, opt.b1, opt.b2, opt.eps, bc1, bc2,
+                                                            opt.clip);
+    }
+}
+
+
+
+// ===========================================================================
+// Learned-guide integrator: PT + NEE + MIS where the directional sample comes
+// from the one-sample mixture c * BSDF + (1 - c) * guide.  MIS weights use
+// the mixture pdf; Russian roulette survival min(rr, 1) only rescales the
+// throughput (unbiased; the plain tracer's PT_FLAG_UNBIASED_MIS mode is the
+// same estimator with c = 1, so both converge to the same image).
+// Training data: a path keeps, per surface vertex, the inputs, the sampled
+// direction, its pdfs, the throughput before the bounce and the film total
+// after the vertex's own NEE; when the path ends each vertex yields
+// T = luminance((S_end - S_k) / throughput_k), the importance-weighted
+// integrand along the sampled direction.
+// ===========================================================================
+
+__device__ __forceinline__ float luminance(f3 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
+
+__device__ __forceinline__ void film_add_nn(unsigned long long* film, int pix, f3 c, WaveCounters* ctr) {
+    if (!isfinite(c.x) || !isfinite(c.y) || !isfinite(c.z)) {
+        atomicAdd(&ctr->stat_nonfinite, 1ull);
+        return;
+    }
+    const float s = 4294967296.0f;
+    if (c.x != 0.f) atomicAdd(film + 3 * pix, (unsigned long long)__float2ll_rn(c.x * s));
+    if (c.y != 0.f) atomicAdd(film + 3 * pix + 1, (unsigned long long)__float2ll_rn(c.y * s));
+    if (c.z != 0.f) atomicAdd(film + 3 * pix + 2, (unsigned long long)__float2ll_rn(c.z * s));
+}
+
+__device__ __forceinline__ int warp_append_nn(int* counter, bool pred) {
+    const unsigned mask = __ballot_sync(0xffffffffu, pred);
+    if (mask == 0) return -1;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(counter, __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    return pred ? base + __popc(mask & ((1u << lane) - 1u)) : -1;
+}
+
+// Vertex record k of a path slot (5 float4): 0: pos xyz, n.x  1: n.yz, wo.xy
+// 2: wo.z, wi xyz  3: p_bsdf(wi), throughput before the bounce (rgb)
+// 4: film total after the vertex's own NEE (rgb), valid (guide-sampled, non-delta).
+__global__ void __launch_bounds__(256) k_shade_nn(DevScene S, PathBuffers B, int cur, RenderParams P,
+                                                  WaveCounters* ctr, unsigned long long* __restrict__ film,
+                                                  const float4* __restrict__ params, NNPathData PD, int guided) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = ctr->n_cur;
+    bool push_sh = false, push_cont = false, release = false;
+    float4 sh_o, sh_d, sh_c, no, nd, nt;
+    int4 ninfo;
+    int slot = -1, fin_bounce = 0;
+    if (i < n) {
+        const float4 O = B.o[cur][i], D = B.d[cur][i], Tp = B.thr[cur][i];
+        const int4 I = B.info[cur][i];
+        const float4 H = B.hit[i];
+        const int prim = __float_as_int(H.y);
+        const int pixel = I.x, sample = I.y, bounce = I.z & 0xffff;
+        const bool sdelta = (I.z >> 16) & 1;
+        slot = I.w;
+        const size_t vbase = (size_t)slot * P.max_depth;
+        const float p = O.w;
+        f3 mul = mk(Tp.x, Tp.y, Tp.z);
+        const f3 ro = mk(O.x, O.y, O.z), rd = mk(D.x, D.y, D.z);
+        const bool train = PD.rec_cap > 0;  // vertex records and running totals only while training
+        f3 Ssum = train ? f3of(PD.acc[slot]) : mk(0.f, 0.f, 0.f);
+        if (train && bounce > 0) {  // the previous vertex's incident radiance is what arrives from now on
+            const float w4 = PD.vert[5 * (vbase + bounce - 1) + 4].w;
+            PD.vert[5 * (vbase + bounce - 1) + 4] = make_float4(Ssum.x, Ssum.y, Ssum.z, w4);
+        }
+        bool done = true;
+        if (prim >= 0) {
+            int kind;
+            DevMaterial m;
+            const Surf s = make_surf(S, prim, ro, rd, H.x, H.z, H.w, bounce == 0, &kind, &m);
+            const f3 wo = -rd;
+            if (kind == PT_MAT_EMISSIVE_) {
+                float w = 1.0f;
+                if (!sdelta) {
+                    const int4 vi = __ldg(S.tri_vidx + prim);
+                    const f3 a = f3of(__ldg(S.v_pos + vi.x)), b = f3of(__ldg(S.v_pos + vi.y)),
+                             c = f3of(__ldg(S.v_pos + vi.z));
+                    const float area = length(cross(b - a, c - a)) * 0.5f;
+                    const float pdf_l = (1.0f / (float)S.n_lights) * (1.0f / area);
+                    const float r = H.x;
+                    const float p_nee = pdf_l * r * r / (fabsf(dot(s.n, rd)) + kEps);
+                    w = p / (p + p_nee);
+                }
+                const f3 c = mul * mk(m.r, m.g, m.b) * w;
+                film_add_nn(film, pixel, c, ctr);
+                Ssum = Ssum + c;
+            } else {
+                const Rng4 r0 = rng4(P.seed, sample, pixel, bounce, 0);
+                const Rng4 r1 = rng4(P.seed, sample, pixel, bounce, 1);
+                const bool delta_mat = (m.kind == PT_MAT_DIELECTRIC_) || (m.kind == PT_MAT_GGX_ && m.delta);
+                float prm[kNNParams];
+                float c = 1.0f;
+                if (guided && !delta_mat) {
+                    const float4* pp = params + 11 * (size_t)i;
+#pragma unroll
+                    for (int k = 0; k < 10; k++) {
+                        const float4 q = pp[k];
+                        prm[4 * k] = q.x; prm[4 * k + 1] = q.y; prm[4 * k + 2] = q.z; prm[4 * k + 3] = q.w;
+                    }
+                    prm[40] = pp[10].x;
+                    c = prm[40];
+                }
+                BSample bs;
+                float pmix;
+                if (r1.v[3] < c) {
+                    bs = bsdf_sample(m, s, wo, r0.v[0], r0.v[1]);
+                    pmix = (bs.delta || c >= 1.0f) ? bs.pdf : c * bs.pdf + (1.0f - c) * nn_mix_pdf(prm, bs.wi);
+                } else {
+                    bs.wi = nn_mix_sample(prm, r0.v[0], r0.v[1], r1.v[2]);
+                    bs.delta = false;
+                    bs.pdf = bsdf_pdf(m, s, wo, bs.wi);
+                    pmix = c * bs.pdf + (1.0f - c) * nn_mix_pdf(prm, bs.wi);
+                }
+                if (!bs.delta && S.n_lights > 0) {  // NEE; the MIS weight uses the mixture pdf
+                    const LSample ls = sample_light(S, s.p, r0.v[2], r0.v[3], r1.v[0]);
+                    f3 sd = ls.pos - s.p;
+                    const float len = length(sd);
+                    sd = sd * (1.0f / len);
+                    if (same_hemisphere(s, wo, sd)) {
+                        float pb = bsdf_pdf(m, s, wo, sd);
+                        if (c < 1.0f) pb = c * pb + (1.0f - c) * nn_mix_pdf(prm, sd);
+                        const float pn = ls.pdf * len * len / (fabsf(dot(ls.n, sd)) + kEps);
+                        const float w = pn / (pb + pn);
+                        const f3 f = bsdf_eval(m, s, wo, sd);
+                        const f3 cc = mul * f * ls.le * (1.0f / (ls.pdf * len * len)) * w;
+                        if (cc.x != 0.f || cc.y != 0.f || cc.z != 0.f) {
+                            push_sh = true;
+                            const f3 so = s.p + sd * kEps;
+                            sh_o = make_float4(so.x, so.y, so.z, len - 2.0f * kEps);
+                            sh_d = make_float4(sd.x, sd.y, sd.z, __int_as_float(pixel));
+                            sh_c = make_float4(cc.x, cc.y, cc.z, __int_as_float(slot));
+                        }
+                    }
+                }
+                if (train) {  // this vertex's training record (completed when the path ends)
+                    const size_t vi = 5 * (vbase + bounce);
+                    PD.vert[vi] = make_float4(s.p.x, s.p.y, s.p.z, s.n.x);
+                    PD.vert[vi + 1] = make_float4(s.n.y, s.n.z, wo.x, wo.y);
+                    PD.vert[vi + 2] = make_float4(wo.z, bs.wi.x, bs.wi.y, bs.wi.z);
+                    PD.vert[vi + 3] = make_float4(bs.delta ? 0.f : bs.pdf, mul.x, mul.y, mul.z);
+                    PD.vert[vi + 4] = make_float4(0.f, 0.f, 0.f, bs.delta ? 0.f : 1.f);
+                }
+                if (same_hemisphere(s, wo, bs.wi) && pmix > 0.f) {
+                    const f3 f = bsdf_eval(m, s, wo, bs.wi);
+                    bool alive = true;
+                    float surv = 1.0f;
+                    if (bounce >= P.rr_start) {  // survival min(rr, 1): unbiased
+                        surv = fminf(russian_roulette(f), 1.0f);
+                        if (r1.v[1] > surv) alive = false;
+                    }
+                    if (alive && bounce + 1 < P.max_depth) {
+                        mul = mul * f * (1.0f / (pmix * surv));
+                        const f3 oo = s.p + bs.wi * kEps;
+                        push_cont = true;
+                        done = false;
+                        no = make_float4(oo.x, oo.y, oo.z, pmix);
+                        nd = make_float4(bs.wi.x, bs.wi.y, bs.wi.z, 0.f);
+                        nt = make_float4(mul.x, mul.y, mul.z, 0.f);
+                        ninfo = make_int4(pixel, sample, (bounce + 1) | ((bs.delta ? 1 : 0) << 16), slot);
+                    }
+                }
+            }
+        }
+        if (train) PD.acc[slot] = make_float4(Ssum.x, Ssum.y, Ssum.z, 0.f);
+        // vertices 0 .. bounce-1 had their sampled direction traced; the
+        // records are emitted once this vertex's shadow ray has resolved
+        fin_bounce = bounce;
+        release = done;
+    }
+    const int js = warp_append_nn(&ctr->n_shadow, push_sh);
+    if (push_sh) {
+        B.sh_o[js] = sh_o;
+        B.sh_d[js] = sh_d;
+        B.sh_c[js] = sh_c;
+    }
+    const int jc = warp_append_nn(&ctr->n_next, push_cont);
+    if (push_cont) {
+        const int nx = 1 - cur;
+        B.o[nx][jc] = no;
+        B.d[nx][jc] = nd;
+        B.thr[nx][jc] = nt;
+        B.info[nx][jc] = ninfo;
+    }
+    const int jf = warp_append_nn(&ctr->n_fin, release);
+    if (release) PD.fin[jf] = make_int2(slot, fin_bounce);
+}
+
+// Finished paths: vertex k's target is the film total gathered after its own
+// NEE, T = lum((S_end - S_k) / throughput_k), i.e. the one-sample estimate of
+// f cos L_i / p_mix along the traced direction wi.
+__global__ void __launch_bounds__(256) k_finish_nn(NNPathData PD, WaveCounters* ctr, int max_depth) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = ctr->n_fin;
+    bool release = false;
+    int slot = 0;
+    if (i < n) {
+        const int2 f = PD.fin[i];
+        slot = f.x;
+        release = true;
+        if (PD.rec_cap > 0) {
+            const float4 Se = PD.acc[slot];
+            const size_t vbase = (size_t)slot * max_depth;
+            for (int k = 0; k < f.y; k++) {
+                const float4* vr = PD.vert + 5 * (vbase + k);
+                const float4 v3 = vr[3], v4 = vr[4];
+                if (v4.w == 0.f) continue;
+                const f3 dS = mk(Se.x - v4.x, Se.y - v4.y, Se.z - v4.z);
+                const f3 q = mk(v3.y > 0.f ? dS.x / v3.y : 0.f, v3.z > 0.f ? dS.y / v3.z : 0.f,
+                                v3.w > 0.f ? dS.z / v3.w : 0.f);
+                const float T = luminance(q);
+                if (!(T > 0.f) || !isfinite(T)) continue;
+                const int r = atomicAdd(&ctr->n_rec, 1);
+                if (r >= PD.rec_cap) break;
+                float4* o = PD.rec + 4 * (size_t)r;
+                o[0] = vr[0];
+                o[1] = vr[1];
+                o[2] = vr[2];
+                o[3] = make_float4(v3.x, T, 0.f, 0.f);
+            }
+        }
+    }
+    const int jr = warp_append_nn(&ctr->free_top, release);
+    if (release) PD.slot_stack[jr] = slot;
+}
+
+// NEE shadow rays of the learned-guide integrator: unoccluded contributions
+// go to the film and to the owning path's running total (for its training
+// targets).
+__global__ void __launch_bounds__(256) k_shadow_nn(DevScene S, PathBuffers B, WaveCounters* ctr,
+                                                   unsigned long long* __restrict__ film, NNPathData PD) {
+    __shared__ uint4 snodes[kSmemNodes * 4];
+    const int n = ctr->n_shadow;
+    if (n == 0) return;
+    const int nn = min(S.n_nodes, kSmemNodes) * 4;
+    for (int k = threadIdx.x; k < nn; k += blockDim.x) snodes[k] = __ldg(S.nodes + k);
+    __syncthreads();
+    TraceCount cnt{0u, 0u};
+    persistent_trace<true, false>(
+        S, snodes, n, &ctr->fetch_sh, &ctr->status, cnt,
+        [&](int i, float3& o, float3& d, float& tmax, uint32_t& root) {
+            const float4 a = B.sh_o[i], b = B.sh_d[i];
+            o = make_float3(a.x, a.y, a.z);
+            d = make_float3(b.x, b.y, b.z);
+            tmax = a.w;
+        },
+        [&](int i, const HitRec& h) {
+            if (h.prim < 0) {
+                const float4 c = B.sh_c[i];
+                const f3 cc = mk(c.x, c.y, c.z);
+                film_add_nn(film, __float_as_int(B.sh_d[i].w), cc, ctr);
+                if (PD.rec_cap > 0) {
+                    const int slot = __float_as_int(c.w);
+                    const float4 a = PD.acc[slot];
+                    PD.acc[slot] = make_float4(a.x + cc.x, a.y + cc.y, a.z + cc.z, 0.f);
+                }
+            }
+        });
+}
+
+// Camera paths (stratified like pathtracerMIS.h:148-153) with a vertex slot.
+__global__ void __launch_bounds__(256) k_generate_nn(DevScene S, PathBuffers B, int cur, RenderParams P,
+                                                     WaveCounters* ctr, NNPathData PD) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n_next = ctr->n_next;
+    const int avail = min(B.capacity - n_next, ctr->free_top);
+    const unsigned long long w = ctr->work_next + (unsigned long long)t;
+    if (t >= avail || w >= ctr->work_total) return;
+    const unsigned long long npix = (unsigned long long)P.width * P.height;
+    const int sample = (int)(w / npix);
+    const int pixel = (int)(w - (unsigned long long)sample * npix);
+    const int px = pixel % P.width, py = pixel / P.width;
+    const Rng4 r = rng4(P.seed, sample, pixel, 0xffffu, 2);
+    float cx, cy;
+    if (P.spp_axis > 0) {
+        const int k = sample / P.spp_axis, l = sample - (sample / P.spp_axis) * P.spp_axis;
+        cx = (((float)px + ((float)k + r.v[0]) / (float)P.spp_axis) / (float)P.width) * 2.0f - 1.0f;
+        cy = -((((float)py + ((float)l + r.v[1]) / (float)P.spp_axis) / (float)P.height) * 2.0f - 1.0f);
+    } else {
+        cx = (((float)px + r.v[0]) / (float)P.width) * 2.0f - 1.0f;
+        cy = -((((float)py + r.v[1]) / (float)P.height) * 2.0f - 1.0f);
+    }
+    const DevCamera& C = S.cam;
+    const float dx = cx * C.tan_fovy * C.aspect, dy = cy * C.tan_fovy, dz = -1.0f;
+    const f3 d = normalized(mk(C.m[0] * dx + C.m[1] * dy + C.m[2] * dz, C.m[3] * dx + C.m[4] * dy + C.m[5] * dz,
+                               C.m[6] * dx + C.m[7] * dy + C.m[8] * dz));
+    const int nx = 1 - cur;
+    const int j = n_next + t;
+    const int slot = PD.slot_stack[ctr->free_top - 1 - t];
+    PD.acc[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+    B.o[nx][j] = make_float4(C.o[0], C.o[1], C.o[2], 1.0f);
+    B.d[nx][j] = make_float4(d.x, d.y, d.z, 0.f);
+    B.thr[nx][j] = make_float4(1.f, 1.f, 1.f, 0.f);
+    B.info[nx][j] = make_int4(pixel, sample, 1 << 16, slot);
+}
+
+__global__ void k_advance_nn(WaveCounters* ctr, int capacity) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int n_next = ctr->n_next;
+    const unsigned long long left = ctr->work_total - ctr->work_next;
+    unsigned long long room = (unsigned long long)(capacity - n_next);
+    if ((unsigned long long)ctr->free_top < room) room = (unsigned long long)ctr->free_top;
+    const unsigned long long added = left < room ? left : room;
+    ctr->work_next += added;
+    ctr->stat_paths += added;
+    ctr->stat_shadow += (unsigned long long)ctr->n_shadow;
+    ctr->free_top -= (int)added;
+    ctr->n_cur = n_next + (int)added;
+    ctr->stat_closest += (unsigned long long)ctr->n_cur;
+    ctr->n_next = 0;
+    ctr->n_shadow = 0;
+    ctr->n_fin = 0;
+    ctr->fetch_ext = 0;
+    ctr->fetch_sh = 0;
+    ctr->stat_iters += 1;
+}
+
+__global__ void k_sum_T(const float4* __restrict__ rec, int n, float* out) {
+    float s = 0.f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) s += rec[4 * (size_t)i + 3].y;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, s);
+}
+
+void launch_nn_shade(const DevScene& S, const PathBuffers& B, int cur, const RenderParams& P, WaveCounters* ctr,
+                     unsigned long long* film, const float4* params, const NNPathData& PD, bool guided,
+                     cudaStream_t st) {
+    k_shade_nn<<<(B.capacity + 255) / 256, 256, 0, st>>>(S, B, cur, P, ctr, film, params, PD, guided ? 1 : 0);
+}
+void launch_nn_shadow(const DevScene& S, const PathBuffers& B, WaveCounters* ctr, unsigned long long* film,
+                      const NNPathData& PD, int num_sms, cudaStream_t st) {
+    k_shadow_nn<<<num_sms * 4, 256, 0, st>>>(S, B, ctr, film, PD);
+}
+void launch_nn_generate(const DevScene& S, const PathBuffers& B, int cur, const RenderParams& P, WaveCounters* ctr,
+                        const NNPathData& PD, cudaStream_t st) {
+    k_generate_nn<<<(B.capacity + 255) / 256, 256, 0, st>>>(S, B, cur, P, ctr, PD);
+    k_advance_nn<<<1, 32, 0, st>>>(ctr, B.capacity);
+}
+void launch_nn_finish(const NNPathData& PD, WaveCounters* ctr, int max_depth, int capacity, cudaStream_t st) {
+    k_finish_nn<<<(capacity + 255) / 256, 256, 0, st>>>(PD, ctr, max_depth);
+}
+void launch_sum_T(const float4* rec, int n, float* out, cudaStream_t st) {
+    k_sum_T<<<std::max(1, std::min(1024, (n + 255) / 256)), 256, 0, st>>>(rec, n, out);
+}
+
+}  // namespace cpppt_gb300

@@ -1,0 +1,141 @@
+// Learned path guide: network layout, input encoding and the von Mises-Fisher
+// mixture it outputs.  (No counterpart in the reference, which has only the
+// SD-tree guide; the learned guide is compared against it and against plain
+// PT.)
+//
+// Network: 64 inputs -> 64 -> 64 -> 64 (ReLU) -> 48 outputs, no biases
+// (the constant input feature acts as one), BF16 weights and activations,
+// FP32 accumulation (mma.sync m16n8k16 bf16).
+// Inputs (64): frequency encoding of the position normalised to the scene
+// box (3 axes x 8 octaves x sin/cos = 48), shading normal (3), direction to
+// the previous vertex wo (3), 1, zero padding.
+// Outputs (48): 8 lobes x (mean direction raw xyz) = 24, 8 concentrations,
+// 8 mixture logits, 1 selection logit, 7 unused.
+// Mixture: lobe j has mean mu_j = normalise(raw), kappa_j = softplus(raw) +
+// 0.1 (clamped to 5e3), weight w_j = softmax; the guide is chosen with
+// probability 1 - c where c = c_lo + (c_hi - c_lo) sigmoid(selection logit)
+// is the BSDF fraction; c_lo >= 0.1 (default range [0.1, 0.9]) keeps BSDF
+// sampling at 10% or more, so the estimator stays unbiased wherever the BSDF
+// is non-zero.
+#pragma once
+#include <cuda_bf16.h>
+
+#include "shade.cuh"
+
+namespace cpppt_gb300 {
+
+constexpr int kNNIn = 64;
+constexpr int kNNHidden = 64;
+constexpr int kNNOut = 48;
+constexpr int kNNLobes = 8;
+constexpr int kNNLayers = 4;  // 64x64, 64x64, 64x64, 64x48
+// weights: three 64x64 matrices and one 64x48, in->out
+constexpr int kNNWeights = 3 * 64 * 64 + 64 * 48;
+constexpr int kNNParams = 41;  // post-processed mixture per sample: 8 x (mu xyz, kappa, w) + c
+
+__host__ __device__ constexpr int nn_layer_out(int l) { return l == kNNLayers - 1 ? kNNOut : kNNHidden; }
+__host__ __device__ constexpr int nn_layer_offset(int l) { return l * 64 * 64; }
+
+// Input feature j of a sample (pos already normalised to [0,1]^3).
+__device__ __forceinline__ float nn_feature(int j, f3 pn, f3 n, f3 wo) {
+    if (j < 48) {
+        const int c = j >> 4, k = (j >> 1) & 7;
+        const float x = c == 0 ? pn.x : (c == 1 ? pn.y : pn.z);
+        const float a = x * (float)(1 << k) * kPi;
+        return (j & 1) ? __cosf(a) : __sinf(a);
+    }
+    switch (j) {
+        case 48: return n.x;
+        case 49: return n.y;
+        case 50: return n.z;
+        case 51: return wo.x;
+        case 52: return wo.y;
+        case 53: return wo.z;
+        case 54: return 1.0f;
+        default: return 0.0f;
+    }
+}
+
+__device__ __forceinline__ float softplusf(float x) { return x > 15.f ? x : log1pf(__expf(x)); }
+
+// vMF lobe pdf over the sphere: kappa / (2 pi (1 - e^{-2 kappa})) e^{kappa (mu.w - 1)}
+__device__ __forceinline__ float vmf_pdf(f3 mu, float kappa, f3 w) {
+    const float norm = kappa / (2.0f * kPi * (-expm1f(-2.0f * kappa)));
+    return norm * __expf(kappa * (dot(mu, w) - 1.0f));
+}
+
+// Sampling a vMF lobe (Jakob 2012, "Numerically stable sampling of the von
+// Mises-Fisher distribution on S^2"): cos = 1 + log(u1 + (1-u1) e^{-2 kappa}) / kappa.
+__device__ __forceinline__ f3 vmf_sample(f3 mu, float kappa, float u1, float u2) {
+    const float w = 1.0f + __logf(u1 + (1.0f - u1) * __expf(-2.0f * kappa)) / kappa;
+    const float cw = fminf(1.0f, fmaxf(-1.0f, w));
+    const float sw = sqrtf(fmaxf(0.0f, 1.0f - cw * cw));
+    float sp, cp;
+    sincosf(2.0f * kPi * u2, &sp, &cp);
+    // orthonormal basis around mu (Duff et al. 2017, "Building an Orthonormal Basis, Revisited")
+    const float sign = copysignf(1.0f, mu.z);
+    const float a = -1.0f / (sign + mu.z);
+    const float b = mu.x * mu.y * a;
+    const f3 t = mk(1.0f + sign * mu.x * mu.x * a, sign * b, -sign * mu.x);
+    const f3 bt = mk(b, sign + mu.y * mu.y * a, -mu.y);
+    return t * (sw * cp) + bt * (sw * sp) + mu * cw;
+}
+
+// Mixture parameters of one sample, post-processed from the raw outputs.
+struct NNMix {
+    f3 mu[kNNLobes];
+    float kappa[kNNLobes];
+    float w[kNNLobes];
+    float c;  // probability of sampling the BSDF
+};
+
+__device__ __forceinline__ void nn_postprocess(const float* raw, float* out /*41*/, float c_lo, float c_hi) {
+    float mx = -1e30f;
+    for (int j = 0; j < kNNLobes; j++) mx = fmaxf(mx, raw[32 + j]);
+    float e[kNNLobes], sum = 0.f;
+    for (int j = 0; j < kNNLobes; j++) { e[j] = __expf(raw[32 + j] - mx); sum += e[j]; }
+    for (int j = 0; j < kNNLobes; j++) {
+        f3 m = mk(raw[3 * j], raw[3 * j + 1], raw[3 * j + 2]);
+        const float l = sqrtf(dot(m, m));
+        m = l > 1e-20f ? m * (1.0f / l) : mk(0.f, 0.f, 1.f);
+        out[5 * j] = m.x;
+        out[5 * j + 1] = m.y;
+        out[5 * j + 2] = m.z;
+        out[5 * j + 3] = fminf(softplusf(raw[24 + j]) + 0.1f, 5000.0f);
+        out[5 * j + 4] = e[j] / sum;
+    }
+    out[40] = c_lo + (c_hi - c_lo) / (1.0f + __expf(-raw[40]));
+}
+
+__device__ __forceinline__ float nn_mix_pdf(const float* p /*41*/, f3 w) {
+    float pdf = 0.f;
+    for (int j = 0; j < kNNLobes; j++)
+        pdf += p[5 * j + 4] * vmf_pdf(mk(p[5 * j], p[5 * j + 1], p[5 * j + 2]), p[5 * j + 3], w);
+    return pdf;
+}
+
+__device__ __forceinline__ f3 nn_mix_sample(const float* p /*41*/, float u0, float u1, float u2) {
+    int j = kNNLobes - 1;
+    float acc = 0.f;
+    for (int k = 0; k < kNNLobes; k++) {
+        acc += p[5 * k + 4];
+        if (u0 < acc) { j = k; break; }
+    }
+    return vmf_sample(mk(p[5 * j], p[5 * j + 1], p[5 * j + 2]), p[5 * j + 3], u1, u2);
+}
+
+// ---- bf16 tensor-core helpers (mma.sync m16n8k16, row.col, f32 accumulate) ----
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+__device__ __forceinline__ void mma_bf16(float c[4], const uint32_t a[4], const uint32_t b[2]) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+}  // namespace cpppt_gb300

@@ -61,7 +61,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_closest(DevScene S, con
     TraceCount cnt{0u, 0u};
     persistent_trace<false, false>(
         S, snodes, n, counter, status, cnt,
-        [&](int i, float3& o, float3& d, float& tmax) {
+        [&](int i, float3& o, float3& d, float& tmax, uint32_t& root) {
             const float* r = rays + 7 * (size_t)i;
             o = make_float3(r[0], r[1], r[2]);
             d = make_float3(r[3], r[4], r[5]);
@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_any(DevScene S, const f
     TraceCount cnt{0u, 0u};
     persistent_trace<true, false>(
         S, snodes, n, counter, status, cnt,
-        [&](int i, float3& o, float3& d, float& tmax) {
+        [&](int i, float3& o, float3& d, float& tmax, uint32_t& root) {
             const float* r = rays + 7 * (size_t)i;
             o = make_float3(r[0], r[1], r[2]);
             d = make_float3(r[3], r[4], r[5]);
@@ -108,7 +108,7 @@ void launch_trace_any(const DevScene& S, const float* rays, int n, uint8_t* occ,
 // Integer addition is associative, so a render's image does not depend on
 // the order in which contributions arrive (bit-identical across schedules,
 // batch sizes and launch shapes).  The final division by spp happens in FP64.
-__device__ __forceinline__ void film_add(unsigned long long* film, int pix, float r, float g, float b,
+__device__ __forceinline__ void film_add(unsigned long long* film, size_t pix, float r, float g, float b,
                                          WaveCounters* ctr) {
     if (!isfinite(r) || !isfinite(g) || !isfinite(b)) {
         atomicAdd(&ctr->stat_nonfinite, 1ull);
@@ -132,11 +132,12 @@ __global__ void __launch_bounds__(kTraceThreads) k_extend(DevScene S, PathBuffer
     TraceCount cnt{0u, 0u};
     persistent_trace<false, COUNT>(
         S, snodes, n, &ctr->fetch_ext, &ctr->status, cnt,
-        [&](int i, float3& o, float3& d, float& tmax) {
+        [&](int i, float3& o, float3& d, float& tmax, uint32_t& root) {
             const float4 a = O[i], b = D[i];
             o = make_float3(a.x, a.y, a.z);
             d = make_float3(b.x, b.y, b.z);
             tmax = __int_as_float(0x7f800000);
+            if (root != kTravDone) root = __float_as_uint(b.w);  // the path's scene root (0 unbatched)
         },
         [&](int i, const HitRec& h) { Hout[i] = make_float4(h.t, __int_as_float(h.prim), h.beta, h.gamma); });
     if (COUNT) {
@@ -158,22 +159,28 @@ __global__ void __launch_bounds__(kTraceThreads) k_shadow(DevScene S, PathBuffer
     TraceCount cnt{0u, 0u};
     persistent_trace<true, false>(
         S, snodes, n, &ctr->fetch_sh, &ctr->status, cnt,
-        [&](int i, float3& o, float3& d, float& tmax) {
+        [&](int i, float3& o, float3& d, float& tmax, uint32_t& root) {
             const float4 a = B.sh_o[i], b = B.sh_d[i];
             o = make_float3(a.x, a.y, a.z);
             d = make_float3(b.x, b.y, b.z);
             tmax = a.w;
+            if (root != kTravDone) root = __float_as_uint(B.sh_c[i].w);
         },
         [&](int i, const HitRec& h) {
             if (h.prim < 0) {  // unoccluded: the NEE contribution reaches the film
                 const float4 c = B.sh_c[i];
-                film_add(film, __float_as_int(B.sh_d[i].w), c.x, c.y, c.z, ctr);
+                film_add(film, (uint32_t)__float_as_int(B.sh_d[i].w), c.x, c.y, c.z, ctr);
             }
         });
 }
 
+// BATCH: paths of several scenes of a merged arena; info.w is the path's
+// job, whose table entry replaces the render parameters, light list and film
+// offset.  The per-path arithmetic is the same in both forms.
+template <bool BATCH>
 __global__ void __launch_bounds__(256) k_shade(DevScene S, PathBuffers B, int cur, RenderParams P, WaveCounters* ctr,
-                                               unsigned long long* __restrict__ film) {
+                                               unsigned long long* __restrict__ film,
+                                               const DevBatchJob* __restrict__ jobs) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = ctr->n_cur;
     bool push_sh = false, push_cont = false;
@@ -186,6 +193,20 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, PathBuffers B, int cu
         const int prim = __float_as_int(H.y);
         const int pixel = I.x, sample = I.y, bounce = I.z & 0xffff;
         const bool sdelta = (I.z >> 16) & 1;
+        uint32_t seed = P.seed;
+        int rr_start = P.rr_start, max_depth = P.max_depth;
+        size_t fpix = (uint32_t)pixel;
+        if (BATCH) {
+            const DevBatchJob* J = jobs + I.w;
+            seed = J->seed;
+            rr_start = J->rr_start;
+            max_depth = J->max_depth;
+            fpix += J->film_off;
+            const int lo = J->light_off;
+            S.light_prim += lo;
+            S.light_area += lo;
+            S.n_lights = J->n_lights;
+        }
         float p = O.w;
         f3 mul = mk(T.x, T.y, T.z);
         const f3 ro = mk(O.x, O.y, O.z), rd = mk(D.x, D.y, D.z);
@@ -207,10 +228,10 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, PathBuffers B, int cu
                     const float p_nee = pdf_l * r * r / cos_theta;
                     w = p / (p + p_nee);
                 }
-                film_add(film, pixel, mul.x * m.r * w, mul.y * m.g * w, mul.z * m.b * w, ctr);
+                film_add(film, fpix, mul.x * m.r * w, mul.y * m.g * w, mul.z * m.b * w, ctr);
             } else {
-                const Rng4 r0 = rng4(P.seed, sample, pixel, bounce, 0);
-                const Rng4 r1 = rng4(P.seed, sample, pixel, bounce, 1);
+                const Rng4 r0 = rng4(seed, sample, pixel, bounce, 0);
+                const Rng4 r1 = rng4(seed, sample, pixel, bounce, 1);
                 const BSample bs = bsdf_sample(m, s, wo, r0.v[0], r0.v[1]);
                 p = bs.pdf;
                 if (!bs.delta && S.n_lights > 0) {  // NEE, pathtracerMIS.h:79-106
@@ -229,27 +250,27 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, PathBuffers B, int cu
                             push_sh = true;
                             const f3 so = s.p + sd * kEps;
                             sh_o = make_float4(so.x, so.y, so.z, len - 2.0f * kEps);
-                            sh_d = make_float4(sd.x, sd.y, sd.z, __int_as_float(pixel));
-                            sh_c = make_float4(c.x, c.y, c.z, 0.f);
+                            sh_d = make_float4(sd.x, sd.y, sd.z, __int_as_float((int)(uint32_t)fpix));
+                            sh_c = make_float4(c.x, c.y, c.z, D.w);  // w: the scene root
                         }
                     }
                 }
                 if (same_hemisphere(s, wo, bs.wi)) {  // pathtracerMIS.h:112-126
                     const f3 f = bsdf_eval(m, s, wo, bs.wi);
                     bool alive = true;
-                    if (bounce >= P.rr_start) {
+                    if (bounce >= rr_start) {
                         const float rr = russian_roulette(f);
                         if (r1.v[1] > rr) alive = false;
                         else p = p * rr;
                     }
-                    if (alive && bounce + 1 < P.max_depth) {
+                    if (alive && bounce + 1 < max_depth) {
                         mul = mul * f * (1.0f / p);
                         const f3 oo = s.p + bs.wi * kEps;
                         push_cont = true;
                         no = make_float4(oo.x, oo.y, oo.z, p);
-                        nd = make_float4(bs.wi.x, bs.wi.y, bs.wi.z, 0.f);
+                        nd = make_float4(bs.wi.x, bs.wi.y, bs.wi.z, D.w);
                         nt = make_float4(mul.x, mul.y, mul.z, 0.f);
-                        ninfo = make_int4(pixel, sample, (bounce + 1) | ((bs.delta ? 1 : 0) << 16), 0);
+                        ninfo = make_int4(pixel, sample, (bounce + 1) | ((bs.delta ? 1 : 0) << 16), I.w);
                     }
                 }
             }
@@ -271,38 +292,64 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, PathBuffers B, int cu
     }
 }
 
+// Index of the job whose work range holds w (job work ranges ascend).
+__device__ __forceinline__ int find_job(const DevBatchJob* __restrict__ jobs, int n_jobs, unsigned long long w) {
+    int lo = 0, hi = n_jobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&jobs[mid].work_begin) <= w) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <bool BATCH>
 __global__ void __launch_bounds__(256) k_generate(DevScene S, PathBuffers B, int cur, RenderParams P,
-                                                  WaveCounters* ctr) {
+                                                  WaveCounters* ctr, const DevBatchJob* __restrict__ jobs,
+                                                  int n_jobs) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int n_next = ctr->n_next;
     const int avail = B.capacity - n_next;
-    const unsigned long long w = ctr->work_next + (unsigned long long)t;
+    unsigned long long w = ctr->work_next + (unsigned long long)t;
     if (t >= avail || w >= ctr->work_total) return;
-    const unsigned long long npix = (unsigned long long)P.width * P.height;
+    int job = 0, width = P.width, height = P.height, spp_axis = P.spp_axis;
+    uint32_t seed = P.seed, root = S.n_tris > 0 ? 0u : kTravDone;
+    const DevCamera* C = &S.cam;
+    if (BATCH) {
+        job = find_job(jobs, n_jobs, w);
+        const DevBatchJob* J = jobs + job;
+        w -= J->work_begin;
+        C = &J->cam;
+        width = C->width;
+        height = C->height;
+        spp_axis = J->spp_axis;
+        seed = J->seed;
+        root = J->root;
+    }
+    const unsigned long long npix = (unsigned long long)width * height;
     const int sample = (int)(w / npix);
     const int pixel = (int)(w - (unsigned long long)sample * npix);
-    const int px = pixel % P.width, py = pixel / P.width;
-    const Rng4 r = rng4(P.seed, sample, pixel, 0xffffu, 2);
+    const int px = pixel % width, py = pixel / width;
+    const Rng4 r = rng4(seed, sample, pixel, 0xffffu, 2);
     float cx, cy;
-    if (P.spp_axis > 0) {  // pathtracerMIS.h:148-153: spp x spp strata
-        const int k = sample / P.spp_axis, l = sample - (sample / P.spp_axis) * P.spp_axis;
-        cx = (((float)px + ((float)k + r.v[0]) / (float)P.spp_axis) / (float)P.width) * 2.0f - 1.0f;
-        cy = -((((float)py + ((float)l + r.v[1]) / (float)P.spp_axis) / (float)P.height) * 2.0f - 1.0f);
+    if (spp_axis > 0) {  // pathtracerMIS.h:148-153: spp x spp strata
+        const int k = sample / spp_axis, l = sample - (sample / spp_axis) * spp_axis;
+        cx = (((float)px + ((float)k + r.v[0]) / (float)spp_axis) / (float)width) * 2.0f - 1.0f;
+        cy = -((((float)py + ((float)l + r.v[1]) / (float)spp_axis) / (float)height) * 2.0f - 1.0f);
     } else {
-        cx = (((float)px + r.v[0]) / (float)P.width) * 2.0f - 1.0f;
-        cy = -((((float)py + r.v[1]) / (float)P.height) * 2.0f - 1.0f);
+        cx = (((float)px + r.v[0]) / (float)width) * 2.0f - 1.0f;
+        cy = -((((float)py + r.v[1]) / (float)height) * 2.0f - 1.0f);
     }
     // CameraPerspective::get_ray (camera_perspective.h:30-39)
-    const DevCamera& C = S.cam;
-    const float dx = cx * C.tan_fovy * C.aspect, dy = cy * C.tan_fovy, dz = -1.0f;
-    const f3 d = normalized(mk(C.m[0] * dx + C.m[1] * dy + C.m[2] * dz, C.m[3] * dx + C.m[4] * dy + C.m[5] * dz,
-                               C.m[6] * dx + C.m[7] * dy + C.m[8] * dz));
+    const float dx = cx * C->tan_fovy * C->aspect, dy = cy * C->tan_fovy, dz = -1.0f;
+    const f3 d = normalized(mk(C->m[0] * dx + C->m[1] * dy + C->m[2] * dz, C->m[3] * dx + C->m[4] * dy + C->m[5] * dz,
+                               C->m[6] * dx + C->m[7] * dy + C->m[8] * dz));
     const int nx = 1 - cur;
     const int j = n_next + t;
-    B.o[nx][j] = make_float4(C.o[0], C.o[1], C.o[2], 1.0f);
-    B.d[nx][j] = make_float4(d.x, d.y, d.z, 0.f);
+    B.o[nx][j] = make_float4(C->o[0], C->o[1], C->o[2], 1.0f);
+    B.d[nx][j] = make_float4(d.x, d.y, d.z, __uint_as_float(root));
     B.thr[nx][j] = make_float4(1.f, 1.f, 1.f, 0.f);
-    B.info[nx][j] = make_int4(pixel, sample, 0 | (1 << 16), 0);  // sampled_delta starts true (:34)
+    B.info[nx][j] = make_int4(pixel, sample, 0 | (1 << 16), job);  // sampled_delta starts true (:34)
 }
 
 __global__ void k_advance(WaveCounters* ctr, int capacity) {
@@ -334,16 +381,18 @@ void launch_extend(const DevScene& S, const PathBuffers& B, int cur, WaveCounter
     else k_extend<false><<<num_sms * kTraceBlocksPerSM, kTraceThreads, 0, st>>>(S, B, cur, ctr);
 }
 void launch_shade(const DevScene& S, const PathBuffers& B, int cur, const RenderParams& P, WaveCounters* ctr,
-                  unsigned long long* film, cudaStream_t st) {
-    k_shade<<<(B.capacity + 255) / 256, 256, 0, st>>>(S, B, cur, P, ctr, film);
+                  unsigned long long* film, cudaStream_t st, const DevBatchJob* jobs) {
+    if (jobs) k_shade<true><<<(B.capacity + 255) / 256, 256, 0, st>>>(S, B, cur, P, ctr, film, jobs);
+    else k_shade<false><<<(B.capacity + 255) / 256, 256, 0, st>>>(S, B, cur, P, ctr, film, nullptr);
 }
 void launch_shadow(const DevScene& S, const PathBuffers& B, WaveCounters* ctr, unsigned long long* film, int num_sms,
                    cudaStream_t st) {
     k_shadow<<<num_sms * kTraceBlocksPerSM, kTraceThreads, 0, st>>>(S, B, ctr, film);
 }
 void launch_generate(const DevScene& S, const PathBuffers& B, int cur, const RenderParams& P, WaveCounters* ctr,
-                     cudaStream_t st) {
-    k_generate<<<(B.capacity + 255) / 256, 256, 0, st>>>(S, B, cur, P, ctr);
+                     cudaStream_t st, const DevBatchJob* jobs, int n_jobs) {
+    if (jobs) k_generate<true><<<(B.capacity + 255) / 256, 256, 0, st>>>(S, B, cur, P, ctr, jobs, n_jobs);
+    else k_generate<false><<<(B.capacity + 255) / 256, 256, 0, st>>>(S, B, cur, P, ctr, nullptr, 0);
     k_advance<<<1, 32, 0, st>>>(ctr, B.capacity);
 }
 void launch_film_resolve(const unsigned long long* film, float* out, int n, double scale, cudaStream_t st) {

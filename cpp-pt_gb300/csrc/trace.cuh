@@ -140,7 +140,10 @@ struct TravStack {
     float t[kStackSize];
 };
 
-__device__ __forceinline__ void trav_init(Trav& T, const DevScene& S, float3 o, float3 d, float tmax0) {
+// root: wide-node index where the traversal starts (0 for a scene of its own;
+// the scene's first node inside a merged multi-scene arena; kTravDone for a
+// scene without triangles).
+__device__ __forceinline__ void trav_init(Trav& T, float3 o, float3 d, float tmax0, uint32_t root) {
     T.o = o;
     T.d = d;
     T.tmax0 = tmax0;
@@ -159,7 +162,7 @@ __device__ __forceinline__ void trav_init(Trav& T, const DevScene& S, float3 o, 
     T.oiy = o.y * T.idy;
     T.oiz = o.z * T.idz;
     T.neg = (T.idx < 0.f ? 1u : 0u) | (T.idy < 0.f ? 2u : 0u) | (T.idz < 0.f ? 4u : 0u);
-    T.cur = S.n_tris > 0 ? 0u : kTravDone;
+    T.cur = root;
     T.sp = 0;
     T.steps = 0;
 }
@@ -277,7 +280,9 @@ __device__ __forceinline__ bool trav_step(Trav& T, TravStack& K, const DevScene&
 // Persistent ray loop.  Each warp takes chunks of kChunk consecutive rays
 // from a global counter into a warp-private range; a lane whose ray finishes
 // takes the next ray of the range at once (no waiting for the other lanes),
-// and the warp runs one traversal step per iteration.
+// and the warp runs one traversal step per iteration.  load(i, o, d, tmax,
+// root) fetches ray i; root arrives set to the scene's own root and may be
+// replaced (rays of a merged multi-scene arena).
 constexpr int kChunk = 64;
 
 template <bool ANY, bool COUNT, class Load, class Store>
@@ -309,8 +314,9 @@ __device__ __forceinline__ void persistent_trace(const DevScene& S, const uint4*
                     ray = pool_next + r;
                     float3 o, d;
                     float tmax;
-                    load(ray, o, d, tmax);
-                    trav_init(T, S, o, d, tmax);
+                    uint32_t root = S.n_tris > 0 ? 0u : kTravDone;
+                    load(ray, o, d, tmax, root);
+                    trav_init(T, o, d, tmax, root);
                 }
                 pool_next += min(avail, __popc(idle));
             }
@@ -330,7 +336,7 @@ __device__ __forceinline__ bool traverse(const DevScene& S, const uint4* __restr
     Trav T;
     TravStack K;
     TraceCount cnt{0u, 0u};
-    trav_init(T, S, o, d, tmax0);
+    trav_init(T, o, d, tmax0, S.n_tris > 0 ? 0u : kTravDone);
     while (!trav_step<ANY, false>(T, K, S, snodes, status, cnt)) {
     }
     best = T.best;

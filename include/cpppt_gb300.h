@@ -129,6 +129,10 @@ typedef struct {
 /* pt_render_desc.flags */
 #define PT_FLAG_TIME_KERNELS 1 /* launch iterations directly with CUDA events around the traversal kernels */
 #define PT_FLAG_COUNT 2        /* counting build of the extension kernel (visited nodes / tested triangles) */
+#define PT_FLAG_UNBIASED_MIS 4 /* PT_MODE_MIS with MIS weights on the unscaled pdf and Russian roulette
+                                  survival min(rr, 1): the unbiased estimator the learned guide also uses
+                                  (the default keeps the reference's RR-scaled weights, pathtracerMIS.h:118-124) */
+#define PT_FLAG_NN_FREEZE 8    /* PT_MODE_NN: use the current network without training it */
 
 /* Replaces: Loader::load_scene + BVH::add/build (loader.h:314-374,
  * bvh.h:205-216) for a scene given as flat arrays.  Builds the
@@ -195,6 +199,42 @@ pt_status pt_render_stats_get(pt_scene* scene, pt_render_stats* stats);
 /* Writes <prefix>.png (sRGB, 8-bit, clipped as pixel_ops::put2char1) and
  * <prefix>.hdr (Radiance RGBE), as Image::save (rgb_image.h:300-318). */
 pt_status pt_image_save(const char* prefix, const float* rgb, int32_t width, int32_t height);
+
+/* Learned guide (PT_MODE_NN) state of a scene: the network's FP32 weights
+ * (15360 floats: 64x64, 64x64, 64x64, 64x48, each row-major [in][out]).
+ * Has no counterpart in the reference (its only guide is the SD-tree). */
+#define PT_NN_WEIGHTS 15360
+pt_status pt_nn_get_weights(pt_scene* scene, float* weights);
+pt_status pt_nn_set_weights(pt_scene* scene, const float* weights); /* also resets Adam */
+pt_status pt_nn_reset(pt_scene* scene, uint32_t seed);                 /* fresh random weights */
+/* training steps taken and the mean loss of the last step */
+pt_status pt_nn_stats(pt_scene* scene, double* steps, double* last_loss, double* records_used);
+
+/* Online training and sampling settings of a scene's learned guide.  The
+ * BSDF selection probability is c = bsdf_frac_min + (bsdf_frac_max -
+ * bsdf_frac_min) sigmoid(logit); 0.1 <= bsdf_frac_min <= bsdf_frac_max <= 1
+ * (equal values fix c).  batch: training records per Adam step, in
+ * [1024, 262144].  Defaults: 1e-3, 0.1, 0.9, 262144. */
+typedef struct pt_nn_config {
+    float learning_rate;
+    float bsdf_frac_min;
+    float bsdf_frac_max;
+    int32_t batch;
+} pt_nn_config;
+pt_status pt_nn_configure(pt_scene* scene, const pt_nn_config* config);
+pt_status pt_nn_config_get(pt_scene* scene, pt_nn_config* config);
+
+/* Diagnostics of the learned guide on the current CUDA device (no scene):
+ * forward: inputs 9 floats per sample (position, shading normal, wo),
+ *   positions normalised with lo/hi; out 41 floats per sample (8 lobes x
+ *   (mean xyz, kappa, weight), BSDF selection probability).
+ * grad: records 16 floats each (pos, normal, wo, wi, p_bsdf(wi), T, 0, 0);
+ *   out_grad receives dL/dW (PT_NN_WEIGHTS floats) of
+ *   L = -sum T log(c p_bsdf + (1-c) q(wi)) / sum T, out_loss receives L. */
+pt_status pt_debug_nn_forward(const float* weights, const float* lo, const float* hi, const float* inputs, int32_t n,
+                              float* out);
+pt_status pt_debug_nn_grad(const float* weights, const float* lo, const float* hi, const float* records, int32_t n,
+                           float* out_grad, float* out_loss);
 
 /* Message of the last failed call on this thread ("" when none). */
 const char* pt_last_error(void);

@@ -1,0 +1,93 @@
+"""Learned guide: the GPU network (BF16 tensor-core MLP, FP32 accumulation)
+against the torch FP64 oracle (oracle/nn_oracle.py) for the forward pass
+and the training gradient, and the guided render against plain PT."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+LO, HI = [0.0, 0.0, 0.0], [10.0, 4.0, 10.0]
+
+
+def random_inputs(n, seed):
+    rng = np.random.default_rng(seed)
+    pos = rng.uniform(LO, HI, (n, 3))
+    nrm = rng.normal(size=(n, 3)); nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    wo = rng.normal(size=(n, 3)); wo /= np.linalg.norm(wo, axis=1, keepdims=True)
+    return np.hstack([pos, nrm, wo]).astype(np.float32)
+
+
+def random_weights(seed):
+    rng = np.random.default_rng(seed)
+    w = []
+    for l, (i, o) in enumerate([(64, 64), (64, 64), (64, 64), (64, 48)]):
+        w.append(rng.normal(0, 0.5 if l == 3 else np.sqrt(2 / 64), i * o))
+    return np.concatenate(w).astype(np.float32)
+
+
+def test_forward_matches_oracle(gpu_lib):
+    from cpppt import lib
+    from oracle import nn_oracle
+    w = random_weights(1)
+    x = random_inputs(1000, 2)
+    got = lib.nn_forward(w, LO, HI, x)
+    ref = nn_oracle.forward(w, LO, HI, x)
+    # mixture weights, selection probability and lobe means; bf16 activations
+    assert np.abs(got[:, 40] - ref[:, 40]).max() < 2e-2
+    wcols = [5 * j + 4 for j in range(8)]
+    assert np.abs(got[:, wcols] - ref[:, wcols]).max() < 3e-2
+    mcols = [5 * j + k for j in range(8) for k in range(3)]
+    assert np.abs(got[:, mcols] - ref[:, mcols]).mean() < 1e-2
+    kcols = [5 * j + 3 for j in range(8)]
+    np.testing.assert_allclose(got[:, kcols], ref[:, kcols], rtol=5e-2, atol=2e-2)
+    # the mixture weights sum to one
+    np.testing.assert_allclose(got[:, wcols].sum(1), 1.0, atol=1e-5)
+
+
+def test_gradient_matches_oracle(gpu_lib):
+    from cpppt import lib
+    from oracle import nn_oracle
+    rng = np.random.default_rng(3)
+    w = random_weights(4)
+    n = 4096
+    x = random_inputs(n, 5)
+    wi = rng.normal(size=(n, 3)); wi /= np.linalg.norm(wi, axis=1, keepdims=True)
+    pb = rng.uniform(0.05, 0.5, n)
+    T = rng.exponential(1.0, n)
+    rec = np.zeros((n, 16), np.float32)
+    rec[:, 0:9] = x
+    rec[:, 9:12] = wi
+    rec[:, 12] = pb
+    rec[:, 13] = T
+    loss, g = lib.nn_grad(w, LO, HI, rec)
+    rloss, rg = nn_oracle.loss_and_grad(w, LO, HI, rec)
+    assert abs(loss - rloss) < 1e-2 * max(1.0, abs(rloss))
+    off = 0
+    for i, o in [(64, 64), (64, 64), (64, 64), (64, 48)]:
+        a, b = g[off:off + i * o], rg[off:off + i * o]
+        cos = float(a @ b / (np.linalg.norm(a) * np.linalg.norm(b) + 1e-30))
+        rel = float(np.linalg.norm(a - b) / (np.linalg.norm(b) + 1e-30))
+        assert cos > 0.995 and rel < 0.1, (off, cos, rel)
+        off += i * o
+
+
+def test_guided_render_converges_to_plain(gpu_lib):
+    """Both estimators are unbiased (PT_FLAG_UNBIASED_MIS for plain PT), so
+    after training the guided image must match the plain one statistically."""
+    from cpppt import scenes
+    from cpppt.lib import FLAG_UNBIASED_MIS, MODE_MIS, MODE_NN, GpuScene
+    from tests.test_gpu_render import check_z, tile_means, ztest
+    sc = scenes.slit_room(seed=4, n_boxes=60, box_subdiv=2, width=64, height=32)
+    gs = GpuScene(sc)
+    cfg = gs.nn_configure(batch=1 << 14)
+    assert cfg["batch"] == 1 << 14
+    for k in range(6):  # train the guide
+        gs.render(256, max_depth=12, seed=1000 + k, mode=MODE_NN)
+    st = gs.nn_stats()
+    assert st["steps"] >= 4, st
+    R, tile = 8, 16
+    g = np.stack([gs.render(256, max_depth=12, seed=50 + r, mode=MODE_NN) for r in range(R)])
+    p = np.stack([gs.render(256, max_depth=12, seed=90 + r, mode=MODE_MIS, flags=FLAG_UNBIASED_MIS)
+                  for r in range(R)])
+    assert np.isfinite(g).all() and np.isfinite(p).all()
+    check_z(ztest(tile_means(g, tile), tile_means(p, tile)), max_abs=6.0, frac3=0.1)
