@@ -51,7 +51,7 @@ def _commands(extra_cuda: list[str] | None = None):
     nvcc = _nvcc()
     common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
     jobs = []
-    for name in ("render.cu", "guide.cu", "nn.cu", "host.cpp", "bvh.cpp", "sdtree.cpp"):
+    for name in ("render.cu", "guide.cu", "nn.cu", "batch.cu", "host.cpp", "batch.cpp", "bvh.cpp", "sdtree.cpp"):
         src = os.path.join(CSRC, name)
         out = os.path.join(OBJ, name + ".o")
         cmd = [nvcc, "-c", src, "-o", out] + common

@@ -26,7 +26,9 @@ EXPORTS = ["pt_scene_create", "pt_scene_load", "pt_scene_destroy", "pt_scene_inf
            "pt_render_device_noalloc",
            "pt_render_stats_get", "pt_image_save", "pt_last_error", "pt_debug_ref_topology",
            "pt_debug_sdtree_run", "pt_nn_get_weights", "pt_nn_set_weights", "pt_nn_reset", "pt_nn_stats",
-           "pt_debug_nn_forward", "pt_debug_nn_grad", "pt_nn_configure", "pt_nn_config_get"]
+           "pt_debug_nn_forward", "pt_debug_nn_grad", "pt_nn_configure", "pt_nn_config_get",
+           "pt_batch_create", "pt_batch_destroy", "pt_batch_render", "pt_batch_render_device", "pt_batch_set_tuning",
+           "pt_batch_get_tuning", "pt_batch_stats", "pt_batch_autotune"]
 
 
 class PtMaterial(C.Structure):
@@ -60,6 +62,16 @@ class PtRenderStats(C.Structure):
 class PtNNConfig(C.Structure):
     _fields_ = [("learning_rate", C.c_float), ("bsdf_frac_min", C.c_float), ("bsdf_frac_max", C.c_float),
                 ("batch", C.c_int32)]
+
+
+class PtBatchJob(C.Structure):
+    _fields_ = [("scene", C.c_int32), ("spp", C.c_int32), ("max_depth", C.c_int32), ("rr_start", C.c_int32),
+                ("seed", C.c_uint32)]
+
+
+class PtBatchTuning(C.Structure):
+    _fields_ = [("capacity", C.c_int32), ("iters_per_graph", C.c_int32), ("tile_w", C.c_int32),
+                ("tile_h", C.c_int32)]
 
 
 class PtError(RuntimeError):
@@ -105,9 +117,19 @@ def load(path: str = LIB_PATH):
     lib.pt_debug_nn_grad.argtypes = [P, P, P, P, C.c_int32, P, P]
     lib.pt_nn_configure.argtypes = [P, P]
     lib.pt_nn_config_get.argtypes = [P, P]
+    lib.pt_batch_create.argtypes = [P, C.c_int32, C.POINTER(P)]
+    lib.pt_batch_destroy.argtypes = [P]
+    lib.pt_batch_destroy.restype = None
+    lib.pt_batch_render.argtypes = [P, P, C.c_int32, P]
+    lib.pt_batch_render_device.argtypes = [P, P, C.c_int32, P]
+    lib.pt_batch_set_tuning.argtypes = [P, P]
+    lib.pt_batch_get_tuning.argtypes = [P, P]
+    lib.pt_batch_stats.argtypes = [P, C.POINTER(PtRenderStats)]
+    lib.pt_batch_autotune.argtypes = [P, P, C.c_int32, C.c_int32, P, P]
     lib.pt_debug_sdtree_run.argtypes = [P, P, C.c_int32, P, P, C.c_int32, P, P, P, P, C.c_int32, P, P, P]
     for name in EXPORTS:
-        getattr(lib, name).restype = C.c_int32 if name not in ("pt_scene_destroy", "pt_last_error") else \
+        getattr(lib, name).restype = C.c_int32 if name not in ("pt_scene_destroy", "pt_last_error",
+                                                               "pt_batch_destroy") else \
             getattr(lib, name).restype
     _lib = lib
     return lib
@@ -162,7 +184,9 @@ class GpuScene:
         d.camera.tan_fovy = float(cam[9])
         d.camera.width, d.camera.height = sc.width, sc.height
         _check(lib.pt_scene_create(C.byref(d), C.byref(self.h)))
+        self._keep = None  # the library has its own copies
         self.width, self.height = sc.width, sc.height
+        self.n_triangles, self.n_lights = sc.n_triangles, None
 
     def close(self):
         if self.h:
@@ -260,6 +284,84 @@ class GpuScene:
         s = PtRenderStats()
         _check(_lib.pt_render_stats_get(self.h, C.byref(s)))
         return {n: getattr(s, n) for n, _ in PtRenderStats._fields_}
+
+
+class GpuBatch:
+    """Several GpuScenes merged for batched rendering (pt_batch).  jobs:
+    sequence of dicts with scene, spp, and optionally max_depth (32),
+    rr_start (3), seed (0)."""
+
+    def __init__(self, scenes):
+        lib = load()
+        self.scenes = list(scenes)  # keeps the members alive
+        arr = (C.c_void_p * len(self.scenes))(*[s.h.value for s in self.scenes])
+        self.h = C.c_void_p()
+        _check(lib.pt_batch_create(arr, len(self.scenes), C.byref(self.h)))
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            _lib.pt_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def _jobs(jobs):
+        arr = (PtBatchJob * len(jobs))()
+        for a, j in zip(arr, jobs):
+            a.scene, a.spp = j["scene"], j["spp"]
+            a.max_depth, a.rr_start, a.seed = j.get("max_depth", 32), j.get("rr_start", 3), j.get("seed", 0)
+        return arr
+
+    def render(self, jobs, outputs=True):
+        """Renders the jobs; returns one (H, W, 3) image per job (or None)."""
+        arr = self._jobs(jobs)
+        if not all(0 <= j["scene"] < len(self.scenes) for j in jobs):
+            outputs = False  # the library reports the bad job
+        if not outputs:
+            _check(_lib.pt_batch_render(self.h, arr, len(jobs), None))
+            return None
+        imgs = [np.zeros((self.scenes[j["scene"]].height, self.scenes[j["scene"]].width, 3), np.float32)
+                for j in jobs]
+        ptrs = (C.c_void_p * len(jobs))(*[_ptr(x) for x in imgs])
+        _check(_lib.pt_batch_render(self.h, arr, len(jobs), ptrs))
+        return imgs
+
+    def render_device(self, jobs, d_outs):
+        arr = self._jobs(jobs)
+        ptrs = (C.c_void_p * len(jobs))(*d_outs)
+        _check(_lib.pt_batch_render_device(self.h, arr, len(jobs), ptrs))
+
+    def tuning(self) -> dict:
+        t = PtBatchTuning()
+        _check(_lib.pt_batch_get_tuning(self.h, C.byref(t)))
+        return {k: getattr(t, k) for k, _ in PtBatchTuning._fields_}
+
+    def set_tuning(self, **kw):
+        t = PtBatchTuning()
+        _check(_lib.pt_batch_get_tuning(self.h, C.byref(t)))
+        for k, v in kw.items():
+            if k not in dict(PtBatchTuning._fields_):
+                raise KeyError(k)
+            setattr(t, k, v)
+        _check(_lib.pt_batch_set_tuning(self.h, C.byref(t)))
+        return self.tuning()
+
+    def autotune(self, jobs, spp_divisor: int = 16):
+        arr = self._jobs(jobs)
+        t = PtBatchTuning()
+        rate = C.c_double()
+        _check(_lib.pt_batch_autotune(self.h, arr, len(jobs), spp_divisor, C.byref(t), C.byref(rate)))
+        return {k: getattr(t, k) for k, _ in PtBatchTuning._fields_}, rate.value
+
+    def stats(self) -> dict:
+        s = PtRenderStats()
+        _check(_lib.pt_batch_stats(self.h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in PtRenderStats._fields_}
 
 
 def save_image(prefix: str, rgb: np.ndarray):

@@ -1,0 +1,439 @@
+// Multi-scene batches (pt_batch_*): many scenes of uneven size, resolution
+// and spp rendered by one wavefront.
+//
+// pt_batch_create merges the scenes' device arrays into one arena with the
+// cross-references rebased (batch.cu), so the traversal kernels run on the
+// arena unchanged; each path carries its job, whose table entry gives the
+// scene root, camera, light list, film range and render parameters.  Jobs are
+// laid out back to back in one work range: while the last paths of a job
+// drain, the first paths of the next one fill the freed wavefront slots, so
+// the GPU stays full across scenes and the whole batch is one chain of
+// graph-captured iterations.  The RNG is keyed by (job seed, sample, pixel,
+// bounce) and the film is fixed point, so each job's image is bit-identical
+// to pt_render of the same scene with the same parameters.
+#include "batch.h"
+#include "host_internal.h"
+
+using namespace cpppt_gb300::hostimpl;
+
+struct pt_batch {
+    int device = 0, num_sms = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<void*> owned;  // arena
+    DevScene arena{};
+    struct Member {
+        uint32_t root;
+        int light_off, n_lights, width, height;
+        DevCamera cam;
+    };
+    std::vector<Member> members;
+
+    pt_batch_tuning tuning{1 << 21, 16, 1, 1};
+    PathBuffers pb{};
+    std::vector<void*> pb_owned;
+    unsigned long long* film = nullptr;
+    size_t film_cap = 0;  // u64 elements
+    float* d_out = nullptr;
+    size_t out_cap = 0;
+    DevBatchJob* d_jobs = nullptr;
+    DevBatchJob* h_jobs = nullptr;  // pinned
+    int jobs_cap = 0;
+    WaveCounters* d_ctr = nullptr;
+    WaveCounters* h_ctr = nullptr;  // pinned
+    cudaGraphExec_t graph = nullptr;
+    struct GraphKey {
+        const void* film;
+        int n_jobs, capacity, iters;
+        bool operator==(const GraphKey& o) const {
+            return film == o.film && n_jobs == o.n_jobs && capacity == o.capacity && iters == o.iters;
+        }
+    } graph_key{nullptr, 0, 0, 0};
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    pt_render_stats stats{};
+
+    ~pt_batch() {
+        if (stream) cudaStreamSynchronize(stream);
+        if (graph) cudaGraphExecDestroy(graph);
+        for (void* p : owned) cudaFree(p);
+        for (void* p : pb_owned) cudaFree(p);
+        if (film) cudaFree(film);
+        if (d_out) cudaFree(d_out);
+        if (d_jobs) cudaFree(d_jobs);
+        if (h_jobs) cudaFreeHost(h_jobs);
+        if (h_ctr) cudaFreeHost(h_ctr);  // d_ctr is in pb_owned
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+constexpr int kMaxBatchCapacity = 1 << 22;
+constexpr unsigned long long kMaxBatchPixels = 1ull << 30;  // film pixel index travels as a 32-bit word
+
+template <class T>
+void d2d(T* dst, const T* src, size_t n, cudaStream_t st) {
+    if (n) ck(cudaMemcpyAsync(dst, src, sizeof(T) * n, cudaMemcpyDeviceToDevice, st), "arena copy");
+}
+
+void create_batch(pt_scene* const* scenes, int n, pt_batch* b) {
+    if (!scenes || n < 1) throw std::invalid_argument("a batch needs at least one scene");
+    for (int i = 0; i < n; i++)
+        if (!scenes[i]) throw std::invalid_argument("null scene in batch");
+    b->device = scenes[0]->device;
+    b->num_sms = scenes[0]->num_sms;
+    int cur = 0;
+    ck(cudaGetDevice(&cur), "cudaGetDevice");
+    for (int i = 0; i < n; i++)
+        if (scenes[i]->device != b->device) throw std::invalid_argument("batch scenes live on different devices");
+    if (cur != b->device) throw std::invalid_argument("the current device is not the scenes' device");
+    ck(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    // arena sizes and offsets
+    unsigned long long nn = 0, nt = 0, nr = 0, nv = 0, nm = 0, nl = 0;
+    for (int i = 0; i < n; i++) {
+        const pt_scene* s = scenes[i];
+        nn += s->dev.n_nodes;
+        nt += s->n_tris;
+        nr += s->n_rbox;
+        nv += s->n_verts;
+        nm += s->n_mats;
+        nl += s->dev.n_lights;
+    }
+    if (nt >= (1ull << 27)) throw Fail(PT_ERR_LIMIT, "batch exceeds 2^27 - 1 triangles (leaf reference range)");
+    if (nn >= (1ull << 31) || nr >= (1ull << 31) || nv >= (1ull << 31) || nm >= (1ull << 31))
+        throw Fail(PT_ERR_LIMIT, "batch arena exceeds 32-bit indices");
+    DevScene& A = b->arena;
+    uint4* nodes = dalloc<uint4>(b->owned, 4 * nn);
+    float4* tris = dalloc<float4>(b->owned, 3 * nt);
+    float4* rbox = dalloc<float4>(b->owned, 2 * nr);
+    int4* vidx = dalloc<int4>(b->owned, nt);
+    float4* vpos = dalloc<float4>(b->owned, nv);
+    float4* vnrm = dalloc<float4>(b->owned, nv);
+    float4* vbt = dalloc<float4>(b->owned, nv);
+    DevMaterial* mats = dalloc<DevMaterial>(b->owned, nm);
+    int32_t* lprim = dalloc<int32_t>(b->owned, nl);
+    float* larea = dalloc<float>(b->owned, nl);
+    cudaStream_t st = b->stream;
+    int on = 0, ot = 0, orb = 0, ov = 0, om = 0, ol = 0;
+    for (int i = 0; i < n; i++) {
+        const pt_scene* s = scenes[i];
+        const DevScene& S = s->dev;
+        // the source scene's uploads ran on its own stream
+        ck(cudaStreamSynchronize(s->stream), "scene stream");
+        launch_rebase_nodes(nodes + 4 * (size_t)on, S.nodes, S.n_nodes, (uint32_t)on, (uint32_t)ot, st);
+        launch_rebase_tris(tris + 3 * (size_t)ot, S.tris, s->n_tris, orb, ot, st);
+        d2d(rbox + 2 * (size_t)orb, S.ref_box, 2 * (size_t)s->n_rbox, st);
+        launch_rebase_vidx(vidx + ot, S.tri_vidx, s->n_tris, ov, om, st);
+        d2d(vpos + ov, S.v_pos, s->n_verts, st);
+        d2d(vnrm + ov, S.v_nrm, s->n_verts, st);
+        d2d(vbt + ov, S.v_btan, s->n_verts, st);
+        d2d(mats + om, S.mats, s->n_mats, st);
+        launch_offset_i32(lprim + ol, S.light_prim, S.n_lights, ot, st);
+        d2d(larea + ol, S.light_area, S.n_lights, st);
+        pt_batch::Member m;
+        m.root = s->n_tris > 0 ? (uint32_t)on : 0xffffffffu;
+        m.light_off = ol;
+        m.n_lights = S.n_lights;
+        m.width = s->width;
+        m.height = s->height;
+        m.cam = S.cam;
+        b->members.push_back(m);
+        on += S.n_nodes;
+        ot += s->n_tris;
+        orb += s->n_rbox;
+        ov += s->n_verts;
+        om += s->n_mats;
+        ol += S.n_lights;
+    }
+    ck(cudaGetLastError(), "arena merge");
+    A.nodes = nodes;
+    A.n_nodes = on;
+    A.n_tris = ot;
+    A.tris = tris;
+    A.ref_box = rbox;
+    A.tri_vidx = vidx;
+    A.v_pos = vpos;
+    A.v_nrm = vnrm;
+    A.v_btan = vbt;
+    A.mats = mats;
+    A.light_prim = lprim;
+    A.light_area = larea;
+    A.n_lights = ol;
+    A.cam = b->members[0].cam;  // unused by the batch kernels
+    b->d_ctr = dalloc<WaveCounters>(b->pb_owned, 1);
+    ck(cudaMallocHost(&b->h_ctr, sizeof(WaveCounters)), "cudaMallocHost");
+    ck(cudaEventCreate(&b->ev0), "cudaEventCreate");
+    ck(cudaEventCreate(&b->ev1), "cudaEventCreate");
+    ck(cudaStreamSynchronize(st), "arena merge");
+}
+
+void check_tuning(const pt_batch_tuning& t) {
+    if (t.capacity < 1024 || t.capacity > kMaxBatchCapacity || t.capacity % 1024)
+        throw std::invalid_argument("capacity must be a multiple of 1024 in [1024, 4194304]");
+    if (t.iters_per_graph < 2 || t.iters_per_graph > 256 || t.iters_per_graph % 2)
+        throw std::invalid_argument("iters_per_graph must be even, in [2, 256]");
+    if (t.tile_w < 1 || t.tile_h < 1 || t.tile_w * t.tile_h > 1024)
+        throw std::invalid_argument("tile sides must be >= 1 with at most 1024 pixels per tile");
+}
+
+void ensure_buffers(pt_batch* b, int capacity, size_t film_n, int n_jobs) {
+    if (b->pb.capacity != capacity) {
+        // keep the counters block (first entry), drop the path buffers
+        void* ctr = b->d_ctr;
+        for (void* p : b->pb_owned)
+            if (p != ctr) cudaFree(p);
+        b->pb_owned.assign(1, ctr);
+        PathBuffers& B = b->pb;
+        for (int k = 0; k < 2; k++) {
+            B.o[k] = dalloc<float4>(b->pb_owned, capacity);
+            B.d[k] = dalloc<float4>(b->pb_owned, capacity);
+            B.thr[k] = dalloc<float4>(b->pb_owned, capacity);
+            B.info[k] = dalloc<int4>(b->pb_owned, capacity);
+        }
+        B.hit = dalloc<float4>(b->pb_owned, capacity);
+        B.sh_o = dalloc<float4>(b->pb_owned, capacity);
+        B.sh_d = dalloc<float4>(b->pb_owned, capacity);
+        B.sh_c = dalloc<float4>(b->pb_owned, capacity);
+        B.capacity = capacity;
+        if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+    }
+    if (b->film_cap < film_n) {
+        if (b->film) cudaFree(b->film);
+        if (b->d_out) cudaFree(b->d_out);
+        b->film = nullptr;
+        b->d_out = nullptr;
+        ck(cudaMalloc(&b->film, sizeof(unsigned long long) * film_n), "cudaMalloc film");
+        ck(cudaMalloc(&b->d_out, sizeof(float) * film_n), "cudaMalloc film");
+        b->film_cap = film_n;
+        b->out_cap = film_n;
+        if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+    }
+    if (b->jobs_cap < n_jobs) {
+        if (b->d_jobs) cudaFree(b->d_jobs);
+        if (b->h_jobs) cudaFreeHost(b->h_jobs);
+        b->d_jobs = nullptr;
+        b->h_jobs = nullptr;
+        ck(cudaMalloc(&b->d_jobs, sizeof(DevBatchJob) * n_jobs), "cudaMalloc jobs");
+        ck(cudaMallocHost(&b->h_jobs, sizeof(DevBatchJob) * n_jobs), "cudaMallocHost jobs");
+        b->jobs_cap = n_jobs;
+        if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+    }
+}
+
+// Builds the job table; returns total work and total film pixels.
+void build_jobs(pt_batch* b, const pt_batch_job* jobs, int n_jobs, const pt_batch_tuning& t,
+                std::vector<DevBatchJob>& out, unsigned long long* work, unsigned long long* pixels) {
+    if (!jobs || n_jobs < 1) throw std::invalid_argument("a batch render needs at least one job");
+    out.resize(n_jobs);
+    unsigned long long w = 0, px = 0;
+    for (int i = 0; i < n_jobs; i++) {
+        const pt_batch_job& j = jobs[i];
+        if (j.scene < 0 || j.scene >= (int)b->members.size()) throw std::invalid_argument("job scene out of range");
+        if (j.spp < 1) throw std::invalid_argument("spp must be >= 1");
+        if (j.max_depth < 1 || j.max_depth > 0xffff) throw std::invalid_argument("max_depth must be in [1, 65535]");
+        const pt_batch::Member& m = b->members[j.scene];
+        DevBatchJob& d = out[i];
+        d = DevBatchJob{};
+        d.cam = m.cam;
+        d.work_begin = w;
+        d.film_off = px;
+        d.root = m.root;
+        d.light_off = m.light_off;
+        d.n_lights = m.n_lights;
+        d.spp = j.spp;
+        const int ax = (int)std::lround(std::sqrt((double)j.spp));
+        d.spp_axis = (ax * ax == j.spp) ? ax : 0;  // as pt_render
+        d.max_depth = j.max_depth;
+        d.rr_start = j.rr_start;
+        d.seed = j.seed;
+        const bool tiles = m.width % t.tile_w == 0 && m.height % t.tile_h == 0;
+        d.tile_w = tiles ? t.tile_w : 1;
+        d.tile_h = tiles ? t.tile_h : 1;
+        const unsigned long long npx = (unsigned long long)m.width * m.height;
+        w += npx * (unsigned long long)j.spp;
+        px += npx;
+    }
+    if (px > kMaxBatchPixels) throw Fail(PT_ERR_LIMIT, "batch film exceeds 2^30 pixels");
+    *work = w;
+    *pixels = px;
+}
+
+// Renders the jobs; d_dst[i] (device, 3 floats per pixel) receive the images,
+// or the batch's own output buffer when d_dst is null.
+void render_batch(pt_batch* b, const pt_batch_job* jobs, int n_jobs, float* const* d_dst, const pt_batch_tuning& t) {
+    check_tuning(t);
+    std::vector<DevBatchJob> table;
+    unsigned long long total = 0, pixels = 0;
+    build_jobs(b, jobs, n_jobs, t, table, &total, &pixels);
+    const int capacity = (int)std::min<unsigned long long>(t.capacity, (total + 1023) / 1024 * 1024);
+    ensure_buffers(b, capacity, 3 * pixels, n_jobs);
+    cudaStream_t st = b->stream;
+    std::memcpy(b->h_jobs, table.data(), sizeof(DevBatchJob) * n_jobs);
+    ck(cudaMemcpyAsync(b->d_jobs, b->h_jobs, sizeof(DevBatchJob) * n_jobs, cudaMemcpyHostToDevice, st), "jobs");
+    const pt_batch::GraphKey key{b->film, n_jobs, capacity, t.iters_per_graph};
+    if (!b->graph || !(b->graph_key == key)) {
+        if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+        cudaGraph_t g;
+        ck(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
+        for (int k = 0; k < t.iters_per_graph; k++) {
+            const int cur = k & 1;
+            launch_extend(b->arena, b->pb, cur, b->d_ctr, b->num_sms, st);
+            launch_shade(b->arena, b->pb, cur, b->d_ctr, b->film, b->d_jobs, st);
+            launch_shadow(b->arena, b->pb, b->d_ctr, b->film, b->num_sms, st);
+            launch_generate(b->arena, b->pb, cur, b->d_ctr, b->d_jobs, n_jobs, st);
+        }
+        ck(cudaStreamEndCapture(st, &g), "end capture");
+        ck(cudaGraphInstantiate(&b->graph, g, 0), "graph instantiate");
+        cudaGraphDestroy(g);
+        b->graph_key = key;
+    }
+    ck(cudaEventRecord(b->ev0, st), "event");
+    ck(cudaMemsetAsync(b->film, 0, sizeof(unsigned long long) * 3 * pixels, st), "memset film");
+    WaveCounters init{};
+    init.work_total = total;
+    *b->h_ctr = init;
+    ck(cudaMemcpyAsync(b->d_ctr, b->h_ctr, sizeof(WaveCounters), cudaMemcpyHostToDevice, st), "init counters");
+    launch_generate(b->arena, b->pb, 1, b->d_ctr, b->d_jobs, n_jobs, st);  // fills buffer 0
+    int max_depth = 1;
+    for (const DevBatchJob& j : table) max_depth = std::max(max_depth, j.max_depth);
+    const unsigned long long max_rounds =
+        64 + (total / (unsigned long long)capacity + 2 + (unsigned long long)n_jobs) *
+                 (unsigned long long)(max_depth + 2) * 4 / (unsigned long long)t.iters_per_graph;
+    unsigned long long rounds = 0;
+    double launches = 2;
+    while (true) {
+        ck(cudaGraphLaunch(b->graph, st), "graph launch");
+        launches += kKernelsPerIteration * t.iters_per_graph;
+        ck(cudaMemcpyAsync(b->h_ctr, b->d_ctr, sizeof(WaveCounters), cudaMemcpyDeviceToHost, st), "read counters");
+        ck(cudaStreamSynchronize(st), "batch render");
+        const uint32_t status = b->h_ctr->status;
+        if (status & kStatusStackOverflow) throw Fail(PT_ERR_LIMIT, "traversal stack overflow");
+        if (status & kStatusIterLimit) throw Fail(PT_ERR_LIMIT, "traversal step limit reached");
+        if (status & kStatusQueueOverflow) throw Fail(PT_ERR_LIMIT, "wavefront queue overflow");
+        rounds++;
+        if (b->h_ctr->n_cur == 0 && b->h_ctr->work_next >= b->h_ctr->work_total) break;
+        if (rounds > max_rounds) throw Fail(PT_ERR_LIMIT, "batch render did not converge within the iteration bound");
+    }
+    for (int i = 0; i < n_jobs; i++) {
+        const pt_batch::Member& m = b->members[jobs[i].scene];
+        const size_t off = 3 * (size_t)table[i].film_off;
+        float* dst = (d_dst && d_dst[i]) ? d_dst[i] : b->d_out + off;
+        launch_film_resolve(b->film + off, dst, 3 * m.width * m.height, 1.0 / (double)jobs[i].spp, st);
+        launches += 1;
+    }
+    ck(cudaEventRecord(b->ev1, st), "event");
+    ck(cudaStreamSynchronize(st), "batch render");
+    ck(cudaGetLastError(), "batch kernels");
+    float ms = 0;
+    ck(cudaEventElapsedTime(&ms, b->ev0, b->ev1), "elapsed");
+    pt_render_stats& R = b->stats;
+    R = pt_render_stats{};
+    R.paths = (double)b->h_ctr->stat_paths;
+    R.closest_rays = (double)b->h_ctr->stat_closest;
+    R.shadow_rays = (double)b->h_ctr->stat_shadow;
+    R.iterations = (double)b->h_ctr->stat_iters;
+    R.render_ms = ms;
+    R.kernel_launches = launches;
+    R.nonfinite = (double)b->h_ctr->stat_nonfinite;
+    R.h2d_bytes = (double)(sizeof(WaveCounters) + sizeof(DevBatchJob) * n_jobs);
+    R.d2h_bytes = (double)(rounds * sizeof(WaveCounters));
+}
+
+}  // namespace
+
+pt_status pt_batch_create(pt_scene* const* scenes, int32_t n_scenes, pt_batch** out) {
+    if (!out) { g_error = "null argument"; return PT_ERR_INVALID; }
+    *out = nullptr;
+    pt_batch* b = new (std::nothrow) pt_batch;
+    if (!b) { g_error = "host allocation failed"; return PT_ERR_MEMORY; }
+    const pt_status r = guarded([&] { create_batch(scenes, n_scenes, b); });
+    if (r != PT_OK) { delete b; return r; }
+    *out = b;
+    return PT_OK;
+}
+
+void pt_batch_destroy(pt_batch* b) { delete b; }
+
+pt_status pt_batch_render_device(pt_batch* b, const pt_batch_job* jobs, int32_t n_jobs, float* const* d_rgb_out) {
+    if (!b) { g_error = "null batch"; return PT_ERR_INVALID; }
+    return guarded([&] { render_batch(b, jobs, n_jobs, d_rgb_out, b->tuning); });
+}
+
+pt_status pt_batch_render(pt_batch* b, const pt_batch_job* jobs, int32_t n_jobs, float* const* rgb_out) {
+    if (!b) { g_error = "null batch"; return PT_ERR_INVALID; }
+    return guarded([&] {
+        render_batch(b, jobs, n_jobs, nullptr, b->tuning);
+        if (!rgb_out) return;
+        size_t off = 0, bytes = 0;
+        for (int i = 0; i < n_jobs; i++) {
+            const pt_batch::Member& m = b->members[jobs[i].scene];
+            const size_t n = 3 * (size_t)m.width * m.height;
+            if (rgb_out[i]) {
+                ck(cudaMemcpyAsync(rgb_out[i], b->d_out + off, sizeof(float) * n, cudaMemcpyDeviceToHost, b->stream),
+                   "copy image");
+                bytes += sizeof(float) * n;
+            }
+            off += n;
+        }
+        ck(cudaStreamSynchronize(b->stream), "copy images");
+        b->stats.d2h_bytes += (double)bytes;
+    });
+}
+
+pt_status pt_batch_set_tuning(pt_batch* b, const pt_batch_tuning* t) {
+    if (!b || !t) { g_error = "null argument"; return PT_ERR_INVALID; }
+    return guarded([&] {
+        check_tuning(*t);
+        b->tuning = *t;
+    });
+}
+
+pt_status pt_batch_get_tuning(pt_batch* b, pt_batch_tuning* t) {
+    if (!b || !t) { g_error = "null argument"; return PT_ERR_INVALID; }
+    *t = b->tuning;
+    return PT_OK;
+}
+
+pt_status pt_batch_stats(pt_batch* b, pt_render_stats* out) {
+    if (!b || !out) { g_error = "null argument"; return PT_ERR_INVALID; }
+    *out = b->stats;
+    return PT_OK;
+}
+
+// Autotuner: renders a reduced copy of the job list (spp divided by
+// spp_divisor, at least 1) once per candidate setting and keeps the one with
+// the highest paths per second.  Candidates: wavefront capacity 2^19..2^22,
+// 8/16/32 iterations per graph, and scanline or 8x4 / 4x8 / 16x2 pixel tiles.
+pt_status pt_batch_autotune(pt_batch* b, const pt_batch_job* jobs, int32_t n_jobs, int32_t spp_divisor,
+                            pt_batch_tuning* best_out, double* best_mpaths) {
+    if (!b) { g_error = "null batch"; return PT_ERR_INVALID; }
+    return guarded([&] {
+        if (!jobs || n_jobs < 1) throw std::invalid_argument("a batch render needs at least one job");
+        if (spp_divisor < 1) throw std::invalid_argument("spp_divisor must be >= 1");
+        std::vector<pt_batch_job> sample(jobs, jobs + n_jobs);
+        for (pt_batch_job& j : sample) j.spp = std::max(1, j.spp / spp_divisor);
+        const int caps[] = {1 << 19, 1 << 20, 1 << 21, 1 << 22};
+        const int iters[] = {8, 16, 32};
+        const int tiles[][2] = {{1, 1}, {8, 4}, {4, 8}, {16, 2}};
+        pt_batch_tuning best = b->tuning;
+        double best_rate = -1.0;
+        auto trial = [&](const pt_batch_tuning& t) {
+            render_batch(b, sample.data(), n_jobs, nullptr, t);  // warm-up: buffers and graph
+            render_batch(b, sample.data(), n_jobs, nullptr, t);
+            const double rate = b->stats.paths / (b->stats.render_ms * 1e3);
+            if (rate > best_rate) { best_rate = rate; best = t; }
+        };
+        // capacity and graph length first (scanline order), then the tile shape
+        for (int c : caps)
+            for (int it : iters) trial(pt_batch_tuning{c, it, 1, 1});
+        const pt_batch_tuning base = best;
+        for (const auto& tl : tiles) {
+            if (tl[0] == 1 && tl[1] == 1) continue;
+            trial(pt_batch_tuning{base.capacity, base.iters_per_graph, tl[0], tl[1]});
+        }
+        b->tuning = best;
+        if (best_out) *best_out = best;
+        if (best_mpaths) *best_mpaths = best_rate;
+    });
+}

@@ -55,6 +55,7 @@ struct DevBatchJob {
     int32_t light_off, n_lights;    // the scene's emissive triangles in the arena's light list
     int32_t spp, spp_axis, max_depth, rr_start;
     uint32_t seed;
+    int32_t tile_w, tile_h;  // pixel order of a pass: tiles of tile_w x tile_h (both divide the resolution)
 };
 
 // Ray-batch status word bits (kernel-side bounded loops report here).

@@ -178,6 +178,8 @@ void create_scene(const pt_scene_desc* d, pt_scene* s) {
     s->d_status = reinterpret_cast<uint32_t*>(s->d_counter + 1);
     s->d_ctr = dalloc<WaveCounters>(s->owned, 1);
     ck(cudaMallocHost(&s->h_ctr, sizeof(WaveCounters)), "cudaMallocHost");
+    s->d_job = dalloc<DevBatchJob>(s->owned, 1);
+    ck(cudaMallocHost(&s->h_job, sizeof(DevBatchJob)), "cudaMallocHost");
     ck(cudaEventCreate(&s->ev0), "cudaEventCreate");
     ck(cudaEventCreate(&s->ev1), "cudaEventCreate");
     ck(cudaStreamSynchronize(s->stream), "scene upload");
@@ -262,15 +264,15 @@ void ensure_wave(pt_scene* s, int capacity, int film_n) {
     }
 }
 
-bool same_params(const RenderParams& a, const RenderParams& b) { return std::memcmp(&a, &b, sizeof(a)) == 0; }
-
-void enqueue_iterations(pt_scene* s, const RenderParams& P, int iters) {
+// The render parameters live in the scene's one-entry job table, so the
+// captured iterations stay valid across renders.
+void enqueue_iterations(pt_scene* s, int iters) {
     for (int k = 0; k < iters; k++) {
         const int cur = k & 1;
         launch_extend(s->dev, s->pb, cur, s->d_ctr, s->num_sms, s->stream);
-        launch_shade(s->dev, s->pb, cur, P, s->d_ctr, s->film, s->stream);
+        launch_shade(s->dev, s->pb, cur, s->d_ctr, s->film, s->d_job, s->stream);
         launch_shadow(s->dev, s->pb, s->d_ctr, s->film, s->num_sms, s->stream);
-        launch_generate(s->dev, s->pb, cur, P, s->d_ctr, s->stream);
+        launch_generate(s->dev, s->pb, cur, s->d_ctr, s->d_job, 1, s->stream);
     }
 }
 
@@ -483,10 +485,10 @@ void render_nn(pt_scene* s, const pt_render_desc* desc, float* d_dst, bool guide
         ~Free() { for (void* p : v) cudaFree(p); }
     } guard{tmp};
     NNPathData PD;
-    PD.vert = dalloc<float4>(tmp, (size_t)capacity * P.max_depth * 5);
+    PD.vert = dalloc<float4>(tmp, train ? (size_t)capacity * P.max_depth * kNNVertFloat4 : 1);
     PD.acc = dalloc<float4>(tmp, capacity);
     PD.slot_stack = dalloc<int>(tmp, capacity);
-    PD.fin = dalloc<int2>(tmp, capacity);
+    PD.fin = dalloc<int4>(tmp, capacity);
     const int batch = s->nn_cfg.batch;
     PD.rec_cap = train ? batch : 0;
     PD.rec = train ? s->nn_rec : nullptr;
@@ -601,15 +603,13 @@ void render_impl(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
     const bool timed = (desc->flags & PT_FLAG_TIME_KERNELS) != 0;
     const bool count = (desc->flags & PT_FLAG_COUNT) != 0;
     const bool direct = timed || count;
-    if (!direct && (!s->graph || !same_params(s->graph_params, P))) {
-        if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
+    if (!direct && !s->graph) {
         cudaGraph_t g;
         ck(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
-        enqueue_iterations(s, P, kItersPerGraph);
+        enqueue_iterations(s, kItersPerGraph);
         ck(cudaStreamEndCapture(st, &g), "end capture");
         ck(cudaGraphInstantiate(&s->graph, g, 0), "graph instantiate");
         cudaGraphDestroy(g);
-        s->graph_params = P;
     }
     ck(cudaEventRecord(s->ev0, st), "event");
     ck(cudaMemsetAsync(s->film, 0, sizeof(unsigned long long) * film_n, st), "memset film");
@@ -617,7 +617,9 @@ void render_impl(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
     init.work_total = total;
     *s->h_ctr = init;
     ck(cudaMemcpyAsync(s->d_ctr, s->h_ctr, sizeof(WaveCounters), cudaMemcpyHostToDevice, st), "init counters");
-    launch_generate(s->dev, s->pb, 1, P, s->d_ctr, st);  // fills buffer 0
+    *s->h_job = single_job(s->dev, P);
+    ck(cudaMemcpyAsync(s->d_job, s->h_job, sizeof(DevBatchJob), cudaMemcpyHostToDevice, st), "job table");
+    launch_generate(s->dev, s->pb, 1, s->d_ctr, s->d_job, 1, st);  // fills buffer 0
     double launches = 2;
     const unsigned long long max_rounds = 64 + (total / (unsigned long long)capacity + 2) *
                                                    (unsigned long long)(desc->max_depth + 2) * 4 / kItersPerGraph;
@@ -634,11 +636,11 @@ void render_impl(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
                 if (timed) ck(cudaEventRecord(e[0], st), "event");
                 launch_extend(s->dev, s->pb, cur, s->d_ctr, s->num_sms, st, count);
                 if (timed) ck(cudaEventRecord(e[1], st), "event");
-                launch_shade(s->dev, s->pb, cur, P, s->d_ctr, s->film, st);
+                launch_shade(s->dev, s->pb, cur, s->d_ctr, s->film, s->d_job, st);
                 if (timed) ck(cudaEventRecord(e[2], st), "event");
                 launch_shadow(s->dev, s->pb, s->d_ctr, s->film, s->num_sms, st);
                 if (timed) ck(cudaEventRecord(e[3], st), "event");
-                launch_generate(s->dev, s->pb, cur, P, s->d_ctr, st);
+                launch_generate(s->dev, s->pb, cur, s->d_ctr, s->d_job, 1, st);
             }
         } else {
             ck(cudaGraphLaunch(s->graph, st), "graph launch");

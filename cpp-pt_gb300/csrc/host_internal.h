@@ -120,8 +120,8 @@ struct pt_scene {
     WaveCounters* d_ctr = nullptr;
     WaveCounters* h_ctr = nullptr;  // pinned
     cudaGraphExec_t graph = nullptr;
-    RenderParams graph_params{};
-    int graph_iters = 0;
+    DevBatchJob* d_job = nullptr;  // one-entry job table of the wavefront kernels
+    DevBatchJob* h_job = nullptr;  // pinned staging copy
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     pt_render_stats stats{};
 
@@ -147,6 +147,7 @@ struct pt_scene {
         if (d_out) cudaFree(d_out);
         if (d_io) cudaFree(d_io);
         if (h_ctr) cudaFreeHost(h_ctr);
+        if (h_job) cudaFreeHost(h_job);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (stream) cudaStreamDestroy(stream);

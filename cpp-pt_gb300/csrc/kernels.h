@@ -42,13 +42,16 @@ struct RenderParams {
 // shadow (any hit + film), generate (new camera paths) + advance (counters).
 void launch_extend(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, int num_sms, cudaStream_t st,
                    bool count = false);
-// jobs != nullptr: a multi-scene batch over a merged arena (DevBatchJob).
-void launch_shade(const DevScene& S, const PathBuffers& B, int cur, const RenderParams& P, WaveCounters* ctr,
-                  unsigned long long* film, cudaStream_t st, const DevBatchJob* jobs = nullptr);
+// jobs: device table of n_jobs DevBatchJob (one entry for a single-scene
+// render; several for a batch over a merged arena, ascending work ranges).
+void launch_shade(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, unsigned long long* film,
+                  const DevBatchJob* jobs, cudaStream_t st);
 void launch_shadow(const DevScene& S, const PathBuffers& B, WaveCounters* ctr, unsigned long long* film, int num_sms,
                    cudaStream_t st);
-void launch_generate(const DevScene& S, const PathBuffers& B, int cur, const RenderParams& P, WaveCounters* ctr,
-                     cudaStream_t st, const DevBatchJob* jobs = nullptr, int n_jobs = 0);
+void launch_generate(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, const DevBatchJob* jobs,
+                     int n_jobs, cudaStream_t st);
+// The job-table entry of a single-scene render of S with parameters P.
+DevBatchJob single_job(const DevScene& S, const RenderParams& P);
 constexpr int kKernelsPerIteration = 5;
 // Allocation-free render: the wavefront of launch_* above with its scratch in
 // a file-scope __device__ array (see render.cu).  Synchronises `st`.

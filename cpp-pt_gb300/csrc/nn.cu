@@ -600,9 +600,11 @@ __device__ __forceinline__ int warp_append_nn(int* counter, bool pred) {
     return pred ? base + __popc(mask & ((1u << lane) - 1u)) : -1;
 }
 
-// Vertex record k of a path slot (5 float4): 0: pos xyz, n.x  1: n.yz, wo.xy
+// Vertex record k of a path slot (kNNVert float4): 0: pos xyz, n.x  1: n.yz, wo.xy
 // 2: wo.z, wi xyz  3: p_bsdf(wi), throughput before the bounce (rgb)
-// 4: film total after the vertex's own NEE (rgb), valid (guide-sampled, non-delta).
+// 4: film total after the vertex's own NEE (rgb), wi valid (non-delta)
+// 5: film total before the NEE (rgb), p_bsdf(wi_nee)  6: wi_nee xyz, NEE valid.
+constexpr int kNNVert = kNNVertFloat4;
 __global__ void __launch_bounds__(256) k_shade_nn(DevScene S, PathBuffers B, int cur, RenderParams P,
                                                   WaveCounters* ctr, unsigned long long* __restrict__ film,
                                                   const float4* __restrict__ params, NNPathData PD, int guided) {
@@ -611,7 +613,7 @@ __global__ void __launch_bounds__(256) k_shade_nn(DevScene S, PathBuffers B, int
     bool push_sh = false, push_cont = false, release = false;
     float4 sh_o, sh_d, sh_c, no, nd, nt;
     int4 ninfo;
-    int slot = -1, fin_bounce = 0;
+    int slot = -1, fin_bounce = 0, fin_nv = 0;
     if (i < n) {
         const float4 O = B.o[cur][i], D = B.d[cur][i], Tp = B.thr[cur][i];
         const int4 I = B.info[cur][i];
@@ -627,8 +629,8 @@ __global__ void __launch_bounds__(256) k_shade_nn(DevScene S, PathBuffers B, int
         const bool train = PD.rec_cap > 0;  // vertex records and running totals only while training
         f3 Ssum = train ? f3of(PD.acc[slot]) : mk(0.f, 0.f, 0.f);
         if (train && bounce > 0) {  // the previous vertex's incident radiance is what arrives from now on
-            const float w4 = PD.vert[5 * (vbase + bounce - 1) + 4].w;
-            PD.vert[5 * (vbase + bounce - 1) + 4] = make_float4(Ssum.x, Ssum.y, Ssum.z, w4);
+            const float w4 = PD.vert[kNNVert * (vbase + bounce - 1) + 4].w;
+            PD.vert[kNNVert * (vbase + bounce - 1) + 4] = make_float4(Ssum.x, Ssum.y, Ssum.z, w4);
         }
         bool done = true;
         if (prim >= 0) {
@@ -678,6 +680,8 @@ __global__ void __launch_bounds__(256) k_shade_nn(DevScene S, PathBuffers B, int
                     bs.pdf = bsdf_pdf(m, s, wo, bs.wi);
                     pmix = c * bs.pdf + (1.0f - c) * nn_mix_pdf(prm, bs.wi);
                 }
+                f3 nee_wi = mk(0.f, 0.f, 0.f);
+                float nee_pb = 0.f, nee_ok = 0.f;
                 if (!bs.delta && S.n_lights > 0) {  // NEE; the MIS weight uses the mixture pdf
                     const LSample ls = sample_light(S, s.p, r0.v[2], r0.v[3], r1.v[0]);
                     f3 sd = ls.pos - s.p;
@@ -685,9 +689,14 @@ __global__ void __launch_bounds__(256) k_shade_nn(DevScene S, PathBuffers B, int
                     sd = sd * (1.0f / len);
                     if (same_hemisphere(s, wo, sd)) {
                         float pb = bsdf_pdf(m, s, wo, sd);
+                        nee_wi = sd;
+                        nee_pb = pb;
+                        nee_ok = 1.f;
                         if (c < 1.0f) pb = c * pb + (1.0f - c) * nn_mix_pdf(prm, sd);
                         const float pn = ls.pdf * len * len / (fabsf(dot(ls.n, sd)) + kEps);
-                        const float w = pn / (pb + pn);
+                        // at the last vertex no sampled direction follows, so NEE takes the full
+                        // weight (the two estimators then converge to the same depth-limited image)
+                        const float w = bounce + 1 < P.max_depth ? pn / (pb + pn) : 1.0f;
                         const f3 f = bsdf_eval(m, s, wo, sd);
                         const f3 cc = mul * f * ls.le * (1.0f / (ls.pdf * len * len)) * w;
                         if (cc.x != 0.f || cc.y != 0.f || cc.z != 0.f) {
@@ -699,13 +708,16 @@ __global__ void __launch_bounds__(256) k_shade_nn(DevScene S, PathBuffers B, int
                         }
                     }
                 }
-                if (train) {  // this vertex's training record (completed when the path ends)
-                    const size_t vi = 5 * (vbase + bounce);
+                if (train) {  // this vertex's training records (completed when the path ends)
+                    const size_t vi = kNNVert * (vbase + bounce);
                     PD.vert[vi] = make_float4(s.p.x, s.p.y, s.p.z, s.n.x);
                     PD.vert[vi + 1] = make_float4(s.n.y, s.n.z, wo.x, wo.y);
                     PD.vert[vi + 2] = make_float4(wo.z, bs.wi.x, bs.wi.y, bs.wi.z);
                     PD.vert[vi + 3] = make_float4(bs.delta ? 0.f : bs.pdf, mul.x, mul.y, mul.z);
-                    PD.vert[vi + 4] = make_float4(0.f, 0.f, 0.f, bs.delta ? 0.f : 1.f);
+                    PD.vert[vi + 4] = make_float4(Ssum.x, Ssum.y, Ssum.z, bs.delta ? 0.f : 1.f);
+                    PD.vert[vi + 5] = make_float4(Ssum.x, Ssum.y, Ssum.z, nee_pb);
+                    PD.vert[vi + 6] = make_float4(nee_wi.x, nee_wi.y, nee_wi.z, nee_ok);
+                    fin_nv = bounce + 1;
                 }
                 if (same_hemisphere(s, wo, bs.wi) && pmix > 0.f) {
                     const f3 f = bsdf_eval(m, s, wo, bs.wi);
@@ -732,6 +744,7 @@ __global__ void __launch_bounds__(256) k_shade_nn(DevScene S, PathBuffers B, int
         // vertices 0 .. bounce-1 had their sampled direction traced; the
         // records are emitted once this vertex's shadow ray has resolved
         fin_bounce = bounce;
+        if (fin_nv < bounce) fin_nv = bounce;
         release = done;
     }
     const int js = warp_append_nn(&ctr->n_shadow, push_sh);
@@ -749,40 +762,61 @@ __global__ void __launch_bounds__(256) k_shade_nn(DevScene S, PathBuffers B, int
         B.info[nx][jc] = ninfo;
     }
     const int jf = warp_append_nn(&ctr->n_fin, release);
-    if (release) PD.fin[jf] = make_int2(slot, fin_bounce);
+    if (release) PD.fin[jf] = make_int4(slot, fin_bounce, fin_nv, 0);
 }
 
-// Finished paths: vertex k's target is the film total gathered after its own
-// NEE, T = lum((S_end - S_k) / throughput_k), i.e. the one-sample estimate of
-// f cos L_i / p_mix along the traced direction wi.
+// Finished paths.  Two records per vertex, both MIS-weighted one-sample
+// estimates of f cos L_i / p along their direction (together an unbiased
+// estimate of the gradient of the loss, one sample from each technique):
+// * the sampled direction wi (traced for vertices 0 .. f.y-1):
+//   T = lum((S_end - S_after_nee_k) / throughput_k);
+// * the NEE direction, where the shadow ray was unoccluded:
+//   T = lum((S_after_nee_k - S_before_nee_k) / throughput_k).
+// S_after_nee of the last vertex is S_end (its shadow ray resolved before
+// this kernel runs).
+__device__ __forceinline__ bool emit_record(const NNPathData& PD, WaveCounters* ctr, const float4* vr, f3 wi,
+                                            float pb, float T) {
+    if (!(T > 0.f) || !isfinite(T)) return true;
+    const int r = atomicAdd(&ctr->n_rec, 1);
+    if (r >= PD.rec_cap) return false;
+    float4* o = PD.rec + 4 * (size_t)r;
+    o[0] = vr[0];
+    o[1] = vr[1];
+    o[2] = make_float4(vr[2].x, wi.x, wi.y, wi.z);
+    o[3] = make_float4(pb, T, 0.f, 0.f);
+    return true;
+}
+
 __global__ void __launch_bounds__(256) k_finish_nn(NNPathData PD, WaveCounters* ctr, int max_depth) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = ctr->n_fin;
     bool release = false;
     int slot = 0;
     if (i < n) {
-        const int2 f = PD.fin[i];
+        const int4 f = PD.fin[i];
         slot = f.x;
         release = true;
         if (PD.rec_cap > 0) {
             const float4 Se = PD.acc[slot];
             const size_t vbase = (size_t)slot * max_depth;
-            for (int k = 0; k < f.y; k++) {
-                const float4* vr = PD.vert + 5 * (vbase + k);
-                const float4 v3 = vr[3], v4 = vr[4];
-                if (v4.w == 0.f) continue;
-                const f3 dS = mk(Se.x - v4.x, Se.y - v4.y, Se.z - v4.z);
-                const f3 q = mk(v3.y > 0.f ? dS.x / v3.y : 0.f, v3.z > 0.f ? dS.y / v3.z : 0.f,
-                                v3.w > 0.f ? dS.z / v3.w : 0.f);
-                const float T = luminance(q);
-                if (!(T > 0.f) || !isfinite(T)) continue;
-                const int r = atomicAdd(&ctr->n_rec, 1);
-                if (r >= PD.rec_cap) break;
-                float4* o = PD.rec + 4 * (size_t)r;
-                o[0] = vr[0];
-                o[1] = vr[1];
-                o[2] = vr[2];
-                o[3] = make_float4(v3.x, T, 0.f, 0.f);
+            for (int k = 0; k < f.z; k++) {
+                const float4* vr = PD.vert + kNNVert * (vbase + k);
+                const float4 v2 = vr[2], v3 = vr[3], v4 = vr[4], v5 = vr[5], v6 = vr[6];
+                const f3 inv = mk(v3.y > 0.f ? 1.0f / v3.y : 0.f, v3.z > 0.f ? 1.0f / v3.z : 0.f,
+                                  v3.w > 0.f ? 1.0f / v3.w : 0.f);
+                const f3 after = k < f.z - 1 || k < f.y ? mk(v4.x, v4.y, v4.z) : mk(Se.x, Se.y, Se.z);
+                if (v6.w != 0.f) {
+                    const f3 dn = mk(after.x - v5.x, after.y - v5.y, after.z - v5.z);
+                    if (!emit_record(PD, ctr, vr, mk(v6.x, v6.y, v6.z), v5.w,
+                                     luminance(mk(dn.x * inv.x, dn.y * inv.y, dn.z * inv.z))))
+                        break;
+                }
+                if (k < f.y && v4.w != 0.f) {
+                    const f3 dS = mk(Se.x - after.x, Se.y - after.y, Se.z - after.z);
+                    if (!emit_record(PD, ctr, vr, mk(v2.y, v2.z, v2.w), v3.x,
+                                     luminance(mk(dS.x * inv.x, dS.y * inv.y, dS.z * inv.z))))
+                        break;
+                }
             }
         }
     }

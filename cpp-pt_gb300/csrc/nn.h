@@ -27,12 +27,14 @@ struct NNTrainBuf {
     int cap;
 };
 
+constexpr int kNNVertFloat4 = 7;  // float4 per recorded path vertex
+
 // Per-path state of the learned-guide integrator (slot = path's free-list entry).
 struct NNPathData {
-    float4* vert;        // 5 float4 per vertex, max_depth vertices per slot
+    float4* vert;        // kNNVertFloat4 float4 per vertex, max_depth vertices per slot
     float4* acc;         // film total gathered by the path so far (rgb)
     int* slot_stack;     // free list of slots
-    int2* fin;           // paths finished this iteration: slot, traced vertices
+    int4* fin;           // paths finished this iteration: slot, traced vertices, extra target of the last
     float4* rec;         // training records, 4 float4 each
     int rec_cap;
 };

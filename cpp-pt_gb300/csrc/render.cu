@@ -174,11 +174,11 @@ __global__ void __launch_bounds__(kTraceThreads) k_shadow(DevScene S, PathBuffer
         });
 }
 
-// BATCH: paths of several scenes of a merged arena; info.w is the path's
-// job, whose table entry replaces the render parameters, light list and film
-// offset.  The per-path arithmetic is the same in both forms.
-template <bool BATCH>
-__global__ void __launch_bounds__(256) k_shade(DevScene S, PathBuffers B, int cur, RenderParams P, WaveCounters* ctr,
+// info.w is the path's job: its table entry holds the render parameters,
+// the scene's light list inside the arena and the job's film offset.  A
+// single-scene render is a table of one job (so batched and single renders
+// run the same instructions and give bit-identical images).
+__global__ void __launch_bounds__(256) k_shade(DevScene S, PathBuffers B, int cur, WaveCounters* ctr,
                                                unsigned long long* __restrict__ film,
                                                const DevBatchJob* __restrict__ jobs) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -193,20 +193,13 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, PathBuffers B, int cu
         const int prim = __float_as_int(H.y);
         const int pixel = I.x, sample = I.y, bounce = I.z & 0xffff;
         const bool sdelta = (I.z >> 16) & 1;
-        uint32_t seed = P.seed;
-        int rr_start = P.rr_start, max_depth = P.max_depth;
-        size_t fpix = (uint32_t)pixel;
-        if (BATCH) {
-            const DevBatchJob* J = jobs + I.w;
-            seed = J->seed;
-            rr_start = J->rr_start;
-            max_depth = J->max_depth;
-            fpix += J->film_off;
-            const int lo = J->light_off;
-            S.light_prim += lo;
-            S.light_area += lo;
-            S.n_lights = J->n_lights;
-        }
+        const DevBatchJob* J = jobs + I.w;
+        const uint32_t seed = J->seed;
+        const int rr_start = J->rr_start, max_depth = J->max_depth;
+        const size_t fpix = (size_t)(uint32_t)pixel + J->film_off;
+        S.light_prim += J->light_off;
+        S.light_area += J->light_off;
+        S.n_lights = J->n_lights;
         float p = O.w;
         f3 mul = mk(T.x, T.y, T.z);
         const f3 ro = mk(O.x, O.y, O.z), rd = mk(D.x, D.y, D.z);
@@ -303,32 +296,33 @@ __device__ __forceinline__ int find_job(const DevBatchJob* __restrict__ jobs, in
     return lo;
 }
 
-template <bool BATCH>
-__global__ void __launch_bounds__(256) k_generate(DevScene S, PathBuffers B, int cur, RenderParams P,
-                                                  WaveCounters* ctr, const DevBatchJob* __restrict__ jobs,
-                                                  int n_jobs) {
+// New camera paths for the free slots of the next buffer; work index w
+// (global over the jobs' pixel x sample ranges) selects job, sample, pixel.
+__global__ void __launch_bounds__(256) k_generate(DevScene S, PathBuffers B, int cur, WaveCounters* ctr,
+                                                  const DevBatchJob* __restrict__ jobs, int n_jobs) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int n_next = ctr->n_next;
     const int avail = B.capacity - n_next;
     unsigned long long w = ctr->work_next + (unsigned long long)t;
     if (t >= avail || w >= ctr->work_total) return;
-    int job = 0, width = P.width, height = P.height, spp_axis = P.spp_axis;
-    uint32_t seed = P.seed, root = S.n_tris > 0 ? 0u : kTravDone;
-    const DevCamera* C = &S.cam;
-    if (BATCH) {
-        job = find_job(jobs, n_jobs, w);
-        const DevBatchJob* J = jobs + job;
-        w -= J->work_begin;
-        C = &J->cam;
-        width = C->width;
-        height = C->height;
-        spp_axis = J->spp_axis;
-        seed = J->seed;
-        root = J->root;
-    }
+    const int job = n_jobs > 1 ? find_job(jobs, n_jobs, w) : 0;
+    const DevBatchJob* J = jobs + job;
+    w -= J->work_begin;
+    const DevCamera* C = &J->cam;
+    const int width = C->width, height = C->height, spp_axis = J->spp_axis;
+    const uint32_t seed = J->seed, root = J->root;
     const unsigned long long npix = (unsigned long long)width * height;
     const int sample = (int)(w / npix);
-    const int pixel = (int)(w - (unsigned long long)sample * npix);
+    int pixel = (int)(w - (unsigned long long)sample * npix);
+    {  // visit the pass in tiles (a bijection of the pixels; the RNG is keyed by pixel, not by order)
+        const int tw = J->tile_w, th = J->tile_h;
+        if (tw * th > 1) {
+            const int tile = pixel / (tw * th), r = pixel - tile * (tw * th);
+            const int tiles_x = width / tw;
+            const int ty = tile / tiles_x, tx = tile - ty * tiles_x;
+            pixel = (ty * th + r / tw) * width + tx * tw + r % tw;
+        }
+    }
     const int px = pixel % width, py = pixel / width;
     const Rng4 r = rng4(seed, sample, pixel, 0xffffu, 2);
     float cx, cy;
@@ -380,20 +374,36 @@ void launch_extend(const DevScene& S, const PathBuffers& B, int cur, WaveCounter
     if (count) k_extend<true><<<num_sms * kTraceBlocksPerSM, kTraceThreads, 0, st>>>(S, B, cur, ctr);
     else k_extend<false><<<num_sms * kTraceBlocksPerSM, kTraceThreads, 0, st>>>(S, B, cur, ctr);
 }
-void launch_shade(const DevScene& S, const PathBuffers& B, int cur, const RenderParams& P, WaveCounters* ctr,
-                  unsigned long long* film, cudaStream_t st, const DevBatchJob* jobs) {
-    if (jobs) k_shade<true><<<(B.capacity + 255) / 256, 256, 0, st>>>(S, B, cur, P, ctr, film, jobs);
-    else k_shade<false><<<(B.capacity + 255) / 256, 256, 0, st>>>(S, B, cur, P, ctr, film, nullptr);
+void launch_shade(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, unsigned long long* film,
+                  const DevBatchJob* jobs, cudaStream_t st) {
+    k_shade<<<(B.capacity + 255) / 256, 256, 0, st>>>(S, B, cur, ctr, film, jobs);
 }
 void launch_shadow(const DevScene& S, const PathBuffers& B, WaveCounters* ctr, unsigned long long* film, int num_sms,
                    cudaStream_t st) {
     k_shadow<<<num_sms * kTraceBlocksPerSM, kTraceThreads, 0, st>>>(S, B, ctr, film);
 }
-void launch_generate(const DevScene& S, const PathBuffers& B, int cur, const RenderParams& P, WaveCounters* ctr,
-                     cudaStream_t st, const DevBatchJob* jobs, int n_jobs) {
-    if (jobs) k_generate<true><<<(B.capacity + 255) / 256, 256, 0, st>>>(S, B, cur, P, ctr, jobs, n_jobs);
-    else k_generate<false><<<(B.capacity + 255) / 256, 256, 0, st>>>(S, B, cur, P, ctr, nullptr, 0);
+void launch_generate(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, const DevBatchJob* jobs,
+                     int n_jobs, cudaStream_t st) {
+    k_generate<<<(B.capacity + 255) / 256, 256, 0, st>>>(S, B, cur, ctr, jobs, n_jobs);
     k_advance<<<1, 32, 0, st>>>(ctr, B.capacity);
+}
+
+DevBatchJob single_job(const DevScene& S, const RenderParams& P) {
+    DevBatchJob j{};
+    j.cam = S.cam;
+    j.work_begin = 0;
+    j.film_off = 0;
+    j.root = S.n_tris > 0 ? 0u : kTravDone;
+    j.light_off = 0;
+    j.n_lights = S.n_lights;
+    j.spp = P.spp;
+    j.spp_axis = P.spp_axis;
+    j.max_depth = P.max_depth;
+    j.rr_start = P.rr_start;
+    j.seed = P.seed;
+    j.tile_w = 1;
+    j.tile_h = 1;
+    return j;
 }
 void launch_film_resolve(const unsigned long long* film, float* out, int n, double scale, cudaStream_t st) {
     k_resolve<<<min((n + 255) / 256, 4096), 256, 0, st>>>(film, out, n, scale * (1.0 / 4294967296.0));
@@ -420,7 +430,9 @@ constexpr int kNoAllocMaxPixels = 1 << 18;  // e.g. 512 x 512
 constexpr size_t kNoAllocPathBytes = (size_t)kNoAllocPaths * 16;  // one float4 / int4 array
 constexpr size_t kNoAllocFilmOffset = 12 * kNoAllocPathBytes;
 constexpr size_t kNoAllocCtrOffset = kNoAllocFilmOffset + (size_t)3 * kNoAllocMaxPixels * 8;
-constexpr size_t kNoAllocBytes = kNoAllocCtrOffset + 256;
+constexpr size_t kNoAllocJobOffset = kNoAllocCtrOffset + 256;
+constexpr size_t kNoAllocBytes = kNoAllocJobOffset + 256;
+static_assert(sizeof(WaveCounters) <= 256 && sizeof(DevBatchJob) <= 256, "scratch slots");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
@@ -472,6 +484,7 @@ cudaError_t render_noalloc(const DevScene& S, const RenderParams& P, int num_sms
     B.capacity = kNoAllocPaths;
     unsigned long long* film = reinterpret_cast<unsigned long long*>(b + kNoAllocFilmOffset);
     WaveCounters* ctr = reinterpret_cast<WaveCounters*>(b + kNoAllocCtrOffset);
+    DevBatchJob* job = reinterpret_cast<DevBatchJob*>(b + kNoAllocJobOffset);
     const int film_n = 3 * P.width * P.height;
     const unsigned long long total = (unsigned long long)P.width * P.height * (unsigned long long)P.spp;
     e = cudaMemsetAsync(film, 0, sizeof(unsigned long long) * film_n, st);
@@ -480,7 +493,10 @@ cudaError_t render_noalloc(const DevScene& S, const RenderParams& P, int num_sms
     init.work_total = total;
     e = cudaMemcpyAsync(ctr, &init, sizeof(init), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return e;
-    launch_generate(S, B, 1, P, ctr, st);
+    const DevBatchJob hjob = single_job(S, P);
+    e = cudaMemcpyAsync(job, &hjob, sizeof(hjob), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return e;
+    launch_generate(S, B, 1, ctr, job, 1, st);
     const int iters = 16;
     const unsigned long long max_rounds =
         64 + (total / (unsigned long long)kNoAllocPaths + 2) * (unsigned long long)(max_depth + 2) * 4 / iters;
@@ -489,9 +505,9 @@ cudaError_t render_noalloc(const DevScene& S, const RenderParams& P, int num_sms
         for (int k = 0; k < iters; k++) {
             const int cur = k & 1;
             launch_extend(S, B, cur, ctr, num_sms, st, false);
-            launch_shade(S, B, cur, P, ctr, film, st);
+            launch_shade(S, B, cur, ctr, film, job, st);
             launch_shadow(S, B, ctr, film, num_sms, st);
-            launch_generate(S, B, cur, P, ctr, st);
+            launch_generate(S, B, cur, ctr, job, 1, st);
         }
         e = cudaMemcpyAsync(&h, ctr, sizeof(h), cudaMemcpyDeviceToHost, st);
         if (e != cudaSuccess) return e;

@@ -123,13 +123,19 @@ struct TraceCount {
 };
 
 constexpr uint32_t kTravDone = 0xffffffffu;  // never a valid node or leaf reference
+constexpr uint32_t kLeafRef = 0x80000000u;
+
+__device__ __forceinline__ bool is_inner(uint32_t r) { return !(r & kLeafRef); }  // kTravDone has the bit set
+__device__ __forceinline__ bool is_leaf(uint32_t r) { return (r & kLeafRef) && r != kTravDone; }
 
 struct Trav {
     float3 o, d;
     float idx, idy, idz, oix, oiy, oiz;
     float tmax0;
-    uint32_t neg;  // bit k: direction component k is negative
-    uint32_t cur;
+    uint32_t neg;   // bit k: direction component k is negative
+    uint32_t cur;   // next node or leaf to visit (kTravDone: nothing left on the stack)
+    float cur_t;    // entry distance of cur
+    uint32_t leaf;  // leaf postponed to the warp's next leaf phase (kTravDone: none)
     int sp, steps;
     HitRec best;
 };
@@ -163,126 +169,150 @@ __device__ __forceinline__ void trav_init(Trav& T, float3 o, float3 d, float tma
     T.oiz = o.z * T.idz;
     T.neg = (T.idx < 0.f ? 1u : 0u) | (T.idy < 0.f ? 2u : 0u) | (T.idz < 0.f ? 4u : 0u);
     T.cur = root;
+    T.cur_t = 0.f;
+    T.leaf = kTravDone;
     T.sp = 0;
     T.steps = 0;
 }
 
-// Advances the ray by one wide node or one leaf.  Returns true when the
-// traversal is finished (result in T.best).
-template <bool ANY, bool COUNT>
-__device__ __forceinline__ bool trav_step(Trav& T, TravStack& K, const DevScene& S, const uint4* __restrict__ snodes,
-                                          uint32_t* status, TraceCount& cnt) {
-    if (T.cur == kTravDone) return true;
-    if (++T.steps > kMaxTraversalSteps) {
-        atomicOr(status, kStatusIterLimit);
-        T.cur = kTravDone;
-        return true;
-    }
-    if (!(T.cur & 0x80000000u)) {
-        if (COUNT) cnt.nodes++;
-        const uint32_t cur = T.cur;
-        uint4 w0, w1, w2, w3;
-        if (cur < (uint32_t)kSmemNodes) {
-            w0 = snodes[4 * cur]; w1 = snodes[4 * cur + 1]; w2 = snodes[4 * cur + 2]; w3 = snodes[4 * cur + 3];
-        } else {
-            const uint4* np = S.nodes + 4 * (size_t)cur;
-            w0 = __ldg(np); w1 = __ldg(np + 1); w2 = __ldg(np + 2); w3 = __ldg(np + 3);
-        }
-        const float cull = T.best.t * kCullScale + 1e-6f;
-        // slab distance of quantised coordinate q on axis k:
-        //   (p + q s - o) / d = q (s/d) + (p - o)/d = q B + A
-        const float ax = fmaf(__uint_as_float(w0.x), T.idx, -T.oix);
-        const float ay = fmaf(__uint_as_float(w0.y), T.idy, -T.oiy);
-        const float az = fmaf(__uint_as_float(w0.z), T.idz, -T.oiz);
-        const float bx = __uint_as_float((w0.w & 0xffu) << 23) * T.idx;
-        const float by = __uint_as_float(((w0.w >> 8) & 0xffu) << 23) * T.idy;
-        const float bz = __uint_as_float(((w0.w >> 16) & 0xffu) << 23) * T.idz;
-        // words: lo_x lo_y lo_z hi_x | hi_y hi_z ref0 ref1 | ref2 ref3
-        const bool nxs = T.neg & 1u, nys = T.neg & 2u, nzs = T.neg & 4u;
-        const uint32_t nx = nxs ? w1.w : w1.x, fx = nxs ? w1.x : w1.w;
-        const uint32_t ny = nys ? w2.x : w1.y, fy = nys ? w1.y : w2.x;
-        const uint32_t nz = nzs ? w2.y : w1.z, fz = nzs ? w1.z : w2.y;
-        uint32_t key[4];
-#pragma unroll
-        for (int c = 0; c < 4; c++) {
-            const float tnx = fmaf(byte_to_float(nx, c), bx, ax);
-            const float tny = fmaf(byte_to_float(ny, c), by, ay);
-            const float tnz = fmaf(byte_to_float(nz, c), bz, az);
-            const float tfx = fmaf(byte_to_float(fx, c), bx, ax);
-            const float tfy = fmaf(byte_to_float(fy, c), by, ay);
-            const float tfz = fmaf(byte_to_float(fz, c), bz, az);
-            const float tn = fmax3(tnx, tny, fmaxf(tnz, 0.0f));
-            const float tf = fmin3(tfx, tfy, fminf(tfz, cull));
-            const bool hit = tn <= tf * 1.0000005f;
-            key[c] = hit ? ((__float_as_uint(tn) & ~3u) | (uint32_t)c) : 0xffffffffu;
-        }
-#define CSWAP(a, b) { uint32_t lo_ = min(key[a], key[b]), hi_ = max(key[a], key[b]); key[a] = lo_; key[b] = hi_; }
-        CSWAP(0, 1) CSWAP(2, 3) CSWAP(0, 2) CSWAP(1, 3) CSWAP(1, 2)
-#undef CSWAP
-        if (key[0] != 0xffffffffu) {
-            const uint32_t refs[4] = {w2.z, w2.w, w3.x, w3.y};
-            if (T.sp + 3 > kStackSize) {
-                atomicOr(status, kStatusStackOverflow);
-                T.cur = kTravDone;
-                return true;
-            }
-            // far children first; an invalid key is written but not counted
-#pragma unroll
-            for (int k = 3; k >= 1; k--) {
-                K.ref[T.sp] = refs[key[k] & 3u];
-                K.t[T.sp] = __uint_as_float(key[k] & ~3u);
-                T.sp += (key[k] != 0xffffffffu) ? 1 : 0;
-            }
-            T.cur = refs[key[0] & 3u];
-            return false;
-        }
-    } else {
-        const uint32_t start = T.cur & 0x7ffffffu;
-        const uint32_t count = ((T.cur >> 27) & 15u) + 1u;
-        if (COUNT) cnt.tris += count;
-        for (uint32_t k = 0; k < count; k++) {
-            const float4* tp = S.tris + 3 * (size_t)(start + k);
-            const float4 A = __ldg(tp), E1 = __ldg(tp + 1), E2 = __ldg(tp + 2);
-            float t, beta, gamma;
-            // ANY: the reference tests against the ray's own max_t
-            if (!tri_exact(A, E1, E2, T.o, T.d, ANY ? T.tmax0 : T.best.t, t, beta, gamma)) continue;
-            const int32_t rank = __float_as_int(A.w);
-            if (!ANY && !(t < T.best.t || rank > T.best.rank)) continue;  // equal t: the later-visited wins
-            const int32_t parent = __float_as_int(E1.w);
-            if (parent >= 0) {
-                const float4 lo = __ldg(S.ref_box + 2 * parent), hi = __ldg(S.ref_box + 2 * parent + 1);
-                if (!ref_box_exact(lo, hi, T.o, T.d, t)) continue;
-            }
-            T.best.t = t;
-            T.best.rank = rank;
-            T.best.prim = __float_as_int(E2.w);
-            T.best.beta = beta;
-            T.best.gamma = gamma;
-            if (ANY) {
-                T.cur = kTravDone;
-                return true;
-            }
-        }
-    }
-    // pop the next node that is still in front of the best hit
-    const float cull2 = T.best.t * kCullScale + 1e-6f;
+__device__ __forceinline__ float cull_dist(const Trav& T) { return T.best.t * kCullScale + 1e-6f; }
+
+// Next stacked node that is still in front of the best hit.
+__device__ __forceinline__ void trav_pop(Trav& T, const TravStack& K) {
+    const float cull = cull_dist(T);
     while (T.sp > 0) {
         T.sp--;
-        if (K.t[T.sp] <= cull2) {
+        if (K.t[T.sp] <= cull) {
             T.cur = K.ref[T.sp];
-            return false;
+            T.cur_t = K.t[T.sp];
+            return;
         }
     }
     T.cur = kTravDone;
-    return true;
+}
+
+__device__ __forceinline__ void trav_abort(Trav& T, uint32_t* status, uint32_t bit) {
+    atomicOr(status, bit);
+    T.cur = kTravDone;
+    T.leaf = kTravDone;
+    T.sp = 0;
+}
+
+// One inner node (T.cur): the children the ray enters in front of the best
+// hit, nearest first; far children are pushed.
+template <bool COUNT>
+__device__ __forceinline__ void trav_node(Trav& T, TravStack& K, const DevScene& S, const uint4* __restrict__ snodes,
+                                          uint32_t* status, TraceCount& cnt) {
+    if (COUNT) cnt.nodes++;
+    const uint32_t cur = T.cur;
+    uint4 w0, w1, w2, w3;
+    if (cur < (uint32_t)kSmemNodes) {
+        w0 = snodes[4 * cur]; w1 = snodes[4 * cur + 1]; w2 = snodes[4 * cur + 2]; w3 = snodes[4 * cur + 3];
+    } else {
+        const uint4* np = S.nodes + 4 * (size_t)cur;
+        w0 = __ldg(np); w1 = __ldg(np + 1); w2 = __ldg(np + 2); w3 = __ldg(np + 3);
+    }
+    const float cull = cull_dist(T);
+    // slab distance of quantised coordinate q on axis k:
+    //   (p + q s - o) / d = q (s/d) + (p - o)/d = q B + A
+    const float ax = fmaf(__uint_as_float(w0.x), T.idx, -T.oix);
+    const float ay = fmaf(__uint_as_float(w0.y), T.idy, -T.oiy);
+    const float az = fmaf(__uint_as_float(w0.z), T.idz, -T.oiz);
+    const float bx = __uint_as_float((w0.w & 0xffu) << 23) * T.idx;
+    const float by = __uint_as_float(((w0.w >> 8) & 0xffu) << 23) * T.idy;
+    const float bz = __uint_as_float(((w0.w >> 16) & 0xffu) << 23) * T.idz;
+    // words: lo_x lo_y lo_z hi_x | hi_y hi_z ref0 ref1 | ref2 ref3
+    const bool nxs = T.neg & 1u, nys = T.neg & 2u, nzs = T.neg & 4u;
+    const uint32_t nx = nxs ? w1.w : w1.x, fx = nxs ? w1.x : w1.w;
+    const uint32_t ny = nys ? w2.x : w1.y, fy = nys ? w1.y : w2.x;
+    const uint32_t nz = nzs ? w2.y : w1.z, fz = nzs ? w1.z : w2.y;
+    uint32_t key[4];
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        const float tnx = fmaf(byte_to_float(nx, c), bx, ax);
+        const float tny = fmaf(byte_to_float(ny, c), by, ay);
+        const float tnz = fmaf(byte_to_float(nz, c), bz, az);
+        const float tfx = fmaf(byte_to_float(fx, c), bx, ax);
+        const float tfy = fmaf(byte_to_float(fy, c), by, ay);
+        const float tfz = fmaf(byte_to_float(fz, c), bz, az);
+        const float tn = fmax3(tnx, tny, fmaxf(tnz, 0.0f));
+        const float tf = fmin3(tfx, tfy, fminf(tfz, cull));
+        const bool hit = tn <= tf * 1.0000005f;
+        key[c] = hit ? ((__float_as_uint(tn) & ~3u) | (uint32_t)c) : 0xffffffffu;
+    }
+#define CSWAP(a, b) { uint32_t lo_ = min(key[a], key[b]), hi_ = max(key[a], key[b]); key[a] = lo_; key[b] = hi_; }
+    CSWAP(0, 1) CSWAP(2, 3) CSWAP(0, 2) CSWAP(1, 3) CSWAP(1, 2)
+#undef CSWAP
+    if (key[0] == 0xffffffffu) {
+        trav_pop(T, K);
+        return;
+    }
+    const uint32_t refs[4] = {w2.z, w2.w, w3.x, w3.y};
+    if (T.sp + 3 > kStackSize) {
+        trav_abort(T, status, kStatusStackOverflow);
+        return;
+    }
+    // far children first; an invalid key is written but not counted
+#pragma unroll
+    for (int k = 3; k >= 1; k--) {
+        K.ref[T.sp] = refs[key[k] & 3u];
+        K.t[T.sp] = __uint_as_float(key[k] & ~3u);
+        T.sp += (key[k] != 0xffffffffu) ? 1 : 0;
+    }
+    T.cur = refs[key[0] & 3u];
+    T.cur_t = __uint_as_float(key[0] & ~3u);
+}
+
+// The postponed leaf T.leaf.  Returns true when an any-hit query is answered.
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ bool trav_leaf(Trav& T, const DevScene& S, TraceCount& cnt) {
+    const uint32_t start = T.leaf & 0x7ffffffu;
+    const uint32_t count = ((T.leaf >> 27) & 15u) + 1u;
+    T.leaf = kTravDone;
+    if (COUNT) cnt.tris += count;
+    for (uint32_t k = 0; k < count; k++) {
+        const float4* tp = S.tris + 3 * (size_t)(start + k);
+        const float4 A = __ldg(tp), E1 = __ldg(tp + 1), E2 = __ldg(tp + 2);
+        float t, beta, gamma;
+        // ANY: the reference tests against the ray's own max_t
+        if (!tri_exact(A, E1, E2, T.o, T.d, ANY ? T.tmax0 : T.best.t, t, beta, gamma)) continue;
+        const int32_t rank = __float_as_int(A.w);
+        if (!ANY && !(t < T.best.t || rank > T.best.rank)) continue;  // equal t: the later-visited wins
+        const int32_t parent = __float_as_int(E1.w);
+        if (parent >= 0) {
+            const float4 lo = __ldg(S.ref_box + 2 * parent), hi = __ldg(S.ref_box + 2 * parent + 1);
+            if (!ref_box_exact(lo, hi, T.o, T.d, t)) continue;
+        }
+        T.best.t = t;
+        T.best.rank = rank;
+        T.best.prim = __float_as_int(E2.w);
+        T.best.beta = beta;
+        T.best.gamma = gamma;
+        if (ANY) {
+            T.cur = kTravDone;
+            T.sp = 0;
+            return true;
+        }
+    }
+    return false;
 }
 
 // Persistent ray loop.  Each warp takes chunks of kChunk consecutive rays
 // from a global counter into a warp-private range; a lane whose ray finishes
-// takes the next ray of the range at once (no waiting for the other lanes),
-// and the warp runs one traversal step per iteration.  load(i, o, d, tmax,
-// root) fetches ray i; root arrives set to the scene's own root and may be
-// replaced (rays of a merged multi-scene arena).
+// takes the next ray of the range at once (no waiting for the other lanes).
+// load(i, o, d, tmax, root) fetches ray i; root arrives set to the scene's
+// own root and may be replaced (rays of a merged multi-scene arena).
+//
+// Every iteration has a node phase and, when enough of the warp is waiting
+// on a leaf, a leaf phase (leaves are postponed as in Aila and Laine 2009,
+// "Understanding the efficiency of ray traversal on GPUs"): a lane that
+// reaches a leaf parks it and keeps descending inner nodes, and the warp
+// tests triangles together once half of its active lanes cannot continue
+// without their leaf, or no lane has an inner node left.  Inner-node and
+// triangle code then run with most lanes converged instead of alternating
+// per lane.  The result does not depend on the visiting order: the closest
+// hit is the minimum over the tested triangles of (t, -rank), and a node is
+// culled only when its entry distance lies behind the best hit found so far.
 constexpr int kChunk = 64;
 
 template <bool ANY, bool COUNT, class Load, class Store>
@@ -321,26 +351,35 @@ __device__ __forceinline__ void persistent_trace(const DevScene& S, const uint4*
                 pool_next += min(avail, __popc(idle));
             }
         }
-        if (__ballot_sync(0xffffffffu, ray >= 0) == 0) break;
-        if (ray >= 0 && trav_step<ANY, COUNT>(T, K, S, snodes, status, cnt)) {
+        const bool active = ray >= 0;
+        if (__ballot_sync(0xffffffffu, active) == 0) break;
+        // node phase: one inner node per lane (a node that fell behind the
+        // best hit since it was queued is dropped for the next one)
+        if (active && is_inner(T.cur)) {
+            if (++T.steps > kMaxTraversalSteps) trav_abort(T, status, kStatusIterLimit);
+            else if (T.cur_t > cull_dist(T)) trav_pop(T, K);
+            else trav_node<COUNT>(T, K, S, snodes, status, cnt);
+        }
+        if (active && T.leaf == kTravDone && is_leaf(T.cur)) {  // park the leaf, continue below the stack
+            T.leaf = T.cur;
+            trav_pop(T, K);
+        }
+        // leaf phase (warp-uniform decision)
+        const bool waiting = active && T.leaf != kTravDone && !is_inner(T.cur);
+        const unsigned act = __ballot_sync(0xffffffffu, active);
+        const unsigned wait = __ballot_sync(0xffffffffu, waiting);
+        const unsigned inner = __ballot_sync(0xffffffffu, active && is_inner(T.cur));
+        if (2 * __popc(wait) >= __popc(act) || inner == 0) {
+            if (active && T.leaf != kTravDone) {
+                ++T.steps;
+                if (trav_leaf<ANY, COUNT>(T, S, cnt)) T.leaf = kTravDone;
+            }
+        }
+        if (active && T.cur == kTravDone && T.leaf == kTravDone) {
             store(ray, T.best);
             ray = -1;
         }
     }
-}
-
-// One ray, start to finish (used where rays are not batched).
-template <bool ANY>
-__device__ __forceinline__ bool traverse(const DevScene& S, const uint4* __restrict__ snodes, float3 o, float3 d,
-                                         float tmax0, HitRec& best, uint32_t* status) {
-    Trav T;
-    TravStack K;
-    TraceCount cnt{0u, 0u};
-    trav_init(T, o, d, tmax0, S.n_tris > 0 ? 0u : kTravDone);
-    while (!trav_step<ANY, false>(T, K, S, snodes, status, cnt)) {
-    }
-    best = T.best;
-    return best.prim >= 0;
 }
 
 }  // namespace cpppt_gb300

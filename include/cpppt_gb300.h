@@ -129,9 +129,11 @@ typedef struct {
 /* pt_render_desc.flags */
 #define PT_FLAG_TIME_KERNELS 1 /* launch iterations directly with CUDA events around the traversal kernels */
 #define PT_FLAG_COUNT 2        /* counting build of the extension kernel (visited nodes / tested triangles) */
-#define PT_FLAG_UNBIASED_MIS 4 /* PT_MODE_MIS with MIS weights on the unscaled pdf and Russian roulette
-                                  survival min(rr, 1): the unbiased estimator the learned guide also uses
-                                  (the default keeps the reference's RR-scaled weights, pathtracerMIS.h:118-124) */
+#define PT_FLAG_UNBIASED_MIS 4 /* PT_MODE_MIS with MIS weights on the unscaled pdf, Russian roulette
+                                  survival min(rr, 1) and full NEE weight at the last vertex: the
+                                  unbiased estimator of the depth-limited image that the learned guide
+                                  also uses (the default keeps the reference's RR-scaled weights,
+                                  pathtracerMIS.h:118-124, and its MIS weight at the last vertex) */
 #define PT_FLAG_NN_FREEZE 8    /* PT_MODE_NN: use the current network without training it */
 
 /* Replaces: Loader::load_scene + BVH::add/build (loader.h:314-374,
@@ -195,6 +197,47 @@ pt_status pt_render_device(pt_scene* scene, const pt_render_desc* desc, float* d
 pt_status pt_render_device_noalloc(pt_scene* scene, const pt_render_desc* desc, float* d_rgb_out, void* stream);
 
 pt_status pt_render_stats_get(pt_scene* scene, pt_render_stats* stats);
+
+/* Multi-scene batches.  No counterpart in the reference, which renders one
+ * scene per process (main.cpp); each job of a batch is the equivalent of one
+ * pt_render call (PathtracerMIS::render, pathtracerMIS.h:145-167) and gives
+ * the bit-identical image, but all jobs share one wavefront on the GPU.
+ * pt_batch_create copies the scenes' device data into one merged arena (the
+ * scenes stay valid and independent; at most 2^27 - 1 triangles in total).
+ * A job renders scene `scene` (index into the creation list) with spp,
+ * max_depth, rr_start and seed as pt_render_desc with PT_MODE_MIS, flags 0.
+ * rgb_out[i] / d_rgb_out[i]: 3 floats per pixel of job i's scene (host or
+ * device memory; a null entry skips that copy). */
+typedef struct pt_batch pt_batch;
+typedef struct pt_batch_job {
+    int32_t scene;
+    int32_t spp;
+    int32_t max_depth;
+    int32_t rr_start;
+    uint32_t seed;
+} pt_batch_job;
+/* Launch shape of a batch: paths in flight (multiple of 1024, <= 2^22),
+ * wavefront iterations per CUDA graph launch (even), pixel tile of the
+ * path order (1 x 1 = scanline; used where it divides the resolution).
+ * None of them changes the images. */
+typedef struct pt_batch_tuning {
+    int32_t capacity;
+    int32_t iters_per_graph;
+    int32_t tile_w;
+    int32_t tile_h;
+} pt_batch_tuning;
+pt_status pt_batch_create(pt_scene* const* scenes, int32_t n_scenes, pt_batch** batch);
+void pt_batch_destroy(pt_batch* batch);
+pt_status pt_batch_render(pt_batch* batch, const pt_batch_job* jobs, int32_t n_jobs, float* const* rgb_out);
+pt_status pt_batch_render_device(pt_batch* batch, const pt_batch_job* jobs, int32_t n_jobs, float* const* d_rgb_out);
+pt_status pt_batch_set_tuning(pt_batch* batch, const pt_batch_tuning* tuning);
+pt_status pt_batch_get_tuning(pt_batch* batch, pt_batch_tuning* tuning);
+/* Statistics of the last batch render (paths, rays, time; per batch). */
+pt_status pt_batch_stats(pt_batch* batch, pt_render_stats* stats);
+/* Times every candidate launch shape on the jobs with spp / spp_divisor
+ * (at least 1) and keeps the fastest; returns it and its Mpaths/s. */
+pt_status pt_batch_autotune(pt_batch* batch, const pt_batch_job* jobs, int32_t n_jobs, int32_t spp_divisor,
+                            pt_batch_tuning* best, double* best_mpaths);
 
 /* Writes <prefix>.png (sRGB, 8-bit, clipped as pixel_ops::put2char1) and
  * <prefix>.hdr (Radiance RGBE), as Image::save (rgb_image.h:300-318). */

@@ -1,0 +1,99 @@
+"""Multi-scene batches: every job's image must be bit-identical to pt_render
+of the same scene with the same parameters, whatever the launch shape."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def members(gpu_lib):
+    from cpppt import scenes
+    from cpppt.lib import GpuScene
+    scs = [
+        scenes.cornell(32, 32),
+        scenes.soup(seed=11, n_spheres=40, freq=3, width=24, height=16),
+        scenes.slit_room(seed=4, n_boxes=20, box_subdiv=2, width=16, height=8),
+        scenes.soup(seed=12, n_spheres=300, freq=4, width=40, height=24),
+        scenes.cornell(8, 8),
+    ]
+    return [GpuScene(s) for s in scs]
+
+
+JOBS = [
+    dict(scene=0, spp=16, max_depth=8, seed=3),
+    dict(scene=1, spp=9, max_depth=10, seed=5),
+    dict(scene=2, spp=4, max_depth=12, seed=7),
+    dict(scene=3, spp=7, max_depth=10, seed=9),
+    dict(scene=0, spp=5, max_depth=4, rr_start=1, seed=11),  # the same scene again, other parameters
+    dict(scene=4, spp=64, max_depth=8, seed=13),
+]
+
+
+def unbatched(members, j):
+    return members[j["scene"]].render(j["spp"], max_depth=j.get("max_depth", 32), rr_start=j.get("rr_start", 3),
+                                      seed=j.get("seed", 0))
+
+
+def test_batch_matches_unbatched_bit_exact(members):
+    from cpppt.lib import GpuBatch
+    b = GpuBatch(members)
+    imgs = b.render(JOBS)
+    st = b.stats()
+    assert st["paths"] == sum(members[j["scene"]].width * members[j["scene"]].height * j["spp"] for j in JOBS)
+    for j, img in zip(JOBS, imgs):
+        ref = unbatched(members, j)
+        assert img.shape == ref.shape
+        assert np.array_equal(img.view(np.uint32), ref.view(np.uint32)), j
+        assert img.mean() > 0
+
+
+@pytest.mark.parametrize("tuning", [dict(capacity=1024, iters_per_graph=2, tile_w=1, tile_h=1),
+                                    dict(capacity=4096, iters_per_graph=8, tile_w=8, tile_h=4),
+                                    dict(capacity=1 << 20, iters_per_graph=32, tile_w=4, tile_h=8)])
+def test_launch_shape_does_not_change_images(members, tuning):
+    from cpppt.lib import GpuBatch
+    b = GpuBatch(members)
+    ref = b.render(JOBS)
+    got = b.set_tuning(**tuning)
+    assert got == tuning
+    imgs = b.render(JOBS)
+    for a, r in zip(imgs, ref):
+        assert np.array_equal(a.view(np.uint32), r.view(np.uint32))
+
+
+def test_autotune_picks_a_valid_shape(members):
+    from cpppt.lib import GpuBatch
+    b = GpuBatch(members)
+    best, rate = b.autotune(JOBS, spp_divisor=2)
+    assert rate > 0
+    assert best == b.tuning()
+    assert best["capacity"] % 1024 == 0 and best["iters_per_graph"] % 2 == 0
+    imgs = b.render(JOBS[:2])
+    for j, img in zip(JOBS[:2], imgs):
+        assert np.array_equal(img.view(np.uint32), unbatched(members, j).view(np.uint32))
+
+
+def test_device_outputs(members):
+    import torch
+    from cpppt.lib import GpuBatch
+    b = GpuBatch(members)
+    outs = [torch.zeros((members[j["scene"]].height, members[j["scene"]].width, 3), dtype=torch.float32,
+                        device="cuda") for j in JOBS]
+    b.render_device(JOBS, [o.data_ptr() for o in outs])
+    for j, o in zip(JOBS, outs):
+        assert np.array_equal(o.cpu().numpy().view(np.uint32), unbatched(members, j).view(np.uint32))
+
+
+def test_batch_errors(members):
+    from cpppt.lib import GpuBatch, PtError
+    b = GpuBatch(members)
+    with pytest.raises(PtError):
+        b.render([dict(scene=len(members), spp=1)])
+    with pytest.raises(PtError):
+        b.render([dict(scene=0, spp=0)])
+    with pytest.raises(PtError):
+        b.set_tuning(capacity=1000)
+    with pytest.raises(PtError):
+        b.set_tuning(iters_per_graph=3)
+    b.render([dict(scene=0, spp=1)])  # still usable

@@ -45,6 +45,33 @@ def test_closest_matches_oracle_large_batch(gpu_lib):
     assert np.array_equal(gt.view(np.uint32), ot.view(np.uint32))
 
 
+@pytest.mark.parametrize("config", ["cornell256", "soup1M"])
+def test_full_size_ray_batch_matches_oracle(gpu_lib, config):
+    """2^20 rays (seed 6: camera, secondary, edge/vertex and axis-parallel
+    rays) on the Cornell box and on the 1M-triangle soup: closest-hit ids and
+    distances bit-exact, any-hit answers identical for max_t around the hit."""
+    from cpppt.lib import GpuScene
+    from oracle.oracle import Oracle
+    sc = scenes.cornell(256, 256) if config == "cornell256" else scenes.soup(seed=2)
+    rays = scenes.hit_ray_batch(sc, 1 << 20, seed=6)
+    osc = Oracle("port").scene(sc)
+    oi, ot = osc.trace_closest(rays)
+    gs = GpuScene(sc)
+    gi, gt, _, _ = gs.trace_closest(rays)
+    assert (oi >= 0).mean() > 0.5
+    bad = np.nonzero(gi != oi)[0]
+    assert bad.size == 0, (bad.size, bad[:8])
+    assert np.array_equal(gt.view(np.uint32), ot.view(np.uint32))
+    sh = rays.copy()
+    rng = np.random.default_rng(7)
+    hit = oi >= 0
+    sh[hit, 6] = ot[hit] * rng.uniform(0.5, 1.5, size=hit.sum()).astype(np.float32)
+    oo = osc.trace_any(sh)
+    go = gs.trace_any(sh)
+    assert 0.2 < oo.mean() < 0.9
+    assert np.array_equal(go, oo)
+
+
 def test_empty_and_degenerate_inputs(gpu_lib):
     from cpppt.lib import GpuScene
     sc = scenes.cornell(16, 16)
