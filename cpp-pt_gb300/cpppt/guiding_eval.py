@@ -2,121 +2,170 @@
 the occluded-light room (emitter behind a 0.05-wide slit, indirect light
 dominates).
 
-    python -m cpppt.guiding_eval [--budgets 10 30 60] [--ref-spp 4096]
+    python -m cpppt.guiding_eval [--budgets 10 30 60] [--ref-spp 16384]
 
 All three estimators converge to the same image on this all-Lambert scene
 (albedo <= 0.8 keeps the Russian-roulette survival below 1), so each is
-scored by relMSE = mean (x - ref)^2 / (ref^2 + 1e-2) against one
-high-spp reference rendered with the plain tracer (PT_FLAG_UNBIASED_MIS):
+scored by relMSE = mean over pixels and channels of (x - ref)^2 / (ref^2 +
+1e-2) against one high-spp reference rendered with the plain tracer
+(PT_FLAG_UNBIASED_MIS):
 
 * plain  -- PT + NEE + MIS, BSDF sampling only (PT_FLAG_UNBIASED_MIS);
 * nn     -- PT + NEE + MIS with the learned vMF-mixture guide, trained
-            online from fresh weights inside the time budget;
+            online from fresh weights inside the time budget (training time
+            counts);
 * sdtree -- the reference's practical path guiding (PPG: SD-tree, no NEE),
             one render whose spp is sized to the budget.
 
-Prints one JSON line per method and budget, then a summary with the time
-each method needs to reach plain PT's relMSE at the largest budget.
+Plain and nn accumulate chunks of spp on the GPU; relMSE is taken at
+checkpoints spaced by sqrt(2) up to the largest budget.  Prints one JSON
+line per method and checkpoint, then a summary: relMSE of each method at
+each budget, and the time nn needs to reach plain's relMSE at that budget
+(linear interpolation of log relMSE over log time between checkpoints).
 """
 from __future__ import annotations
 
 import argparse
 import json
+import math
 import time
 
 import numpy as np
+import torch
 
 from . import scenes
-from .lib import FLAG_UNBIASED_MIS, MODE_MIS, MODE_NN, MODE_SDTREE, GpuScene
+from .lib import FLAG_NN_FREEZE, FLAG_UNBIASED_MIS, MODE_MIS, MODE_NN, MODE_SDTREE, GpuScene
 
 
-def rel_mse(x, ref):
-    return float(np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2)))
+def rel_mse(x: torch.Tensor, ref: torch.Tensor) -> float:
+    return float(((x - ref) ** 2 / (ref ** 2 + 1e-2)).mean())
 
 
 def progressive(gs, mode, flags, budget_s, chunk_spp, depth, seed0, ref, checkpoints):
-    """Renders chunks until the budget is spent; returns [(elapsed, spp, relMSE)] at each checkpoint."""
-    acc = None
-    spp_total = 0
-    out = []
-    t0 = time.perf_counter()
-    k = 0
+    """Renders chunks until the budget is spent, accumulating on the GPU;
+    returns [(seconds, spp, relMSE)] at the checkpoints and the final image."""
+    H, W = ref.shape[:2]
+    img = torch.zeros((H, W, 3), dtype=torch.float32, device="cuda")
+    acc = torch.zeros((H, W, 3), dtype=torch.float64, device="cuda")
+    spp_total, k = 0, 0
+    snaps = []
     cps = sorted(checkpoints)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
     while True:
-        img = gs.render(chunk_spp, max_depth=depth, seed=seed0 + k, mode=mode, flags=flags)
+        gs.render_device(img.data_ptr(), chunk_spp, max_depth=depth, seed=seed0 + k, mode=mode, flags=flags)
+        acc += img.double() * chunk_spp
         k += 1
-        acc = img * chunk_spp if acc is None else acc + img * chunk_spp
         spp_total += chunk_spp
         el = time.perf_counter() - t0
         while cps and el >= cps[0]:
-            out.append((cps.pop(0), spp_total, rel_mse(acc / spp_total, ref)))
+            snaps.append((cps.pop(0), spp_total, (acc / spp_total).float().clone()))
         if not cps or el >= budget_s:
             break
-    return out, acc / spp_total, spp_total
+    torch.cuda.synchronize()
+    out = [(t, spp, rel_mse(x, ref)) for t, spp, x in snaps]
+    return out, (acc / spp_total).float(), spp_total
+
+
+def time_to_reach(rows, target):
+    """First time the (log time, log relMSE) curve crosses target."""
+    prev = None
+    for t, _, r in rows:
+        if r <= target:
+            if prev is None:
+                return t
+            t0, r0 = prev
+            a = (math.log(target) - math.log(r0)) / (math.log(r) - math.log(r0))
+            return math.exp(math.log(t0) + a * (math.log(t) - math.log(t0)))
+        prev = (t, r)
+    return None
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--budgets", type=float, nargs="+", default=[10, 30, 60])
-    ap.add_argument("--ref-spp", type=int, default=4096)
+    ap.add_argument("--ref-spp", type=int, default=16384)
     ap.add_argument("--width", type=int, default=1280)
     ap.add_argument("--height", type=int, default=720)
     ap.add_argument("--boxes", type=int, default=1000)
     ap.add_argument("--depth", type=int, default=12)
-    ap.add_argument("--chunk", type=int, default=4)
+    ap.add_argument("--chunk", type=int, default=8)
+    ap.add_argument("--nn-config", action="append", default=None,
+                    help="JSON settings for GpuScene.nn_configure; repeat to compare several learned guides")
+    ap.add_argument("--no-sdtree", action="store_true")
     ap.add_argument("--save", default="")
     a = ap.parse_args()
     sc = scenes.slit_room(seed=4, n_boxes=a.boxes, box_subdiv=4, width=a.width, height=a.height)
     gs = GpuScene(sc)
-    # reference: plain (unbiased) PT at ref_spp, rendered in chunks
+    H, W = a.height, a.width
+    # reference: plain (unbiased) PT at ref_spp, accumulated on the GPU in FP64
+    img = torch.zeros((H, W, 3), dtype=torch.float32, device="cuda")
+    acc = torch.zeros((H, W, 3), dtype=torch.float64, device="cuda")
     t0 = time.perf_counter()
-    ref = None
     step = 256
     for k in range(0, a.ref_spp, step):
-        img = gs.render(step, max_depth=a.depth, seed=777000 + k, mode=MODE_MIS, flags=FLAG_UNBIASED_MIS)
-        ref = img if ref is None else ref + img
-    ref /= a.ref_spp // step
+        gs.render_device(img.data_ptr(), step, max_depth=a.depth, seed=777000 + k, mode=MODE_MIS,
+                         flags=FLAG_UNBIASED_MIS)
+        acc += img.double()
+    ref = (acc / (a.ref_spp // step)).float()
+    torch.cuda.synchronize()
     ref_s = time.perf_counter() - t0
     print(json.dumps({"reference": {"spp": a.ref_spp, "seconds": ref_s, "mean": float(ref.mean()),
-                                    "triangles": sc.n_triangles, "resolution": [a.width, a.height]}}), flush=True)
+                                    "triangles": sc.n_triangles, "resolution": [W, H], "depth": a.depth}}),
+          flush=True)
     # warm-up (graph capture, allocations, kernel loading)
-    gs.render(1, max_depth=a.depth, seed=1, mode=MODE_MIS, flags=FLAG_UNBIASED_MIS)
-    gs.render(1, max_depth=a.depth, seed=1, mode=MODE_NN)
+    gs.render_device(img.data_ptr(), 1, max_depth=a.depth, seed=1, mode=MODE_MIS, flags=FLAG_UNBIASED_MIS)
+    gs.render_device(img.data_ptr(), 1, max_depth=a.depth, seed=1, mode=MODE_NN, flags=FLAG_NN_FREEZE)
     B = max(a.budgets)
+    cps = sorted(set([B * 2 ** (-k / 2) for k in range(0, 13)] + list(a.budgets)))
     results = {}
-    res_plain, img_plain, spp_plain = progressive(gs, MODE_MIS, FLAG_UNBIASED_MIS, B, a.chunk, a.depth, 10_000, ref,
-                                                  a.budgets)
+    res_plain, img_plain, _ = progressive(gs, MODE_MIS, FLAG_UNBIASED_MIS, B, a.chunk, a.depth, 10_000, ref, cps)
     results["plain"] = res_plain
-    gs.nn_reset(2024)
-    res_nn, img_nn, spp_nn = progressive(gs, MODE_NN, 0, B, a.chunk, a.depth, 20_000, ref, a.budgets)
-    results["nn"] = res_nn
-    nn_stats = gs.nn_stats()
-    # SD-tree: time one pass size, then one render per budget
-    t0 = time.perf_counter()
-    gs.render(4, max_depth=a.depth, seed=5, mode=MODE_SDTREE)
-    t4 = time.perf_counter() - t0
-    res_sd = []
-    for bud in a.budgets:
-        spp = 4
-        while spp * 2 * t4 / 3.0 * 2 < bud * 3 and spp < 1 << 16:  # passes 1..spp/2 cost ~ spp paths
-            spp *= 2
+    nn_runs = {}
+    for q, text in enumerate(a.nn_config or ["{}"]):
+        gs.nn_reset(2024)
+        cfg = gs.nn_configure(**json.loads(text))
+        rows, img_nn, _ = progressive(gs, MODE_NN, 0, B, a.chunk, a.depth, 20_000, ref, cps)
+        name = "nn" if q == 0 else f"nn{q}"
+        results[name] = rows
+        nn_runs[name] = {"config": cfg, "training": gs.nn_stats()}
+    if not a.no_sdtree:
+        # SD-tree (PPG): one render per budget; passes of 1, 2, 4, ... spp cost ~2x the last pass
         t0 = time.perf_counter()
-        img = gs.render(spp, max_depth=a.depth, seed=30_000 + spp, mode=MODE_SDTREE)
-        el = time.perf_counter() - t0
-        res_sd.append((el, spp, rel_mse(img, ref)))
-    results["sdtree"] = res_sd
+        gs.render(4, max_depth=a.depth, seed=5, mode=MODE_SDTREE)
+        t4 = time.perf_counter() - t0
+        res_sd = []
+        for bud in a.budgets:
+            spp = 4
+            while spp * 2 * t4 / 4.0 < bud and spp < 1 << 16:
+                spp *= 2
+            t0 = time.perf_counter()
+            x = gs.render(spp, max_depth=a.depth, seed=30_000 + spp, mode=MODE_SDTREE)
+            el = time.perf_counter() - t0
+            res_sd.append((el, spp, rel_mse(torch.from_numpy(x).cuda(), ref)))
+        results["sdtree"] = res_sd
     for name, rows in results.items():
         for el, spp, r in rows:
             print(json.dumps({"method": name, "seconds": el, "spp": spp, "relMSE": r}), flush=True)
-    # time for each method to reach plain's relMSE at the largest budget
-    target = res_plain[-1][2]
-    summ = {"target_relMSE_plain_at_s": [res_plain[-1][0], target], "nn_training": nn_stats}
-    for name in ("nn", "sdtree"):
-        reach = [el for el, spp, r in results[name] if r <= target]
-        summ[f"{name}_reaches_target_at_s"] = min(reach) if reach else None
+    summ = {"learned": nn_runs, "budgets": {}}
+    for bud in a.budgets:
+        p = [r for t, _, r in res_plain if t == bud]
+        if not p:
+            continue
+        row = {"plain_relMSE": p[0]}
+        for name in nn_runs:
+            n = [r for t, _, r in results[name] if t == bud]
+            t_nn = time_to_reach(results[name], p[0])
+            row[name] = {"relMSE": n[0] if n else None, "seconds_to_plain_relMSE": t_nn,
+                         "time_fraction": None if t_nn is None else t_nn / bud}
+        if "sdtree" in results:
+            sd = [r for (el, spp, r), b2 in zip(results["sdtree"], a.budgets) if b2 == bud]
+            row["sdtree_relMSE"] = sd[0] if sd else None
+        summ["budgets"][str(bud)] = row
     print(json.dumps({"summary": summ}), flush=True)
     if a.save:
-        np.savez_compressed(a.save, ref=ref, plain=img_plain, nn=img_nn)
+        np.savez_compressed(a.save, ref=ref.cpu().numpy(), plain=img_plain.cpu().numpy(),
+                            nn=img_nn.cpu().numpy())
 
 
 if __name__ == "__main__":

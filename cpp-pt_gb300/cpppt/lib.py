@@ -19,6 +19,7 @@ STATUS_NAMES = {0: "PT_OK", 1: "PT_ERR_INVALID", 2: "PT_ERR_CUDA", 3: "PT_ERR_ME
 MODE_MIS, MODE_SDTREE, MODE_NN = 0, 1, 2
 FLAG_TIME_KERNELS, FLAG_COUNT, FLAG_UNBIASED_MIS, FLAG_NN_FREEZE = 1, 2, 4, 8
 NN_WEIGHTS = 15360
+NN_KL, NN_CHI2 = 0, 1
 
 # every function the header declares
 EXPORTS = ["pt_scene_create", "pt_scene_load", "pt_scene_destroy", "pt_scene_info", "pt_trace_closest", "pt_trace_any",
@@ -61,7 +62,7 @@ class PtRenderStats(C.Structure):
 
 class PtNNConfig(C.Structure):
     _fields_ = [("learning_rate", C.c_float), ("bsdf_frac_min", C.c_float), ("bsdf_frac_max", C.c_float),
-                ("batch", C.c_int32)]
+                ("batch", C.c_int32), ("divergence", C.c_int32)]
 
 
 class PtBatchJob(C.Structure):
@@ -260,7 +261,7 @@ class GpuScene:
 
     def nn_configure(self, **kw):
         """Updates the learned guide's settings (learning_rate, bsdf_frac_min,
-        bsdf_frac_max, batch); returns the new settings."""
+        bsdf_frac_max, batch, divergence: NN_KL / NN_CHI2); returns the new settings."""
         c = PtNNConfig()
         _check(_lib.pt_nn_config_get(self.h, C.byref(c)))
         for k, v in kw.items():

@@ -525,6 +525,7 @@ void render_nn(pt_scene* s, const pt_render_desc* desc, float* d_dst, bool guide
         if (train && s->h_ctr->n_rec >= batch) {
             // one Adam step on the batch of records, then start a new batch
             ck(cudaMemsetAsync(s->nn_scalars, 0, sizeof(float) * 4, st), "memset");
+            if (s->nn_cfg.divergence == PT_NN_CHI2) launch_square_T(PD.rec, batch, st);
             launch_sum_T(PD.rec, batch, s->nn_scalars + 1, st);
             float tsum = 0.f;
             ck(cudaMemcpyAsync(&tsum, s->nn_scalars + 1, sizeof(float), cudaMemcpyDeviceToHost, st), "copy");
@@ -1152,6 +1153,10 @@ pt_status pt_nn_configure(pt_scene* s, const pt_nn_config* c) {
     }
     if (c->batch < 1024 || c->batch > kNNBatch) {
         g_error = "batch must be in [1024, 262144]";
+        return PT_ERR_INVALID;
+    }
+    if (c->divergence != PT_NN_KL && c->divergence != PT_NN_CHI2) {
+        g_error = "divergence must be PT_NN_KL or PT_NN_CHI2";
         return PT_ERR_INVALID;
     }
     s->nn_cfg = *c;

@@ -136,7 +136,7 @@ struct pt_scene {
     double nn_last_loss = 0, nn_records = 0;
     float4* nn_rec = nullptr;  // training records carried across renders
     int nn_rec_count = 0;
-    pt_nn_config nn_cfg{1e-3f, 0.1f, 0.9f, 1 << 18};
+    pt_nn_config nn_cfg{1e-3f, 0.1f, 0.9f, 1 << 18, PT_NN_KL};
 
     ~pt_scene() {
         for (void* p : nn_owned) cudaFree(p);

@@ -939,6 +939,15 @@ void launch_nn_generate(const DevScene& S, const PathBuffers& B, int cur, const 
 void launch_nn_finish(const NNPathData& PD, WaveCounters* ctr, int max_depth, int capacity, cudaStream_t st) {
     k_finish_nn<<<(capacity + 255) / 256, 256, 0, st>>>(PD, ctr, max_depth);
 }
+__global__ void k_square_T(float4* __restrict__ rec, int n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float t = rec[4 * (size_t)i + 3].y;
+        rec[4 * (size_t)i + 3].y = t * t;
+    }
+}
+void launch_square_T(float4* rec, int n, cudaStream_t st) {
+    k_square_T<<<std::max(1, std::min(1024, (n + 255) / 256)), 256, 0, st>>>(rec, n);
+}
 void launch_sum_T(const float4* rec, int n, float* out, cudaStream_t st) {
     k_sum_T<<<std::max(1, std::min(1024, (n + 255) / 256)), 256, 0, st>>>(rec, n, out);
 }

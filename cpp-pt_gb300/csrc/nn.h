@@ -68,6 +68,8 @@ void launch_nn_generate(const DevScene& S, const PathBuffers& B, int cur, const 
 // Emits the training records of the paths that finished this iteration (after
 // the shadow stage, so their last NEE is counted) and frees their slots.
 void launch_nn_finish(const NNPathData& PD, WaveCounters* ctr, int max_depth, int capacity, cudaStream_t st);
+// T -> T^2 for every record (chi-square training)
+void launch_square_T(float4* rec, int n, cudaStream_t st);
 void launch_sum_T(const float4* rec, int n, float* out, cudaStream_t st);
 
 }  // namespace cpppt_gb300

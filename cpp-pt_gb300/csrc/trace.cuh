@@ -140,10 +140,10 @@ struct Trav {
     HitRec best;
 };
 
-// Traversal stack of one lane: node references and their entry distances.
+// Traversal stack of one lane: {node reference, entry distance bits}, one
+// 8-byte local-memory access per push and pop.
 struct TravStack {
-    uint32_t ref[kStackSize];
-    float t[kStackSize];
+    uint2 e[kStackSize];
 };
 
 // root: wide-node index where the traversal starts (0 for a scene of its own;
@@ -182,9 +182,10 @@ __device__ __forceinline__ void trav_pop(Trav& T, const TravStack& K) {
     const float cull = cull_dist(T);
     while (T.sp > 0) {
         T.sp--;
-        if (K.t[T.sp] <= cull) {
-            T.cur = K.ref[T.sp];
-            T.cur_t = K.t[T.sp];
+        const uint2 e = K.e[T.sp];
+        if (__uint_as_float(e.y) <= cull) {
+            T.cur = e.x;
+            T.cur_t = __uint_as_float(e.y);
             return;
         }
     }
@@ -255,8 +256,7 @@ __device__ __forceinline__ void trav_node(Trav& T, TravStack& K, const DevScene&
     // far children first; an invalid key is written but not counted
 #pragma unroll
     for (int k = 3; k >= 1; k--) {
-        K.ref[T.sp] = refs[key[k] & 3u];
-        K.t[T.sp] = __uint_as_float(key[k] & ~3u);
+        K.e[T.sp] = make_uint2(refs[key[k] & 3u], key[k] & ~3u);
         T.sp += (key[k] != 0xffffffffu) ? 1 : 0;
     }
     T.cur = refs[key[0] & 3u];

@@ -257,12 +257,18 @@ pt_status pt_nn_stats(pt_scene* scene, double* steps, double* last_loss, double*
  * BSDF selection probability is c = bsdf_frac_min + (bsdf_frac_max -
  * bsdf_frac_min) sigmoid(logit); 0.1 <= bsdf_frac_min <= bsdf_frac_max <= 1
  * (equal values fix c).  batch: training records per Adam step, in
- * [1024, 262144].  Defaults: 1e-3, 0.1, 0.9, 262144. */
+ * [1024, 262144].  divergence: PT_NN_KL weighs each record by its target
+ * T (Kullback-Leibler), PT_NN_CHI2 by T^2 (Pearson chi-square: the variance
+ * of the estimator; it favours the rare bright directions).
+ * Defaults: 1e-3, 0.1, 0.9, 262144, PT_NN_KL. */
+#define PT_NN_KL 0
+#define PT_NN_CHI2 1
 typedef struct pt_nn_config {
     float learning_rate;
     float bsdf_frac_min;
     float bsdf_frac_max;
     int32_t batch;
+    int32_t divergence;
 } pt_nn_config;
 pt_status pt_nn_configure(pt_scene* scene, const pt_nn_config* config);
 pt_status pt_nn_config_get(pt_scene* scene, pt_nn_config* config);
