@@ -62,6 +62,7 @@ struct DevBatchJob {
 constexpr uint32_t kStatusIterLimit = 1u;
 constexpr uint32_t kStatusStackOverflow = 2u;
 constexpr uint32_t kStatusQueueOverflow = 4u;
+constexpr uint32_t kStatusTensorTimeout = 8u;  // a tensor-core completion wait ran out (bounded spin)
 
 // Wavefront counters, one block of device memory per scene.
 struct WaveCounters {

@@ -198,6 +198,7 @@ void check_status(pt_scene* s, uint32_t status) {
     if (status & kStatusIterLimit) throw Fail(PT_ERR_LIMIT, "traversal step limit reached");
     if (status & kStatusStackOverflow) throw Fail(PT_ERR_LIMIT, "traversal stack overflow");
     if (status & kStatusQueueOverflow) throw Fail(PT_ERR_LIMIT, "wavefront queue overflow");
+    if (status & kStatusTensorTimeout) throw Fail(PT_ERR_CUDA, "tensor-core completion wait timed out");
 }
 
 void trace_device(pt_scene* s, const pt_ray* rays, int n, void* out, bool any, cudaStream_t st) {
@@ -1221,11 +1222,16 @@ pt_status pt_debug_nn_forward(const float* weights, const float* lo, const float
         nn_upload(W, weights, c.st);
         float* din = dalloc<float>(c.owned, (size_t)9 * n);
         float* dout = dalloc<float>(c.owned, (size_t)41 * n);
+        uint32_t* dstat = dalloc<uint32_t>(c.owned, 1);
+        ck(cudaMemsetAsync(dstat, 0, sizeof(uint32_t), c.st), "memset");
         ck(cudaMemcpyAsync(din, inputs, sizeof(float) * 9 * n, cudaMemcpyHostToDevice, c.st), "copy");
-        launch_nn_forward_debug(W, norm_from(lo, hi), din, n, dout, c.sms, c.st);
+        launch_nn_forward_debug(W, norm_from(lo, hi), din, n, dout, dstat, c.sms, c.st);
         ck(cudaMemcpyAsync(out, dout, sizeof(float) * 41 * n, cudaMemcpyDeviceToHost, c.st), "copy");
+        uint32_t hstat = 0;
+        ck(cudaMemcpyAsync(&hstat, dstat, sizeof(uint32_t), cudaMemcpyDeviceToHost, c.st), "copy");
         ck(cudaStreamSynchronize(c.st), "forward");
         ck(cudaGetLastError(), "forward");
+        if (hstat & kStatusTensorTimeout) throw Fail(PT_ERR_CUDA, "tensor-core completion wait timed out");
     });
 }
 

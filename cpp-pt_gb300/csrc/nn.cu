@@ -14,6 +14,7 @@
 #include "nn.h"
 #include "nn.cuh"
 #include "trace.cuh"
+#include "umma.cuh"
 
 namespace cpppt_gb300 {
 
@@ -128,53 +129,130 @@ __device__ __forceinline__ void stage_weights(const NNWeights& W, __nv_bfloat16*
 }
 
 // ---------------------------------------------------------------------------
-// Inference: raw outputs -> 41 mixture parameters per sample.
+// Inference on the 5th-generation tensor cores: tiles of 128 samples, one
+// sample per thread.  Thread r writes its sample's 64 input features (bf16)
+// as row r of the A tile; per layer one thread issues the 128 x N x 64 MMA
+// chain (four K = 16 steps) into a 128 x 64 FP32 accumulator in tensor
+// memory, commits it to an mbarrier, and every thread reads its row back
+// (tensor-memory lane r), applies ReLU and writes the next layer's A row.
+// The output row (48 floats) never leaves the thread: it is post-processed
+// into the mixture parameters in registers.
 // ---------------------------------------------------------------------------
+constexpr int kTcRows = 128;                     // samples per tile (MMA M)
+constexpr uint32_t kTcCols = 64;                 // tensor-memory columns per CTA
+constexpr uint32_t kTcSBO = 8 * 128;             // K = 64: 8 core matrices per 8-row group
+constexpr int kTcWLayerBytes = 64 * 64 * 2;      // W_l^T slot (N x 64 bf16)
+constexpr int kTcABytes = kTcRows * 64 * 2;      // activation tile (128 x 64 bf16)
+constexpr int kTcSmem = kNNLayers * kTcWLayerBytes + kTcABytes + 64;
+
+// W_l^T (N = outputs rows x K = inputs) in the canonical K-major layout, from
+// the padded transposed copy wt[l][out][in].
+__device__ __forceinline__ void tc_stage_weights(const NNWeights& W, unsigned char* s_w) {
+    for (int c = threadIdx.x; c < kNNLayers * 64 * 8; c += blockDim.x) {
+        const int l = c >> 9, rem = c & 511, nrow = rem >> 3, k8 = rem & 7;
+        if (nrow >= nn_layer_out(l)) continue;
+        const uint4 v = *reinterpret_cast<const uint4*>(W.wt + (size_t)l * kWLayer + nrow * kWStride + k8 * 8);
+        *reinterpret_cast<uint4*>(s_w + l * kTcWLayerBytes + umma_offset(nrow, k8 * 8, 64)) = v;
+    }
+}
+
+// Row `row` of the A tile from 64 floats (optionally through ReLU).
+__device__ __forceinline__ void tc_store_row(unsigned char* s_a, int row, const float* v, bool relu) {
+#pragma unroll
+    for (int g = 0; g < 8; g++) {
+        float x[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) x[j] = relu ? fmaxf(v[8 * g + j], 0.f) : v[8 * g + j];
+        uint4 q;
+        q.x = pack_bf16(x[0], x[1]);
+        q.y = pack_bf16(x[2], x[3]);
+        q.z = pack_bf16(x[4], x[5]);
+        q.w = pack_bf16(x[6], x[7]);
+        *reinterpret_cast<uint4*>(s_a + umma_offset(row, 8 * g, 64)) = q;
+    }
+}
+
+// get_in(i, NNIn&) -> bool valid; put(i, const float* prm41).  All threads of
+// the CTA (kTcRows of them) must call it.  status: kStatusTensorTimeout when a
+// completion wait runs out (the CTA then stops, frees its tensor memory and
+// returns).
 template <class GetIn, class Put>
-__device__ __forceinline__ void infer_loop(int n, const __nv_bfloat16* s_wt, float* s_tile /*per warp 32x48*/,
-                                           float c_lo, float c_hi, GetIn get_in, Put put) {
-    const int lane = threadIdx.x & 31;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int base = warp * 32; base < n; base += nwarps * 32) {
-        const int i = base + lane;
-        NNIn mine;
-        bool valid = false;
-        if (i < n) valid = get_in(i, mine);
-        if (!valid) { mine.pn = mk(0.f, 0.f, 0.f); mine.n = mine.pn; mine.wo = mine.pn; }
+__device__ __forceinline__ void tc_infer_loop(int n, unsigned char* smem, const NNWeights& W, float c_lo, float c_hi,
+                                              uint32_t* status, GetIn get_in, Put put) {
+    unsigned char* s_w = smem;
+    unsigned char* s_a = smem + kNNLayers * kTcWLayerBytes;
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_a + kTcABytes);
+    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(s_bar + 1);
+    const int warp = threadIdx.x >> 5;
+    const int row = threadIdx.x;  // tensor-memory lane of this thread's sample
+    tc_stage_weights(W, s_w);
+    if (threadIdx.x == 0) mbar_init(smem_u32(s_bar), 1);
+    if (warp == 0) tmem_alloc(s_tmem, kTcCols);
+    tc_fence_before_sync();
+    __syncthreads();
+    tc_fence_after_sync();
+    const uint32_t tmem = *s_tmem;
+    const uint32_t t_row = tmem + ((uint32_t)(warp * 32) << 16);
+    const uint32_t bar = smem_u32(s_bar), a_addr = smem_u32(s_a), w_addr = smem_u32(s_w);
+    uint32_t phase = 0;
+    bool ok = true;
+    for (int base = blockIdx.x * kTcRows; base < n && ok; base += gridDim.x * kTcRows) {
+        const int i = base + row;
+        NNIn in;
+        const bool valid = i < n && get_in(i, in);
+        float v[64];
 #pragma unroll
-        for (int mt = 0; mt < 2; mt++) {
-            uint32_t a[4][4];
-            float acc[8][4];
-            input_frags(mine, mt, lane, a);
-            for (int l = 0; l < kNNLayers - 1; l++) hidden_layer(s_wt + l * kWLayer, lane, a, acc);
-            float out[6][4];
-            output_layer(s_wt + (kNNLayers - 1) * kWLayer, lane, a, out);
-            store_out_tile(s_tile + mt * 16 * kNNOut, out, lane);
+        for (int j = 0; j < 64; j++) v[j] = valid ? nn_feature(j, in.pn, in.n, in.wo) : 0.f;
+        tc_store_row(s_a, row, v, false);
+        for (int l = 0; l < kNNLayers; l++) {
+            fence_proxy_async_smem();
+            tc_fence_before_sync();
+            __syncthreads();
+            tc_fence_after_sync();
+            if (threadIdx.x == 0) {
+                const uint32_t idesc = umma_idesc_bf16_f32(kTcRows, nn_layer_out(l));
+#pragma unroll
+                for (int ks = 0; ks < 4; ks++)
+                    umma_bf16(tmem, umma_desc(a_addr + ks * 2 * kUmmaLBO, kTcSBO),
+                              umma_desc(w_addr + l * kTcWLayerBytes + ks * 2 * kUmmaLBO, kTcSBO), idesc,
+                              ks > 0 ? 1u : 0u);
+                umma_commit(bar);
+            }
+            ok = __syncthreads_and(mbar_wait_bounded(bar, phase)) != 0;
+            phase ^= 1u;
+            if (!ok) break;
+            tc_fence_after_sync();
+            const int nout = nn_layer_out(l);
+#pragma unroll
+            for (int c = 0; c < 64; c += 16)
+                if (c < nout) tmem_ld16(t_row + (uint32_t)c, v + c);
+            if (l < kNNLayers - 1) tc_store_row(s_a, row, v, true);
         }
-        __syncwarp();
-        if (i < n && valid) {
-            float raw[kNNOut];
-#pragma unroll
-            for (int k = 0; k < kNNOut; k++) raw[k] = s_tile[lane * kNNOut + k];
+        if (ok && valid) {
             float prm[kNNParams];
-            nn_postprocess(raw, prm, c_lo, c_hi);
+            nn_postprocess(v, prm, c_lo, c_hi);
             put(i, prm);
         }
-        __syncwarp();
+    }
+    if (!ok) {
+        if (threadIdx.x == 0) atomicOr(status, kStatusTensorTimeout);
+        mbar_wait_bounded(bar, phase ^ 1u);  // the MMAs of the timed-out phase, if they still finish
+    }
+    tc_fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after_sync();
+        tmem_dealloc(tmem, kTcCols);
     }
 }
 
 constexpr int kNNThreads = 128;
 
-__global__ void __launch_bounds__(kNNThreads) k_nn_forward_debug(NNWeights W, NNNorm N, const float* __restrict__ in,
-                                                                 int n, float* __restrict__ out) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    __nv_bfloat16* s_wt = reinterpret_cast<__nv_bfloat16*>(smem);
-    float* s_tile = reinterpret_cast<float*>(smem + kNNLayers * kWLayer * 2) + (threadIdx.x >> 5) * 32 * kNNOut;
-    stage_weights(W, s_wt, nullptr, false);
-    infer_loop(
-        n, s_wt, s_tile, N.c_lo, N.c_hi,
+__global__ void __launch_bounds__(kTcRows) k_nn_forward_debug(NNWeights W, NNNorm N, const float* __restrict__ in,
+                                                              int n, float* __restrict__ out, uint32_t* status) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    tc_infer_loop(
+        n, smem, W, N.c_lo, N.c_hi, status,
         [&](int i, NNIn& v) {
             const float* p = in + 9 * (size_t)i;
             v.pn = mk((p[0] - N.lo[0]) * N.inv_ext[0], (p[1] - N.lo[1]) * N.inv_ext[1], (p[2] - N.lo[2]) * N.inv_ext[2]);
@@ -188,16 +266,13 @@ __global__ void __launch_bounds__(kNNThreads) k_nn_forward_debug(NNWeights W, NN
 }
 
 // Guide parameters for every live path's hit (run between extend and shade).
-__global__ void __launch_bounds__(kNNThreads) k_nn_infer(DevScene S, PathBuffers B, int cur, WaveCounters* ctr,
-                                                         NNWeights W, NNNorm N, float4* __restrict__ params) {
-    extern __shared__ __align__(16) unsigned char smem[];
+__global__ void __launch_bounds__(kTcRows) k_nn_infer(DevScene S, PathBuffers B, int cur, WaveCounters* ctr,
+                                                      NNWeights W, NNNorm N, float4* __restrict__ params) {
+    extern __shared__ __align__(1024) unsigned char smem[];
     const int n = ctr->n_cur;
     if (n == 0) return;
-    __nv_bfloat16* s_wt = reinterpret_cast<__nv_bfloat16*>(smem);
-    float* s_tile = reinterpret_cast<float*>(smem + kNNLayers * kWLayer * 2) + (threadIdx.x >> 5) * 32 * kNNOut;
-    stage_weights(W, s_wt, nullptr, false);
-    infer_loop(
-        n, s_wt, s_tile, N.c_lo, N.c_hi,
+    tc_infer_loop(
+        n, smem, W, N.c_lo, N.c_hi, &ctr->status,
         [&](int i, NNIn& v) {
             const float4 H = B.hit[i];
             const int prim = __float_as_int(H.y);
@@ -520,7 +595,7 @@ __global__ void k_nn_pack(NNWeights W) {
     W.w[l * kWLayer + in * kWStride + out] = b;
 }
 
-size_t nn_smem_infer() { return (size_t)kNNLayers * kWLayer * 2 + (kNNThreads / 32) * 32 * kNNOut * 4; }
+size_t nn_smem_infer() { return (size_t)kTcSmem; }
 size_t nn_smem_train() { return (size_t)2 * kNNLayers * kWLayer * 2 + (kNNThreads / 32) * 32 * kNNOut * 4; }
 size_t nn_wcopy_elems() { return (size_t)kNNLayers * kWLayer; }
 
@@ -536,14 +611,14 @@ cudaError_t nn_set_smem_limits() {
 void launch_nn_pack(const NNWeights& W, cudaStream_t st) {
     k_nn_pack<<<(kNNWeights + 255) / 256, 256, 0, st>>>(W);
 }
-void launch_nn_forward_debug(const NNWeights& W, const NNNorm& N, const float* in, int n, float* out, int num_sms,
-                             cudaStream_t st) {
-    const int blocks = std::max(1, std::min(num_sms * 4, (n + kNNThreads - 1) / kNNThreads));
-    k_nn_forward_debug<<<blocks, kNNThreads, nn_smem_infer(), st>>>(W, N, in, n, out);
+void launch_nn_forward_debug(const NNWeights& W, const NNNorm& N, const float* in, int n, float* out,
+                             uint32_t* status, int num_sms, cudaStream_t st) {
+    const int blocks = std::max(1, std::min(num_sms * 4, (n + kTcRows - 1) / kTcRows));
+    k_nn_forward_debug<<<blocks, kTcRows, nn_smem_infer(), st>>>(W, N, in, n, out, status);
 }
 void launch_nn_infer(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, const NNWeights& W,
                      const NNNorm& N, float4* params, int num_sms, cudaStream_t st) {
-    k_nn_infer<<<num_sms * 4, kNNThreads, nn_smem_infer(), st>>>(S, B, cur, ctr, W, N, params);
+    k_nn_infer<<<num_sms * 4, kTcRows, nn_smem_infer(), st>>>(S, B, cur, ctr, W, N, params);
 }
 void launch_nn_train_step(const NNWeights& W, const NNNorm& N, const float4* rec, int n, float tsum,
                           const NNTrainBuf& TB, float* grad, float* loss, const NNAdam& opt, int step, int num_sms,

@@ -48,8 +48,9 @@ size_t nn_smem_train();
 size_t nn_wcopy_elems();  // bf16 elements of one padded weight copy
 cudaError_t nn_set_smem_limits();
 void launch_nn_pack(const NNWeights& W, cudaStream_t st);
-void launch_nn_forward_debug(const NNWeights& W, const NNNorm& N, const float* in, int n, float* out, int num_sms,
-                             cudaStream_t st);
+// status: one zeroed word; receives kStatusTensorTimeout if a wait ran out.
+void launch_nn_forward_debug(const NNWeights& W, const NNNorm& N, const float* in, int n, float* out,
+                             uint32_t* status, int num_sms, cudaStream_t st);
 void launch_nn_infer(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, const NNWeights& W,
                      const NNNorm& N, float4* params, int num_sms, cudaStream_t st);
 // grad (kNNWeights floats) receives dL/dW; loss accumulates the batch loss;
