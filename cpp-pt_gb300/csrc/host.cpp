@@ -536,10 +536,14 @@ void render_nn(pt_scene* s, const pt_render_desc* desc, float* d_dst, bool guide
             launch_nn_train_step(s->nnw, N, PD.rec, batch, tsum, s->nn_tb, s->nn_grad, s->nn_scalars, opt,
                                  ++s->nn_steps, s->num_sms, st, true);
             launches += 5;
-            float loss = 0.f;
-            ck(cudaMemcpyAsync(&loss, s->nn_scalars, sizeof(float), cudaMemcpyDeviceToHost, st), "copy");
+            float sc[4] = {0.f, 0.f, 0.f, 0.f};
+            ck(cudaMemcpyAsync(sc, s->nn_scalars, sizeof(sc), cudaMemcpyDeviceToHost, st), "copy");
             ck(cudaMemsetAsync(&s->d_ctr->n_rec, 0, sizeof(int), st), "reset records");
             ck(cudaStreamSynchronize(st), "train");
+            uint32_t tstat;
+            std::memcpy(&tstat, &sc[2], sizeof(tstat));
+            check_status(s, tstat);
+            const float loss = sc[0];
             s->nn_last_loss = loss;
             records += batch;
             s->nn_records += batch;
@@ -1253,11 +1257,14 @@ pt_status pt_debug_nn_grad(const float* weights, const float* lo, const float* h
         NNAdam opt;
         launch_nn_train_step(W, norm_from(lo, hi), drec, n, (float)tsum, TB, grad, scal, opt, 1, c.sms, c.st, false);
         ck(cudaMemcpyAsync(out_grad, grad, sizeof(float) * kNNWeightCount, cudaMemcpyDeviceToHost, c.st), "copy");
-        float loss = 0;
-        ck(cudaMemcpyAsync(&loss, scal, sizeof(float), cudaMemcpyDeviceToHost, c.st), "copy");
+        float sc[4] = {0.f, 0.f, 0.f, 0.f};
+        ck(cudaMemcpyAsync(sc, scal, sizeof(sc), cudaMemcpyDeviceToHost, c.st), "copy");
         ck(cudaStreamSynchronize(c.st), "grad");
         ck(cudaGetLastError(), "grad");
-        if (out_loss) *out_loss = loss;
+        uint32_t tstat;
+        std::memcpy(&tstat, &sc[2], sizeof(tstat));
+        if (tstat & kStatusTensorTimeout) throw Fail(PT_ERR_CUDA, "tensor-core completion wait timed out");
+        if (out_loss) *out_loss = sc[0];
     });
 }
 

@@ -2,11 +2,11 @@
 //
 // Layout of the weights in device memory (one contiguous block per copy):
 //   master  float  [kNNWeights]          layer l at nn_layer_offset(l), row-major [in][out]
-//   wt      bf16   [4 layers][64][72]    transposed [out][in], rows padded to 72 (bank-conflict free)
+//   wt      bf16   [4 layers][64][72]    transposed [out][in], rows padded to 72
 //   w       bf16   [4 layers][64][72]    row-major  [in][out] padded (backward data pass)
-// A warp runs 32 samples as two 16-row tiles through all layers with the
-// activations held in mma fragments: the accumulator fragment of one layer
-// is, after ReLU and packing, exactly the A fragment of the next.
+// Inference and the training forward/backward run on tcgen05 (tiles of 128
+// samples, one sample per thread, accumulators in tensor memory); the
+// weight-gradient reduction over the batch runs on mma.sync fragments.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -21,112 +21,10 @@ namespace cpppt_gb300 {
 constexpr int kWStride = 72;  // padded row of 64 bf16
 constexpr int kWLayer = 64 * kWStride;
 
-// B fragment of W (k = input, n = output) from the transposed copy wt[out][in].
-__device__ __forceinline__ void load_b_fwd(const __nv_bfloat16* wt_l, int nt, int kt, int lane, uint32_t b[2]) {
-    const int g = lane >> 2, t = lane & 3;
-    const __nv_bfloat16* p = wt_l + (nt * 8 + g) * kWStride + kt * 16 + 2 * t;
-    b[0] = *reinterpret_cast<const uint32_t*>(p);
-    b[1] = *reinterpret_cast<const uint32_t*>(p + 8);
-}
-// B fragment of W^T (k = output, n = input) from the row-major copy w[in][out].
-__device__ __forceinline__ void load_b_bwd(const __nv_bfloat16* w_l, int nt, int kt, int lane, uint32_t b[2]) {
-    const int g = lane >> 2, t = lane & 3;
-    const __nv_bfloat16* p = w_l + (nt * 8 + g) * kWStride + kt * 16 + 2 * t;
-    b[0] = *reinterpret_cast<const uint32_t*>(p);
-    b[1] = *reinterpret_cast<const uint32_t*>(p + 8);
-}
-
-// Sample inputs of one lane's sample, gathered by the lanes that need them.
+// Network inputs of one sample.
 struct NNIn {
     f3 pn, n, wo;
 };
-
-__device__ __forceinline__ NNIn shfl_in(const NNIn& v, int src) {
-    NNIn r;
-    r.pn = mk(__shfl_sync(0xffffffffu, v.pn.x, src), __shfl_sync(0xffffffffu, v.pn.y, src),
-              __shfl_sync(0xffffffffu, v.pn.z, src));
-    r.n = mk(__shfl_sync(0xffffffffu, v.n.x, src), __shfl_sync(0xffffffffu, v.n.y, src),
-             __shfl_sync(0xffffffffu, v.n.z, src));
-    r.wo = mk(__shfl_sync(0xffffffffu, v.wo.x, src), __shfl_sync(0xffffffffu, v.wo.y, src),
-              __shfl_sync(0xffffffffu, v.wo.z, src));
-    return r;
-}
-
-// A fragments of the input layer for 16-row tile `mt` (rows mt*16 .. +15 of
-// the warp's 32 samples, sample r owned by lane r).
-__device__ __forceinline__ void input_frags(const NNIn& mine, int mt, int lane, uint32_t a[4][4]) {
-    const int g = lane >> 2, t = lane & 3;
-    const NNIn r0 = shfl_in(mine, mt * 16 + g), r1 = shfl_in(mine, mt * 16 + g + 8);
-#pragma unroll
-    for (int kt = 0; kt < 4; kt++) {
-        const int c = kt * 16 + 2 * t;
-        a[kt][0] = pack_bf16(nn_feature(c, r0.pn, r0.n, r0.wo), nn_feature(c + 1, r0.pn, r0.n, r0.wo));
-        a[kt][1] = pack_bf16(nn_feature(c, r1.pn, r1.n, r1.wo), nn_feature(c + 1, r1.pn, r1.n, r1.wo));
-        a[kt][2] = pack_bf16(nn_feature(c + 8, r0.pn, r0.n, r0.wo), nn_feature(c + 9, r0.pn, r0.n, r0.wo));
-        a[kt][3] = pack_bf16(nn_feature(c + 8, r1.pn, r1.n, r1.wo), nn_feature(c + 9, r1.pn, r1.n, r1.wo));
-    }
-}
-
-// One hidden layer: acc = A W; then A <- bf16(relu(acc)).
-__device__ __forceinline__ void hidden_layer(const __nv_bfloat16* wt_l, int lane, uint32_t a[4][4], float acc[8][4]) {
-#pragma unroll
-    for (int nt = 0; nt < 8; nt++) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
-#pragma unroll
-    for (int kt = 0; kt < 4; kt++)
-#pragma unroll
-        for (int nt = 0; nt < 8; nt++) {
-            uint32_t b[2];
-            load_b_fwd(wt_l, nt, kt, lane, b);
-            mma_bf16(acc[nt], a[kt], b);
-        }
-#pragma unroll
-    for (int kt = 0; kt < 4; kt++) {
-        a[kt][0] = pack_bf16(fmaxf(acc[2 * kt][0], 0.f), fmaxf(acc[2 * kt][1], 0.f));
-        a[kt][1] = pack_bf16(fmaxf(acc[2 * kt][2], 0.f), fmaxf(acc[2 * kt][3], 0.f));
-        a[kt][2] = pack_bf16(fmaxf(acc[2 * kt + 1][0], 0.f), fmaxf(acc[2 * kt + 1][1], 0.f));
-        a[kt][3] = pack_bf16(fmaxf(acc[2 * kt + 1][2], 0.f), fmaxf(acc[2 * kt + 1][3], 0.f));
-    }
-}
-
-__device__ __forceinline__ void output_layer(const __nv_bfloat16* wt_l, int lane, const uint32_t a[4][4],
-                                             float out[6][4]) {
-#pragma unroll
-    for (int nt = 0; nt < 6; nt++) out[nt][0] = out[nt][1] = out[nt][2] = out[nt][3] = 0.f;
-#pragma unroll
-    for (int kt = 0; kt < 4; kt++)
-#pragma unroll
-        for (int nt = 0; nt < 6; nt++) {
-            uint32_t b[2];
-            load_b_fwd(wt_l, nt, kt, lane, b);
-            mma_bf16(out[nt], a[kt], b);
-        }
-}
-
-// Writes a 16 x 48 output tile's fragments to a row-major smem tile.
-__device__ __forceinline__ void store_out_tile(float* tile /*16 x 48*/, const float out[6][4], int lane) {
-    const int g = lane >> 2, t = lane & 3;
-#pragma unroll
-    for (int nt = 0; nt < 6; nt++) {
-        tile[g * kNNOut + nt * 8 + 2 * t] = out[nt][0];
-        tile[g * kNNOut + nt * 8 + 2 * t + 1] = out[nt][1];
-        tile[(g + 8) * kNNOut + nt * 8 + 2 * t] = out[nt][2];
-        tile[(g + 8) * kNNOut + nt * 8 + 2 * t + 1] = out[nt][3];
-    }
-}
-
-__device__ __forceinline__ void stage_weights(const NNWeights& W, __nv_bfloat16* s_wt, __nv_bfloat16* s_w,
-                                              bool with_w) {
-    const uint4* src = reinterpret_cast<const uint4*>(W.wt);
-    uint4* dst = reinterpret_cast<uint4*>(s_wt);
-    const int n16 = kNNLayers * kWLayer * 2 / 16;
-    for (int i = threadIdx.x; i < n16; i += blockDim.x) dst[i] = src[i];
-    if (with_w) {
-        const uint4* s2 = reinterpret_cast<const uint4*>(W.w);
-        uint4* d2 = reinterpret_cast<uint4*>(s_w);
-        for (int i = threadIdx.x; i < n16; i += blockDim.x) d2[i] = s2[i];
-    }
-    __syncthreads();
-}
 
 // ---------------------------------------------------------------------------
 // Inference on the 5th-generation tensor cores: tiles of 128 samples, one
@@ -156,10 +54,12 @@ __device__ __forceinline__ void tc_stage_weights(const NNWeights& W, unsigned ch
     }
 }
 
-// Row `row` of the A tile from 64 floats (optionally through ReLU).
-__device__ __forceinline__ void tc_store_row(unsigned char* s_a, int row, const float* v, bool relu) {
+// Row `row` of a K-column A tile (K = 48 or 64) from K floats, optionally
+// through ReLU.
+__device__ __forceinline__ void tc_store_row(unsigned char* s_a, int row, const float* v, bool relu, int K = 64) {
 #pragma unroll
     for (int g = 0; g < 8; g++) {
+        if (8 * g >= K) break;
         float x[8];
 #pragma unroll
         for (int j = 0; j < 8; j++) x[j] = relu ? fmaxf(v[8 * g + j], 0.f) : v[8 * g + j];
@@ -168,7 +68,52 @@ __device__ __forceinline__ void tc_store_row(unsigned char* s_a, int row, const 
         q.y = pack_bf16(x[2], x[3]);
         q.z = pack_bf16(x[4], x[5]);
         q.w = pack_bf16(x[6], x[7]);
-        *reinterpret_cast<uint4*>(s_a + umma_offset(row, 8 * g, 64)) = q;
+        *reinterpret_cast<uint4*>(s_a + umma_offset(row, 8 * g, K)) = q;
+    }
+}
+
+// One layer on the tensor cores: every thread's shared-memory writes are made
+// visible to the async proxy, thread 0 issues D = A B^T over K (K / 16 MMAs,
+// M = 128, N columns) and commits; all threads wait for the completion.
+// Returns false (for every thread) when the bounded wait ran out.
+__device__ __forceinline__ bool tc_layer(uint32_t tmem, uint32_t a_addr, uint32_t a_sbo, uint32_t b_addr,
+                                         uint32_t b_sbo, int K, int N, uint32_t bar, uint32_t& phase) {
+    fence_proxy_async_smem();
+    tc_fence_before_sync();
+    __syncthreads();
+    tc_fence_after_sync();
+    if (threadIdx.x == 0) {
+        const uint32_t idesc = umma_idesc_bf16_f32(kTcRows, N);
+        for (int ks = 0; ks < K / 16; ks++)
+            umma_bf16(tmem, umma_desc(a_addr + ks * 2 * kUmmaLBO, a_sbo), umma_desc(b_addr + ks * 2 * kUmmaLBO, b_sbo),
+                      idesc, ks > 0 ? 1u : 0u);
+        umma_commit(bar);
+    }
+    const bool ok = __syncthreads_and(mbar_wait_bounded(bar, phase)) != 0;
+    phase ^= 1u;
+    if (ok) tc_fence_after_sync();
+    return ok;
+}
+
+// Tensor memory and the completion barrier of a CTA (call with all threads).
+__device__ __forceinline__ uint32_t tc_begin(uint64_t* s_bar, uint32_t* s_tmem) {
+    if (threadIdx.x == 0) mbar_init(smem_u32(s_bar), 1);
+    if ((threadIdx.x >> 5) == 0) tmem_alloc(s_tmem, kTcCols);
+    tc_fence_before_sync();
+    __syncthreads();
+    tc_fence_after_sync();
+    return *s_tmem;
+}
+__device__ __forceinline__ void tc_end(bool ok, uint32_t tmem, uint32_t bar, uint32_t phase, uint32_t* status) {
+    if (!ok) {
+        if (threadIdx.x == 0) atomicOr(status, kStatusTensorTimeout);
+        mbar_wait_bounded(bar, phase ^ 1u);  // the MMAs of the timed-out phase, if they still finish
+    }
+    tc_fence_before_sync();
+    __syncthreads();
+    if ((threadIdx.x >> 5) == 0) {
+        tc_fence_after_sync();
+        tmem_dealloc(tmem, kTcCols);
     }
 }
 
@@ -186,12 +131,7 @@ __device__ __forceinline__ void tc_infer_loop(int n, unsigned char* smem, const 
     const int warp = threadIdx.x >> 5;
     const int row = threadIdx.x;  // tensor-memory lane of this thread's sample
     tc_stage_weights(W, s_w);
-    if (threadIdx.x == 0) mbar_init(smem_u32(s_bar), 1);
-    if (warp == 0) tmem_alloc(s_tmem, kTcCols);
-    tc_fence_before_sync();
-    __syncthreads();
-    tc_fence_after_sync();
-    const uint32_t tmem = *s_tmem;
+    const uint32_t tmem = tc_begin(s_bar, s_tmem);
     const uint32_t t_row = tmem + ((uint32_t)(warp * 32) << 16);
     const uint32_t bar = smem_u32(s_bar), a_addr = smem_u32(s_a), w_addr = smem_u32(s_w);
     uint32_t phase = 0;
@@ -205,24 +145,9 @@ __device__ __forceinline__ void tc_infer_loop(int n, unsigned char* smem, const 
         for (int j = 0; j < 64; j++) v[j] = valid ? nn_feature(j, in.pn, in.n, in.wo) : 0.f;
         tc_store_row(s_a, row, v, false);
         for (int l = 0; l < kNNLayers; l++) {
-            fence_proxy_async_smem();
-            tc_fence_before_sync();
-            __syncthreads();
-            tc_fence_after_sync();
-            if (threadIdx.x == 0) {
-                const uint32_t idesc = umma_idesc_bf16_f32(kTcRows, nn_layer_out(l));
-#pragma unroll
-                for (int ks = 0; ks < 4; ks++)
-                    umma_bf16(tmem, umma_desc(a_addr + ks * 2 * kUmmaLBO, kTcSBO),
-                              umma_desc(w_addr + l * kTcWLayerBytes + ks * 2 * kUmmaLBO, kTcSBO), idesc,
-                              ks > 0 ? 1u : 0u);
-                umma_commit(bar);
-            }
-            ok = __syncthreads_and(mbar_wait_bounded(bar, phase)) != 0;
-            phase ^= 1u;
-            if (!ok) break;
-            tc_fence_after_sync();
             const int nout = nn_layer_out(l);
+            ok = tc_layer(tmem, a_addr, kTcSBO, w_addr + l * kTcWLayerBytes, kTcSBO, 64, nout, bar, phase);
+            if (!ok) break;
 #pragma unroll
             for (int c = 0; c < 64; c += 16)
                 if (c < nout) tmem_ld16(t_row + (uint32_t)c, v + c);
@@ -234,19 +159,9 @@ __device__ __forceinline__ void tc_infer_loop(int n, unsigned char* smem, const 
             put(i, prm);
         }
     }
-    if (!ok) {
-        if (threadIdx.x == 0) atomicOr(status, kStatusTensorTimeout);
-        mbar_wait_bounded(bar, phase ^ 1u);  // the MMAs of the timed-out phase, if they still finish
-    }
-    tc_fence_before_sync();
-    __syncthreads();
-    if (warp == 0) {
-        tc_fence_after_sync();
-        tmem_dealloc(tmem, kTcCols);
-    }
+    tc_end(ok, tmem, bar, phase, status);
 }
 
-constexpr int kNNThreads = 128;
 
 __global__ void __launch_bounds__(kTcRows) k_nn_forward_debug(NNWeights W, NNNorm N, const float* __restrict__ in,
                                                               int n, float* __restrict__ out, uint32_t* status) {
@@ -352,147 +267,130 @@ __device__ __forceinline__ float nn_loss_grad(const float* raw, f3 wi, float p_b
     return -T * __logf(m);
 }
 
-// Forward + loss gradient + backward through the data, 16 records at a time
-// per warp.  Stores every layer's bf16 input activation A_l (B x 64) and the
-// gradient of its output dZ_l (B x out_l, bf16) for the weight-gradient pass;
-// the backward pass reads A_l back (each thread its own fragment elements)
-// for the ReLU mask.
-__device__ __forceinline__ void store_frag_rows(__nv_bfloat16* M, const uint32_t f[4][4], int row0, int row1, int n,
-                                                int ncols, int t) {
-#pragma unroll
-    for (int kt = 0; kt < 4; kt++) {
-        const int c = kt * 16 + 2 * t;
-        if (c >= ncols) continue;
-        if (row0 < n) {
-            *reinterpret_cast<uint32_t*>(M + (size_t)row0 * 64 + c) = f[kt][0];
-            *reinterpret_cast<uint32_t*>(M + (size_t)row0 * 64 + c + 8) = f[kt][2];
-        }
-        if (row1 < n) {
-            *reinterpret_cast<uint32_t*>(M + (size_t)row1 * 64 + c) = f[kt][1];
-            *reinterpret_cast<uint32_t*>(M + (size_t)row1 * 64 + c + 8) = f[kt][3];
-        }
+// Forward + loss gradient + backward through the data on the tensor cores,
+// 128 records per tile, one record per thread.  Every layer's bf16 input
+// activation A_l (B x 64) and the gradient of its output dZ_l (B x out_l,
+// bf16) go to TB for the weight-gradient pass; the backward pass reads the
+// thread's own A_l row back for the ReLU mask.  Backward layer l is
+// dH = dZ_l W_l^T: A = dZ_l (K = out_l), B = W_l as 64 inputs x out_l.
+constexpr int kTcTrainSmem = 2 * kNNLayers * kTcWLayerBytes + kTcABytes + 64;
+
+__device__ __forceinline__ void tc_stage_weights_bwd(const NNWeights& W, unsigned char* s_b) {
+    for (int c = threadIdx.x; c < kNNLayers * 64 * 8; c += blockDim.x) {
+        const int l = c >> 9, rem = c & 511, nrow = rem >> 3, k8 = rem & 7;
+        const int K = nn_layer_out(l);
+        if (8 * k8 >= K) continue;
+        const uint4 v = *reinterpret_cast<const uint4*>(W.w + (size_t)l * kWLayer + nrow * kWStride + k8 * 8);
+        *reinterpret_cast<uint4*>(s_b + l * kTcWLayerBytes + umma_offset(nrow, k8 * 8, K)) = v;
     }
 }
 
-__device__ __forceinline__ void load_frag_rows(const __nv_bfloat16* M, uint32_t f[4][4], int row0, int row1, int n,
-                                               int t) {
+// Row of K bf16 values (K = 48 or 64) to a 64-wide global row.
+__device__ __forceinline__ void store_row_bf16(__nv_bfloat16* dst, const float* v, int K, bool relu) {
 #pragma unroll
-    for (int kt = 0; kt < 4; kt++) {
-        const int c = kt * 16 + 2 * t;
-        f[kt][0] = row0 < n ? *reinterpret_cast<const uint32_t*>(M + (size_t)row0 * 64 + c) : 0u;
-        f[kt][2] = row0 < n ? *reinterpret_cast<const uint32_t*>(M + (size_t)row0 * 64 + c + 8) : 0u;
-        f[kt][1] = row1 < n ? *reinterpret_cast<const uint32_t*>(M + (size_t)row1 * 64 + c) : 0u;
-        f[kt][3] = row1 < n ? *reinterpret_cast<const uint32_t*>(M + (size_t)row1 * 64 + c + 8) : 0u;
+    for (int g = 0; g < 8; g++) {
+        if (8 * g >= K) break;
+        float x[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) x[j] = relu ? fmaxf(v[8 * g + j], 0.f) : v[8 * g + j];
+        uint4 q;
+        q.x = pack_bf16(x[0], x[1]);
+        q.y = pack_bf16(x[2], x[3]);
+        q.z = pack_bf16(x[4], x[5]);
+        q.w = pack_bf16(x[6], x[7]);
+        *reinterpret_cast<uint4*>(dst + 8 * g) = q;
     }
 }
 
-__device__ __forceinline__ uint32_t relu_mask(uint32_t act, float lo, float hi) {
-    const __nv_bfloat162 h = *reinterpret_cast<const __nv_bfloat162*>(&act);
-    return pack_bf16(__low2float(h) > 0.f ? lo : 0.f, __high2float(h) > 0.f ? hi : 0.f);
-}
+constexpr int kNNThreads = 128;
 
-__global__ void __launch_bounds__(kNNThreads) k_nn_train_fb(NNWeights W, NNNorm N, const float4* __restrict__ rec,
-                                                            int n, float inv_tsum, NNTrainBuf TB,
-                                                            float* __restrict__ loss_out) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    __nv_bfloat16* s_wt = reinterpret_cast<__nv_bfloat16*>(smem);
-    __nv_bfloat16* s_w = s_wt + kNNLayers * kWLayer;
-    float* s_tile = reinterpret_cast<float*>(smem + 2 * kNNLayers * kWLayer * 2) + (threadIdx.x >> 5) * 32 * kNNOut;
-    stage_weights(W, s_wt, s_w, true);
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+__global__ void __launch_bounds__(kTcRows) k_nn_train_fb(NNWeights W, NNNorm N, const float4* __restrict__ rec, int n,
+                                                         float inv_tsum, NNTrainBuf TB, float* __restrict__ loss_out,
+                                                         uint32_t* status) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char* s_wf = smem;                                  // forward B tiles: W_l^T (out x in)
+    unsigned char* s_wb = smem + kNNLayers * kTcWLayerBytes;     // backward B tiles: W_l (in x out)
+    unsigned char* s_a = smem + 2 * kNNLayers * kTcWLayerBytes;  // A tile: activations, then output gradients
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_a + kTcABytes);
+    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(s_bar + 1);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row = threadIdx.x;
+    tc_stage_weights(W, s_wf);
+    tc_stage_weights_bwd(W, s_wb);
+    const uint32_t tmem = tc_begin(s_bar, s_tmem);
+    const uint32_t t_row = tmem + ((uint32_t)(warp * 32) << 16);
+    const uint32_t bar = smem_u32(s_bar), a_addr = smem_u32(s_a);
+    const uint32_t wf_addr = smem_u32(s_wf), wb_addr = smem_u32(s_wb);
+    uint32_t phase = 0;
+    bool ok = true;
     float loss_acc = 0.f;
-    for (int base = warp * 32; base < n; base += nwarps * 32) {
-        const int i = base + lane;
-        NNIn mine;
+    for (int base = blockIdx.x * kTcRows; base < n && ok; base += gridDim.x * kTcRows) {
+        const int i = base + row;
+        const bool valid = i < n;
+        NNIn in;
         f3 wi = mk(0.f, 0.f, 1.f);
         float pb = 0.f, T = 0.f;
-        if (i < n) {
+        if (valid) {
             const float4 r0 = rec[4 * (size_t)i], r1 = rec[4 * (size_t)i + 1], r2 = rec[4 * (size_t)i + 2],
                          r3 = rec[4 * (size_t)i + 3];
-            mine.pn = mk((r0.x - N.lo[0]) * N.inv_ext[0], (r0.y - N.lo[1]) * N.inv_ext[1],
-                         (r0.z - N.lo[2]) * N.inv_ext[2]);
-            mine.n = mk(r0.w, r1.x, r1.y);
-            mine.wo = mk(r1.z, r1.w, r2.x);
+            in.pn = mk((r0.x - N.lo[0]) * N.inv_ext[0], (r0.y - N.lo[1]) * N.inv_ext[1], (r0.z - N.lo[2]) * N.inv_ext[2]);
+            in.n = mk(r0.w, r1.x, r1.y);
+            in.wo = mk(r1.z, r1.w, r2.x);
             wi = mk(r2.y, r2.z, r2.w);
             pb = r3.x;
             T = r3.y * inv_tsum;
-        } else {
-            mine.pn = mine.n = mine.wo = mk(0.f, 0.f, 0.f);
         }
-        for (int mt = 0; mt < 2; mt++) {
-            const int row0 = base + mt * 16 + g, row1 = row0 + 8;
-            // forward; the input of every layer goes to TB.act
-            uint32_t a[4][4];
-            float acc[8][4];
-            input_frags(mine, mt, lane, a);
-            for (int l = 0; l < kNNLayers - 1; l++) {
-                store_frag_rows(TB.act + (size_t)l * TB.cap * 64, a, row0, row1, n, 64, t);
-                hidden_layer(s_wt + l * kWLayer, lane, a, acc);
+        float v[64];
+#pragma unroll
+        for (int j = 0; j < 64; j++) v[j] = valid ? nn_feature(j, in.pn, in.n, in.wo) : 0.f;
+        tc_store_row(s_a, row, v, false);
+        if (valid) store_row_bf16(TB.act + (size_t)i * 64, v, 64, false);
+        for (int l = 0; l < kNNLayers; l++) {
+            const int nout = nn_layer_out(l);
+            ok = tc_layer(tmem, a_addr, kTcSBO, wf_addr + l * kTcWLayerBytes, kTcSBO, 64, nout, bar, phase);
+            if (!ok) break;
+#pragma unroll
+            for (int c = 0; c < 64; c += 16)
+                if (c < nout) tmem_ld16(t_row + (uint32_t)c, v + c);
+            if (l < kNNLayers - 1) {
+                tc_store_row(s_a, row, v, true);
+                if (valid) store_row_bf16(TB.act + ((size_t)(l + 1) * TB.cap + i) * 64, v, 64, true);
             }
-            store_frag_rows(TB.act + (size_t)(kNNLayers - 1) * TB.cap * 64, a, row0, row1, n, 64, t);
-            {
-                float out[6][4];
-                output_layer(s_wt + (kNNLayers - 1) * kWLayer, lane, a, out);
-                store_out_tile(s_tile, out, lane);
-            }
-            __syncwarp();
-            // loss gradient of the tile's 16 records: lane mt*16 + r owns row r
-            if ((lane >> 4) == mt) {
-                const int r = lane & 15;
-                float raw[kNNOut], gr[kNNOut];
+        }
+        if (!ok) break;
+        float g[64];
 #pragma unroll
-                for (int k = 0; k < kNNOut; k++) raw[k] = s_tile[r * kNNOut + k];
-                loss_acc += (i < n) ? nn_loss_grad(raw, wi, pb, T, N.c_lo, N.c_hi, gr) : 0.f;
+        for (int k = 0; k < 64; k++) g[k] = 0.f;
+        if (valid) loss_acc += nn_loss_grad(v, wi, pb, T, N.c_lo, N.c_hi, g);
+        for (int l = kNNLayers - 1; l >= 0; l--) {
+            const int K = nn_layer_out(l);
+            if (valid) store_row_bf16(TB.grad + ((size_t)l * TB.cap + i) * 64, g, K, false);
+            if (l == 0) break;
+            tc_store_row(s_a, row, g, false, K);
+            const uint32_t sbo = (uint32_t)(K / 8) * 128u;
+            ok = tc_layer(tmem, a_addr, sbo, wb_addr + l * kTcWLayerBytes, sbo, K, 64, bar, phase);
+            if (!ok) break;
+            float dh[64];
 #pragma unroll
-                for (int k = 0; k < kNNOut; k++) s_tile[r * kNNOut + k] = (i < n) ? gr[k] : 0.f;
-            }
-            __syncwarp();
-            // dZ of the output layer as A fragments (k = 48 outputs, 3 k-tiles)
-            uint32_t dz[4][4];
+            for (int c = 0; c < 64; c += 16) tmem_ld16(t_row + (uint32_t)c, dh + c);
+            // dZ_{l-1} = dH where A_l > 0 (A_l = relu(Z_{l-1}), this thread's own row)
+            if (valid) {
+                const uint4* ar = reinterpret_cast<const uint4*>(TB.act + ((size_t)l * TB.cap + i) * 64);
 #pragma unroll
-            for (int kt = 0; kt < 4; kt++) {
-                const float* q0 = s_tile + g * kNNOut;
-                const float* q1 = s_tile + (g + 8) * kNNOut;
-                const int c = kt * 16 + 2 * t;
-                if (kt < 3) {
-                    dz[kt][0] = pack_bf16(q0[c], q0[c + 1]);
-                    dz[kt][1] = pack_bf16(q1[c], q1[c + 1]);
-                    dz[kt][2] = pack_bf16(q0[c + 8], q0[c + 9]);
-                    dz[kt][3] = pack_bf16(q1[c + 8], q1[c + 9]);
-                } else {
-                    dz[kt][0] = dz[kt][1] = dz[kt][2] = dz[kt][3] = 0u;
-                }
-            }
-            __syncwarp();
-            for (int l = kNNLayers - 1; l >= 0; l--) {
-                const int nout = nn_layer_out(l);
-                store_frag_rows(TB.grad + (size_t)l * TB.cap * 64, dz, row0, row1, n, nout, t);
-                if (l == 0) break;
-                // dH = dZ_l W_l^T (16 x 64); dZ_{l-1} = dH where A_l > 0
+                for (int q = 0; q < 8; q++) {
+                    const uint4 a4 = ar[q];
+                    const uint32_t w4[4] = {a4.x, a4.y, a4.z, a4.w};
 #pragma unroll
-                for (int nt = 0; nt < 8; nt++) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
-                const int kts = (nout + 15) / 16;
-                for (int kt = 0; kt < kts; kt++)
-#pragma unroll
-                    for (int nt = 0; nt < 8; nt++) {
-                        uint32_t b[2];
-                        load_b_bwd(s_w + l * kWLayer, nt, kt, lane, b);
-                        mma_bf16(acc[nt], dz[kt], b);
+                    for (int h = 0; h < 4; h++) {
+                        const __nv_bfloat162 b2 = *reinterpret_cast<const __nv_bfloat162*>(&w4[h]);
+                        g[8 * q + 2 * h] = __low2float(b2) > 0.f ? dh[8 * q + 2 * h] : 0.f;
+                        g[8 * q + 2 * h + 1] = __high2float(b2) > 0.f ? dh[8 * q + 2 * h + 1] : 0.f;
                     }
-                uint32_t al[4][4];
-                load_frag_rows(TB.act + (size_t)l * TB.cap * 64, al, row0, row1, n, t);
-#pragma unroll
-                for (int kt = 0; kt < 4; kt++) {
-                    dz[kt][0] = relu_mask(al[kt][0], acc[2 * kt][0], acc[2 * kt][1]);
-                    dz[kt][1] = relu_mask(al[kt][1], acc[2 * kt][2], acc[2 * kt][3]);
-                    dz[kt][2] = relu_mask(al[kt][2], acc[2 * kt + 1][0], acc[2 * kt + 1][1]);
-                    dz[kt][3] = relu_mask(al[kt][3], acc[2 * kt + 1][2], acc[2 * kt + 1][3]);
                 }
             }
         }
     }
+    tc_end(ok, tmem, bar, phase, status);
     float ls = loss_acc;
     for (int o = 16; o > 0; o >>= 1) ls += __shfl_xor_sync(0xffffffffu, ls, o);
     if (loss_out && lane == 0) atomicAdd(loss_out, ls);
@@ -596,7 +494,7 @@ __global__ void k_nn_pack(NNWeights W) {
 }
 
 size_t nn_smem_infer() { return (size_t)kTcSmem; }
-size_t nn_smem_train() { return (size_t)2 * kNNLayers * kWLayer * 2 + (kNNThreads / 32) * 32 * kNNOut * 4; }
+size_t nn_smem_train() { return (size_t)kTcTrainSmem; }
 size_t nn_wcopy_elems() { return (size_t)kNNLayers * kWLayer; }
 
 cudaError_t nn_set_smem_limits() {
@@ -624,9 +522,10 @@ void launch_nn_train_step(const NNWeights& W, const NNNorm& N, const float4* rec
                           const NNTrainBuf& TB, float* grad, float* loss, const NNAdam& opt, int step, int num_sms,
                           cudaStream_t st, bool apply) {
     cudaMemsetAsync(grad, 0, sizeof(float) * kNNWeights, st);
-    const int blocks = std::max(1, std::min(num_sms * 4, (n + kNNThreads - 1) / kNNThreads));
-    k_nn_train_fb<<<blocks, kNNThreads, nn_smem_train(), st>>>(W, N, rec, n, tsum > 0.f ? 1.0f / tsum : 0.f, TB,
-                                                               loss);
+    // two CTAs per SM fit (80 KB of shared memory each)
+    const int blocks = std::max(1, std::min(num_sms * 2, (n + kTcRows - 1) / kTcRows));
+    k_nn_train_fb<<<blocks, kTcRows, nn_smem_train(), st>>>(W, N, rec, n, tsum > 0.f ? 1.0f / tsum : 0.f, TB, loss,
+                                                            reinterpret_cast<uint32_t*>(loss + 2));
     dim3 gw(std::max(1, std::min(num_sms, (n + kWGRows - 1) / kWGRows)), kNNLayers);
     k_nn_wgrad<<<gw, kNNThreads, 0, st>>>(TB, n, grad);
     if (apply) {
@@ -635,8 +534,6 @@ void launch_nn_train_step(const NNWeights& W, const NNNorm& N, const float4* rec
                                                             opt.clip);
     }
 }
-
-
 
 // ===========================================================================
 // Learned-guide integrator: PT + NEE + MIS where the directional sample comes

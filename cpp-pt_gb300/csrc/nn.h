@@ -53,7 +53,8 @@ void launch_nn_forward_debug(const NNWeights& W, const NNNorm& N, const float* i
                              uint32_t* status, int num_sms, cudaStream_t st);
 void launch_nn_infer(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, const NNWeights& W,
                      const NNNorm& N, float4* params, int num_sms, cudaStream_t st);
-// grad (kNNWeights floats) receives dL/dW; loss accumulates the batch loss;
+// grad (kNNWeights floats) receives dL/dW; loss[0] accumulates the batch
+// loss and the word at loss + 2 collects status bits (kStatusTensorTimeout);
 // apply: also take one Adam step (step counts from 1).
 void launch_nn_train_step(const NNWeights& W, const NNNorm& N, const float4* rec, int n, float tsum,
                           const NNTrainBuf& TB, float* grad, float* loss, const NNAdam& opt, int step, int num_sms,
