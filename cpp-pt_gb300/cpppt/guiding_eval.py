@@ -21,7 +21,9 @@ Plain and nn accumulate chunks of spp on the GPU; relMSE is taken at
 checkpoints spaced by sqrt(2) up to the largest budget.  Prints one JSON
 line per method and checkpoint, then a summary: relMSE of each method at
 each budget, and the time nn needs to reach plain's relMSE at that budget
-(linear interpolation of log relMSE over log time between checkpoints).
+(linear interpolation of log relMSE over log time between checkpoints),
+both as measured and with the reference's own noise (estimated from its two
+independent halves) subtracted.
 """
 from __future__ import annotations
 
@@ -99,20 +101,26 @@ def main():
     gs = GpuScene(sc)
     H, W = a.height, a.width
     # reference: plain (unbiased) PT at ref_spp, accumulated on the GPU in FP64
+    # as two independent halves; relMSE(half A, half B) / 4 estimates the
+    # reference's own noise, which adds to every method's measured relMSE
     img = torch.zeros((H, W, 3), dtype=torch.float32, device="cuda")
-    acc = torch.zeros((H, W, 3), dtype=torch.float64, device="cuda")
+    halves = [torch.zeros((H, W, 3), dtype=torch.float64, device="cuda") for _ in range(2)]
     t0 = time.perf_counter()
     step = 256
-    for k in range(0, a.ref_spp, step):
+    for q, k in enumerate(range(0, a.ref_spp, step)):
         gs.render_device(img.data_ptr(), step, max_depth=a.depth, seed=777000 + k, mode=MODE_MIS,
                          flags=FLAG_UNBIASED_MIS)
-        acc += img.double()
-    ref = (acc / (a.ref_spp // step)).float()
+        halves[q & 1] += img.double()
+    n_steps = a.ref_spp // step
+    ref = ((halves[0] + halves[1]) / n_steps).float()
+    ha = (halves[0] / ((n_steps + 1) // 2)).float()
+    hb = (halves[1] / max(1, n_steps // 2)).float()
+    ref_noise = float(((ha - hb) ** 2 / (ref ** 2 + 1e-2)).mean()) / 4.0
     torch.cuda.synchronize()
     ref_s = time.perf_counter() - t0
     print(json.dumps({"reference": {"spp": a.ref_spp, "seconds": ref_s, "mean": float(ref.mean()),
-                                    "triangles": sc.n_triangles, "resolution": [W, H], "depth": a.depth}}),
-          flush=True)
+                                    "relMSE_noise_estimate": ref_noise, "triangles": sc.n_triangles,
+                                    "resolution": [W, H], "depth": a.depth}}), flush=True)
     # warm-up (graph capture, allocations, kernel loading)
     gs.render_device(img.data_ptr(), 1, max_depth=a.depth, seed=1, mode=MODE_MIS, flags=FLAG_UNBIASED_MIS)
     gs.render_device(img.data_ptr(), 1, max_depth=a.depth, seed=1, mode=MODE_NN, flags=FLAG_NN_FREEZE)
@@ -122,9 +130,10 @@ def main():
     res_plain, img_plain, _ = progressive(gs, MODE_MIS, FLAG_UNBIASED_MIS, B, a.chunk, a.depth, 10_000, ref, cps)
     results["plain"] = res_plain
     nn_runs = {}
+    defaults = gs.nn_config()
     for q, text in enumerate(a.nn_config or ["{}"]):
         gs.nn_reset(2024)
-        cfg = gs.nn_configure(**json.loads(text))
+        cfg = gs.nn_configure(**{**defaults, **json.loads(text)})
         rows, img_nn, _ = progressive(gs, MODE_NN, 0, B, a.chunk, a.depth, 20_000, ref, cps)
         name = "nn" if q == 0 else f"nn{q}"
         results[name] = rows
@@ -147,17 +156,22 @@ def main():
     for name, rows in results.items():
         for el, spp, r in rows:
             print(json.dumps({"method": name, "seconds": el, "spp": spp, "relMSE": r}), flush=True)
-    summ = {"learned": nn_runs, "budgets": {}}
+    summ = {"learned": nn_runs, "reference_noise_relMSE": ref_noise, "budgets": {}}
+    corrected = {k: [(t, spp, max(r - ref_noise, 1e-12)) for t, spp, r in v] for k, v in results.items()}
     for bud in a.budgets:
         p = [r for t, _, r in res_plain if t == bud]
         if not p:
             continue
-        row = {"plain_relMSE": p[0]}
+        pc = p[0] - ref_noise
+        row = {"plain_relMSE": p[0], "plain_relMSE_noise_corrected": pc}
         for name in nn_runs:
             n = [r for t, _, r in results[name] if t == bud]
             t_nn = time_to_reach(results[name], p[0])
+            t_nc = time_to_reach(corrected[name], max(pc, 1e-12))
             row[name] = {"relMSE": n[0] if n else None, "seconds_to_plain_relMSE": t_nn,
-                         "time_fraction": None if t_nn is None else t_nn / bud}
+                         "time_fraction": None if t_nn is None else t_nn / bud,
+                         "relMSE_noise_corrected": None if not n else n[0] - ref_noise,
+                         "time_fraction_noise_corrected": None if t_nc is None else t_nc / bud}
         if "sdtree" in results:
             sd = [r for (el, spp, r), b2 in zip(results["sdtree"], a.budgets) if b2 == bud]
             row["sdtree_relMSE"] = sd[0] if sd else None

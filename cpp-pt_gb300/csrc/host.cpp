@@ -394,7 +394,9 @@ void render_ppg(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
 // ---------------------------------------------------------------------------
 // Learned guide: network state and the NN / unbiased-MIS render driver
 // ---------------------------------------------------------------------------
-constexpr int kNNBatch = 1 << 18;  // training records per step
+constexpr int kNNBatch = 1 << 18;               // largest training batch (records per Adam step)
+constexpr int kNNMaxStepsPerRound = 16;
+constexpr int kNNRecordCap = kNNMaxStepsPerRound * kNNBatch;  // record buffer (64 B each, 268 MB)
 constexpr int kNNWeightCount = 3 * 64 * 64 + 64 * 48;
 static_assert(kNNWeightCount == PT_NN_WEIGHTS, "weight count");
 
@@ -439,8 +441,9 @@ void nn_upload(const NNWeights& W, const float* host, cudaStream_t st) {
 void nn_ensure(pt_scene* s) {
     if (s->nn_ready) return;
     nn_alloc(s->nn_owned, &s->nnw, &s->nn_tb, &s->nn_grad, &s->nn_scalars, kNNBatch);
-    s->nn_rec = dalloc<float4>(s->nn_owned, (size_t)kNNBatch * 4);
+    s->nn_rec = dalloc<float4>(s->nn_owned, (size_t)kNNRecordCap * 4);
     s->nn_rec_count = 0;
+    if (!s->h_rec_left) ck(cudaMallocHost(&s->h_rec_left, sizeof(int)), "cudaMallocHost");
     std::vector<float> w = nn_random_weights(12345u);
     nn_upload(s->nnw, w.data(), s->stream);
     ck(cudaStreamSynchronize(s->stream), "nn init");
@@ -458,6 +461,28 @@ NNNorm scene_norm(const pt_scene* s) {
     N.c_lo = s->nn_cfg.bsdf_frac_min;
     N.c_hi = s->nn_cfg.bsdf_frac_max;
     return N;
+}
+
+// Per-path buffers of the slot-based wavefront, kept by the scene and grown
+// on demand (capacity paths; vertex records for `depth` vertices per path
+// when training; guide parameters when the guide is used).
+NNPathData nn_path_buffers(pt_scene* s, int capacity, int depth) {
+    const bool grow = capacity > s->nnpd_cap || depth > s->nnpd_depth;
+    if (grow) {
+        for (void* p : s->nnpd_owned) cudaFree(p);
+        s->nnpd_owned.clear();
+        s->nnpd = NNPathData{};
+        s->nn_params = nullptr;
+        s->nnpd_cap = std::max(capacity, s->nnpd_cap);
+        s->nnpd_depth = std::max(depth, s->nnpd_depth);
+        const int cap = s->nnpd_cap;
+        s->nnpd.vert = dalloc<float4>(s->nnpd_owned, (size_t)cap * std::max(1, s->nnpd_depth) * kNNVertFloat4);
+        s->nnpd.acc = dalloc<float4>(s->nnpd_owned, cap);
+        s->nnpd.slot_stack = dalloc<int>(s->nnpd_owned, cap);
+        s->nnpd.fin = dalloc<int4>(s->nnpd_owned, cap);
+        s->nn_params = dalloc<float4>(s->nnpd_owned, (size_t)cap * 11);
+    }
+    return s->nnpd;
 }
 
 // PT + NEE + MIS on the slot-based wavefront (nn.cu).  guided: the learned
@@ -480,20 +505,12 @@ void render_nn(pt_scene* s, const pt_render_desc* desc, float* d_dst, bool guide
     const int capacity = (int)std::min<unsigned long long>(1 << 20, (total + 1023) / 1024 * 1024);
     const int film_n = 3 * s->width * s->height;
     ensure_wave(s, capacity, film_n);
-    std::vector<void*> tmp;
-    struct Free {
-        std::vector<void*>& v;
-        ~Free() { for (void* p : v) cudaFree(p); }
-    } guard{tmp};
-    NNPathData PD;
-    PD.vert = dalloc<float4>(tmp, train ? (size_t)capacity * P.max_depth * kNNVertFloat4 : 1);
-    PD.acc = dalloc<float4>(tmp, capacity);
-    PD.slot_stack = dalloc<int>(tmp, capacity);
-    PD.fin = dalloc<int4>(tmp, capacity);
+    NNPathData PD = nn_path_buffers(s, capacity, train ? P.max_depth : 0);
     const int batch = s->nn_cfg.batch;
-    PD.rec_cap = train ? batch : 0;
+    const int rec_cap = std::min(kNNRecordCap, s->nn_cfg.steps_per_round * batch);
+    PD.rec_cap = train ? rec_cap : 0;
     PD.rec = train ? s->nn_rec : nullptr;
-    float4* params = guided ? dalloc<float4>(tmp, (size_t)capacity * 11) : nullptr;
+    float4* params = guided ? s->nn_params : nullptr;
     const NNNorm N = scene_norm(s);
     ck(cudaEventRecord(s->ev0, st), "event");
     ck(cudaMemsetAsync(s->film, 0, sizeof(unsigned long long) * film_n, st), "memset film");
@@ -509,6 +526,7 @@ void render_nn(pt_scene* s, const pt_render_desc* desc, float* d_dst, bool guide
     const unsigned long long max_rounds =
         64 + (total / (unsigned long long)capacity + 2) * (unsigned long long)(desc->max_depth + 2) * 4 / kItersPerGraph;
     double records = 0;
+    int rec_left = -1;  // records kept after the last round's training (-1: that round did not train)
     for (unsigned long long round = 0;; round++) {
         for (int k = 0; k < kItersPerGraph; k++) {
             const int cur = k & 1;
@@ -523,35 +541,44 @@ void render_nn(pt_scene* s, const pt_render_desc* desc, float* d_dst, bool guide
         ck(cudaMemcpyAsync(s->h_ctr, s->d_ctr, sizeof(WaveCounters), cudaMemcpyDeviceToHost, st), "read counters");
         ck(cudaStreamSynchronize(st), "render");
         check_status(s, s->h_ctr->status);
+        rec_left = -1;
         if (train && s->h_ctr->n_rec >= batch) {
-            // one Adam step on the batch of records, then start a new batch
-            ck(cudaMemsetAsync(s->nn_scalars, 0, sizeof(float) * 4, st), "memset");
-            if (s->nn_cfg.divergence == PT_NN_CHI2) launch_square_T(PD.rec, batch, st);
-            launch_sum_T(PD.rec, batch, s->nn_scalars + 1, st);
-            float tsum = 0.f;
-            ck(cudaMemcpyAsync(&tsum, s->nn_scalars + 1, sizeof(float), cudaMemcpyDeviceToHost, st), "copy");
-            ck(cudaStreamSynchronize(st), "tsum");
+            // as many Adam steps as full batches were recorded (each on its own
+            // records), then start collecting again
+            const int steps = std::min(s->h_ctr->n_rec, rec_cap) / batch;
             NNAdam opt;
             opt.lr = s->nn_cfg.learning_rate;
-            launch_nn_train_step(s->nnw, N, PD.rec, batch, tsum, s->nn_tb, s->nn_grad, s->nn_scalars, opt,
-                                 ++s->nn_steps, s->num_sms, st, true);
-            launches += 5;
+            for (int k = 0; k < steps; k++) {
+                float4* r = PD.rec + (size_t)4 * k * batch;
+                ck(cudaMemsetAsync(s->nn_scalars, 0, sizeof(float) * 4, st), "memset");
+                if (s->nn_cfg.divergence == PT_NN_CHI2) launch_square_T(r, batch, st);
+                launch_sum_T(r, batch, s->nn_scalars + 1, st);
+                launch_nn_train_step(s->nnw, N, r, batch, s->nn_scalars + 1, s->nn_tb, s->nn_grad, s->nn_scalars,
+                                     opt, ++s->nn_steps, s->num_sms, st, true);
+                launches += 5;
+            }
+            // records beyond the last full batch move to the front and stay
+            const int held = std::min(s->h_ctr->n_rec, rec_cap);
+            rec_left = held - steps * batch;
+            if (rec_left > 0)
+                ck(cudaMemcpyAsync(PD.rec, PD.rec + (size_t)4 * steps * batch, sizeof(float4) * 4 * rec_left,
+                                   cudaMemcpyDeviceToDevice, st), "keep records");
+            *s->h_rec_left = rec_left;
+            ck(cudaMemcpyAsync(&s->d_ctr->n_rec, s->h_rec_left, sizeof(int), cudaMemcpyHostToDevice, st), "records");
             float sc[4] = {0.f, 0.f, 0.f, 0.f};
             ck(cudaMemcpyAsync(sc, s->nn_scalars, sizeof(sc), cudaMemcpyDeviceToHost, st), "copy");
-            ck(cudaMemsetAsync(&s->d_ctr->n_rec, 0, sizeof(int), st), "reset records");
             ck(cudaStreamSynchronize(st), "train");
             uint32_t tstat;
             std::memcpy(&tstat, &sc[2], sizeof(tstat));
             check_status(s, tstat);
-            const float loss = sc[0];
-            s->nn_last_loss = loss;
-            records += batch;
-            s->nn_records += batch;
+            s->nn_last_loss = sc[0];
+            records += (double)steps * batch;
+            s->nn_records += (double)steps * batch;
         }
         if (s->h_ctr->n_cur == 0 && s->h_ctr->work_next >= s->h_ctr->work_total) break;
         if (round > max_rounds) throw Fail(PT_ERR_LIMIT, "render did not converge within the iteration bound");
     }
-    if (train) s->nn_rec_count = std::min(s->h_ctr->n_rec, batch);
+    if (train) s->nn_rec_count = rec_left >= 0 ? rec_left : std::min(s->h_ctr->n_rec, rec_cap);
     launch_film_resolve(s->film, d_dst ? d_dst : s->d_out, film_n, 1.0 / (double)desc->spp, st);
     ck(cudaEventRecord(s->ev1, st), "event");
     ck(cudaStreamSynchronize(st), "render");
@@ -1164,6 +1191,10 @@ pt_status pt_nn_configure(pt_scene* s, const pt_nn_config* c) {
         g_error = "divergence must be PT_NN_KL or PT_NN_CHI2";
         return PT_ERR_INVALID;
     }
+    if (c->steps_per_round < 1 || c->steps_per_round > kNNMaxStepsPerRound) {
+        g_error = "steps_per_round must be in [1, 16]";
+        return PT_ERR_INVALID;
+    }
     s->nn_cfg = *c;
     s->nn_rec_count = 0;  // records of the previous batch size are dropped
     return PT_OK;
@@ -1253,9 +1284,10 @@ pt_status pt_debug_nn_grad(const float* weights, const float* lo, const float* h
         ck(cudaMemcpyAsync(drec, records, sizeof(float) * 16 * n, cudaMemcpyHostToDevice, c.st), "copy");
         double tsum = 0;
         for (int i = 0; i < n; i++) tsum += records[16 * i + 13];
-        ck(cudaMemsetAsync(scal, 0, sizeof(float) * 4, c.st), "memset");
+        const float sc0[4] = {0.f, (float)tsum, 0.f, 0.f};
+        ck(cudaMemcpyAsync(scal, sc0, sizeof(sc0), cudaMemcpyHostToDevice, c.st), "copy");
         NNAdam opt;
-        launch_nn_train_step(W, norm_from(lo, hi), drec, n, (float)tsum, TB, grad, scal, opt, 1, c.sms, c.st, false);
+        launch_nn_train_step(W, norm_from(lo, hi), drec, n, scal + 1, TB, grad, scal, opt, 1, c.sms, c.st, false);
         ck(cudaMemcpyAsync(out_grad, grad, sizeof(float) * kNNWeightCount, cudaMemcpyDeviceToHost, c.st), "copy");
         float sc[4] = {0.f, 0.f, 0.f, 0.f};
         ck(cudaMemcpyAsync(sc, scal, sizeof(sc), cudaMemcpyDeviceToHost, c.st), "copy");

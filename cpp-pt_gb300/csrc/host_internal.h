@@ -136,10 +136,16 @@ struct pt_scene {
     double nn_last_loss = 0, nn_records = 0;
     float4* nn_rec = nullptr;  // training records carried across renders
     int nn_rec_count = 0;
-    pt_nn_config nn_cfg{1e-3f, 0.1f, 0.9f, 1 << 18, PT_NN_KL};
+    int* h_rec_left = nullptr;  // pinned staging word for the kept-record count
+    NNPathData nnpd{};          // per-path buffers of the slot-based wavefront (grown on demand)
+    float4* nn_params = nullptr;
+    int nnpd_cap = 0, nnpd_depth = 0;
+    std::vector<void*> nnpd_owned;
+    pt_nn_config nn_cfg{3e-3f, 0.1f, 0.9f, 1 << 18, PT_NN_CHI2, 8};
 
     ~pt_scene() {
         for (void* p : nn_owned) cudaFree(p);
+        for (void* p : nnpd_owned) cudaFree(p);
         if (graph) cudaGraphExecDestroy(graph);
         for (void* p : owned) cudaFree(p);
         for (void* p : pb_owned) cudaFree(p);
@@ -148,6 +154,7 @@ struct pt_scene {
         if (d_io) cudaFree(d_io);
         if (h_ctr) cudaFreeHost(h_ctr);
         if (h_job) cudaFreeHost(h_job);
+        if (h_rec_left) cudaFreeHost(h_rec_left);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (stream) cudaStreamDestroy(stream);

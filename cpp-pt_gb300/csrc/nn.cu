@@ -305,8 +305,8 @@ __device__ __forceinline__ void store_row_bf16(__nv_bfloat16* dst, const float* 
 constexpr int kNNThreads = 128;
 
 __global__ void __launch_bounds__(kTcRows) k_nn_train_fb(NNWeights W, NNNorm N, const float4* __restrict__ rec, int n,
-                                                         float inv_tsum, NNTrainBuf TB, float* __restrict__ loss_out,
-                                                         uint32_t* status) {
+                                                         const float* __restrict__ tsum, NNTrainBuf TB,
+                                                         float* __restrict__ loss_out, uint32_t* status) {
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* s_wf = smem;                                  // forward B tiles: W_l^T (out x in)
     unsigned char* s_wb = smem + kNNLayers * kTcWLayerBytes;     // backward B tiles: W_l (in x out)
@@ -324,6 +324,7 @@ __global__ void __launch_bounds__(kTcRows) k_nn_train_fb(NNWeights W, NNNorm N, 
     uint32_t phase = 0;
     bool ok = true;
     float loss_acc = 0.f;
+    const float inv_tsum = *tsum > 0.f ? 1.0f / *tsum : 0.f;
     for (int base = blockIdx.x * kTcRows; base < n && ok; base += gridDim.x * kTcRows) {
         const int i = base + row;
         const bool valid = i < n;
@@ -518,13 +519,13 @@ void launch_nn_infer(const DevScene& S, const PathBuffers& B, int cur, WaveCount
                      const NNNorm& N, float4* params, int num_sms, cudaStream_t st) {
     k_nn_infer<<<num_sms * 4, kTcRows, nn_smem_infer(), st>>>(S, B, cur, ctr, W, N, params);
 }
-void launch_nn_train_step(const NNWeights& W, const NNNorm& N, const float4* rec, int n, float tsum,
+void launch_nn_train_step(const NNWeights& W, const NNNorm& N, const float4* rec, int n, const float* tsum,
                           const NNTrainBuf& TB, float* grad, float* loss, const NNAdam& opt, int step, int num_sms,
                           cudaStream_t st, bool apply) {
     cudaMemsetAsync(grad, 0, sizeof(float) * kNNWeights, st);
     // two CTAs per SM fit (80 KB of shared memory each)
     const int blocks = std::max(1, std::min(num_sms * 2, (n + kTcRows - 1) / kTcRows));
-    k_nn_train_fb<<<blocks, kTcRows, nn_smem_train(), st>>>(W, N, rec, n, tsum > 0.f ? 1.0f / tsum : 0.f, TB, loss,
+    k_nn_train_fb<<<blocks, kTcRows, nn_smem_train(), st>>>(W, N, rec, n, tsum, TB, loss,
                                                             reinterpret_cast<uint32_t*>(loss + 2));
     dim3 gw(std::max(1, std::min(num_sms, (n + kWGRows - 1) / kWGRows)), kNNLayers);
     k_nn_wgrad<<<gw, kNNThreads, 0, st>>>(TB, n, grad);
@@ -745,55 +746,70 @@ __global__ void __launch_bounds__(256) k_shade_nn(DevScene S, PathBuffers B, int
 // * the NEE direction, where the shadow ray was unoccluded:
 //   T = lum((S_after_nee_k - S_before_nee_k) / throughput_k).
 // S_after_nee of the last vertex is S_end (its shadow ray resolved before
-// this kernel runs).
-__device__ __forceinline__ bool emit_record(const NNPathData& PD, WaveCounters* ctr, const float4* vr, f3 wi,
-                                            float pb, float T) {
-    if (!(T > 0.f) || !isfinite(T)) return true;
-    const int r = atomicAdd(&ctr->n_rec, 1);
-    if (r >= PD.rec_cap) return false;
-    float4* o = PD.rec + 4 * (size_t)r;
-    o[0] = vr[0];
-    o[1] = vr[1];
-    o[2] = make_float4(vr[2].x, wi.x, wi.y, wi.z);
-    o[3] = make_float4(pb, T, 0.f, 0.f);
-    return true;
+// this kernel runs).  visit_records calls emit(vertex record, wi,
+// p_bsdf(wi), T) for every record of the finished path f (slot, traced
+// vertices, recorded vertices).
+template <class Emit>
+__device__ __forceinline__ void visit_records(const NNPathData& PD, int4 f, int max_depth, Emit emit) {
+    const float4 Se = PD.acc[f.x];
+    const size_t vbase = (size_t)f.x * max_depth;
+    for (int k = 0; k < f.z; k++) {
+        const float4* vr = PD.vert + kNNVert * (vbase + k);
+        const float4 v2 = vr[2], v3 = vr[3], v4 = vr[4], v5 = vr[5], v6 = vr[6];
+        const f3 inv = mk(v3.y > 0.f ? 1.0f / v3.y : 0.f, v3.z > 0.f ? 1.0f / v3.z : 0.f,
+                          v3.w > 0.f ? 1.0f / v3.w : 0.f);
+        const f3 after = k < f.z - 1 || k < f.y ? mk(v4.x, v4.y, v4.z) : mk(Se.x, Se.y, Se.z);
+        if (v6.w != 0.f) {
+            const f3 dn = mk(after.x - v5.x, after.y - v5.y, after.z - v5.z);
+            const float T = luminance(mk(dn.x * inv.x, dn.y * inv.y, dn.z * inv.z));
+            if (T > 0.f && isfinite(T)) emit(vr, mk(v6.x, v6.y, v6.z), v5.w, T);
+        }
+        if (k < f.y && v4.w != 0.f) {
+            const f3 dS = mk(Se.x - after.x, Se.y - after.y, Se.z - after.z);
+            const float T = luminance(mk(dS.x * inv.x, dS.y * inv.y, dS.z * inv.z));
+            if (T > 0.f && isfinite(T)) emit(vr, mk(v2.y, v2.z, v2.w), v3.x, T);
+        }
+    }
 }
 
+// Finished paths: records are counted first, one warp-aggregated atomic
+// reserves the warp's range, then written (records beyond the buffer's
+// capacity are dropped); the slots go back to the free list.
 __global__ void __launch_bounds__(256) k_finish_nn(NNPathData PD, WaveCounters* ctr, int max_depth) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = ctr->n_fin;
-    bool release = false;
-    int slot = 0;
-    if (i < n) {
-        const int4 f = PD.fin[i];
-        slot = f.x;
-        release = true;
-        if (PD.rec_cap > 0) {
-            const float4 Se = PD.acc[slot];
-            const size_t vbase = (size_t)slot * max_depth;
-            for (int k = 0; k < f.z; k++) {
-                const float4* vr = PD.vert + kNNVert * (vbase + k);
-                const float4 v2 = vr[2], v3 = vr[3], v4 = vr[4], v5 = vr[5], v6 = vr[6];
-                const f3 inv = mk(v3.y > 0.f ? 1.0f / v3.y : 0.f, v3.z > 0.f ? 1.0f / v3.z : 0.f,
-                                  v3.w > 0.f ? 1.0f / v3.w : 0.f);
-                const f3 after = k < f.z - 1 || k < f.y ? mk(v4.x, v4.y, v4.z) : mk(Se.x, Se.y, Se.z);
-                if (v6.w != 0.f) {
-                    const f3 dn = mk(after.x - v5.x, after.y - v5.y, after.z - v5.z);
-                    if (!emit_record(PD, ctr, vr, mk(v6.x, v6.y, v6.z), v5.w,
-                                     luminance(mk(dn.x * inv.x, dn.y * inv.y, dn.z * inv.z))))
-                        break;
-                }
-                if (k < f.y && v4.w != 0.f) {
-                    const f3 dS = mk(Se.x - after.x, Se.y - after.y, Se.z - after.z);
-                    if (!emit_record(PD, ctr, vr, mk(v2.y, v2.z, v2.w), v3.x,
-                                     luminance(mk(dS.x * inv.x, dS.y * inv.y, dS.z * inv.z))))
-                        break;
-                }
+    const unsigned lane = threadIdx.x & 31u;
+    const bool release = i < n;
+    int4 f = make_int4(0, 0, 0, 0);
+    if (release) f = PD.fin[i];
+    const bool records = release && PD.rec_cap > 0;
+    int count = 0;
+    if (records) visit_records(PD, f, max_depth, [&](const float4*, f3, float, float) { count++; });
+    int incl = count;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (unsigned)o) incl += v;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    int base = 0;
+    if (lane == 31 && total > 0) base = atomicAdd(&ctr->n_rec, total);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    if (records && count > 0) {
+        int r = base + incl - count;
+        visit_records(PD, f, max_depth, [&](const float4* vr, f3 wi, float pb, float T) {
+            if (r < PD.rec_cap) {
+                float4* o = PD.rec + 4 * (size_t)r;
+                o[0] = vr[0];
+                o[1] = vr[1];
+                o[2] = make_float4(vr[2].x, wi.x, wi.y, wi.z);
+                o[3] = make_float4(pb, T, 0.f, 0.f);
             }
-        }
+            r++;
+        });
     }
     const int jr = warp_append_nn(&ctr->free_top, release);
-    if (release) PD.slot_stack[jr] = slot;
+    if (release) PD.slot_stack[jr] = f.x;
 }
 
 // NEE shadow rays of the learned-guide integrator: unoccluded contributions

@@ -56,7 +56,8 @@ void launch_nn_infer(const DevScene& S, const PathBuffers& B, int cur, WaveCount
 // grad (kNNWeights floats) receives dL/dW; loss[0] accumulates the batch
 // loss and the word at loss + 2 collects status bits (kStatusTensorTimeout);
 // apply: also take one Adam step (step counts from 1).
-void launch_nn_train_step(const NNWeights& W, const NNNorm& N, const float4* rec, int n, float tsum,
+// tsum: device pointer to the batch's sum of targets T.
+void launch_nn_train_step(const NNWeights& W, const NNNorm& N, const float4* rec, int n, const float* tsum,
                           const NNTrainBuf& TB, float* grad, float* loss, const NNAdam& opt, int step, int num_sms,
                           cudaStream_t st, bool apply);
 

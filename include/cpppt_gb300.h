@@ -259,8 +259,10 @@ pt_status pt_nn_stats(pt_scene* scene, double* steps, double* last_loss, double*
  * (equal values fix c).  batch: training records per Adam step, in
  * [1024, 262144].  divergence: PT_NN_KL weighs each record by its target
  * T (Kullback-Leibler), PT_NN_CHI2 by T^2 (Pearson chi-square: the variance
- * of the estimator; it favours the rare bright directions).
- * Defaults: 1e-3, 0.1, 0.9, 262144, PT_NN_KL. */
+ * of the estimator; it favours the rare bright directions).  Records are
+ * collected for up to steps_per_round batches between the host's checks of
+ * the wavefront (every 16 iterations); each full batch is one Adam step.
+ * Defaults: 3e-3, 0.1, 0.9, 262144, PT_NN_CHI2, 8. */
 #define PT_NN_KL 0
 #define PT_NN_CHI2 1
 typedef struct pt_nn_config {
@@ -269,6 +271,7 @@ typedef struct pt_nn_config {
     float bsdf_frac_max;
     int32_t batch;
     int32_t divergence;
+    int32_t steps_per_round; /* Adam steps at most per wavefront round (16 iterations), 1..16 */
 } pt_nn_config;
 pt_status pt_nn_configure(pt_scene* scene, const pt_nn_config* config);
 pt_status pt_nn_config_get(pt_scene* scene, pt_nn_config* config);
