@@ -13,7 +13,7 @@ scored by relMSE = mean over pixels and channels of (x - ref)^2 / (ref^2 +
 * plain  -- PT + NEE + MIS, BSDF sampling only (PT_FLAG_UNBIASED_MIS);
 * nn     -- PT + NEE + MIS with the learned vMF-mixture guide, trained
             online from fresh weights inside the time budget (training time
-            counts);
+            counts; optionally frozen after a given number of seconds);
 * sdtree -- the reference's practical path guiding (PPG: SD-tree, no NEE),
             one render whose spp is sized to the budget.
 
@@ -36,16 +36,17 @@ import numpy as np
 import torch
 
 from . import scenes
-from .lib import FLAG_NN_FREEZE, FLAG_UNBIASED_MIS, MODE_MIS, MODE_NN, MODE_SDTREE, GpuScene
+from .lib import FLAG_NN_FREEZE, FLAG_THROUGHPUT_RR, FLAG_UNBIASED_MIS, MODE_MIS, MODE_NN, MODE_SDTREE, GpuScene
 
 
 def rel_mse(x: torch.Tensor, ref: torch.Tensor) -> float:
     return float(((x - ref) ** 2 / (ref ** 2 + 1e-2)).mean())
 
 
-def progressive(gs, mode, flags, budget_s, chunk_spp, depth, seed0, ref, checkpoints):
+def progressive(gs, mode, flags, budget_s, chunk_spp, depth, seed0, ref, checkpoints, freeze_after=None):
     """Renders chunks until the budget is spent, accumulating on the GPU;
-    returns [(seconds, spp, relMSE)] at the checkpoints and the final image."""
+    returns [(seconds, spp, relMSE)] at the checkpoints and the final image.
+    freeze_after: seconds after which the learned guide stops training."""
     H, W = ref.shape[:2]
     img = torch.zeros((H, W, 3), dtype=torch.float32, device="cuda")
     acc = torch.zeros((H, W, 3), dtype=torch.float64, device="cuda")
@@ -55,7 +56,10 @@ def progressive(gs, mode, flags, budget_s, chunk_spp, depth, seed0, ref, checkpo
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     while True:
-        gs.render_device(img.data_ptr(), chunk_spp, max_depth=depth, seed=seed0 + k, mode=mode, flags=flags)
+        f = flags
+        if freeze_after is not None and time.perf_counter() - t0 >= freeze_after:
+            f |= FLAG_NN_FREEZE
+        gs.render_device(img.data_ptr(), chunk_spp, max_depth=depth, seed=seed0 + k, mode=mode, flags=f)
         acc += img.double() * chunk_spp
         k += 1
         spp_total += chunk_spp
@@ -93,8 +97,12 @@ def main():
     ap.add_argument("--depth", type=int, default=12)
     ap.add_argument("--chunk", type=int, default=8)
     ap.add_argument("--nn-config", action="append", default=None,
-                    help="JSON settings for GpuScene.nn_configure; repeat to compare several learned guides")
+                    help="JSON settings for GpuScene.nn_configure, optionally with \"freeze_after\": seconds "
+                         "after which training stops, \"seed\" (weights and render seeds) and \"throughput_rr\"; "
+                         "repeat to compare several learned guides")
     ap.add_argument("--no-sdtree", action="store_true")
+    ap.add_argument("--plain-trr", action="store_true",
+                    help="also run plain PT with Russian roulette on the throughput (method plain_trr)")
     ap.add_argument("--save", default="")
     a = ap.parse_args()
     sc = scenes.slit_room(seed=4, n_boxes=a.boxes, box_subdiv=4, width=a.width, height=a.height)
@@ -129,15 +137,24 @@ def main():
     results = {}
     res_plain, img_plain, _ = progressive(gs, MODE_MIS, FLAG_UNBIASED_MIS, B, a.chunk, a.depth, 10_000, ref, cps)
     results["plain"] = res_plain
+    if a.plain_trr:
+        results["plain_trr"], _, _ = progressive(gs, MODE_MIS, FLAG_UNBIASED_MIS | FLAG_THROUGHPUT_RR, B, a.chunk,
+                                                 a.depth, 10_000, ref, cps)
     nn_runs = {}
     defaults = gs.nn_config()
     for q, text in enumerate(a.nn_config or ["{}"]):
-        gs.nn_reset(2024)
-        cfg = gs.nn_configure(**{**defaults, **json.loads(text)})
-        rows, img_nn, _ = progressive(gs, MODE_NN, 0, B, a.chunk, a.depth, 20_000, ref, cps)
+        opts = json.loads(text)
+        freeze = opts.pop("freeze_after", None)
+        seed = int(opts.pop("seed", 0))
+        flags = FLAG_THROUGHPUT_RR if opts.pop("throughput_rr", False) else 0
+        gs.nn_reset(2024 + seed)
+        cfg = gs.nn_configure(**{**defaults, **opts})
+        rows, img_nn, _ = progressive(gs, MODE_NN, flags, B, a.chunk, a.depth, 20_000 + 100_000 * seed, ref, cps,
+                                      freeze)
         name = "nn" if q == 0 else f"nn{q}"
         results[name] = rows
-        nn_runs[name] = {"config": cfg, "training": gs.nn_stats()}
+        nn_runs[name] = {"config": cfg, "freeze_after": freeze, "seed": seed, "throughput_rr": flags != 0,
+                         "training": gs.nn_stats()}
     if not a.no_sdtree:
         # SD-tree (PPG): one render per budget; passes of 1, 2, 4, ... spp cost ~2x the last pass
         t0 = time.perf_counter()

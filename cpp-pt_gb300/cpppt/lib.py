@@ -16,8 +16,8 @@ LIB_PATH = os.path.join(os.path.dirname(HERE), "lib", "libcpppt_gb300.so")
 PT_OK = 0
 STATUS_NAMES = {0: "PT_OK", 1: "PT_ERR_INVALID", 2: "PT_ERR_CUDA", 3: "PT_ERR_MEMORY", 4: "PT_ERR_LIMIT",
                 5: "PT_ERR_IO", 6: "PT_ERR_NO_DEVICE"}
-MODE_MIS, MODE_SDTREE, MODE_NN = 0, 1, 2
-FLAG_TIME_KERNELS, FLAG_COUNT, FLAG_UNBIASED_MIS, FLAG_NN_FREEZE = 1, 2, 4, 8
+MODE_MIS, MODE_SDTREE, MODE_NN, MODE_NEE, MODE_PT = 0, 1, 2, 3, 4
+FLAG_TIME_KERNELS, FLAG_COUNT, FLAG_UNBIASED_MIS, FLAG_NN_FREEZE, FLAG_THROUGHPUT_RR = 1, 2, 4, 8, 16
 NN_WEIGHTS = 15360
 NN_KL, NN_CHI2 = 0, 1
 
@@ -29,7 +29,7 @@ EXPORTS = ["pt_scene_create", "pt_scene_load", "pt_scene_destroy", "pt_scene_inf
            "pt_debug_sdtree_run", "pt_nn_get_weights", "pt_nn_set_weights", "pt_nn_reset", "pt_nn_stats",
            "pt_debug_nn_forward", "pt_debug_nn_grad", "pt_nn_configure", "pt_nn_config_get",
            "pt_batch_create", "pt_batch_destroy", "pt_batch_render", "pt_batch_render_device", "pt_batch_set_tuning",
-           "pt_batch_get_tuning", "pt_batch_stats", "pt_batch_autotune"]
+           "pt_batch_get_tuning", "pt_batch_stats", "pt_batch_autotune", "pt_set_mesh_cache"]
 
 
 class PtMaterial(C.Structure):
@@ -118,6 +118,8 @@ def load(path: str = LIB_PATH):
     lib.pt_debug_nn_grad.argtypes = [P, P, P, P, C.c_int32, P, P]
     lib.pt_nn_configure.argtypes = [P, P]
     lib.pt_nn_config_get.argtypes = [P, P]
+    lib.pt_set_mesh_cache.argtypes = [C.c_int32]
+    lib.pt_set_mesh_cache.restype = None
     lib.pt_batch_create.argtypes = [P, C.c_int32, C.POINTER(P)]
     lib.pt_batch_destroy.argtypes = [P]
     lib.pt_batch_destroy.restype = None
@@ -130,7 +132,7 @@ def load(path: str = LIB_PATH):
     lib.pt_debug_sdtree_run.argtypes = [P, P, C.c_int32, P, P, C.c_int32, P, P, P, P, C.c_int32, P, P, P]
     for name in EXPORTS:
         getattr(lib, name).restype = C.c_int32 if name not in ("pt_scene_destroy", "pt_last_error",
-                                                               "pt_batch_destroy") else \
+                                                               "pt_batch_destroy", "pt_set_mesh_cache") else \
             getattr(lib, name).restype
     _lib = lib
     return lib

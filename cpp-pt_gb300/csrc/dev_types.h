@@ -56,7 +56,15 @@ struct DevBatchJob {
     int32_t spp, spp_axis, max_depth, rr_start;
     uint32_t seed;
     int32_t tile_w, tile_h;  // pixel order of a pass: tiles of tile_w x tile_h (both divide the resolution)
+    int32_t integrator;      // kIntegratorMIS / kIntegratorNEE / kIntegratorPT
 };
+
+// The reference's three unidirectional estimators on one wavefront:
+// PathtracerMIS (NEE + MIS), Pathtracer (NEE at full weight, emitters only
+// after the camera or a delta bounce), PurePt (no NEE, every emitter hit).
+constexpr int32_t kIntegratorMIS = 0;
+constexpr int32_t kIntegratorNEE = 1;
+constexpr int32_t kIntegratorPT = 2;
 
 // Ray-batch status word bits (kernel-side bounded loops report here).
 constexpr uint32_t kStatusIterLimit = 1u;

@@ -35,6 +35,7 @@ struct RenderParams {
     int rr_start;
     uint32_t seed;
     int width, height;
+    uint32_t flags;      // PT_FLAG_* of the render (read by the learned-guide integrator)
 };
 
 // The stages of one wavefront iteration reading path buffer `cur` (writing

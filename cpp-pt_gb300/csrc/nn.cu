@@ -41,7 +41,6 @@ constexpr uint32_t kTcCols = 64;                 // tensor-memory columns per CT
 constexpr uint32_t kTcSBO = 8 * 128;             // K = 64: 8 core matrices per 8-row group
 constexpr int kTcWLayerBytes = 64 * 64 * 2;      // W_l^T slot (N x 64 bf16)
 constexpr int kTcABytes = kTcRows * 64 * 2;      // activation tile (128 x 64 bf16)
-constexpr int kTcSmem = kNNLayers * kTcWLayerBytes + kTcABytes + 64;
 
 // W_l^T (N = outputs rows x K = inputs) in the canonical K-major layout, from
 // the padded transposed copy wt[l][out][in].
@@ -117,26 +116,80 @@ __device__ __forceinline__ void tc_end(bool ok, uint32_t tmem, uint32_t bar, uin
     }
 }
 
-// get_in(i, NNIn&) -> bool valid; put(i, const float* prm41).  All threads of
-// the CTA (kTcRows of them) must call it.  status: kStatusTensorTimeout when a
-// completion wait runs out (the CTA then stops, frees its tensor memory and
-// returns).
+// Inference CTAs hold two groups of 128 threads that share one copy of the
+// weights: each group runs its own tiles with its own A tile, mbarrier and
+// 64 tensor-memory columns, synchronising on a named barrier of its own, so
+// one group's shared-memory traffic and epilogue overlap the other's MMAs.
+constexpr int kTcGroups = 2;
+constexpr int kTcInferThreads = kTcGroups * kTcRows;
+constexpr int kTcInferSmem = kNNLayers * kTcWLayerBytes + kTcGroups * kTcABytes + 64;
+
+__device__ __forceinline__ void group_sync(int id) {
+    asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory");
+}
+__device__ __forceinline__ bool group_and(int id, bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.and.pred q, %2, 128, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}\n"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(id)
+        : "memory");
+    return r != 0;
+}
+
+// tc_layer for one 128-thread group (named barrier `bar_id`, issuer = the
+// group's first thread).
+__device__ __forceinline__ bool tc_layer_group(int bar_id, uint32_t tmem, uint32_t a_addr, uint32_t b_addr, int N,
+                                               uint32_t bar, uint32_t& phase) {
+    fence_proxy_async_smem();
+    tc_fence_before_sync();
+    group_sync(bar_id);
+    tc_fence_after_sync();
+    if ((threadIdx.x & (kTcRows - 1)) == 0) {
+        const uint32_t idesc = umma_idesc_bf16_f32(kTcRows, N);
+#pragma unroll
+        for (int ks = 0; ks < 4; ks++)
+            umma_bf16(tmem, umma_desc(a_addr + ks * 2 * kUmmaLBO, kTcSBO), umma_desc(b_addr + ks * 2 * kUmmaLBO, kTcSBO),
+                      idesc, ks > 0 ? 1u : 0u);
+        umma_commit(bar);
+    }
+    const bool ok = group_and(bar_id, mbar_wait_bounded(bar, phase));
+    phase ^= 1u;
+    if (ok) tc_fence_after_sync();
+    return ok;
+}
+
+// get_in(i, NNIn&) -> bool valid; put(i, const float* prm41).  All
+// kTcInferThreads threads of the CTA must call it.  status:
+// kStatusTensorTimeout when a completion wait runs out (the group then
+// stops; the CTA frees its tensor memory and returns).
 template <class GetIn, class Put>
 __device__ __forceinline__ void tc_infer_loop(int n, unsigned char* smem, const NNWeights& W, float c_lo, float c_hi,
                                               uint32_t* status, GetIn get_in, Put put) {
-    unsigned char* s_w = smem;
-    unsigned char* s_a = smem + kNNLayers * kTcWLayerBytes;
-    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_a + kTcABytes);
-    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(s_bar + 1);
+    const int group = threadIdx.x / kTcRows;
+    const int row = threadIdx.x & (kTcRows - 1);  // tensor-memory lane of this thread's sample
     const int warp = threadIdx.x >> 5;
-    const int row = threadIdx.x;  // tensor-memory lane of this thread's sample
+    unsigned char* s_w = smem;
+    unsigned char* s_a = smem + kNNLayers * kTcWLayerBytes + group * kTcABytes;
+    uint64_t* s_bars = reinterpret_cast<uint64_t*>(smem + kNNLayers * kTcWLayerBytes + kTcGroups * kTcABytes);
+    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(s_bars + kTcGroups);
     tc_stage_weights(W, s_w);
-    const uint32_t tmem = tc_begin(s_bar, s_tmem);
-    const uint32_t t_row = tmem + ((uint32_t)(warp * 32) << 16);
-    const uint32_t bar = smem_u32(s_bar), a_addr = smem_u32(s_a), w_addr = smem_u32(s_w);
+    if (threadIdx.x < kTcGroups) mbar_init(smem_u32(s_bars + threadIdx.x), 1);
+    if (warp == 0) tmem_alloc(s_tmem, kTcGroups * kTcCols);
+    tc_fence_before_sync();
+    __syncthreads();
+    tc_fence_after_sync();
+    const uint32_t tmem = *s_tmem + (uint32_t)(group * kTcCols);
+    const uint32_t t_row = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+    const uint32_t bar = smem_u32(s_bars + group), a_addr = smem_u32(s_a), w_addr = smem_u32(s_w);
+    const int bar_id = 1 + group;
     uint32_t phase = 0;
     bool ok = true;
-    for (int base = blockIdx.x * kTcRows; base < n && ok; base += gridDim.x * kTcRows) {
+    for (int base = (blockIdx.x * kTcGroups + group) * kTcRows; base < n && ok;
+         base += gridDim.x * kTcGroups * kTcRows) {
         const int i = base + row;
         NNIn in;
         const bool valid = i < n && get_in(i, in);
@@ -146,7 +199,7 @@ __device__ __forceinline__ void tc_infer_loop(int n, unsigned char* smem, const 
         tc_store_row(s_a, row, v, false);
         for (int l = 0; l < kNNLayers; l++) {
             const int nout = nn_layer_out(l);
-            ok = tc_layer(tmem, a_addr, kTcSBO, w_addr + l * kTcWLayerBytes, kTcSBO, 64, nout, bar, phase);
+            ok = tc_layer_group(bar_id, tmem, a_addr, w_addr + l * kTcWLayerBytes, nout, bar, phase);
             if (!ok) break;
 #pragma unroll
             for (int c = 0; c < 64; c += 16)
@@ -159,11 +212,20 @@ __device__ __forceinline__ void tc_infer_loop(int n, unsigned char* smem, const 
             put(i, prm);
         }
     }
-    tc_end(ok, tmem, bar, phase, status);
+    if (!ok) {
+        if (row == 0) atomicOr(status, kStatusTensorTimeout);
+        mbar_wait_bounded(bar, phase ^ 1u);  // the MMAs of the timed-out phase, if they still finish
+    }
+    tc_fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after_sync();
+        tmem_dealloc(*s_tmem, kTcGroups * kTcCols);
+    }
 }
 
 
-__global__ void __launch_bounds__(kTcRows) k_nn_forward_debug(NNWeights W, NNNorm N, const float* __restrict__ in,
+__global__ void __launch_bounds__(kTcInferThreads, 3) k_nn_forward_debug(NNWeights W, NNNorm N, const float* __restrict__ in,
                                                               int n, float* __restrict__ out, uint32_t* status) {
     extern __shared__ __align__(1024) unsigned char smem[];
     tc_infer_loop(
@@ -181,7 +243,7 @@ __global__ void __launch_bounds__(kTcRows) k_nn_forward_debug(NNWeights W, NNNor
 }
 
 // Guide parameters for every live path's hit (run between extend and shade).
-__global__ void __launch_bounds__(kTcRows) k_nn_infer(DevScene S, PathBuffers B, int cur, WaveCounters* ctr,
+__global__ void __launch_bounds__(kTcInferThreads, 3) k_nn_infer(DevScene S, PathBuffers B, int cur, WaveCounters* ctr,
                                                       NNWeights W, NNNorm N, float4* __restrict__ params) {
     extern __shared__ __align__(1024) unsigned char smem[];
     const int n = ctr->n_cur;
@@ -494,7 +556,7 @@ __global__ void k_nn_pack(NNWeights W) {
     W.w[l * kWLayer + in * kWStride + out] = b;
 }
 
-size_t nn_smem_infer() { return (size_t)kTcSmem; }
+size_t nn_smem_infer() { return (size_t)kTcInferSmem; }
 size_t nn_smem_train() { return (size_t)kTcTrainSmem; }
 size_t nn_wcopy_elems() { return (size_t)kNNLayers * kWLayer; }
 
@@ -512,12 +574,13 @@ void launch_nn_pack(const NNWeights& W, cudaStream_t st) {
 }
 void launch_nn_forward_debug(const NNWeights& W, const NNNorm& N, const float* in, int n, float* out,
                              uint32_t* status, int num_sms, cudaStream_t st) {
-    const int blocks = std::max(1, std::min(num_sms * 4, (n + kTcRows - 1) / kTcRows));
-    k_nn_forward_debug<<<blocks, kTcRows, nn_smem_infer(), st>>>(W, N, in, n, out, status);
+    const int blocks = std::max(1, std::min(num_sms * 3, (n + kTcInferThreads - 1) / kTcInferThreads));
+    k_nn_forward_debug<<<blocks, kTcInferThreads, nn_smem_infer(), st>>>(W, N, in, n, out, status);
 }
 void launch_nn_infer(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, const NNWeights& W,
                      const NNNorm& N, float4* params, int num_sms, cudaStream_t st) {
-    k_nn_infer<<<num_sms * 4, kTcRows, nn_smem_infer(), st>>>(S, B, cur, ctr, W, N, params);
+    // three CTAs (six 128-sample groups) per SM fit in shared memory
+    k_nn_infer<<<num_sms * 3, kTcInferThreads, nn_smem_infer(), st>>>(S, B, cur, ctr, W, N, params);
 }
 void launch_nn_train_step(const NNWeights& W, const NNNorm& N, const float4* rec, int n, const float* tsum,
                           const NNTrainBuf& TB, float* grad, float* loss, const NNAdam& opt, int step, int num_sms,
@@ -697,7 +760,12 @@ __global__ void __launch_bounds__(256) k_shade_nn(DevScene S, PathBuffers B, int
                     bool alive = true;
                     float surv = 1.0f;
                     if (bounce >= P.rr_start) {  // survival min(rr, 1): unbiased
-                        surv = fminf(russian_roulette(f), 1.0f);
+                        if (P.flags & PT_FLAG_THROUGHPUT_RR_) {
+                            const f3 mn = mul * f * (1.0f / pmix);
+                            surv = fminf(1.0f, fmaxf(fmaxf(mn.x, mn.y), mn.z));
+                        } else {
+                            surv = fminf(russian_roulette(f), 1.0f);
+                        }
                         if (r1.v[1] > surv) alive = false;
                     }
                     if (alive && bounce + 1 < P.max_depth) {

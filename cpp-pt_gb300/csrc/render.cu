@@ -194,6 +194,7 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, PathBuffers B, int cu
         const int pixel = I.x, sample = I.y, bounce = I.z & 0xffff;
         const bool sdelta = (I.z >> 16) & 1;
         const DevBatchJob* J = jobs + I.w;
+        const int integrator = J->integrator;
         const uint32_t seed = J->seed;
         const int rr_start = J->rr_start, max_depth = J->max_depth;
         const size_t fpix = (size_t)(uint32_t)pixel + J->film_off;
@@ -210,7 +211,9 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, PathBuffers B, int cu
             const f3 wo = -rd;
             if (kind == PT_MAT_EMISSIVE_) {  // pathtracerMIS.h:43-67: emitters end the path
                 float w = 1.0f;
-                if (!sdelta) {
+                if (!sdelta && integrator == kIntegratorNEE) {
+                    w = 0.0f;  // pathtracer.h:41-46: NEE already counted this emitter
+                } else if (!sdelta && integrator == kIntegratorMIS) {
                     const int4 vi = __ldg(S.tri_vidx + prim);
                     const f3 a = f3of(__ldg(S.v_pos + vi.x)), b = f3of(__ldg(S.v_pos + vi.y)),
                              c = f3of(__ldg(S.v_pos + vi.z));
@@ -227,7 +230,7 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, PathBuffers B, int cu
                 const Rng4 r1 = rng4(seed, sample, pixel, bounce, 1);
                 const BSample bs = bsdf_sample(m, s, wo, r0.v[0], r0.v[1]);
                 p = bs.pdf;
-                if (!bs.delta && S.n_lights > 0) {  // NEE, pathtracerMIS.h:79-106
+                if (!bs.delta && S.n_lights > 0 && integrator != kIntegratorPT) {  // NEE, pathtracerMIS.h:79-106
                     const LSample ls = sample_light(S, s.p, r0.v[2], r0.v[3], r1.v[0]);
                     f3 sd = ls.pos - s.p;
                     const float len = length(sd);
@@ -236,7 +239,7 @@ __global__ void __launch_bounds__(256) k_shade(DevScene S, PathBuffers B, int cu
                         const float pb = bsdf_pdf(m, s, wo, sd);
                         const float cosl = fabsf(dot(ls.n, sd)) + kEps;
                         const float pn = ls.pdf * len * len / cosl;
-                        const float w = pn / (pb + pn);
+                        const float w = integrator == kIntegratorMIS ? pn / (pb + pn) : 1.0f;
                         const f3 f = bsdf_eval(m, s, wo, sd);
                         const f3 c = mul * f * ls.le * (1.0f / (ls.pdf * len * len)) * w;
                         if (c.x != 0.f || c.y != 0.f || c.z != 0.f) {
@@ -403,6 +406,7 @@ DevBatchJob single_job(const DevScene& S, const RenderParams& P) {
     j.seed = P.seed;
     j.tile_w = 1;
     j.tile_h = 1;
+    j.integrator = kIntegratorMIS;
     return j;
 }
 void launch_film_resolve(const unsigned long long* film, float* out, int n, double scale, cudaStream_t st) {

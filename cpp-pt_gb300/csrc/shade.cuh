@@ -11,6 +11,7 @@ namespace cpppt_gb300 {
 #define PT_MAT_GGX_ 1
 #define PT_MAT_DIELECTRIC_ 2
 #define PT_MAT_EMISSIVE_ 3
+#define PT_FLAG_THROUGHPUT_RR_ 16u  // PT_FLAG_THROUGHPUT_RR of the C ABI
 
 constexpr float kPi = 3.14159265358979323846f;
 constexpr float kInvPi = 0.318309886183790671538f;

@@ -99,6 +99,8 @@ typedef struct {
 #define PT_MODE_MIS 0       /* PathtracerMIS, reference estimator (default) */
 #define PT_MODE_SDTREE 1    /* SD-tree guided (practical path guiding) */
 #define PT_MODE_NN 2        /* learned (MLP, vMF mixture) guiding */
+#define PT_MODE_NEE 3       /* Pathtracer: NEE without MIS (pathtracer.h:27-102) */
+#define PT_MODE_PT 4        /* PurePt: BSDF sampling only, no NEE (pure_pt.h:28-71) */
 
 typedef struct {
     int32_t spp;        /* samples per pixel (the reference settings value `spp N` means N*N) */
@@ -135,6 +137,10 @@ typedef struct {
                                   also uses (the default keeps the reference's RR-scaled weights,
                                   pathtracerMIS.h:118-124, and its MIS weight at the last vertex) */
 #define PT_FLAG_NN_FREEZE 8    /* PT_MODE_NN: use the current network without training it */
+#define PT_FLAG_THROUGHPUT_RR 16 /* PT_MODE_NN or PT_FLAG_UNBIASED_MIS: Russian roulette on the path
+                                    throughput (survival min(1, max component of the throughput after
+                                    the bounce); survivors are not boosted above 1) instead of the
+                                    reference's survival on the BSDF value (pathtracerMIS.h:118-124) */
 
 /* Replaces: Loader::load_scene + BVH::add/build (loader.h:314-374,
  * bvh.h:205-216) for a scene given as flat arrays.  Builds the
@@ -239,6 +245,14 @@ pt_status pt_batch_stats(pt_batch* batch, pt_render_stats* stats);
 pt_status pt_batch_autotune(pt_batch* batch, const pt_batch_job* jobs, int32_t n_jobs, int32_t spp_divisor,
                             pt_batch_tuning* best, double* best_mpaths);
 
+/* pt_scene_load caches each parsed .ptobj mesh next to it as <file>.gbbin
+ * (positions, normals, tangents, faces; keyed by the source's size and
+ * modification time) and reads the cache instead of the text when it is
+ * current.  Enabled by default; 0 turns reading and writing the cache off
+ * for later loads in this process.  Replaces nothing in the reference (its
+ * text parser, loader.h:209-251, has no cache). */
+void pt_set_mesh_cache(int32_t enabled);
+
 /* Writes <prefix>.png (sRGB, 8-bit, clipped as pixel_ops::put2char1) and
  * <prefix>.hdr (Radiance RGBE), as Image::save (rgb_image.h:300-318). */
 pt_status pt_image_save(const char* prefix, const float* rgb, int32_t width, int32_t height);
@@ -262,7 +276,9 @@ pt_status pt_nn_stats(pt_scene* scene, double* steps, double* last_loss, double*
  * of the estimator; it favours the rare bright directions).  Records are
  * collected for up to steps_per_round batches between the host's checks of
  * the wavefront (every 16 iterations); each full batch is one Adam step.
- * Defaults: 3e-3, 0.1, 0.9, 262144, PT_NN_CHI2, 8. */
+ * Defaults: 3e-3, 0.3, 0.9, 262144, PT_NN_CHI2, 16 (a BSDF fraction of at least
+ * 0.3 bounds the growth of a path's throughput through poorly guided
+ * bounces, the main source of rare very bright samples). */
 #define PT_NN_KL 0
 #define PT_NN_CHI2 1
 typedef struct pt_nn_config {

@@ -36,6 +36,12 @@ if [ -d "$REF/src" ]; then
   sed -i 's/RandomSampler s(i);/RandomSampler s(i + cpppt_harness_seed_offset);/; s/if(i%50==0)/if(cpppt_harness_verbose \&\& i%50==0)/' "$S/renderer/pathtracerMIS.h"
   # (7) renderer/ppg.h: same two settings for the SD-tree guided comparison path
   sed -i 's/RandomSampler s(i);/RandomSampler s(i + cpppt_harness_seed_offset);/' "$S/renderer/ppg.h" || true
+  # (8) renderer/pure_pt.h, renderer/pathtracer.h: the bounce limit, seed offset and quiet progress
+  #     of (5)-(6) for the pure-PT and PT+NEE integrators
+  for f in pure_pt.h pathtracer.h; do
+    sed -i 's/for(int i = 0; i<32; i++){/for(int i = 0; i<cpppt_harness_max_depth; i++){/; s/RandomSampler s(i);/RandomSampler s(i + cpppt_harness_seed_offset);/; s/if(i%50==0)/if(cpppt_harness_verbose \&\& i%50==0)/' "$S/renderer/$f"
+    grep -q 'cpppt_harness_max_depth' "$S/renderer/$f"
+  done
   grep -q 'cpppt_harness_max_depth' "$S/renderer/pathtracerMIS.h"
   grep -q 'unique_ptr<Primitive>&& right' "$S/primitive/bvh.h"
 fi

@@ -88,10 +88,13 @@ class Oracle:
             if kind == "port":
                 lib.or_render_mis.argtypes = [_P, C.c_int, C.c_int, C.c_int, _FP]
                 lib.or_render_mis_cols.argtypes = [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _FP]
+                lib.or_render_variant.argtypes = [_P, C.c_int, C.c_int, C.c_int, C.c_int, _FP]
                 lib.or_bsdf_eval.argtypes = [C.c_int, _FP, _FP, _FP, _FP, _FP, _FP, _FP, _IP]
             else:
                 lib.ref_render_mis.restype = C.c_double
                 lib.ref_render_mis.argtypes = [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_char_p, _FP]
+                lib.ref_render_variant.restype = C.c_double
+                lib.ref_render_variant.argtypes = [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_char_p, _FP]
                 lib.ref_render_ppg.restype = C.c_double
                 lib.ref_render_ppg.argtypes = [_P, C.c_int, C.c_int, C.c_int, C.c_char_p, _FP]
                 lib.ref_scene_error.restype = C.c_char_p
@@ -191,6 +194,23 @@ class OracleScene:
             with tempfile.TemporaryDirectory() as d:
                 sec = self.o.lib.ref_render_mis(self.h, spp_axis, max_depth, seed_offset, threads,
                                                 os.path.join(d, "img").encode(), out)
+        return out.reshape(H, W, 3), sec
+
+    def render_variant(self, integrator: int, spp_axis: int, max_depth: int, seed_offset: int = 0,
+                       threads: int = 0):
+        """integrator 1: Pathtracer (PT + NEE, no MIS); 2: PurePt (no NEE).
+        Returns (image HxWx3 float32, seconds)."""
+        W, H = self.sc.width, self.sc.height
+        out = np.zeros(W * H * 3, np.float32)
+        if self.o.kind == "port":
+            import time
+            t0 = time.perf_counter()
+            self.o.lib.or_render_variant(self.h, integrator, spp_axis, max_depth, seed_offset, out)
+            sec = time.perf_counter() - t0
+        else:
+            with tempfile.TemporaryDirectory() as d:
+                sec = self.o.lib.ref_render_variant(self.h, integrator, spp_axis, max_depth, seed_offset, threads,
+                                                    os.path.join(d, "img").encode(), out)
         return out.reshape(H, W, 3), sec
 
     def render_ppg(self, spp_axis: int, seed_offset: int = 0, threads: int = 0):

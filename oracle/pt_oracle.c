@@ -682,7 +682,12 @@ static ray_t camera_ray(const or_scene* s, float cx, float cy) { /* camera_persp
 }
 
 /* PathtracerMIS::integrate, pathtracerMIS.h:29-131 */
-static v3 integrate_mis(const or_scene* s, float cx, float cy, mt19937* g, int max_depth) {
+/* integrator 0: PathtracerMIS::integrate (pathtracerMIS.h:29-131);
+ * 1: Pathtracer::integrate, NEE without MIS (pathtracer.h:27-102): emitters
+ *    count only after the camera or a delta bounce, NEE at full weight;
+ * 2: PurePt::integrate (pure_pt.h:28-71): no NEE, every emitter hit counts.
+ * The random numbers are drawn in the same order as each reference method. */
+static v3 integrate(const or_scene* s, float cx, float cy, mt19937* g, int max_depth, int integrator) {
     ray_t ray = camera_ray(s, cx, cy);
     v3 col = V(0, 0, 0), mul = V(1, 1, 1);
     int sampled_delta = 1;
@@ -697,9 +702,9 @@ static v3 integrate_mis(const or_scene* s, float cx, float cy, mt19937* g, int m
         bsdf_t b = make_bsdf(s, prim);
         v3 wo = vneg(ray.d);
         if (b.kind == MAT_EMISSIVE) {
-            if (sampled_delta) {
+            if (sampled_delta || integrator == 2) {
                 col = vadd(col, vmul(mul, b.col));
-            } else {
+            } else if (integrator == 0) {
                 float r = ray.max_t;
                 float cos_theta = (float)((double)fabsf(vdot(it.normal, ray.d)) + OR_EPS);
                 float p_nee = light_pdf(s, prim) * r * r / cos_theta;
@@ -712,7 +717,9 @@ static v3 integrate_mis(const or_scene* s, float cx, float cy, mt19937* g, int m
         dsample smp = bsdf_sample(&b, g, wo, &it);
         v3 wi = smp.wi;
         p = smp.pdf;
-        if (!smp.delta) {
+        if (integrator == 2) {
+            /* pure PT: no light sample */
+        } else if (!smp.delta) {
             light_sample ls = light_connect(s, g, &it);
             v3 sd = vsub(ls.position, it.hit);
             float len = vlen(sd);
@@ -724,12 +731,16 @@ static v3 integrate_mis(const or_scene* s, float cx, float cy, mt19937* g, int m
             if (same_hemisphere(&it, wo, sh.d)) {
                 if (!any_hit(s, &sh)) {
                     float r = len;
-                    float p_bsdf = bsdf_pdf(&b, wo, sd, &it);
-                    float cos_l = (float)((double)fabsf(vdot(ls.normal, sd)) + OR_EPS);
-                    float p_nee = ls.pdf * r * r / cos_l;
-                    float w = p_nee / (p_bsdf + p_nee);
                     v3 ev = bsdf_eval(&b, wo, sh.d, &it);
-                    col = vadd(col, vscale(vdivs(vmul(vmul(mul, ev), ls.intensity), ls.pdf * r * r), w));
+                    v3 c = vdivs(vmul(vmul(mul, ev), ls.intensity), ls.pdf * r * r);
+                    if (integrator == 0) {
+                        float p_bsdf = bsdf_pdf(&b, wo, sd, &it);
+                        float cos_l = (float)((double)fabsf(vdot(ls.normal, sd)) + OR_EPS);
+                        float p_nee = ls.pdf * r * r / cos_l;
+                        float w = p_nee / (p_bsdf + p_nee);
+                        c = vscale(c, w);
+                    }
+                    col = vadd(col, c);
                 }
             }
         } else {
@@ -848,7 +859,7 @@ void or_trace_any(void* h, const float* rays, int n, unsigned char* out_hit) {
 /* PathtracerMIS::render (pathtracerMIS.h:135-167): column i uses
  * RandomSampler(i + seed_offset); spp_axis^2 stratified samples per pixel.
  * When x0/x1 restrict the columns, only those columns are written. */
-void or_render_mis_cols(void* h, int spp_axis, int max_depth, int seed_offset, int x0, int x1,
+static void render_cols(void* h, int spp_axis, int max_depth, int seed_offset, int x0, int x1, int integrator,
                         float* rgb_out) {
     const or_scene* s = h;
     int W = s->width, H = s->height;
@@ -863,7 +874,7 @@ void or_render_mis_cols(void* h, int spp_axis, int max_depth, int seed_offset, i
                     float r1 = mt_float(&g), r2 = mt_float(&g);
                     float cx = (float)((double)(((float)i + (float)((float)k + r1) / (float)spp_axis) / (float)W) * 2.0 - 1.0);
                     float cy = (float)-((double)(((float)j + (float)((float)l + r2) / (float)spp_axis) / (float)H) * 2.0 - 1.0);
-                    acc = vadd(acc, integrate_mis(s, cx, cy, &g, max_depth));
+                    acc = vadd(acc, integrate(s, cx, cy, &g, max_depth, integrator));
                 }
             acc = vdivs(acc, (float)(spp_axis * spp_axis));
             float* o = rgb_out + 3 * (i + j * W);
@@ -872,8 +883,19 @@ void or_render_mis_cols(void* h, int spp_axis, int max_depth, int seed_offset, i
     }
 }
 
+void or_render_mis_cols(void* h, int spp_axis, int max_depth, int seed_offset, int x0, int x1,
+                        float* rgb_out) {
+    render_cols(h, spp_axis, max_depth, seed_offset, x0, x1, 0, rgb_out);
+}
+
 void or_render_mis(void* h, int spp_axis, int max_depth, int seed_offset, float* rgb_out) {
-    or_render_mis_cols(h, spp_axis, max_depth, seed_offset, 0, ((or_scene*)h)->width, rgb_out);
+    render_cols(h, spp_axis, max_depth, seed_offset, 0, ((or_scene*)h)->width, 0, rgb_out);
+}
+
+/* Pathtracer::render (integrator 1) / PurePt::render (integrator 2): the
+ * same column seeding and stratification as PathtracerMIS::render. */
+void or_render_variant(void* h, int integrator, int spp_axis, int max_depth, int seed_offset, float* rgb_out) {
+    render_cols(h, spp_axis, max_depth, seed_offset, 0, ((or_scene*)h)->width, integrator, rgb_out);
 }
 
 /* ---- single-vertex BSDF / light primitives for kernel unit tests ----- */

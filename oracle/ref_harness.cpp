@@ -48,6 +48,8 @@ int cpppt_harness_verbose = 0;
 #include <camera/camera_perspective.h>
 #include <light/point_light.h>
 #include <renderer/pathtracerMIS.h>
+#include <renderer/pathtracer.h>
+#include <renderer/pure_pt.h>
 // SDTree's tree sits in the default-private part of a `class`; read it as a
 // struct (its dependencies are already included above).
 #define class struct
@@ -116,6 +118,29 @@ std::shared_ptr<Texture> ctex1(float v) {
 }
 
 }  // namespace
+
+template <class R>
+static double render_with(RefScene* rs, int spp_axis, const char* out_prefix, float* rgb_out) {
+    RenderSettings settings = rs->rs;
+    settings.spp = spp_axis;
+    R renderer(settings);
+    double seconds;
+    {
+        Quiet q;
+        auto t1 = std::chrono::high_resolution_clock::now();
+        renderer.render(rs->scene, out_prefix);
+        auto t2 = std::chrono::high_resolution_clock::now();
+        seconds = std::chrono::duration<double>(t2 - t1).count();
+    }
+    RgbImage& img = rs->scene.camera->get_image();
+    for (int j = 0; j < img.res.y; j++)
+        for (int i = 0; i < img.res.x; i++) {
+            Vec3 p = *img.get_pixel(i, j);
+            float* o = rgb_out + 3 * (i + j * img.res.x);
+            o[0] = p.x; o[1] = p.y; o[2] = p.z;
+        }
+    return seconds;
+}
 
 extern "C" {
 
@@ -331,6 +356,20 @@ double ref_render_mis(void* h, int spp_axis, int max_depth, int seed_offset, int
             o[0] = p.x; o[1] = p.y; o[2] = p.z;
         }
     return seconds;
+}
+
+// The reference's other two integrators on the same scene: which = 1
+// Pathtracer (PT + NEE without MIS, pathtracer.h:27-102), which = 2 PurePt
+// (no NEE, pure_pt.h:28-71).  Same settings as ref_render_mis.
+double ref_render_variant(void* h, int which, int spp_axis, int max_depth, int seed_offset, int threads,
+                          const char* out_prefix, float* rgb_out) {
+    auto* rs = static_cast<RefScene*>(h);
+    cpppt_harness_max_depth = max_depth;
+    cpppt_harness_seed_offset = seed_offset;
+    if (threads > 0) omp_set_num_threads(threads);
+    if (which == 1) return render_with<Pathtracer>(rs, spp_axis, out_prefix, rgb_out);
+    if (which == 2) return render_with<PurePt>(rs, spp_axis, out_prefix, rgb_out);
+    return render_with<PathtracerMIS>(rs, spp_axis, out_prefix, rgb_out);
 }
 
 // PPG::render (SD-tree guided, no NEE; ppg.h:149-215).  The bounce limit of

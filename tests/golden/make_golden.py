@@ -8,7 +8,8 @@ oracle/build_ref.sh):
     python tests/golden/make_golden.py --c1-16k   # 16k-spp Cornell reference (~15 min on 8 cores)
 
 Every array stored here is an output of the reference's own code
-(BVH::build, BVH::intersect / intersect_any, PathtracerMIS::render) on the
+(BVH::build, BVH::intersect / intersect_any, PathtracerMIS::render,
+Pathtracer::render, PurePt::render) on the
 seeded scenes of cpppt.scenes.  Inputs (rays) are stored next to the outputs
 so the fixtures do not depend on numpy's random streams.
 """
@@ -51,11 +52,15 @@ def small():
         occ = rs.trace_any(sh)
         img, _ = rs.render_mis(2, 8, 0, threads=1)
         img32, _ = rs.render_mis(1, 32, 7, threads=1)
+        # the reference's other two integrators (Pathtracer: NEE without MIS; PurePt)
+        nee, _ = rs.render_variant(1, 2, 8, 3, threads=1)
+        pure, _ = rs.render_variant(2, 2, 8, 3, threads=1)
         np.savez_compressed(
             os.path.join(HERE, f"{name}_ref.npz"),
             leaf_order=order, node_boxes=boxes, node_parent=parent, prim_parent=pparent,
             rays=rays, hit_index=idx, hit_t=t, shadow_rays=sh, occluded=occ,
-            render_spp2_d8=img, render_spp1_d32_seed7=img32)
+            render_spp2_d8=img, render_spp1_d32_seed7=img32,
+            render_nee_spp2_d8_seed3=nee, render_pure_spp2_d8_seed3=pure)
         print(name, sc.n_triangles, "tris;", (idx >= 0).mean(), "hit rate")
 
 

@@ -95,26 +95,26 @@ def test_guided_render_converges_to_plain(gpu_lib):
 
 def test_trained_guide_lowers_variance(gpu_lib):
     """What the trained network gains over the method without it: on the
-    occluded-light room (light through a slit), after online training the
-    frozen guide's per-sample variance at depth 3 (direct light and the
-    first two bounces of indirect light) is clearly below plain PT's, with
-    the same estimator otherwise (PT_FLAG_UNBIASED_MIS)."""
+    occluded-light room (1000 boxes, light through a slit, 640x360), after
+    online training the frozen guide's per-sample variance at depth 3
+    (direct light and two bounces of indirect light) is clearly below plain
+    PT's, with the same estimator otherwise (PT_FLAG_UNBIASED_MIS)."""
     from cpppt import scenes
     from cpppt.lib import FLAG_NN_FREEZE, FLAG_UNBIASED_MIS, MODE_MIS, MODE_NN, GpuScene
-    sc = scenes.slit_room(seed=4, n_boxes=200, box_subdiv=2, width=160, height=96)
+    sc = scenes.slit_room(seed=4, n_boxes=1000, box_subdiv=4, width=640, height=360)
     gs = GpuScene(sc)
     gs.nn_reset(11)
-    gs.nn_configure(batch=1 << 16)
-    for k in range(40):
-        gs.render(64, max_depth=12, seed=3000 + k, mode=MODE_NN)
-    assert gs.nn_stats()["steps"] >= 100
+    gs.nn_configure(bsdf_frac_min=0.1)
+    for k in range(200):
+        gs.render(4, max_depth=12, seed=3000 + k, mode=MODE_NN)
+    assert gs.nn_stats()["steps"] >= 200
 
-    def rel_var(mode, flags, seed0, R=16, S=16):
+    def rel_var(mode, flags, seed0, R=8, S=16):
         x = np.stack([gs.render(S, max_depth=3, seed=seed0 + r, mode=mode, flags=flags) for r in range(R)])
         m = x.mean(0)
         return float(np.mean(x.var(0, ddof=1) * S / (m ** 2 + 1e-2))), float(m.mean())
 
     v_plain, m_plain = rel_var(MODE_MIS, FLAG_UNBIASED_MIS, 100)
     v_nn, m_nn = rel_var(MODE_NN, FLAG_NN_FREEZE, 200)
-    assert abs(m_nn - m_plain) < 0.05 * m_plain  # same image
+    assert abs(m_nn - m_plain) < 0.03 * m_plain, (m_nn, m_plain)  # same image
     assert v_nn < 0.85 * v_plain, (v_nn, v_plain)

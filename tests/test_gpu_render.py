@@ -78,6 +78,30 @@ def test_small_scenes_match_oracle(gpu_lib, name):
     assert rel_mse(g_imgs.mean(0), o_imgs.mean(0)) < 0.05
 
 
+@pytest.mark.parametrize("name,integrator", [(n, i) for n in sorted(SMALL_SCENES) for i in (1, 2)
+                                              if not (n == "slitroom" and i == 2)])
+def test_other_integrators_match_oracle(gpu_lib, name, integrator):
+    """PT_MODE_NEE (Pathtracer: NEE without MIS) and PT_MODE_PT (PurePt) on
+    the same wavefront against the oracle port of the reference's own
+    integrators (pinned bit-exact by test_oracle_pins).  Pure PT on the slit
+    room is left out: without NEE, the light behind the slit is reached too
+    rarely for a per-tile test at this size."""
+    from cpppt.lib import MODE_NEE, MODE_PT, GpuScene
+    from oracle.oracle import Oracle
+    sc = SMALL_SCENES[name]()
+    R, tile = 8, 8
+    sc = sc.with_resolution(32, 32) if name == "cornell" else sc.with_resolution(32, 16)
+    ors = Oracle("port").scene(sc)
+    o_imgs = np.stack([ors.render_variant(integrator, 16, 10, 5000 * (r + 1))[0] for r in range(R)])
+    gs = GpuScene(sc)
+    mode = MODE_NEE if integrator == 1 else MODE_PT
+    g_imgs = np.stack([gs.render(1024, max_depth=10, seed=300 + r, mode=mode) for r in range(R)])
+    # 48 z values per scene: at most two beyond 3 sigma (these estimators have
+    # heavier tails than the MIS one, so replica variances are rougher)
+    check_z(ztest(tile_means(g_imgs, tile), tile_means(o_imgs, tile)), frac3=0.045)
+    assert rel_mse(g_imgs.mean(0), o_imgs.mean(0)) < 0.05
+
+
 def test_render_is_deterministic_and_seeded(gpu_lib):
     from cpppt.lib import GpuScene
     gs = GpuScene(scenes.cornell(32, 32))

@@ -72,3 +72,58 @@ def test_cli_renders_files(gpu_lib, tmp_path):
     assert png.exists() and hdr.exists()
     assert png.read_bytes()[:8] == b"\x89PNG\r\n\x1a\n"
     assert hdr.read_bytes().startswith(b"#?RADIANCE")
+
+
+def _read_cache(path):
+    raw = open(path, "rb").read()
+    assert raw[:8] == b"GBPTOBJ1"
+    nv, nf = np.frombuffer(raw[24:32], np.int32)
+    f32 = np.frombuffer(raw[32:32 + 36 * nv], np.float32).reshape(3, nv, 3)
+    faces = np.frombuffer(raw[32 + 36 * nv:], np.int32).reshape(nf, 3)
+    return f32[0], f32[1], f32[2], faces
+
+
+def test_mesh_cache_holds_the_parsed_mesh(tmp_path):
+    """pt_scene_load writes <mesh>.ptobj.gbbin with the parsed arrays (the
+    scene is parsed before any device is touched, so this runs anywhere),
+    reads it back while current, and rewrites it when the mesh changes."""
+    import ctypes as C
+    import glob
+    from cpppt import lib
+    L = lib.load()
+    L.pt_set_mesh_cache(1)
+    settings = _write(tmp_path, "cornell")
+    objs = sorted(glob.glob(str(tmp_path / "cornell*" / "*.ptobj")) + glob.glob(str(tmp_path / "*.ptobj")))
+    assert objs
+
+    def load():
+        h = C.c_void_p()
+        rs = lib.PtRenderDesc()
+        st = L.pt_scene_load(settings.encode(), C.byref(h), C.byref(rs), None, 0)
+        assert st in (0, 2, 6), L.pt_last_error()  # 2 or 6: no usable sm_103 device; the files were read
+        if st == 0:
+            L.pt_scene_destroy(h)
+
+    load()
+    for o in objs:
+        assert os.path.exists(o + ".gbbin")
+        head = open(o).readline().split()
+        nv, nf = int(head[0]), int(head[1])
+        rows = [list(map(float, l.split())) for l in open(o).read().splitlines()[1:1 + nv]]
+        faces = [list(map(int, l.split())) for l in open(o).read().splitlines()[1 + nv:1 + nv + nf]]
+        v, n, t, f = _read_cache(o + ".gbbin")
+        assert np.array_equal(v, np.float32(np.array(rows)[:, 0:3]))
+        assert np.array_equal(n, np.float32(np.array(rows)[:, 5:8]))
+        assert np.array_equal(t, np.float32(np.array(rows)[:, 8:11]))
+        assert np.array_equal(f, np.array(faces, np.int32))
+    # a changed mesh invalidates its cache
+    o = objs[0]
+    text = open(o).read().splitlines()
+    vals = text[1].split()
+    vals[0] = repr(float(vals[0]) + 0.25)
+    text[1] = " ".join(vals)
+    open(o, "w").write("\n".join(text) + "\n")
+    os.utime(o, ns=(os.stat(o).st_atime_ns, os.stat(o).st_mtime_ns + 10 ** 9))
+    load()
+    v, _, _, _ = _read_cache(o + ".gbbin")
+    assert v[0, 0] == np.float32(float(vals[0]))

@@ -46,6 +46,17 @@ def test_render_bitwise(port, golden, name):
     assert np.array_equal(img32.view(np.uint32), g["render_spp1_d32_seed7"].view(np.uint32))
 
 
+@pytest.mark.parametrize("name", sorted(SMALL_SCENES))
+def test_other_integrators_bitwise(port, golden, name):
+    """Pathtracer (NEE without MIS) and PurePt (no NEE) of the reference."""
+    g = golden(f"{name}_ref.npz")
+    s = port.scene(SMALL_SCENES[name]())
+    nee, _ = s.render_variant(1, 2, 8, 3)
+    assert np.array_equal(nee.view(np.uint32), g["render_nee_spp2_d8_seed3"].view(np.uint32))
+    pure, _ = s.render_variant(2, 2, 8, 3)
+    assert np.array_equal(pure.view(np.uint32), g["render_pure_spp2_d8_seed3"].view(np.uint32))
+
+
 def test_reference_harness_matches_fixture(golden):
     """When the reference can be compiled here, it still gives the fixtures."""
     from oracle import oracle as orc
