@@ -185,6 +185,8 @@ void create_scene(const pt_scene_desc* d, pt_scene* s) {
     ck(cudaMallocHost(&s->h_ctr, sizeof(WaveCounters)), "cudaMallocHost");
     s->d_job = dalloc<DevBatchJob>(s->owned, 1);
     ck(cudaMallocHost(&s->h_job, sizeof(DevBatchJob)), "cudaMallocHost");
+    s->d_nnjob = dalloc<DevNNJob>(s->owned, 1);
+    ck(cudaMallocHost(&s->h_nnjob, sizeof(DevNNJob)), "cudaMallocHost");
     ck(cudaEventCreate(&s->ev0), "cudaEventCreate");
     ck(cudaEventCreate(&s->ev1), "cudaEventCreate");
     ck(cudaStreamSynchronize(s->stream), "scene upload");
@@ -485,10 +487,49 @@ NNPathData nn_path_buffers(pt_scene* s, int capacity, int depth) {
         s->nnpd.vert = dalloc<float4>(s->nnpd_owned, (size_t)cap * std::max(1, s->nnpd_depth) * kNNVertFloat4);
         s->nnpd.acc = dalloc<float4>(s->nnpd_owned, cap);
         s->nnpd.slot_stack = dalloc<int>(s->nnpd_owned, cap);
+        s->nnpd.slot_job = dalloc<int>(s->nnpd_owned, cap);
         s->nnpd.fin = dalloc<int4>(s->nnpd_owned, cap);
         s->nn_params = dalloc<float4>(s->nnpd_owned, (size_t)cap * 11);
     }
     return s->nnpd;
+}
+
+// One training round of a scene's guide: as many Adam steps as full batches
+// were recorded (each on its own records; `held` = records counted so far,
+// at most cap of them written); records beyond the last full batch move to
+// the front of the buffer and *d_count is set to their number, which is
+// returned.  Synchronises the stream (reads the step's loss and status).
+int nn_train_round(pt_scene* s, int held, int cap, int* d_count, cudaStream_t st, double* launches) {
+    const int batch = s->nn_cfg.batch;
+    held = std::min(held, cap);
+    const int steps = held / batch;
+    NNAdam opt;
+    opt.lr = s->nn_cfg.learning_rate;
+    const NNNorm N = scene_norm(s);
+    for (int k = 0; k < steps; k++) {
+        float4* r = s->nn_rec + (size_t)4 * k * batch;
+        ck(cudaMemsetAsync(s->nn_scalars, 0, sizeof(float) * 4, st), "memset");
+        if (s->nn_cfg.divergence == PT_NN_CHI2) launch_square_T(r, batch, st);
+        launch_sum_T(r, batch, s->nn_scalars + 1, st);
+        launch_nn_train_step(s->nnw, N, r, batch, s->nn_scalars + 1, s->nn_tb, s->nn_grad, s->nn_scalars, opt,
+                             ++s->nn_steps, s->num_sms, st, true);
+        if (launches) *launches += 5;
+    }
+    const int left = held - steps * batch;
+    if (left > 0 && steps > 0)
+        ck(cudaMemcpyAsync(s->nn_rec, s->nn_rec + (size_t)4 * steps * batch, sizeof(float4) * 4 * left,
+                           cudaMemcpyDeviceToDevice, st), "keep records");
+    *s->h_rec_left = left;
+    ck(cudaMemcpyAsync(d_count, s->h_rec_left, sizeof(int), cudaMemcpyHostToDevice, st), "records");
+    float sc[4] = {0.f, 0.f, 0.f, 0.f};
+    ck(cudaMemcpyAsync(sc, s->nn_scalars, sizeof(sc), cudaMemcpyDeviceToHost, st), "copy");
+    ck(cudaStreamSynchronize(st), "train");
+    uint32_t tstat;
+    std::memcpy(&tstat, &sc[2], sizeof(tstat));
+    check_status(s, tstat);
+    if (steps > 0) s->nn_last_loss = sc[0];
+    s->nn_records += (double)steps * batch;
+    return left;
 }
 
 // PT + NEE + MIS on the slot-based wavefront (nn.cu).  guided: the learned
@@ -516,9 +557,21 @@ void render_nn(pt_scene* s, const pt_render_desc* desc, float* d_dst, bool guide
     const int batch = s->nn_cfg.batch;
     const int rec_cap = std::min(kNNRecordCap, s->nn_cfg.steps_per_round * batch);
     PD.rec_cap = train ? rec_cap : 0;
-    PD.rec = train ? s->nn_rec : nullptr;
     float4* params = guided ? s->nn_params : nullptr;
     const NNNorm N = scene_norm(s);
+    // one-entry job tables (render parameters; the scene's network and records)
+    *s->h_job = single_job(s->dev, P);
+    DevNNJob& nj = *s->h_nnjob;
+    nj = DevNNJob{};
+    nj.wt = guided ? s->nnw.wt : nullptr;
+    for (int k = 0; k < 3; k++) { nj.lo[k] = N.lo[k]; nj.inv_ext[k] = N.inv_ext[k]; }
+    nj.c_lo = N.c_lo;
+    nj.c_hi = N.c_hi;
+    nj.rec = train ? s->nn_rec : nullptr;
+    nj.rec_cap = train ? rec_cap : 0;
+    nj.n_rec = &s->d_ctr->n_rec;
+    ck(cudaMemcpyAsync(s->d_job, s->h_job, sizeof(DevBatchJob), cudaMemcpyHostToDevice, st), "job table");
+    ck(cudaMemcpyAsync(s->d_nnjob, s->h_nnjob, sizeof(DevNNJob), cudaMemcpyHostToDevice, st), "guide job table");
     ck(cudaEventRecord(s->ev0, st), "event");
     ck(cudaMemsetAsync(s->film, 0, sizeof(unsigned long long) * film_n, st), "memset film");
     launch_init_slots(PD.slot_stack, capacity, st);
@@ -528,7 +581,7 @@ void render_nn(pt_scene* s, const pt_render_desc* desc, float* d_dst, bool guide
     init.n_rec = train ? s->nn_rec_count : 0;
     *s->h_ctr = init;
     ck(cudaMemcpyAsync(s->d_ctr, s->h_ctr, sizeof(WaveCounters), cudaMemcpyHostToDevice, st), "init counters");
-    launch_nn_generate(s->dev, s->pb, 1, P, s->d_ctr, PD, st);
+    launch_nn_generate(s->dev, s->pb, 1, s->d_ctr, PD, s->d_job, 1, st);
     double launches = 3;
     const unsigned long long max_rounds =
         64 + (total / (unsigned long long)capacity + 2) * (unsigned long long)(desc->max_depth + 2) * 4 / kItersPerGraph;
@@ -538,11 +591,11 @@ void render_nn(pt_scene* s, const pt_render_desc* desc, float* d_dst, bool guide
         for (int k = 0; k < kItersPerGraph; k++) {
             const int cur = k & 1;
             launch_extend(s->dev, s->pb, cur, s->d_ctr, s->num_sms, st);
-            if (guided) launch_nn_infer(s->dev, s->pb, cur, s->d_ctr, s->nnw, N, params, s->num_sms, st);
-            launch_nn_shade(s->dev, s->pb, cur, P, s->d_ctr, s->film, params, PD, guided, st);
-            launch_nn_shadow(s->dev, s->pb, s->d_ctr, s->film, PD, s->num_sms, st);
-            launch_nn_finish(PD, s->d_ctr, P.max_depth, capacity, st);
-            launch_nn_generate(s->dev, s->pb, cur, P, s->d_ctr, PD, st);
+            if (guided) launch_nn_infer(s->dev, s->pb, cur, s->d_ctr, s->d_nnjob, params, s->num_sms, st);
+            launch_nn_shade(s->dev, s->pb, cur, P, s->d_ctr, s->film, params, PD, guided, s->d_job, st);
+            launch_nn_shadow(s->dev, s->pb, s->d_ctr, s->film, PD, s->d_job, s->num_sms, st);
+            launch_nn_finish(PD, s->d_ctr, s->d_nnjob, P.max_depth, capacity, st);
+            launch_nn_generate(s->dev, s->pb, cur, s->d_ctr, PD, s->d_job, 1, st);
             launches += guided ? 7 : 6;
         }
         ck(cudaMemcpyAsync(s->h_ctr, s->d_ctr, sizeof(WaveCounters), cudaMemcpyDeviceToHost, st), "read counters");
@@ -550,37 +603,8 @@ void render_nn(pt_scene* s, const pt_render_desc* desc, float* d_dst, bool guide
         check_status(s, s->h_ctr->status);
         rec_left = -1;
         if (train && s->h_ctr->n_rec >= batch) {
-            // as many Adam steps as full batches were recorded (each on its own
-            // records), then start collecting again
-            const int steps = std::min(s->h_ctr->n_rec, rec_cap) / batch;
-            NNAdam opt;
-            opt.lr = s->nn_cfg.learning_rate;
-            for (int k = 0; k < steps; k++) {
-                float4* r = PD.rec + (size_t)4 * k * batch;
-                ck(cudaMemsetAsync(s->nn_scalars, 0, sizeof(float) * 4, st), "memset");
-                if (s->nn_cfg.divergence == PT_NN_CHI2) launch_square_T(r, batch, st);
-                launch_sum_T(r, batch, s->nn_scalars + 1, st);
-                launch_nn_train_step(s->nnw, N, r, batch, s->nn_scalars + 1, s->nn_tb, s->nn_grad, s->nn_scalars,
-                                     opt, ++s->nn_steps, s->num_sms, st, true);
-                launches += 5;
-            }
-            // records beyond the last full batch move to the front and stay
-            const int held = std::min(s->h_ctr->n_rec, rec_cap);
-            rec_left = held - steps * batch;
-            if (rec_left > 0)
-                ck(cudaMemcpyAsync(PD.rec, PD.rec + (size_t)4 * steps * batch, sizeof(float4) * 4 * rec_left,
-                                   cudaMemcpyDeviceToDevice, st), "keep records");
-            *s->h_rec_left = rec_left;
-            ck(cudaMemcpyAsync(&s->d_ctr->n_rec, s->h_rec_left, sizeof(int), cudaMemcpyHostToDevice, st), "records");
-            float sc[4] = {0.f, 0.f, 0.f, 0.f};
-            ck(cudaMemcpyAsync(sc, s->nn_scalars, sizeof(sc), cudaMemcpyDeviceToHost, st), "copy");
-            ck(cudaStreamSynchronize(st), "train");
-            uint32_t tstat;
-            std::memcpy(&tstat, &sc[2], sizeof(tstat));
-            check_status(s, tstat);
-            s->nn_last_loss = sc[0];
-            records += (double)steps * batch;
-            s->nn_records += (double)steps * batch;
+            rec_left = nn_train_round(s, s->h_ctr->n_rec, rec_cap, &s->d_ctr->n_rec, st, &launches);
+            records += (double)(std::min(s->h_ctr->n_rec, rec_cap) - rec_left);
         }
         if (s->h_ctr->n_cur == 0 && s->h_ctr->work_next >= s->h_ctr->work_total) break;
         if (round > max_rounds) throw Fail(PT_ERR_LIMIT, "render did not converge within the iteration bound");
@@ -1148,6 +1172,20 @@ void save_hdr(const std::string& path, const float* rgb, int W, int H) {
 
 }  // namespace
 
+// The learned-guide helpers above, for the multi-scene batch (batch.cpp).
+namespace cpppt_gb300 {
+namespace hostimpl {
+void nn_ensure_scene(pt_scene* s) { nn_ensure(s); }
+NNNorm nn_scene_norm(const pt_scene* s) { return scene_norm(s); }
+int nn_record_cap(const pt_scene* s) { return std::min(kNNRecordCap, s->nn_cfg.steps_per_round * s->nn_cfg.batch); }
+int nn_train_scene_round(pt_scene* s, int held, int cap, int* d_count, cudaStream_t st, double* launches) {
+    return nn_train_round(s, held, cap, d_count, st, launches);
+}
+void scene_check_status(pt_scene* s, uint32_t status) { check_status(s, status); }
+}  // namespace hostimpl
+}  // namespace cpppt_gb300
+
+
 extern "C" {
 
 pt_status pt_scene_create(const pt_scene_desc* desc, pt_scene** out) {
@@ -1391,7 +1429,15 @@ pt_status pt_debug_nn_forward(const float* weights, const float* lo, const float
         uint32_t* dstat = dalloc<uint32_t>(c.owned, 1);
         ck(cudaMemsetAsync(dstat, 0, sizeof(uint32_t), c.st), "memset");
         ck(cudaMemcpyAsync(din, inputs, sizeof(float) * 9 * n, cudaMemcpyHostToDevice, c.st), "copy");
-        launch_nn_forward_debug(W, norm_from(lo, hi), din, n, dout, dstat, c.sms, c.st);
+        const NNNorm N = norm_from(lo, hi);
+        DevNNJob hj{};
+        hj.wt = W.wt;
+        for (int k = 0; k < 3; k++) { hj.lo[k] = N.lo[k]; hj.inv_ext[k] = N.inv_ext[k]; }
+        hj.c_lo = N.c_lo;
+        hj.c_hi = N.c_hi;
+        DevNNJob* dj = dalloc<DevNNJob>(c.owned, 1);
+        ck(cudaMemcpyAsync(dj, &hj, sizeof(hj), cudaMemcpyHostToDevice, c.st), "copy");
+        launch_nn_forward_debug(dj, din, n, dout, dstat, c.sms, c.st);
         ck(cudaMemcpyAsync(out, dout, sizeof(float) * 41 * n, cudaMemcpyDeviceToHost, c.st), "copy");
         uint32_t hstat = 0;
         ck(cudaMemcpyAsync(&hstat, dstat, sizeof(uint32_t), cudaMemcpyDeviceToHost, c.st), "copy");

@@ -122,6 +122,8 @@ struct pt_scene {
     cudaGraphExec_t graph = nullptr;
     DevBatchJob* d_job = nullptr;  // one-entry job table of the wavefront kernels
     DevBatchJob* h_job = nullptr;  // pinned staging copy
+    DevNNJob* d_nnjob = nullptr;   // one-entry learned-guide job table
+    DevNNJob* h_nnjob = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     pt_render_stats stats{};
 
@@ -154,9 +156,23 @@ struct pt_scene {
         if (d_io) cudaFree(d_io);
         if (h_ctr) cudaFreeHost(h_ctr);
         if (h_job) cudaFreeHost(h_job);
+        if (h_nnjob) cudaFreeHost(h_nnjob);
         if (h_rec_left) cudaFreeHost(h_rec_left);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (stream) cudaStreamDestroy(stream);
     }
 };
+
+namespace cpppt_gb300 {
+namespace hostimpl {
+// Learned-guide state of a scene (host.cpp), for the multi-scene batch.
+void nn_ensure_scene(pt_scene* s);               // network, Adam state, record and training buffers
+NNNorm nn_scene_norm(const pt_scene* s);         // position normalisation and BSDF-fraction range
+int nn_record_cap(const pt_scene* s);            // records collected per round (steps_per_round batches)
+// Trains on the scene's `held` records (at most cap written) and sets
+// *d_count to the records kept; returns that number.  Synchronises st.
+int nn_train_scene_round(pt_scene* s, int held, int cap, int* d_count, cudaStream_t st, double* launches);
+void scene_check_status(pt_scene* s, uint32_t status);  // throws on kernel status bits
+}  // namespace hostimpl
+}  // namespace cpppt_gb300

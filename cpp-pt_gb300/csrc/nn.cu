@@ -116,125 +116,104 @@ __device__ __forceinline__ void tc_end(bool ok, uint32_t tmem, uint32_t bar, uin
     }
 }
 
-// Inference CTAs hold two groups of 128 threads that share one copy of the
-// weights: each group runs its own tiles with its own A tile, mbarrier and
-// 64 tensor-memory columns, synchronising on a named barrier of its own, so
-// one group's shared-memory traffic and epilogue overlap the other's MMAs.
-constexpr int kTcGroups = 2;
-constexpr int kTcInferThreads = kTcGroups * kTcRows;
-constexpr int kTcInferSmem = kNNLayers * kTcWLayerBytes + kTcGroups * kTcABytes + 64;
+// Inference over the paths of several render jobs (scenes with their own
+// networks): each tile runs once per distinct job among its rows, staging
+// that job's weights when they differ from the staged ones.  Jobs are
+// rendered in order, so nearly every tile holds one job and runs once.
+constexpr int kTcInferThreads = kTcRows;
+constexpr int kTcInferSmem = kNNLayers * kTcWLayerBytes + kTcABytes + 64;
 
-__device__ __forceinline__ void group_sync(int id) {
-    asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory");
-}
-__device__ __forceinline__ bool group_and(int id, bool v) {
-    uint32_t r;
-    asm volatile(
-        "{\n\t.reg .pred p, q;\n\t"
-        "setp.ne.u32 p, %1, 0;\n\t"
-        "bar.red.and.pred q, %2, 128, p;\n\t"
-        "selp.u32 %0, 1, 0, q;\n\t}\n"
-        : "=r"(r)
-        : "r"((uint32_t)v), "r"(id)
-        : "memory");
-    return r != 0;
-}
-
-// tc_layer for one 128-thread group (named barrier `bar_id`, issuer = the
-// group's first thread).
-__device__ __forceinline__ bool tc_layer_group(int bar_id, uint32_t tmem, uint32_t a_addr, uint32_t b_addr, int N,
-                                               uint32_t bar, uint32_t& phase) {
-    fence_proxy_async_smem();
-    tc_fence_before_sync();
-    group_sync(bar_id);
-    tc_fence_after_sync();
-    if ((threadIdx.x & (kTcRows - 1)) == 0) {
-        const uint32_t idesc = umma_idesc_bf16_f32(kTcRows, N);
-#pragma unroll
-        for (int ks = 0; ks < 4; ks++)
-            umma_bf16(tmem, umma_desc(a_addr + ks * 2 * kUmmaLBO, kTcSBO), umma_desc(b_addr + ks * 2 * kUmmaLBO, kTcSBO),
-                      idesc, ks > 0 ? 1u : 0u);
-        umma_commit(bar);
+// W_l^T of one network (padded transposed copy wt[l][out][in]) into the
+// canonical K-major layout.
+__device__ __forceinline__ void tc_stage_wt(const __nv_bfloat16* wt, unsigned char* s_w) {
+    for (int c = threadIdx.x; c < kNNLayers * 64 * 8; c += blockDim.x) {
+        const int l = c >> 9, rem = c & 511, nrow = rem >> 3, k8 = rem & 7;
+        if (nrow >= nn_layer_out(l)) continue;
+        const uint4 v = *reinterpret_cast<const uint4*>(wt + (size_t)l * kWLayer + nrow * kWStride + k8 * 8);
+        *reinterpret_cast<uint4*>(s_w + l * kTcWLayerBytes + umma_offset(nrow, k8 * 8, 64)) = v;
     }
-    const bool ok = group_and(bar_id, mbar_wait_bounded(bar, phase));
-    phase ^= 1u;
-    if (ok) tc_fence_after_sync();
-    return ok;
 }
 
-// get_in(i, NNIn&) -> bool valid; put(i, const float* prm41).  All
-// kTcInferThreads threads of the CTA must call it.  status:
-// kStatusTensorTimeout when a completion wait runs out (the group then
-// stops; the CTA frees its tensor memory and returns).
+// get_in(i, NNIn& in, int& job) -> bool valid, with in.pn NOT yet
+// normalised (world position); put(i, const float* prm41).  All kTcRows
+// threads of the CTA must call it.  status: kStatusTensorTimeout when a
+// completion wait runs out (the CTA then stops, frees its tensor memory and
+// returns).
 template <class GetIn, class Put>
-__device__ __forceinline__ void tc_infer_loop(int n, unsigned char* smem, const NNWeights& W, float c_lo, float c_hi,
+__device__ __forceinline__ void tc_infer_loop(int n, unsigned char* smem, const DevNNJob* __restrict__ nnj,
                                               uint32_t* status, GetIn get_in, Put put) {
-    const int group = threadIdx.x / kTcRows;
-    const int row = threadIdx.x & (kTcRows - 1);  // tensor-memory lane of this thread's sample
-    const int warp = threadIdx.x >> 5;
     unsigned char* s_w = smem;
-    unsigned char* s_a = smem + kNNLayers * kTcWLayerBytes + group * kTcABytes;
-    uint64_t* s_bars = reinterpret_cast<uint64_t*>(smem + kNNLayers * kTcWLayerBytes + kTcGroups * kTcABytes);
-    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(s_bars + kTcGroups);
-    tc_stage_weights(W, s_w);
-    if (threadIdx.x < kTcGroups) mbar_init(smem_u32(s_bars + threadIdx.x), 1);
-    if (warp == 0) tmem_alloc(s_tmem, kTcGroups * kTcCols);
-    tc_fence_before_sync();
-    __syncthreads();
-    tc_fence_after_sync();
-    const uint32_t tmem = *s_tmem + (uint32_t)(group * kTcCols);
-    const uint32_t t_row = tmem + ((uint32_t)((warp & 3) * 32) << 16);
-    const uint32_t bar = smem_u32(s_bars + group), a_addr = smem_u32(s_a), w_addr = smem_u32(s_w);
-    const int bar_id = 1 + group;
+    unsigned char* s_a = smem + kNNLayers * kTcWLayerBytes;
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_a + kTcABytes);
+    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(s_bar + 1);
+    int* s_job = reinterpret_cast<int*>(s_tmem + 1);
+    const int warp = threadIdx.x >> 5;
+    const int row = threadIdx.x;  // tensor-memory lane of this thread's sample
+    const uint32_t tmem = tc_begin(s_bar, s_tmem);
+    const uint32_t t_row = tmem + ((uint32_t)(warp * 32) << 16);
+    const uint32_t bar = smem_u32(s_bar), a_addr = smem_u32(s_a), w_addr = smem_u32(s_w);
     uint32_t phase = 0;
     bool ok = true;
-    for (int base = (blockIdx.x * kTcGroups + group) * kTcRows; base < n && ok;
-         base += gridDim.x * kTcGroups * kTcRows) {
+    const __nv_bfloat16* staged = nullptr;
+    for (int base = blockIdx.x * kTcRows; base < n && ok; base += gridDim.x * kTcRows) {
         const int i = base + row;
         NNIn in;
-        const bool valid = i < n && get_in(i, in);
-        float v[64];
+        in.pn = in.n = in.wo = mk(0.f, 0.f, 0.f);
+        int job = -1;
+        const bool valid = i < n && get_in(i, in, job);
+        bool pending = valid;
+        while (ok) {
+            // smallest job among the rows still waiting
+            if (threadIdx.x == 0) *s_job = 0x7fffffff;
+            __syncthreads();
+            if (pending) atomicMin(s_job, job);
+            __syncthreads();
+            const int J = *s_job;
+            if (J == 0x7fffffff) break;
+            const DevNNJob& nj = nnj[J];
+            if (nj.wt != staged) {  // all earlier MMAs have completed (their waits returned)
+                tc_stage_wt(nj.wt, s_w);
+                staged = nj.wt;
+            }
+            const bool mine = pending && job == J;
+            float v[64];
+            const f3 pn = mk((in.pn.x - nj.lo[0]) * nj.inv_ext[0], (in.pn.y - nj.lo[1]) * nj.inv_ext[1],
+                             (in.pn.z - nj.lo[2]) * nj.inv_ext[2]);
 #pragma unroll
-        for (int j = 0; j < 64; j++) v[j] = valid ? nn_feature(j, in.pn, in.n, in.wo) : 0.f;
-        tc_store_row(s_a, row, v, false);
-        for (int l = 0; l < kNNLayers; l++) {
-            const int nout = nn_layer_out(l);
-            ok = tc_layer_group(bar_id, tmem, a_addr, w_addr + l * kTcWLayerBytes, nout, bar, phase);
-            if (!ok) break;
+            for (int k = 0; k < 64; k++) v[k] = mine ? nn_feature(k, pn, in.n, in.wo) : 0.f;
+            tc_store_row(s_a, row, v, false);
+            for (int l = 0; l < kNNLayers; l++) {
+                const int nout = nn_layer_out(l);
+                ok = tc_layer(tmem, a_addr, kTcSBO, w_addr + l * kTcWLayerBytes, kTcSBO, 64, nout, bar, phase);
+                if (!ok) break;
 #pragma unroll
-            for (int c = 0; c < 64; c += 16)
-                if (c < nout) tmem_ld16(t_row + (uint32_t)c, v + c);
-            if (l < kNNLayers - 1) tc_store_row(s_a, row, v, true);
+                for (int c = 0; c < 64; c += 16)
+                    if (c < nout) tmem_ld16(t_row + (uint32_t)c, v + c);
+                if (l < kNNLayers - 1) tc_store_row(s_a, row, v, true);
+            }
+            if (ok && mine) {
+                float prm[kNNParams];
+                nn_postprocess(v, prm, nj.c_lo, nj.c_hi);
+                put(i, prm);
+            }
+            pending = pending && !mine;
         }
-        if (ok && valid) {
-            float prm[kNNParams];
-            nn_postprocess(v, prm, c_lo, c_hi);
-            put(i, prm);
-        }
     }
-    if (!ok) {
-        if (row == 0) atomicOr(status, kStatusTensorTimeout);
-        mbar_wait_bounded(bar, phase ^ 1u);  // the MMAs of the timed-out phase, if they still finish
-    }
-    tc_fence_before_sync();
-    __syncthreads();
-    if (warp == 0) {
-        tc_fence_after_sync();
-        tmem_dealloc(*s_tmem, kTcGroups * kTcCols);
-    }
+    tc_end(ok, tmem, bar, phase, status);
 }
 
-
-__global__ void __launch_bounds__(kTcInferThreads, 3) k_nn_forward_debug(NNWeights W, NNNorm N, const float* __restrict__ in,
-                                                              int n, float* __restrict__ out, uint32_t* status) {
+__global__ void __launch_bounds__(kTcInferThreads) k_nn_forward_debug(const DevNNJob* __restrict__ nnj,
+                                                                      const float* __restrict__ in, int n,
+                                                                      float* __restrict__ out, uint32_t* status) {
     extern __shared__ __align__(1024) unsigned char smem[];
     tc_infer_loop(
-        n, smem, W, N.c_lo, N.c_hi, status,
-        [&](int i, NNIn& v) {
+        n, smem, nnj, status,
+        [&](int i, NNIn& v, int& job) {
             const float* p = in + 9 * (size_t)i;
-            v.pn = mk((p[0] - N.lo[0]) * N.inv_ext[0], (p[1] - N.lo[1]) * N.inv_ext[1], (p[2] - N.lo[2]) * N.inv_ext[2]);
+            v.pn = mk(p[0], p[1], p[2]);
             v.n = mk(p[3], p[4], p[5]);
             v.wo = mk(p[6], p[7], p[8]);
+            job = 0;
             return true;
         },
         [&](int i, const float* prm) {
@@ -242,15 +221,17 @@ __global__ void __launch_bounds__(kTcInferThreads, 3) k_nn_forward_debug(NNWeigh
         });
 }
 
-// Guide parameters for every live path's hit (run between extend and shade).
-__global__ void __launch_bounds__(kTcInferThreads, 3) k_nn_infer(DevScene S, PathBuffers B, int cur, WaveCounters* ctr,
-                                                      NNWeights W, NNNorm N, float4* __restrict__ params) {
+// Guide parameters for every live path's hit (run between extend and shade),
+// each path with its job's network.
+__global__ void __launch_bounds__(kTcInferThreads) k_nn_infer(DevScene S, PathBuffers B, int cur, WaveCounters* ctr,
+                                                              const DevNNJob* __restrict__ nnj,
+                                                              float4* __restrict__ params) {
     extern __shared__ __align__(1024) unsigned char smem[];
     const int n = ctr->n_cur;
     if (n == 0) return;
     tc_infer_loop(
-        n, smem, W, N.c_lo, N.c_hi, &ctr->status,
-        [&](int i, NNIn& v) {
+        n, smem, nnj, &ctr->status,
+        [&](int i, NNIn& v, int& job) {
             const float4 H = B.hit[i];
             const int prim = __float_as_int(H.y);
             if (prim < 0) return false;
@@ -258,13 +239,12 @@ __global__ void __launch_bounds__(kTcInferThreads, 3) k_nn_infer(DevScene S, Pat
             if (S.mats[vi.w].kind == PT_MAT_EMISSIVE_) return false;
             const float4 O = B.o[cur][i], D = B.d[cur][i];
             const f3 d = mk(D.x, D.y, D.z);
-            const f3 p = mk(O.x, O.y, O.z) + d * H.x;
             const float beta = H.z, gamma = H.w, alpha = 1.0f - (gamma + beta);
-            const f3 nn = normalized(f3of(__ldg(S.v_nrm + vi.x)) * alpha + f3of(__ldg(S.v_nrm + vi.y)) * beta +
-                                     f3of(__ldg(S.v_nrm + vi.z)) * gamma);
-            v.pn = mk((p.x - N.lo[0]) * N.inv_ext[0], (p.y - N.lo[1]) * N.inv_ext[1], (p.z - N.lo[2]) * N.inv_ext[2]);
-            v.n = nn;
+            v.pn = mk(O.x, O.y, O.z) + d * H.x;
+            v.n = normalized(f3of(__ldg(S.v_nrm + vi.x)) * alpha + f3of(__ldg(S.v_nrm + vi.y)) * beta +
+                             f3of(__ldg(S.v_nrm + vi.z)) * gamma);
             v.wo = -d;
+            job = (int)((uint32_t)B.info[cur][i].z >> kNNJobShift);
             return true;
         },
         [&](int i, const float* prm) {
@@ -572,15 +552,15 @@ cudaError_t nn_set_smem_limits() {
 void launch_nn_pack(const NNWeights& W, cudaStream_t st) {
     k_nn_pack<<<(kNNWeights + 255) / 256, 256, 0, st>>>(W);
 }
-void launch_nn_forward_debug(const NNWeights& W, const NNNorm& N, const float* in, int n, float* out,
-                             uint32_t* status, int num_sms, cudaStream_t st) {
-    const int blocks = std::max(1, std::min(num_sms * 3, (n + kTcInferThreads - 1) / kTcInferThreads));
-    k_nn_forward_debug<<<blocks, kTcInferThreads, nn_smem_infer(), st>>>(W, N, in, n, out, status);
+void launch_nn_forward_debug(const DevNNJob* nnj, const float* in, int n, float* out, uint32_t* status, int num_sms,
+                             cudaStream_t st) {
+    const int blocks = std::max(1, std::min(num_sms * 4, (n + kTcInferThreads - 1) / kTcInferThreads));
+    k_nn_forward_debug<<<blocks, kTcInferThreads, nn_smem_infer(), st>>>(nnj, in, n, out, status);
 }
-void launch_nn_infer(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, const NNWeights& W,
-                     const NNNorm& N, float4* params, int num_sms, cudaStream_t st) {
-    // three CTAs (six 128-sample groups) per SM fit in shared memory
-    k_nn_infer<<<num_sms * 3, kTcInferThreads, nn_smem_infer(), st>>>(S, B, cur, ctr, W, N, params);
+void launch_nn_infer(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, const DevNNJob* nnj,
+                     float4* params, int num_sms, cudaStream_t st) {
+    // four CTAs of 128 threads per SM fit in shared memory (48 KB each)
+    k_nn_infer<<<num_sms * 4, kTcInferThreads, nn_smem_infer(), st>>>(S, B, cur, ctr, nnj, params);
 }
 void launch_nn_train_step(const NNWeights& W, const NNNorm& N, const float4* rec, int n, const float* tsum,
                           const NNTrainBuf& TB, float* grad, float* loss, const NNAdam& opt, int step, int num_sms,
@@ -614,7 +594,7 @@ void launch_nn_train_step(const NNWeights& W, const NNNorm& N, const float4* rec
 
 __device__ __forceinline__ float luminance(f3 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
 
-__device__ __forceinline__ void film_add_nn(unsigned long long* film, int pix, f3 c, WaveCounters* ctr) {
+__device__ __forceinline__ void film_add_nn(unsigned long long* film, size_t pix, f3 c, WaveCounters* ctr) {
     if (!isfinite(c.x) || !isfinite(c.y) || !isfinite(c.z)) {
         atomicAdd(&ctr->stat_nonfinite, 1ull);
         return;
@@ -643,7 +623,8 @@ __device__ __forceinline__ int warp_append_nn(int* counter, bool pred) {
 constexpr int kNNVert = kNNVertFloat4;
 __global__ void __launch_bounds__(256) k_shade_nn(DevScene S, PathBuffers B, int cur, RenderParams P,
                                                   WaveCounters* ctr, unsigned long long* __restrict__ film,
-                                                  const float4* __restrict__ params, NNPathData PD, int guided) {
+                                                  const float4* __restrict__ params, NNPathData PD, int guided,
+                                                  const DevBatchJob* __restrict__ jobs) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = ctr->n_cur;
     bool push_sh = false, push_cont = false, release = false;
@@ -657,6 +638,14 @@ __global__ void __launch_bounds__(256) k_shade_nn(DevScene S, PathBuffers B, int
         const int prim = __float_as_int(H.y);
         const int pixel = I.x, sample = I.y, bounce = I.z & 0xffff;
         const bool sdelta = (I.z >> 16) & 1;
+        const int job = (int)((uint32_t)I.z >> kNNJobShift);
+        const DevBatchJob* J = jobs + job;
+        const uint32_t seed = J->seed;
+        const int rr_start = J->rr_start, max_depth = J->max_depth;
+        const size_t fpix = (size_t)(uint32_t)pixel + J->film_off;
+        S.light_prim += J->light_off;
+        S.light_area += J->light_off;
+        S.n_lights = J->n_lights;
         slot = I.w;
         const size_t vbase = (size_t)slot * P.max_depth;
         const float p = O.w;
@@ -687,11 +676,11 @@ __global__ void __launch_bounds__(256) k_shade_nn(DevScene S, PathBuffers B, int
                     w = p / (p + p_nee);
                 }
                 const f3 c = mul * mk(m.r, m.g, m.b) * w;
-                film_add_nn(film, pixel, c, ctr);
+                film_add_nn(film, fpix, c, ctr);
                 Ssum = Ssum + c;
             } else {
-                const Rng4 r0 = rng4(P.seed, sample, pixel, bounce, 0);
-                const Rng4 r1 = rng4(P.seed, sample, pixel, bounce, 1);
+                const Rng4 r0 = rng4(seed, sample, pixel, bounce, 0);
+                const Rng4 r1 = rng4(seed, sample, pixel, bounce, 1);
                 const bool delta_mat = (m.kind == PT_MAT_DIELECTRIC_) || (m.kind == PT_MAT_GGX_ && m.delta);
                 float prm[kNNParams];
                 float c = 1.0f;
@@ -732,14 +721,14 @@ __global__ void __launch_bounds__(256) k_shade_nn(DevScene S, PathBuffers B, int
                         const float pn = ls.pdf * len * len / (fabsf(dot(ls.n, sd)) + kEps);
                         // at the last vertex no sampled direction follows, so NEE takes the full
                         // weight (the two estimators then converge to the same depth-limited image)
-                        const float w = bounce + 1 < P.max_depth ? pn / (pb + pn) : 1.0f;
+                        const float w = bounce + 1 < max_depth ? pn / (pb + pn) : 1.0f;
                         const f3 f = bsdf_eval(m, s, wo, sd);
                         const f3 cc = mul * f * ls.le * (1.0f / (ls.pdf * len * len)) * w;
                         if (cc.x != 0.f || cc.y != 0.f || cc.z != 0.f) {
                             push_sh = true;
                             const f3 so = s.p + sd * kEps;
                             sh_o = make_float4(so.x, so.y, so.z, len - 2.0f * kEps);
-                            sh_d = make_float4(sd.x, sd.y, sd.z, __int_as_float(pixel));
+                            sh_d = make_float4(sd.x, sd.y, sd.z, __int_as_float((int)(uint32_t)fpix));
                             sh_c = make_float4(cc.x, cc.y, cc.z, __int_as_float(slot));
                         }
                     }
@@ -759,7 +748,7 @@ __global__ void __launch_bounds__(256) k_shade_nn(DevScene S, PathBuffers B, int
                     const f3 f = bsdf_eval(m, s, wo, bs.wi);
                     bool alive = true;
                     float surv = 1.0f;
-                    if (bounce >= P.rr_start) {  // survival min(rr, 1): unbiased
+                    if (bounce >= rr_start) {  // survival min(rr, 1): unbiased
                         if (P.flags & PT_FLAG_THROUGHPUT_RR_) {
                             const f3 mn = mul * f * (1.0f / pmix);
                             surv = fminf(1.0f, fmaxf(fmaxf(mn.x, mn.y), mn.z));
@@ -768,15 +757,16 @@ __global__ void __launch_bounds__(256) k_shade_nn(DevScene S, PathBuffers B, int
                         }
                         if (r1.v[1] > surv) alive = false;
                     }
-                    if (alive && bounce + 1 < P.max_depth) {
+                    if (alive && bounce + 1 < max_depth) {
                         mul = mul * f * (1.0f / (pmix * surv));
                         const f3 oo = s.p + bs.wi * kEps;
                         push_cont = true;
                         done = false;
                         no = make_float4(oo.x, oo.y, oo.z, pmix);
-                        nd = make_float4(bs.wi.x, bs.wi.y, bs.wi.z, 0.f);
+                        nd = make_float4(bs.wi.x, bs.wi.y, bs.wi.z, D.w);  // w: the scene root
                         nt = make_float4(mul.x, mul.y, mul.z, 0.f);
-                        ninfo = make_int4(pixel, sample, (bounce + 1) | ((bs.delta ? 1 : 0) << 16), slot);
+                        ninfo = make_int4(pixel, sample,
+                                          (bounce + 1) | ((bs.delta ? 1 : 0) << 16) | (job << kNNJobShift), slot);
                     }
                 }
             }
@@ -840,10 +830,12 @@ __device__ __forceinline__ void visit_records(const NNPathData& PD, int4 f, int 
     }
 }
 
-// Finished paths: records are counted first, one warp-aggregated atomic
-// reserves the warp's range, then written (records beyond the buffer's
+// Finished paths: records are counted first, then one atomic per warp (all
+// lanes of the same job; per lane otherwise) reserves room in the job's
+// record buffer, then they are written (records beyond the buffer's
 // capacity are dropped); the slots go back to the free list.
-__global__ void __launch_bounds__(256) k_finish_nn(NNPathData PD, WaveCounters* ctr, int max_depth) {
+__global__ void __launch_bounds__(256) k_finish_nn(NNPathData PD, WaveCounters* ctr,
+                                                   const DevNNJob* __restrict__ nnj, int max_depth) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = ctr->n_fin;
     const unsigned lane = threadIdx.x & 31u;
@@ -851,23 +843,32 @@ __global__ void __launch_bounds__(256) k_finish_nn(NNPathData PD, WaveCounters* 
     int4 f = make_int4(0, 0, 0, 0);
     if (release) f = PD.fin[i];
     const bool records = release && PD.rec_cap > 0;
+    const int job = records ? PD.slot_job[f.x] : -1;
     int count = 0;
     if (records) visit_records(PD, f, max_depth, [&](const float4*, f3, float, float) { count++; });
-    int incl = count;
+    // one job for the whole warp (the usual case: jobs are rendered in order)?
+    const int job0 = __shfl_sync(0xffffffffu, job, 0);
+    const bool uniform = __all_sync(0xffffffffu, job == job0 || job < 0);
+    int base = 0, incl = count;
+    if (uniform) {
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int v = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= (unsigned)o) incl += v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= (unsigned)o) incl += v;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        const int lead_job = __reduce_max_sync(0xffffffffu, (unsigned)(job + 1)) - 1;
+        if (lane == 31 && total > 0) base = atomicAdd(nnj[lead_job].n_rec, total);
+        base = __shfl_sync(0xffffffffu, base, 31) + incl - count;
+    } else if (count > 0) {
+        base = atomicAdd(nnj[job].n_rec, count);
     }
-    const int total = __shfl_sync(0xffffffffu, incl, 31);
-    int base = 0;
-    if (lane == 31 && total > 0) base = atomicAdd(&ctr->n_rec, total);
-    base = __shfl_sync(0xffffffffu, base, 31);
     if (records && count > 0) {
-        int r = base + incl - count;
+        const DevNNJob& Jn = nnj[job];
+        int r = base;
         visit_records(PD, f, max_depth, [&](const float4* vr, f3 wi, float pb, float T) {
-            if (r < PD.rec_cap) {
-                float4* o = PD.rec + 4 * (size_t)r;
+            if (r < Jn.rec_cap) {
+                float4* o = Jn.rec + 4 * (size_t)r;
                 o[0] = vr[0];
                 o[1] = vr[1];
                 o[2] = make_float4(vr[2].x, wi.x, wi.y, wi.z);
@@ -884,7 +885,8 @@ __global__ void __launch_bounds__(256) k_finish_nn(NNPathData PD, WaveCounters* 
 // go to the film and to the owning path's running total (for its training
 // targets).
 __global__ void __launch_bounds__(256) k_shadow_nn(DevScene S, PathBuffers B, WaveCounters* ctr,
-                                                   unsigned long long* __restrict__ film, NNPathData PD) {
+                                                   unsigned long long* __restrict__ film, NNPathData PD,
+                                                   const DevBatchJob* __restrict__ jobs) {
     __shared__ uint4 snodes[kSmemNodes * 4];
     const int n = ctr->n_shadow;
     if (n == 0) return;
@@ -899,12 +901,13 @@ __global__ void __launch_bounds__(256) k_shadow_nn(DevScene S, PathBuffers B, Wa
             o = make_float3(a.x, a.y, a.z);
             d = make_float3(b.x, b.y, b.z);
             tmax = a.w;
+            if (root != kTravDone) root = jobs[PD.slot_job[__float_as_int(B.sh_c[i].w)]].root;
         },
         [&](int i, const HitRec& h) {
             if (h.prim < 0) {
                 const float4 c = B.sh_c[i];
                 const f3 cc = mk(c.x, c.y, c.z);
-                film_add_nn(film, __float_as_int(B.sh_d[i].w), cc, ctr);
+                film_add_nn(film, (uint32_t)__float_as_int(B.sh_d[i].w), cc, ctr);
                 if (PD.rec_cap > 0) {
                     const int slot = __float_as_int(c.w);
                     const float4 a = PD.acc[slot];
@@ -915,39 +918,61 @@ __global__ void __launch_bounds__(256) k_shadow_nn(DevScene S, PathBuffers B, Wa
 }
 
 // Camera paths (stratified like pathtracerMIS.h:148-153) with a vertex slot.
-__global__ void __launch_bounds__(256) k_generate_nn(DevScene S, PathBuffers B, int cur, RenderParams P,
-                                                     WaveCounters* ctr, NNPathData PD) {
+__global__ void __launch_bounds__(256) k_generate_nn(DevScene S, PathBuffers B, int cur, WaveCounters* ctr,
+                                                     NNPathData PD, const DevBatchJob* __restrict__ jobs,
+                                                     int n_jobs) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int n_next = ctr->n_next;
     const int avail = min(B.capacity - n_next, ctr->free_top);
-    const unsigned long long w = ctr->work_next + (unsigned long long)t;
+    unsigned long long w = ctr->work_next + (unsigned long long)t;
     if (t >= avail || w >= ctr->work_total) return;
-    const unsigned long long npix = (unsigned long long)P.width * P.height;
-    const int sample = (int)(w / npix);
-    const int pixel = (int)(w - (unsigned long long)sample * npix);
-    const int px = pixel % P.width, py = pixel / P.width;
-    const Rng4 r = rng4(P.seed, sample, pixel, 0xffffu, 2);
-    float cx, cy;
-    if (P.spp_axis > 0) {
-        const int k = sample / P.spp_axis, l = sample - (sample / P.spp_axis) * P.spp_axis;
-        cx = (((float)px + ((float)k + r.v[0]) / (float)P.spp_axis) / (float)P.width) * 2.0f - 1.0f;
-        cy = -((((float)py + ((float)l + r.v[1]) / (float)P.spp_axis) / (float)P.height) * 2.0f - 1.0f);
-    } else {
-        cx = (((float)px + r.v[0]) / (float)P.width) * 2.0f - 1.0f;
-        cy = -((((float)py + r.v[1]) / (float)P.height) * 2.0f - 1.0f);
+    int job = 0;
+    if (n_jobs > 1) {  // job ranges ascend (as find_job in render.cu)
+        int lo = 0, hi = n_jobs - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(&jobs[mid].work_begin) <= w) lo = mid;
+            else hi = mid - 1;
+        }
+        job = lo;
     }
-    const DevCamera& C = S.cam;
-    const float dx = cx * C.tan_fovy * C.aspect, dy = cy * C.tan_fovy, dz = -1.0f;
-    const f3 d = normalized(mk(C.m[0] * dx + C.m[1] * dy + C.m[2] * dz, C.m[3] * dx + C.m[4] * dy + C.m[5] * dz,
-                               C.m[6] * dx + C.m[7] * dy + C.m[8] * dz));
+    const DevBatchJob* J = jobs + job;
+    w -= J->work_begin;
+    const DevCamera* C = &J->cam;
+    const int width = C->width, height = C->height, spp_axis = J->spp_axis;
+    const unsigned long long npix = (unsigned long long)width * height;
+    const int sample = (int)(w / npix);
+    int pixel = (int)(w - (unsigned long long)sample * npix);
+    if (J->tile_w * J->tile_h > 1) {  // tiled pass order (a bijection of the pixels)
+        const int tw = J->tile_w, th = J->tile_h;
+        const int tile = pixel / (tw * th), r = pixel - tile * (tw * th);
+        const int tiles_x = width / tw;
+        const int ty = tile / tiles_x, tx = tile - ty * tiles_x;
+        pixel = (ty * th + r / tw) * width + tx * tw + r % tw;
+    }
+    const int px = pixel % width, py = pixel / width;
+    const Rng4 r = rng4(J->seed, sample, pixel, 0xffffu, 2);
+    float cx, cy;
+    if (spp_axis > 0) {  // pathtracerMIS.h:148-153
+        const int k = sample / spp_axis, l = sample - (sample / spp_axis) * spp_axis;
+        cx = (((float)px + ((float)k + r.v[0]) / (float)spp_axis) / (float)width) * 2.0f - 1.0f;
+        cy = -((((float)py + ((float)l + r.v[1]) / (float)spp_axis) / (float)height) * 2.0f - 1.0f);
+    } else {
+        cx = (((float)px + r.v[0]) / (float)width) * 2.0f - 1.0f;
+        cy = -((((float)py + r.v[1]) / (float)height) * 2.0f - 1.0f);
+    }
+    const float dx = cx * C->tan_fovy * C->aspect, dy = cy * C->tan_fovy, dz = -1.0f;
+    const f3 d = normalized(mk(C->m[0] * dx + C->m[1] * dy + C->m[2] * dz, C->m[3] * dx + C->m[4] * dy + C->m[5] * dz,
+                               C->m[6] * dx + C->m[7] * dy + C->m[8] * dz));
     const int nx = 1 - cur;
     const int j = n_next + t;
     const int slot = PD.slot_stack[ctr->free_top - 1 - t];
     PD.acc[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
-    B.o[nx][j] = make_float4(C.o[0], C.o[1], C.o[2], 1.0f);
-    B.d[nx][j] = make_float4(d.x, d.y, d.z, 0.f);
+    PD.slot_job[slot] = job;
+    B.o[nx][j] = make_float4(C->o[0], C->o[1], C->o[2], 1.0f);
+    B.d[nx][j] = make_float4(d.x, d.y, d.z, __uint_as_float(J->root));
     B.thr[nx][j] = make_float4(1.f, 1.f, 1.f, 0.f);
-    B.info[nx][j] = make_int4(pixel, sample, 1 << 16, slot);
+    B.info[nx][j] = make_int4(pixel, sample, (1 << 16) | (job << kNNJobShift), slot);  // sampled_delta starts true
 }
 
 __global__ void k_advance_nn(WaveCounters* ctr, int capacity) {
@@ -980,20 +1005,21 @@ __global__ void k_sum_T(const float4* __restrict__ rec, int n, float* out) {
 
 void launch_nn_shade(const DevScene& S, const PathBuffers& B, int cur, const RenderParams& P, WaveCounters* ctr,
                      unsigned long long* film, const float4* params, const NNPathData& PD, bool guided,
-                     cudaStream_t st) {
-    k_shade_nn<<<(B.capacity + 255) / 256, 256, 0, st>>>(S, B, cur, P, ctr, film, params, PD, guided ? 1 : 0);
+                     const DevBatchJob* jobs, cudaStream_t st) {
+    k_shade_nn<<<(B.capacity + 255) / 256, 256, 0, st>>>(S, B, cur, P, ctr, film, params, PD, guided ? 1 : 0, jobs);
 }
 void launch_nn_shadow(const DevScene& S, const PathBuffers& B, WaveCounters* ctr, unsigned long long* film,
-                      const NNPathData& PD, int num_sms, cudaStream_t st) {
-    k_shadow_nn<<<num_sms * 4, 256, 0, st>>>(S, B, ctr, film, PD);
+                      const NNPathData& PD, const DevBatchJob* jobs, int num_sms, cudaStream_t st) {
+    k_shadow_nn<<<num_sms * 4, 256, 0, st>>>(S, B, ctr, film, PD, jobs);
 }
-void launch_nn_generate(const DevScene& S, const PathBuffers& B, int cur, const RenderParams& P, WaveCounters* ctr,
-                        const NNPathData& PD, cudaStream_t st) {
-    k_generate_nn<<<(B.capacity + 255) / 256, 256, 0, st>>>(S, B, cur, P, ctr, PD);
+void launch_nn_generate(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, const NNPathData& PD,
+                        const DevBatchJob* jobs, int n_jobs, cudaStream_t st) {
+    k_generate_nn<<<(B.capacity + 255) / 256, 256, 0, st>>>(S, B, cur, ctr, PD, jobs, n_jobs);
     k_advance_nn<<<1, 32, 0, st>>>(ctr, B.capacity);
 }
-void launch_nn_finish(const NNPathData& PD, WaveCounters* ctr, int max_depth, int capacity, cudaStream_t st) {
-    k_finish_nn<<<(capacity + 255) / 256, 256, 0, st>>>(PD, ctr, max_depth);
+void launch_nn_finish(const NNPathData& PD, WaveCounters* ctr, const DevNNJob* nnj, int max_depth, int capacity,
+                      cudaStream_t st) {
+    k_finish_nn<<<(capacity + 255) / 256, 256, 0, st>>>(PD, ctr, nnj, max_depth);
 }
 __global__ void k_square_T(float4* __restrict__ rec, int n) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {

@@ -34,10 +34,27 @@ struct NNPathData {
     float4* vert;        // kNNVertFloat4 float4 per vertex, max_depth vertices per slot
     float4* acc;         // film total gathered by the path so far (rgb)
     int* slot_stack;     // free list of slots
-    int4* fin;           // paths finished this iteration: slot, traced vertices, extra target of the last
-    float4* rec;         // training records, 4 float4 each
-    int rec_cap;
+    int* slot_job;       // render job of the path holding each slot
+    int4* fin;           // paths finished this iteration: slot, traced vertices, recorded vertices
+    int rec_cap;         // > 0: vertex records are kept and training records emitted (to DevNNJob::rec)
 };
+
+// Learned-guide data of one render job (device table, one entry per job;
+// a single-scene render is a table of one).  Jobs of one scene share its
+// network and record buffer.
+struct DevNNJob {
+    const __nv_bfloat16* wt;  // forward weights of the job's scene (W_l^T, rows padded to 72)
+    float lo[3], inv_ext[3];  // position normalisation to the scene box
+    float c_lo, c_hi;         // range of the BSDF selection probability
+    float4* rec;              // training records of the job's scene (4 float4 each)
+    int32_t rec_cap;          // capacity of rec (0: no records)
+    int32_t* n_rec;           // record counter of the job's scene
+};
+
+// Path info word z of the slot wavefront: bounce (bits 0-15), sampled delta
+// (bit 16), render job (bits 17-31).
+constexpr int kNNJobShift = 17;
+constexpr int kNNMaxJobs = 1 << 15;
 
 struct NNAdam {
     float lr = 1e-3f, b1 = 0.9f, b2 = 0.99f, eps = 1e-8f, clip = 10.0f;
@@ -49,10 +66,10 @@ size_t nn_wcopy_elems();  // bf16 elements of one padded weight copy
 cudaError_t nn_set_smem_limits();
 void launch_nn_pack(const NNWeights& W, cudaStream_t st);
 // status: one zeroed word; receives kStatusTensorTimeout if a wait ran out.
-void launch_nn_forward_debug(const NNWeights& W, const NNNorm& N, const float* in, int n, float* out,
-                             uint32_t* status, int num_sms, cudaStream_t st);
-void launch_nn_infer(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, const NNWeights& W,
-                     const NNNorm& N, float4* params, int num_sms, cudaStream_t st);
+void launch_nn_forward_debug(const DevNNJob* nnj, const float* in, int n, float* out, uint32_t* status, int num_sms,
+                             cudaStream_t st);
+void launch_nn_infer(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, const DevNNJob* nnj,
+                     float4* params, int num_sms, cudaStream_t st);
 // grad (kNNWeights floats) receives dL/dW; loss[0] accumulates the batch
 // loss and the word at loss + 2 collects status bits (kStatusTensorTimeout);
 // apply: also take one Adam step (step counts from 1).
@@ -61,16 +78,20 @@ void launch_nn_train_step(const NNWeights& W, const NNNorm& N, const float4* rec
                           const NNTrainBuf& TB, float* grad, float* loss, const NNAdam& opt, int step, int num_sms,
                           cudaStream_t st, bool apply);
 
+// The slot wavefront's stages.  jobs: the render jobs (DevBatchJob, as the
+// plain wavefront; one entry for a single render); P carries the flags and
+// the vertex-record stride (P.max_depth: the largest depth of the jobs).
 void launch_nn_shade(const DevScene& S, const PathBuffers& B, int cur, const RenderParams& P, WaveCounters* ctr,
                      unsigned long long* film, const float4* params, const NNPathData& PD, bool guided,
-                     cudaStream_t st);
+                     const DevBatchJob* jobs, cudaStream_t st);
 void launch_nn_shadow(const DevScene& S, const PathBuffers& B, WaveCounters* ctr, unsigned long long* film,
-                      const NNPathData& PD, int num_sms, cudaStream_t st);
-void launch_nn_generate(const DevScene& S, const PathBuffers& B, int cur, const RenderParams& P, WaveCounters* ctr,
-                        const NNPathData& PD, cudaStream_t st);
+                      const NNPathData& PD, const DevBatchJob* jobs, int num_sms, cudaStream_t st);
+void launch_nn_generate(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, const NNPathData& PD,
+                        const DevBatchJob* jobs, int n_jobs, cudaStream_t st);
 // Emits the training records of the paths that finished this iteration (after
 // the shadow stage, so their last NEE is counted) and frees their slots.
-void launch_nn_finish(const NNPathData& PD, WaveCounters* ctr, int max_depth, int capacity, cudaStream_t st);
+void launch_nn_finish(const NNPathData& PD, WaveCounters* ctr, const DevNNJob* nnj, int max_depth, int capacity,
+                      cudaStream_t st);
 // T -> T^2 for every record (chi-square training)
 void launch_square_T(float4* rec, int n, cudaStream_t st);
 void launch_sum_T(const float4* rec, int n, float* out, cudaStream_t st);

@@ -105,9 +105,12 @@ def test_trained_guide_lowers_variance(gpu_lib):
     gs = GpuScene(sc)
     gs.nn_reset(11)
     gs.nn_configure(bsdf_frac_min=0.1)
-    for k in range(200):
+    # training is not deterministic (gradient sums use atomics): after 200
+    # renders the variance ratio below spread over 0.77-0.86 on repeated runs,
+    # after 400 over 0.57-0.71
+    for k in range(400):
         gs.render(4, max_depth=12, seed=3000 + k, mode=MODE_NN)
-    assert gs.nn_stats()["steps"] >= 200
+    assert gs.nn_stats()["steps"] >= 400
 
     def rel_var(mode, flags, seed0, R=8, S=16):
         x = np.stack([gs.render(S, max_depth=3, seed=seed0 + r, mode=mode, flags=flags) for r in range(R)])
