@@ -29,7 +29,8 @@ EXPORTS = ["pt_scene_create", "pt_scene_load", "pt_scene_destroy", "pt_scene_inf
            "pt_debug_sdtree_run", "pt_nn_get_weights", "pt_nn_set_weights", "pt_nn_reset", "pt_nn_stats",
            "pt_debug_nn_forward", "pt_debug_nn_grad", "pt_nn_configure", "pt_nn_config_get",
            "pt_batch_create", "pt_batch_destroy", "pt_batch_render", "pt_batch_render_device", "pt_batch_set_tuning",
-           "pt_batch_get_tuning", "pt_batch_stats", "pt_batch_autotune", "pt_set_mesh_cache"]
+           "pt_batch_get_tuning", "pt_batch_stats", "pt_batch_autotune", "pt_set_mesh_cache",
+           "pt_batch_render_ex", "pt_batch_render_ex_device"]
 
 
 class PtMaterial(C.Structure):
@@ -125,6 +126,8 @@ def load(path: str = LIB_PATH):
     lib.pt_batch_destroy.restype = None
     lib.pt_batch_render.argtypes = [P, P, C.c_int32, P]
     lib.pt_batch_render_device.argtypes = [P, P, C.c_int32, P]
+    lib.pt_batch_render_ex.argtypes = [P, P, C.c_int32, C.c_int32, C.c_uint32, P]
+    lib.pt_batch_render_ex_device.argtypes = [P, P, C.c_int32, C.c_int32, C.c_uint32, P]
     lib.pt_batch_set_tuning.argtypes = [P, P]
     lib.pt_batch_get_tuning.argtypes = [P, P]
     lib.pt_batch_stats.argtypes = [P, C.POINTER(PtRenderStats)]
@@ -321,24 +324,26 @@ class GpuBatch:
             a.max_depth, a.rr_start, a.seed = j.get("max_depth", 32), j.get("rr_start", 3), j.get("seed", 0)
         return arr
 
-    def render(self, jobs, outputs=True):
-        """Renders the jobs; returns one (H, W, 3) image per job (or None)."""
+    def render(self, jobs, outputs=True, mode=MODE_MIS, flags=0):
+        """Renders the jobs; returns one (H, W, 3) image per job (or None).
+        mode / flags as GpuScene.render (not MODE_SDTREE); MODE_NN guides
+        each job with its scene's own learned guide."""
         arr = self._jobs(jobs)
         if not all(0 <= j["scene"] < len(self.scenes) for j in jobs):
             outputs = False  # the library reports the bad job
         if not outputs:
-            _check(_lib.pt_batch_render(self.h, arr, len(jobs), None))
+            _check(_lib.pt_batch_render_ex(self.h, arr, len(jobs), mode, flags, None))
             return None
         imgs = [np.zeros((self.scenes[j["scene"]].height, self.scenes[j["scene"]].width, 3), np.float32)
                 for j in jobs]
         ptrs = (C.c_void_p * len(jobs))(*[_ptr(x) for x in imgs])
-        _check(_lib.pt_batch_render(self.h, arr, len(jobs), ptrs))
+        _check(_lib.pt_batch_render_ex(self.h, arr, len(jobs), mode, flags, ptrs))
         return imgs
 
-    def render_device(self, jobs, d_outs):
+    def render_device(self, jobs, d_outs, mode=MODE_MIS, flags=0):
         arr = self._jobs(jobs)
         ptrs = (C.c_void_p * len(jobs))(*d_outs)
-        _check(_lib.pt_batch_render_device(self.h, arr, len(jobs), ptrs))
+        _check(_lib.pt_batch_render_ex_device(self.h, arr, len(jobs), mode, flags, ptrs))
 
     def tuning(self) -> dict:
         t = PtBatchTuning()

@@ -22,6 +22,7 @@ struct pt_batch {
     std::vector<void*> owned;  // arena
     DevScene arena{};
     struct Member {
+        pt_scene* scene;  // its learned guide serves guided batch renders
         uint32_t root;
         int light_off, n_lights, width, height;
         DevCamera cam;
@@ -51,6 +52,19 @@ struct pt_batch {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     pt_render_stats stats{};
 
+    // slot wavefront (learned guide, PT_FLAG_UNBIASED_MIS): per-path vertex
+    // records and slots, guide parameters, per-job guide table, per-scene
+    // record counters
+    NNPathData pd{};
+    std::vector<void*> pd_owned;
+    int pd_cap = 0, pd_depth = 0;
+    float4* nn_params = nullptr;
+    DevNNJob* d_nnjobs = nullptr;
+    DevNNJob* h_nnjobs = nullptr;  // pinned
+    int nnjobs_cap = 0;
+    int* d_nrec = nullptr;  // one per member scene (in `owned`)
+    int* h_nrec = nullptr;  // pinned
+
     ~pt_batch() {
         if (stream) cudaStreamSynchronize(stream);
         if (graph) cudaGraphExecDestroy(graph);
@@ -61,6 +75,10 @@ struct pt_batch {
         if (d_jobs) cudaFree(d_jobs);
         if (h_jobs) cudaFreeHost(h_jobs);
         if (h_ctr) cudaFreeHost(h_ctr);  // d_ctr is in pb_owned
+        for (void* p : pd_owned) cudaFree(p);
+        if (d_nnjobs) cudaFree(d_nnjobs);
+        if (h_nnjobs) cudaFreeHost(h_nnjobs);
+        if (h_nrec) cudaFreeHost(h_nrec);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (stream) cudaStreamDestroy(stream);
@@ -132,6 +150,7 @@ void create_batch(pt_scene* const* scenes, int n, pt_batch* b) {
         launch_offset_i32(lprim + ol, S.light_prim, S.n_lights, ot, st);
         d2d(larea + ol, S.light_area, S.n_lights, st);
         pt_batch::Member m;
+        m.scene = scenes[i];
         m.root = s->n_tris > 0 ? (uint32_t)on : 0xffffffffu;
         m.light_off = ol;
         m.n_lights = S.n_lights;
@@ -163,6 +182,8 @@ void create_batch(pt_scene* const* scenes, int n, pt_batch* b) {
     A.cam = b->members[0].cam;  // unused by the batch kernels
     b->d_ctr = dalloc<WaveCounters>(b->pb_owned, 1);
     ck(cudaMallocHost(&b->h_ctr, sizeof(WaveCounters)), "cudaMallocHost");
+    b->d_nrec = dalloc<int>(b->owned, n);
+    ck(cudaMallocHost(&b->h_nrec, sizeof(int) * n), "cudaMallocHost");
     ck(cudaEventCreate(&b->ev0), "cudaEventCreate");
     ck(cudaEventCreate(&b->ev1), "cudaEventCreate");
     ck(cudaStreamSynchronize(st), "arena merge");
@@ -222,7 +243,7 @@ void ensure_buffers(pt_batch* b, int capacity, size_t film_n, int n_jobs) {
 }
 
 // Builds the job table; returns total work and total film pixels.
-void build_jobs(pt_batch* b, const pt_batch_job* jobs, int n_jobs, const pt_batch_tuning& t,
+void build_jobs(pt_batch* b, const pt_batch_job* jobs, int n_jobs, const pt_batch_tuning& t, int integrator,
                 std::vector<DevBatchJob>& out, unsigned long long* work, unsigned long long* pixels) {
     if (!jobs || n_jobs < 1) throw std::invalid_argument("a batch render needs at least one job");
     out.resize(n_jobs);
@@ -247,6 +268,7 @@ void build_jobs(pt_batch* b, const pt_batch_job* jobs, int n_jobs, const pt_batc
         d.max_depth = j.max_depth;
         d.rr_start = j.rr_start;
         d.seed = j.seed;
+        d.integrator = integrator;
         const bool tiles = m.width % t.tile_w == 0 && m.height % t.tile_h == 0;
         d.tile_w = tiles ? t.tile_w : 1;
         d.tile_h = tiles ? t.tile_h : 1;
@@ -261,11 +283,12 @@ void build_jobs(pt_batch* b, const pt_batch_job* jobs, int n_jobs, const pt_batc
 
 // Renders the jobs; d_dst[i] (device, 3 floats per pixel) receive the images,
 // or the batch's own output buffer when d_dst is null.
-void render_batch(pt_batch* b, const pt_batch_job* jobs, int n_jobs, float* const* d_dst, const pt_batch_tuning& t) {
+void render_batch(pt_batch* b, const pt_batch_job* jobs, int n_jobs, float* const* d_dst, const pt_batch_tuning& t,
+                  int integrator = kIntegratorMIS) {
     check_tuning(t);
     std::vector<DevBatchJob> table;
     unsigned long long total = 0, pixels = 0;
-    build_jobs(b, jobs, n_jobs, t, table, &total, &pixels);
+    build_jobs(b, jobs, n_jobs, t, integrator, table, &total, &pixels);
     const int capacity = (int)std::min<unsigned long long>(t.capacity, (total + 1023) / 1024 * 1024);
     ensure_buffers(b, capacity, 3 * pixels, n_jobs);
     cudaStream_t st = b->stream;
@@ -340,6 +363,215 @@ void render_batch(pt_batch* b, const pt_batch_job* jobs, int n_jobs, float* cons
     R.d2h_bytes = (double)(rounds * sizeof(WaveCounters));
 }
 
+// Per-path buffers of the slot wavefront, grown on demand.
+NNPathData slot_buffers(pt_batch* b, int capacity, int depth, bool params) {
+    if (capacity > b->pd_cap || depth > b->pd_depth || (params && !b->nn_params)) {
+        for (void* p : b->pd_owned) cudaFree(p);
+        b->pd_owned.clear();
+        b->pd = NNPathData{};
+        b->nn_params = nullptr;
+        b->pd_cap = std::max(capacity, b->pd_cap);
+        b->pd_depth = std::max(depth, b->pd_depth);
+        const int cap = b->pd_cap;
+        b->pd.vert = dalloc<float4>(b->pd_owned, (size_t)cap * std::max(1, b->pd_depth) * kNNVertFloat4);
+        b->pd.acc = dalloc<float4>(b->pd_owned, cap);
+        b->pd.slot_stack = dalloc<int>(b->pd_owned, cap);
+        b->pd.slot_job = dalloc<int>(b->pd_owned, cap);
+        b->pd.fin = dalloc<int4>(b->pd_owned, cap);
+        if (params) b->nn_params = dalloc<float4>(b->pd_owned, (size_t)cap * 11);
+    }
+    return b->pd;
+}
+
+// The jobs on the slot wavefront (nn.cu): PT + NEE + MIS with each job's
+// scene's learned guide (guided; trained online from the batch's paths
+// unless PT_FLAG_NN_FREEZE, each scene's network on its own records), or the
+// same estimator with BSDF sampling alone (PT_FLAG_UNBIASED_MIS).  Each
+// job's image equals pt_render of its scene with the same parameters and
+// mode when the guides are frozen (training order depends on the batch).
+void render_batch_slot(pt_batch* b, const pt_batch_job* jobs, int n_jobs, float* const* d_dst,
+                       const pt_batch_tuning& t, bool guided, uint32_t flags) {
+    check_tuning(t);
+    if (n_jobs > kNNMaxJobs) throw Fail(PT_ERR_LIMIT, "the slot wavefront takes at most 32768 jobs");
+    const bool train = guided && !(flags & PT_FLAG_NN_FREEZE);
+    std::vector<DevBatchJob> table;
+    unsigned long long total = 0, pixels = 0;
+    build_jobs(b, jobs, n_jobs, t, kIntegratorMIS, table, &total, &pixels);
+    int max_depth = 1;
+    for (const DevBatchJob& j : table) max_depth = std::max(max_depth, j.max_depth);
+    const int capacity = (int)std::min<unsigned long long>(t.capacity, (total + 1023) / 1024 * 1024);
+    ensure_buffers(b, capacity, 3 * pixels, n_jobs);
+    cudaStream_t st = b->stream;
+    const int n_members = (int)b->members.size();
+    std::vector<char> used(n_members, 0);
+    for (int i = 0; i < n_jobs; i++) used[jobs[i].scene] = 1;
+    std::vector<int> cap(n_members, 0);
+    int max_cap = 0;
+    if (guided)
+        for (int m = 0; m < n_members; m++) {
+            if (!used[m]) continue;
+            pt_scene* s = b->members[m].scene;
+            nn_ensure_scene(s);
+            cap[m] = train ? nn_record_cap(s) : 0;
+            max_cap = std::max(max_cap, cap[m]);
+        }
+    NNPathData PD = slot_buffers(b, capacity, train ? max_depth : 0, guided);
+    PD.rec_cap = max_cap;
+    if (b->nnjobs_cap < n_jobs) {
+        if (b->d_nnjobs) cudaFree(b->d_nnjobs);
+        if (b->h_nnjobs) cudaFreeHost(b->h_nnjobs);
+        b->d_nnjobs = nullptr;
+        b->h_nnjobs = nullptr;
+        ck(cudaMalloc(&b->d_nnjobs, sizeof(DevNNJob) * n_jobs), "cudaMalloc guide jobs");
+        ck(cudaMallocHost(&b->h_nnjobs, sizeof(DevNNJob) * n_jobs), "cudaMallocHost guide jobs");
+        b->nnjobs_cap = n_jobs;
+    }
+    for (int i = 0; i < n_jobs; i++) {
+        const int m = jobs[i].scene;
+        DevNNJob& nj = b->h_nnjobs[i];
+        nj = DevNNJob{};
+        nj.n_rec = b->d_nrec + m;
+        if (!guided) continue;
+        pt_scene* s = b->members[m].scene;
+        const NNNorm N = nn_scene_norm(s);
+        nj.wt = s->nnw.wt;
+        for (int k = 0; k < 3; k++) {
+            nj.lo[k] = N.lo[k];
+            nj.inv_ext[k] = N.inv_ext[k];
+        }
+        nj.c_lo = N.c_lo;
+        nj.c_hi = N.c_hi;
+        nj.rec = train ? s->nn_rec : nullptr;
+        nj.rec_cap = cap[m];
+    }
+    for (int m = 0; m < n_members; m++) b->h_nrec[m] = train && used[m] ? b->members[m].scene->nn_rec_count : 0;
+    std::memcpy(b->h_jobs, table.data(), sizeof(DevBatchJob) * n_jobs);
+    ck(cudaMemcpyAsync(b->d_jobs, b->h_jobs, sizeof(DevBatchJob) * n_jobs, cudaMemcpyHostToDevice, st), "jobs");
+    ck(cudaMemcpyAsync(b->d_nnjobs, b->h_nnjobs, sizeof(DevNNJob) * n_jobs, cudaMemcpyHostToDevice, st),
+       "guide jobs");
+    ck(cudaMemcpyAsync(b->d_nrec, b->h_nrec, sizeof(int) * n_members, cudaMemcpyHostToDevice, st), "records");
+    RenderParams P{};
+    P.max_depth = max_depth;  // vertex-record stride of a slot
+    P.flags = flags;
+    ck(cudaEventRecord(b->ev0, st), "event");
+    ck(cudaMemsetAsync(b->film, 0, sizeof(unsigned long long) * 3 * pixels, st), "memset film");
+    launch_init_slots(PD.slot_stack, capacity, st);
+    WaveCounters init{};
+    init.work_total = total;
+    init.free_top = capacity;
+    *b->h_ctr = init;
+    ck(cudaMemcpyAsync(b->d_ctr, b->h_ctr, sizeof(WaveCounters), cudaMemcpyHostToDevice, st), "init counters");
+    launch_nn_generate(b->arena, b->pb, 1, b->d_ctr, PD, b->d_jobs, n_jobs, st);  // fills buffer 0
+    const unsigned long long max_rounds =
+        64 + (total / (unsigned long long)capacity + 2 + (unsigned long long)n_jobs) *
+                 (unsigned long long)(max_depth + 2) * 4 / (unsigned long long)t.iters_per_graph;
+    std::vector<int> left(n_members, -1);  // records kept after a scene's last training round (-1: none)
+    double launches = 5;
+    unsigned long long rounds = 0;
+    while (true) {
+        for (int k = 0; k < t.iters_per_graph; k++) {
+            const int cur = k & 1;
+            launch_extend(b->arena, b->pb, cur, b->d_ctr, b->num_sms, st);
+            if (guided) launch_nn_infer(b->arena, b->pb, cur, b->d_ctr, b->d_nnjobs, b->nn_params, b->num_sms, st);
+            launch_nn_shade(b->arena, b->pb, cur, P, b->d_ctr, b->film, b->nn_params, PD, guided, b->d_jobs, st);
+            launch_nn_shadow(b->arena, b->pb, b->d_ctr, b->film, PD, b->d_jobs, b->num_sms, st);
+            launch_nn_finish(PD, b->d_ctr, b->d_nnjobs, max_depth, capacity, st);
+            launch_nn_generate(b->arena, b->pb, cur, b->d_ctr, PD, b->d_jobs, n_jobs, st);
+            launches += guided ? 7 : 6;
+        }
+        ck(cudaMemcpyAsync(b->h_ctr, b->d_ctr, sizeof(WaveCounters), cudaMemcpyDeviceToHost, st), "read counters");
+        if (train)
+            ck(cudaMemcpyAsync(b->h_nrec, b->d_nrec, sizeof(int) * n_members, cudaMemcpyDeviceToHost, st),
+               "read records");
+        ck(cudaStreamSynchronize(st), "batch render");
+        const uint32_t status = b->h_ctr->status;
+        if (status & kStatusStackOverflow) throw Fail(PT_ERR_LIMIT, "traversal stack overflow");
+        if (status & kStatusIterLimit) throw Fail(PT_ERR_LIMIT, "traversal step limit reached");
+        if (status & kStatusQueueOverflow) throw Fail(PT_ERR_LIMIT, "wavefront queue overflow");
+        if (status & kStatusTensorTimeout) throw Fail(PT_ERR_CUDA, "tensor-core completion wait timed out");
+        if (status) throw Fail(PT_ERR_CUDA, "batch render reported an error status");
+        if (train)
+            for (int m = 0; m < n_members; m++) {
+                left[m] = -1;
+                if (!used[m]) continue;
+                pt_scene* s = b->members[m].scene;
+                if (b->h_nrec[m] >= s->nn_cfg.batch)
+                    left[m] = nn_train_scene_round(s, b->h_nrec[m], cap[m], b->d_nrec + m, st, &launches);
+            }
+        rounds++;
+        if (b->h_ctr->n_cur == 0 && b->h_ctr->work_next >= b->h_ctr->work_total) break;
+        if (rounds > max_rounds) throw Fail(PT_ERR_LIMIT, "batch render did not converge within the iteration bound");
+    }
+    if (train)
+        for (int m = 0; m < n_members; m++)
+            if (used[m])
+                b->members[m].scene->nn_rec_count = left[m] >= 0 ? left[m] : std::min(b->h_nrec[m], cap[m]);
+    for (int i = 0; i < n_jobs; i++) {
+        const pt_batch::Member& m = b->members[jobs[i].scene];
+        const size_t off = 3 * (size_t)table[i].film_off;
+        float* dst = (d_dst && d_dst[i]) ? d_dst[i] : b->d_out + off;
+        launch_film_resolve(b->film + off, dst, 3 * m.width * m.height, 1.0 / (double)jobs[i].spp, st);
+        launches += 1;
+    }
+    ck(cudaEventRecord(b->ev1, st), "event");
+    ck(cudaStreamSynchronize(st), "batch render");
+    ck(cudaGetLastError(), "batch kernels");
+    float ms = 0;
+    ck(cudaEventElapsedTime(&ms, b->ev0, b->ev1), "elapsed");
+    pt_render_stats& R = b->stats;
+    R = pt_render_stats{};
+    R.paths = (double)b->h_ctr->stat_paths;
+    R.closest_rays = (double)b->h_ctr->stat_closest;
+    R.shadow_rays = (double)b->h_ctr->stat_shadow;
+    R.iterations = (double)b->h_ctr->stat_iters;
+    R.render_ms = ms;
+    R.kernel_launches = launches;
+    R.nonfinite = (double)b->h_ctr->stat_nonfinite;
+    R.h2d_bytes = (double)(sizeof(WaveCounters) + (sizeof(DevBatchJob) + sizeof(DevNNJob)) * n_jobs +
+                           sizeof(int) * n_members);
+    R.d2h_bytes = (double)(rounds * (sizeof(WaveCounters) + (train ? sizeof(int) * n_members : 0)));
+}
+
+// Dispatch on the render mode (as pt_render's modes, without the SD-tree).
+void render_batch_mode(pt_batch* b, const pt_batch_job* jobs, int n_jobs, float* const* d_dst, int32_t mode,
+                       uint32_t flags) {
+    if (mode == PT_MODE_NN) {
+        if (flags & ~(PT_FLAG_NN_FREEZE | PT_FLAG_UNBIASED_MIS | PT_FLAG_THROUGHPUT_RR))
+            throw Fail(PT_ERR_INVALID, "unsupported flags for the learned-guide render");
+        render_batch_slot(b, jobs, n_jobs, d_dst, b->tuning, true, flags);
+        return;
+    }
+    if (mode == PT_MODE_MIS && (flags & PT_FLAG_UNBIASED_MIS)) {
+        if (flags & ~(PT_FLAG_UNBIASED_MIS | PT_FLAG_THROUGHPUT_RR))
+            throw Fail(PT_ERR_INVALID, "PT_FLAG_UNBIASED_MIS combines only with PT_FLAG_THROUGHPUT_RR");
+        render_batch_slot(b, jobs, n_jobs, d_dst, b->tuning, false, flags);
+        return;
+    }
+    if (flags != 0) throw Fail(PT_ERR_INVALID, "unsupported flags for a batch render in this mode");
+    if (mode == PT_MODE_SDTREE) throw Fail(PT_ERR_INVALID, "the SD-tree guide does not render in batches");
+    if (mode != PT_MODE_MIS && mode != PT_MODE_NEE && mode != PT_MODE_PT) throw Fail(PT_ERR_INVALID, "unknown render mode");
+    render_batch(b, jobs, n_jobs, d_dst, b->tuning,
+                 mode == PT_MODE_NEE ? kIntegratorNEE : mode == PT_MODE_PT ? kIntegratorPT : kIntegratorMIS);
+}
+
+// Copies the batch's own output images to host buffers (null entries skipped).
+void copy_out(pt_batch* b, const pt_batch_job* jobs, int n_jobs, float* const* rgb_out) {
+    if (!rgb_out) return;
+    size_t off = 0, bytes = 0;
+    for (int i = 0; i < n_jobs; i++) {
+        const pt_batch::Member& m = b->members[jobs[i].scene];
+        const size_t n = 3 * (size_t)m.width * m.height;
+        if (rgb_out[i]) {
+            ck(cudaMemcpyAsync(rgb_out[i], b->d_out + off, sizeof(float) * n, cudaMemcpyDeviceToHost, b->stream),
+               "copy image");
+            bytes += sizeof(float) * n;
+        }
+        off += n;
+    }
+    ck(cudaStreamSynchronize(b->stream), "copy images");
+    b->stats.d2h_bytes += (double)bytes;
+}
+
 }  // namespace
 
 pt_status pt_batch_create(pt_scene* const* scenes, int32_t n_scenes, pt_batch** out) {
@@ -364,21 +596,23 @@ pt_status pt_batch_render(pt_batch* b, const pt_batch_job* jobs, int32_t n_jobs,
     if (!b) { g_error = "null batch"; return PT_ERR_INVALID; }
     return guarded([&] {
         render_batch(b, jobs, n_jobs, nullptr, b->tuning);
-        if (!rgb_out) return;
-        size_t off = 0, bytes = 0;
-        for (int i = 0; i < n_jobs; i++) {
-            const pt_batch::Member& m = b->members[jobs[i].scene];
-            const size_t n = 3 * (size_t)m.width * m.height;
-            if (rgb_out[i]) {
-                ck(cudaMemcpyAsync(rgb_out[i], b->d_out + off, sizeof(float) * n, cudaMemcpyDeviceToHost, b->stream),
-                   "copy image");
-                bytes += sizeof(float) * n;
-            }
-            off += n;
-        }
-        ck(cudaStreamSynchronize(b->stream), "copy images");
-        b->stats.d2h_bytes += (double)bytes;
+        copy_out(b, jobs, n_jobs, rgb_out);
     });
+}
+
+pt_status pt_batch_render_ex(pt_batch* b, const pt_batch_job* jobs, int32_t n_jobs, int32_t mode, uint32_t flags,
+                             float* const* rgb_out) {
+    if (!b) { g_error = "null batch"; return PT_ERR_INVALID; }
+    return guarded([&] {
+        render_batch_mode(b, jobs, n_jobs, nullptr, mode, flags);
+        copy_out(b, jobs, n_jobs, rgb_out);
+    });
+}
+
+pt_status pt_batch_render_ex_device(pt_batch* b, const pt_batch_job* jobs, int32_t n_jobs, int32_t mode,
+                                    uint32_t flags, float* const* d_rgb_out) {
+    if (!b) { g_error = "null batch"; return PT_ERR_INVALID; }
+    return guarded([&] { render_batch_mode(b, jobs, n_jobs, d_rgb_out, mode, flags); });
 }
 
 pt_status pt_batch_set_tuning(pt_batch* b, const pt_batch_tuning* t) {

@@ -236,6 +236,20 @@ pt_status pt_batch_create(pt_scene* const* scenes, int32_t n_scenes, pt_batch** 
 void pt_batch_destroy(pt_batch* batch);
 pt_status pt_batch_render(pt_batch* batch, const pt_batch_job* jobs, int32_t n_jobs, float* const* rgb_out);
 pt_status pt_batch_render_device(pt_batch* batch, const pt_batch_job* jobs, int32_t n_jobs, float* const* d_rgb_out);
+/* pt_batch_render with a render mode and flags as pt_render_desc (all
+ * modes but PT_MODE_SDTREE).  PT_MODE_NN: every job is guided by its scene's
+ * own learned guide (pt_nn_configure / pt_nn_reset / pt_nn_stats of that
+ * scene), and each scene's guide trains online on the records of that
+ * scene's paths unless PT_FLAG_NN_FREEZE; PT_MODE_MIS with
+ * PT_FLAG_UNBIASED_MIS: the same estimator with BSDF sampling only.  With
+ * frozen guides each job's image is bit-identical to pt_render of the same
+ * scene, mode and flags.  PT_MODE_NN needs the scenes the batch was made
+ * from to be alive (the guides live in them).  Replaces nothing in the
+ * reference (it renders one scene at a time). */
+pt_status pt_batch_render_ex(pt_batch* batch, const pt_batch_job* jobs, int32_t n_jobs, int32_t mode, uint32_t flags,
+                             float* const* rgb_out);
+pt_status pt_batch_render_ex_device(pt_batch* batch, const pt_batch_job* jobs, int32_t n_jobs, int32_t mode,
+                                    uint32_t flags, float* const* d_rgb_out);
 pt_status pt_batch_set_tuning(pt_batch* batch, const pt_batch_tuning* tuning);
 pt_status pt_batch_get_tuning(pt_batch* batch, pt_batch_tuning* tuning);
 /* Statistics of the last batch render (paths, rays, time; per batch). */

@@ -85,6 +85,74 @@ def test_device_outputs(members):
         assert np.array_equal(o.cpu().numpy().view(np.uint32), unbatched(members, j).view(np.uint32))
 
 
+def test_batch_modes_match_unbatched(members):
+    """The other integrators (PT_MODE_NEE, PT_MODE_PT) and the slot
+    wavefront's unbiased MIS estimator, batched, bit-identical to pt_render."""
+    from cpppt.lib import FLAG_THROUGHPUT_RR, FLAG_UNBIASED_MIS, MODE_MIS, MODE_NEE, MODE_PT, GpuBatch
+    b = GpuBatch(members)
+    for mode, flags in [(MODE_NEE, 0), (MODE_PT, 0), (MODE_MIS, FLAG_UNBIASED_MIS),
+                        (MODE_MIS, FLAG_UNBIASED_MIS | FLAG_THROUGHPUT_RR)]:
+        imgs = b.render(JOBS, mode=mode, flags=flags)
+        for j, img in zip(JOBS, imgs):
+            ref = members[j["scene"]].render(j["spp"], max_depth=j.get("max_depth", 32),
+                                             rr_start=j.get("rr_start", 3), seed=j.get("seed", 0), mode=mode,
+                                             flags=flags)
+            assert np.array_equal(img.view(np.uint32), ref.view(np.uint32)), (mode, flags, j)
+
+
+@pytest.fixture(scope="module")
+def guided(gpu_lib):
+    """Three scenes, each with its own learned guide, trained a little by
+    single-scene renders (batch of 1024 records, so small renders train)."""
+    from cpppt import scenes
+    from cpppt.lib import MODE_NN, GpuScene
+    scs = [scenes.slit_room(seed=4, n_boxes=20, box_subdiv=2, width=32, height=16),
+           scenes.slit_room(seed=5, n_boxes=40, box_subdiv=2, width=24, height=24),
+           scenes.cornell(16, 16)]
+    gs = [GpuScene(s) for s in scs]
+    for k, g in enumerate(gs):
+        g.nn_reset(100 + k)
+        g.nn_configure(**{**g.nn_config(), "batch": 1024})
+        for r in range(4):
+            g.render(16, max_depth=8, seed=50 + r, mode=MODE_NN)
+        assert g.nn_stats()["steps"] > 0
+    return gs
+
+
+GUIDED_JOBS = [dict(scene=0, spp=16, max_depth=8, seed=1), dict(scene=2, spp=9, max_depth=6, seed=2),
+               dict(scene=1, spp=4, max_depth=12, seed=3), dict(scene=0, spp=5, max_depth=3, seed=4)]
+
+
+def test_frozen_guides_batched_bit_exact(guided):
+    """Every job is guided by its own scene's network: with the guides frozen
+    the batched images equal the single-scene guided renders bit for bit."""
+    from cpppt.lib import FLAG_NN_FREEZE, FLAG_THROUGHPUT_RR, MODE_NN, GpuBatch
+    b = GpuBatch(guided)
+    for flags in (FLAG_NN_FREEZE, FLAG_NN_FREEZE | FLAG_THROUGHPUT_RR):
+        imgs = b.render(GUIDED_JOBS, mode=MODE_NN, flags=flags)
+        for j, img in zip(GUIDED_JOBS, imgs):
+            ref = guided[j["scene"]].render(j["spp"], max_depth=j["max_depth"], seed=j["seed"], mode=MODE_NN,
+                                            flags=flags)
+            assert np.isfinite(img).all() and img.mean() > 0
+            assert np.array_equal(img.view(np.uint32), ref.view(np.uint32)), (flags, j)
+
+
+def test_batch_trains_each_scene_guide(guided):
+    """An unfrozen batched render trains the guide of every scene it
+    renders, on that scene's records, and leaves the others alone."""
+    from cpppt.lib import MODE_NN, GpuBatch
+    b = GpuBatch(guided)
+    w0 = [g.nn_weights().copy() for g in guided]
+    s0 = [g.nn_stats()["steps"] for g in guided]
+    jobs = [dict(scene=0, spp=32, max_depth=8, seed=7), dict(scene=2, spp=32, max_depth=8, seed=8)]
+    imgs = b.render(jobs, mode=MODE_NN)
+    assert all(np.isfinite(x).all() and x.mean() > 0 for x in imgs)
+    for k, g in enumerate(guided):
+        trained = k in (0, 2)
+        assert (g.nn_stats()["steps"] > s0[k]) == trained, k
+        assert (not np.array_equal(g.nn_weights(), w0[k])) == trained, k
+
+
 def test_batch_errors(members):
     from cpppt.lib import GpuBatch, PtError
     b = GpuBatch(members)
@@ -96,4 +164,13 @@ def test_batch_errors(members):
         b.set_tuning(capacity=1000)
     with pytest.raises(PtError):
         b.set_tuning(iters_per_graph=3)
+    from cpppt.lib import FLAG_NN_FREEZE, FLAG_UNBIASED_MIS, MODE_MIS, MODE_NEE, MODE_SDTREE
+    with pytest.raises(PtError):
+        b.render([dict(scene=0, spp=1)], mode=MODE_SDTREE)
+    with pytest.raises(PtError):
+        b.render([dict(scene=0, spp=1)], mode=MODE_NEE, flags=FLAG_UNBIASED_MIS)
+    with pytest.raises(PtError):
+        b.render([dict(scene=0, spp=1)], mode=MODE_MIS, flags=FLAG_UNBIASED_MIS | FLAG_NN_FREEZE)
+    with pytest.raises(PtError):
+        b.render([dict(scene=0, spp=1)], mode=99)
     b.render([dict(scene=0, spp=1)])  # still usable
