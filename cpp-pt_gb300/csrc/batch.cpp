@@ -64,6 +64,8 @@ struct pt_batch {
     int nnjobs_cap = 0;
     int* d_nrec = nullptr;  // one per member scene (in `owned`)
     int* h_nrec = nullptr;  // pinned
+    NNTrainTask* d_tasks = nullptr;  // fused training steps: 16 per member scene (in `owned`)
+    NNTrainTask* h_tasks = nullptr;  // pinned
 
     ~pt_batch() {
         if (stream) cudaStreamSynchronize(stream);
@@ -79,6 +81,7 @@ struct pt_batch {
         if (d_nnjobs) cudaFree(d_nnjobs);
         if (h_nnjobs) cudaFreeHost(h_nnjobs);
         if (h_nrec) cudaFreeHost(h_nrec);
+        if (h_tasks) cudaFreeHost(h_tasks);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (stream) cudaStreamDestroy(stream);
@@ -184,6 +187,8 @@ void create_batch(pt_scene* const* scenes, int n, pt_batch* b) {
     ck(cudaMallocHost(&b->h_ctr, sizeof(WaveCounters)), "cudaMallocHost");
     b->d_nrec = dalloc<int>(b->owned, n);
     ck(cudaMallocHost(&b->h_nrec, sizeof(int) * n), "cudaMallocHost");
+    b->d_tasks = dalloc<NNTrainTask>(b->owned, (size_t)n * 16);
+    ck(cudaMallocHost(&b->h_tasks, sizeof(NNTrainTask) * n * 16), "cudaMallocHost");
     ck(cudaEventCreate(&b->ev0), "cudaEventCreate");
     ck(cudaEventCreate(&b->ev1), "cudaEventCreate");
     ck(cudaStreamSynchronize(st), "arena merge");
@@ -490,14 +495,17 @@ void render_batch_slot(pt_batch* b, const pt_batch_job* jobs, int n_jobs, float*
         if (status & kStatusQueueOverflow) throw Fail(PT_ERR_LIMIT, "wavefront queue overflow");
         if (status & kStatusTensorTimeout) throw Fail(PT_ERR_CUDA, "tensor-core completion wait timed out");
         if (status) throw Fail(PT_ERR_CUDA, "batch render reported an error status");
-        if (train)
+        if (train) {
+            // every scene with a full batch of records trains, all in the same fused steps
+            std::vector<pt_scene*> sc(n_members, nullptr);
+            std::vector<int*> d_count(n_members);
             for (int m = 0; m < n_members; m++) {
-                left[m] = -1;
-                if (!used[m]) continue;
-                pt_scene* s = b->members[m].scene;
-                if (b->h_nrec[m] >= s->nn_cfg.batch)
-                    left[m] = nn_train_scene_round(s, b->h_nrec[m], cap[m], b->d_nrec + m, st, &launches);
+                if (used[m]) sc[m] = b->members[m].scene;
+                d_count[m] = b->d_nrec + m;
             }
+            nn_train_scenes(sc.data(), b->h_nrec, cap.data(), d_count.data(), n_members, b->d_tasks, b->h_tasks,
+                            b->num_sms, st, &launches, left.data());
+        }
         rounds++;
         if (b->h_ctr->n_cur == 0 && b->h_ctr->work_next >= b->h_ctr->work_total) break;
         if (rounds > max_rounds) throw Fail(PT_ERR_LIMIT, "batch render did not converge within the iteration bound");

@@ -452,6 +452,9 @@ void nn_ensure(pt_scene* s) {
     s->nn_rec = dalloc<float4>(s->nn_owned, (size_t)kNNRecordCap * 4);
     s->nn_rec_count = 0;
     if (!s->h_rec_left) ck(cudaMallocHost(&s->h_rec_left, sizeof(int)), "cudaMallocHost");
+    if (!s->h_scal) ck(cudaMallocHost(&s->h_scal, sizeof(float) * 4), "cudaMallocHost");
+    if (!s->h_tasks) ck(cudaMallocHost(&s->h_tasks, sizeof(NNTrainTask) * kNNMaxStepsPerRound), "cudaMallocHost");
+    s->d_tasks = dalloc<NNTrainTask>(s->nn_owned, kNNMaxStepsPerRound);
     std::vector<float> w = nn_random_weights(12345u);
     nn_upload(s->nnw, w.data(), s->stream);
     ck(cudaStreamSynchronize(s->stream), "nn init");
@@ -494,42 +497,78 @@ NNPathData nn_path_buffers(pt_scene* s, int capacity, int depth) {
     return s->nnpd;
 }
 
-// One training round of a scene's guide: as many Adam steps as full batches
-// were recorded (each on its own records; `held` = records counted so far,
-// at most cap of them written); records beyond the last full batch move to
-// the front of the buffer and *d_count is set to their number, which is
-// returned.  Synchronises the stream (reads the step's loss and status).
-int nn_train_round(pt_scene* s, int held, int cap, int* d_count, cudaStream_t st, double* launches) {
-    const int batch = s->nn_cfg.batch;
-    held = std::min(held, cap);
-    const int steps = held / batch;
-    NNAdam opt;
-    opt.lr = s->nn_cfg.learning_rate;
-    const NNNorm N = scene_norm(s);
-    for (int k = 0; k < steps; k++) {
-        float4* r = s->nn_rec + (size_t)4 * k * batch;
-        ck(cudaMemsetAsync(s->nn_scalars, 0, sizeof(float) * 4, st), "memset");
-        if (s->nn_cfg.divergence == PT_NN_CHI2) launch_square_T(r, batch, st);
-        launch_sum_T(r, batch, s->nn_scalars + 1, st);
-        launch_nn_train_step(s->nnw, N, r, batch, s->nn_scalars + 1, s->nn_tb, s->nn_grad, s->nn_scalars, opt,
-                             ++s->nn_steps, s->num_sms, st, true);
+// Training rounds of one or several scenes' guides (declared in
+// host_internal.h): every scene's step j runs in the same fused launch.
+void train_scenes(pt_scene* const* sc, const int* held, const int* caps, int* const* d_count, int n,
+                  NNTrainTask* d_tasks, NNTrainTask* h_tasks, int num_sms, cudaStream_t st, double* launches,
+                  int* left) {
+    const NNAdam opt;
+    std::vector<int> steps(n, 0);
+    int max_steps = 0;
+    for (int k = 0; k < n; k++) {
+        left[k] = -1;
+        if (!sc[k]) continue;
+        steps[k] = std::min(held[k], caps[k]) / sc[k]->nn_cfg.batch;
+        max_steps = std::max(max_steps, steps[k]);
+    }
+    if (max_steps == 0) return;
+    // task table: step level j holds the scenes with more than j steps
+    std::vector<int> off(max_steps + 1, 0), max_n(max_steps, 0);
+    int t = 0;
+    for (int j = 0; j < max_steps; j++) {
+        off[j] = t;
+        for (int k = 0; k < n; k++) {
+            if (steps[k] <= j) continue;
+            pt_scene* s = sc[k];
+            NNTrainTask& T = h_tasks[t++];
+            T = NNTrainTask{};
+            T.W = s->nnw;
+            T.N = scene_norm(s);
+            T.rec = s->nn_rec + (size_t)4 * j * s->nn_cfg.batch;
+            T.n = s->nn_cfg.batch;
+            T.chi2 = s->nn_cfg.divergence == PT_NN_CHI2 ? 1 : 0;
+            T.scal = s->nn_scalars;
+            T.TB = s->nn_tb;
+            T.grad = s->nn_grad;
+            T.lr = s->nn_cfg.learning_rate;
+            const int step = s->nn_steps + j + 1;
+            T.bc1 = 1.0f - powf(opt.b1, (float)step);
+            T.bc2 = 1.0f - powf(opt.b2, (float)step);
+            max_n[j] = std::max(max_n[j], T.n);
+        }
+    }
+    off[max_steps] = t;
+    ck(cudaMemcpyAsync(d_tasks, h_tasks, sizeof(NNTrainTask) * t, cudaMemcpyHostToDevice, st), "training tasks");
+    for (int k = 0; k < n; k++)
+        if (steps[k] > 0) ck(cudaMemsetAsync(sc[k]->nn_scalars + 2, 0, sizeof(float), st), "memset status");
+    for (int j = 0; j < max_steps; j++) {
+        launch_nn_train_tasks(d_tasks + off[j], off[j + 1] - off[j], max_n[j], num_sms, st, true, true);
         if (launches) *launches += 5;
     }
-    const int left = held - steps * batch;
-    if (left > 0 && steps > 0)
-        ck(cudaMemcpyAsync(s->nn_rec, s->nn_rec + (size_t)4 * steps * batch, sizeof(float4) * 4 * left,
-                           cudaMemcpyDeviceToDevice, st), "keep records");
-    *s->h_rec_left = left;
-    ck(cudaMemcpyAsync(d_count, s->h_rec_left, sizeof(int), cudaMemcpyHostToDevice, st), "records");
-    float sc[4] = {0.f, 0.f, 0.f, 0.f};
-    ck(cudaMemcpyAsync(sc, s->nn_scalars, sizeof(sc), cudaMemcpyDeviceToHost, st), "copy");
+    for (int k = 0; k < n; k++) {
+        if (steps[k] == 0) continue;
+        pt_scene* s = sc[k];
+        const int batch = s->nn_cfg.batch;
+        const int kept = std::min(held[k], caps[k]) - steps[k] * batch;
+        if (kept > 0)
+            ck(cudaMemcpyAsync(s->nn_rec, s->nn_rec + (size_t)4 * steps[k] * batch, sizeof(float4) * 4 * kept,
+                               cudaMemcpyDeviceToDevice, st), "keep records");
+        *s->h_rec_left = kept;
+        ck(cudaMemcpyAsync(d_count[k], s->h_rec_left, sizeof(int), cudaMemcpyHostToDevice, st), "records");
+        ck(cudaMemcpyAsync(s->h_scal, s->nn_scalars, sizeof(float) * 4, cudaMemcpyDeviceToHost, st), "copy");
+        left[k] = kept;
+    }
     ck(cudaStreamSynchronize(st), "train");
-    uint32_t tstat;
-    std::memcpy(&tstat, &sc[2], sizeof(tstat));
-    check_status(s, tstat);
-    if (steps > 0) s->nn_last_loss = sc[0];
-    s->nn_records += (double)steps * batch;
-    return left;
+    for (int k = 0; k < n; k++) {
+        if (steps[k] == 0) continue;
+        pt_scene* s = sc[k];
+        uint32_t tstat;
+        std::memcpy(&tstat, &s->h_scal[2], sizeof(tstat));
+        check_status(s, tstat);
+        s->nn_steps += steps[k];
+        s->nn_last_loss = s->h_scal[0];
+        s->nn_records += (double)steps[k] * s->nn_cfg.batch;
+    }
 }
 
 // PT + NEE + MIS on the slot-based wavefront (nn.cu).  guided: the learned
@@ -603,7 +642,9 @@ void render_nn(pt_scene* s, const pt_render_desc* desc, float* d_dst, bool guide
         check_status(s, s->h_ctr->status);
         rec_left = -1;
         if (train && s->h_ctr->n_rec >= batch) {
-            rec_left = nn_train_round(s, s->h_ctr->n_rec, rec_cap, &s->d_ctr->n_rec, st, &launches);
+            int* d_count = &s->d_ctr->n_rec;
+            train_scenes(&s, &s->h_ctr->n_rec, &rec_cap, &d_count, 1, s->d_tasks, s->h_tasks, s->num_sms, st,
+                         &launches, &rec_left);
             records += (double)(std::min(s->h_ctr->n_rec, rec_cap) - rec_left);
         }
         if (s->h_ctr->n_cur == 0 && s->h_ctr->work_next >= s->h_ctr->work_total) break;
@@ -1178,8 +1219,10 @@ namespace hostimpl {
 void nn_ensure_scene(pt_scene* s) { nn_ensure(s); }
 NNNorm nn_scene_norm(const pt_scene* s) { return scene_norm(s); }
 int nn_record_cap(const pt_scene* s) { return std::min(kNNRecordCap, s->nn_cfg.steps_per_round * s->nn_cfg.batch); }
-int nn_train_scene_round(pt_scene* s, int held, int cap, int* d_count, cudaStream_t st, double* launches) {
-    return nn_train_round(s, held, cap, d_count, st, launches);
+void nn_train_scenes(pt_scene* const* scenes, const int* held, const int* caps, int* const* d_count, int n,
+                     NNTrainTask* d_tasks, NNTrainTask* h_tasks, int num_sms, cudaStream_t st, double* launches,
+                     int* left) {
+    train_scenes(scenes, held, caps, d_count, n, d_tasks, h_tasks, num_sms, st, launches, left);
 }
 void scene_check_status(pt_scene* s, uint32_t status) { check_status(s, status); }
 }  // namespace hostimpl
@@ -1463,8 +1506,17 @@ pt_status pt_debug_nn_grad(const float* weights, const float* lo, const float* h
         for (int i = 0; i < n; i++) tsum += records[16 * i + 13];
         const float sc0[4] = {0.f, (float)tsum, 0.f, 0.f};
         ck(cudaMemcpyAsync(scal, sc0, sizeof(sc0), cudaMemcpyHostToDevice, c.st), "copy");
-        NNAdam opt;
-        launch_nn_train_step(W, norm_from(lo, hi), drec, n, scal + 1, TB, grad, scal, opt, 1, c.sms, c.st, false);
+        NNTrainTask task{};
+        task.W = W;
+        task.N = norm_from(lo, hi);
+        task.rec = drec;
+        task.n = n;
+        task.scal = scal;
+        task.TB = TB;
+        task.grad = grad;
+        NNTrainTask* dtask = dalloc<NNTrainTask>(c.owned, 1);
+        ck(cudaMemcpyAsync(dtask, &task, sizeof(task), cudaMemcpyHostToDevice, c.st), "copy");
+        launch_nn_train_tasks(dtask, 1, n, c.sms, c.st, false, false);
         ck(cudaMemcpyAsync(out_grad, grad, sizeof(float) * kNNWeightCount, cudaMemcpyDeviceToHost, c.st), "copy");
         float sc[4] = {0.f, 0.f, 0.f, 0.f};
         ck(cudaMemcpyAsync(sc, scal, sizeof(sc), cudaMemcpyDeviceToHost, c.st), "copy");

@@ -133,7 +133,10 @@ struct pt_scene {
     NNWeights nnw{};
     NNTrainBuf nn_tb{};
     float* nn_grad = nullptr;
-    float* nn_scalars = nullptr;  // [0] loss, [1] sum of T
+    float* nn_scalars = nullptr;  // [0] loss, [1] sum of T, [2] status bits
+    float* h_scal = nullptr;      // pinned copy of nn_scalars
+    NNTrainTask* d_tasks = nullptr;  // training task table (one per step of a round)
+    NNTrainTask* h_tasks = nullptr;  // pinned
     int nn_steps = 0;
     double nn_last_loss = 0, nn_records = 0;
     float4* nn_rec = nullptr;  // training records carried across renders
@@ -158,6 +161,8 @@ struct pt_scene {
         if (h_job) cudaFreeHost(h_job);
         if (h_nnjob) cudaFreeHost(h_nnjob);
         if (h_rec_left) cudaFreeHost(h_rec_left);
+        if (h_scal) cudaFreeHost(h_scal);
+        if (h_tasks) cudaFreeHost(h_tasks);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (stream) cudaStreamDestroy(stream);
@@ -170,9 +175,16 @@ namespace hostimpl {
 void nn_ensure_scene(pt_scene* s);               // network, Adam state, record and training buffers
 NNNorm nn_scene_norm(const pt_scene* s);         // position normalisation and BSDF-fraction range
 int nn_record_cap(const pt_scene* s);            // records collected per round (steps_per_round batches)
-// Trains on the scene's `held` records (at most cap written) and sets
-// *d_count to the records kept; returns that number.  Synchronises st.
-int nn_train_scene_round(pt_scene* s, int held, int cap, int* d_count, cudaStream_t st, double* launches);
+// One training round of several scenes' guides.  Scene k counted held[k]
+// records this round (at most caps[k] of them written); it takes as many
+// Adam steps as it holds full batches, the steps of all scenes fused per
+// step (d_tasks / h_tasks: room for n * 16 task entries); records beyond
+// the last full batch move to the front of its buffer and *d_count[k]
+// receives their number, as does left[k] (-1: no full batch, nothing
+// changed).  Synchronises st once.
+void nn_train_scenes(pt_scene* const* scenes, const int* held, const int* caps, int* const* d_count, int n,
+                     NNTrainTask* d_tasks, NNTrainTask* h_tasks, int num_sms, cudaStream_t st, double* launches,
+                     int* left);
 void scene_check_status(pt_scene* s, uint32_t status);  // throws on kernel status bits
 }  // namespace hostimpl
 }  // namespace cpppt_gb300

@@ -346,10 +346,17 @@ __device__ __forceinline__ void store_row_bf16(__nv_bfloat16* dst, const float* 
 
 constexpr int kNNThreads = 128;
 
-__global__ void __launch_bounds__(kTcRows) k_nn_train_fb(NNWeights W, NNNorm N, const float4* __restrict__ rec, int n,
-                                                         const float* __restrict__ tsum, NNTrainBuf TB,
-                                                         float* __restrict__ loss_out, uint32_t* status) {
+// blockIdx.y: the network (task) of a fused multi-network step.
+__global__ void __launch_bounds__(kTcRows) k_nn_train_fb(const NNTrainTask* __restrict__ tasks) {
     extern __shared__ __align__(1024) unsigned char smem[];
+    const NNTrainTask& task = tasks[blockIdx.y];
+    const NNWeights W = task.W;
+    const NNNorm N = task.N;
+    const NNTrainBuf TB = task.TB;
+    const float4* __restrict__ rec = task.rec;
+    const int n = task.n;
+    float* loss_out = task.scal;
+    uint32_t* status = reinterpret_cast<uint32_t*>(task.scal + 2);
     unsigned char* s_wf = smem;                                  // forward B tiles: W_l^T (out x in)
     unsigned char* s_wb = smem + kNNLayers * kTcWLayerBytes;     // backward B tiles: W_l (in x out)
     unsigned char* s_a = smem + 2 * kNNLayers * kTcWLayerBytes;  // A tile: activations, then output gradients
@@ -366,7 +373,8 @@ __global__ void __launch_bounds__(kTcRows) k_nn_train_fb(NNWeights W, NNNorm N, 
     uint32_t phase = 0;
     bool ok = true;
     float loss_acc = 0.f;
-    const float inv_tsum = *tsum > 0.f ? 1.0f / *tsum : 0.f;
+    const float tsum = task.scal[1];
+    const float inv_tsum = tsum > 0.f ? 1.0f / tsum : 0.f;
     for (int base = blockIdx.x * kTcRows; base < n && ok; base += gridDim.x * kTcRows) {
         const int i = base + row;
         const bool valid = i < n;
@@ -436,16 +444,21 @@ __global__ void __launch_bounds__(kTcRows) k_nn_train_fb(NNWeights W, NNNorm N, 
     tc_end(ok, tmem, bar, phase, status);
     float ls = loss_acc;
     for (int o = 16; o > 0; o >>= 1) ls += __shfl_xor_sync(0xffffffffu, ls, o);
-    if (loss_out && lane == 0) atomicAdd(loss_out, ls);
+    if (lane == 0) atomicAdd(loss_out, ls);
 }
 
 // dW_l = A_l^T dZ_l over the batch: one CTA reduces a slice of rows into a
 // 64 x out_l tile with mma (A^T fragments read transposed from smem), then
 // adds it to the FP32 gradient.  blockIdx.y = layer.
 constexpr int kWGRows = 64;
-__global__ void __launch_bounds__(kNNThreads) k_nn_wgrad(NNTrainBuf TB, int n, float* __restrict__ grad) {
+// blockIdx.z: the network (task).
+__global__ void __launch_bounds__(kNNThreads) k_nn_wgrad(const NNTrainTask* __restrict__ tasks) {
     __shared__ __align__(16) __nv_bfloat16 sA[kWGRows][72];
     __shared__ __align__(16) __nv_bfloat16 sG[kWGRows][72];
+    const NNTrainTask& task = tasks[blockIdx.z];
+    const NNTrainBuf TB = task.TB;
+    const int n = task.n;
+    float* __restrict__ grad = task.grad;
     const int l = blockIdx.y;
     const int nout = nn_layer_out(l);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, g = lane >> 2, t = lane & 3;
@@ -503,10 +516,14 @@ __global__ void __launch_bounds__(kNNThreads) k_nn_wgrad(NNTrainBuf TB, int n, f
 
 // Adam (Kingma & Ba 2015) on the FP32 master weights; refreshes the two
 // BF16 copies the kernels read.
-__global__ void k_nn_adam(NNWeights W, const float* __restrict__ grad, float lr, float b1, float b2, float eps,
-                          float bc1, float bc2, float clip) {
+// blockIdx.y: the network (task); learning rate and bias corrections are the task's.
+__global__ void k_nn_adam(const NNTrainTask* __restrict__ tasks, float b1, float b2, float eps, float clip) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kNNWeights) return;
+    const NNTrainTask& task = tasks[blockIdx.y];
+    const NNWeights W = task.W;
+    const float* __restrict__ grad = task.grad;
+    const float lr = task.lr, bc1 = task.bc1, bc2 = task.bc2;
     float gi = grad[i];
     gi = fminf(fmaxf(gi, -clip), clip);
     const float m = b1 * W.m[i] + (1.0f - b1) * gi;
@@ -562,21 +579,52 @@ void launch_nn_infer(const DevScene& S, const PathBuffers& B, int cur, WaveCount
     // four CTAs of 128 threads per SM fit in shared memory (48 KB each)
     k_nn_infer<<<num_sms * 4, kTcInferThreads, nn_smem_infer(), st>>>(S, B, cur, ctr, nnj, params);
 }
-void launch_nn_train_step(const NNWeights& W, const NNNorm& N, const float4* rec, int n, const float* tsum,
-                          const NNTrainBuf& TB, float* grad, float* loss, const NNAdam& opt, int step, int num_sms,
-                          cudaStream_t st, bool apply) {
-    cudaMemsetAsync(grad, 0, sizeof(float) * kNNWeights, st);
-    // two CTAs per SM fit (80 KB of shared memory each)
-    const int blocks = std::max(1, std::min(num_sms * 2, (n + kTcRows - 1) / kTcRows));
-    k_nn_train_fb<<<blocks, kTcRows, nn_smem_train(), st>>>(W, N, rec, n, tsum, TB, loss,
-                                                            reinterpret_cast<uint32_t*>(loss + 2));
-    dim3 gw(std::max(1, std::min(num_sms, (n + kWGRows - 1) / kWGRows)), kNNLayers);
-    k_nn_wgrad<<<gw, kNNThreads, 0, st>>>(TB, n, grad);
-    if (apply) {
-        const float bc1 = 1.0f - powf(opt.b1, (float)step), bc2 = 1.0f - powf(opt.b2, (float)step);
-        k_nn_adam<<<(kNNWeights + 255) / 256, 256, 0, st>>>(W, grad, opt.lr, opt.b1, opt.b2, opt.eps, bc1, bc2,
-                                                            opt.clip);
+// Zeroes each task's gradient and loss (and, with prep, its T sum).
+__global__ void k_nn_task_zero(const NNTrainTask* __restrict__ tasks, int prep) {
+    const NNTrainTask& task = tasks[blockIdx.y];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < kNNWeights) task.grad[i] = 0.f;
+    if (i == 0) {
+        task.scal[0] = 0.f;
+        if (prep) task.scal[1] = 0.f;
     }
+}
+
+// Chi-square targets (T squared in place) and the sum of T of each task.
+__global__ void k_nn_task_T(const NNTrainTask* __restrict__ tasks) {
+    const NNTrainTask& task = tasks[blockIdx.y];
+    float4* __restrict__ rec = task.rec;
+    float s = 0.f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < task.n; i += gridDim.x * blockDim.x) {
+        float t = rec[4 * (size_t)i + 3].y;
+        if (task.chi2) {
+            t *= t;
+            rec[4 * (size_t)i + 3].y = t;
+        }
+        s += t;
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(task.scal + 1, s);
+}
+
+void launch_nn_train_tasks(const NNTrainTask* tasks, int n_tasks, int max_n, int num_sms, cudaStream_t st, bool prep,
+                           bool apply) {
+    if (n_tasks < 1) return;
+    const NNAdam opt;
+    const dim3 gz((kNNWeights + 255) / 256, n_tasks);
+    k_nn_task_zero<<<gz, 256, 0, st>>>(tasks, prep ? 1 : 0);
+    if (prep) {
+        const dim3 gt(std::max(1, std::min(std::max(1, 1024 / n_tasks), (max_n + 255) / 256)), n_tasks);
+        k_nn_task_T<<<gt, 256, 0, st>>>(tasks);
+    }
+    // two CTAs per SM fit (80 KB of shared memory each), shared by the tasks
+    const int per_task = std::max(1, (num_sms * 2 + n_tasks - 1) / n_tasks);
+    const dim3 gf(std::max(1, std::min(per_task, (max_n + kTcRows - 1) / kTcRows)), n_tasks);
+    k_nn_train_fb<<<gf, kTcRows, nn_smem_train(), st>>>(tasks);
+    const int per_task_w = std::max(1, (num_sms + n_tasks - 1) / n_tasks);
+    const dim3 gw(std::max(1, std::min(per_task_w, (max_n + kWGRows - 1) / kWGRows)), kNNLayers, n_tasks);
+    k_nn_wgrad<<<gw, kNNThreads, 0, st>>>(tasks);
+    if (apply) k_nn_adam<<<gz, 256, 0, st>>>(tasks, opt.b1, opt.b2, opt.eps, opt.clip);
 }
 
 // ===========================================================================
@@ -996,12 +1044,6 @@ __global__ void k_advance_nn(WaveCounters* ctr, int capacity) {
     ctr->stat_iters += 1;
 }
 
-__global__ void k_sum_T(const float4* __restrict__ rec, int n, float* out) {
-    float s = 0.f;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) s += rec[4 * (size_t)i + 3].y;
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(out, s);
-}
 
 void launch_nn_shade(const DevScene& S, const PathBuffers& B, int cur, const RenderParams& P, WaveCounters* ctr,
                      unsigned long long* film, const float4* params, const NNPathData& PD, bool guided,
@@ -1020,18 +1062,6 @@ void launch_nn_generate(const DevScene& S, const PathBuffers& B, int cur, WaveCo
 void launch_nn_finish(const NNPathData& PD, WaveCounters* ctr, const DevNNJob* nnj, int max_depth, int capacity,
                       cudaStream_t st) {
     k_finish_nn<<<(capacity + 255) / 256, 256, 0, st>>>(PD, ctr, nnj, max_depth);
-}
-__global__ void k_square_T(float4* __restrict__ rec, int n) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float t = rec[4 * (size_t)i + 3].y;
-        rec[4 * (size_t)i + 3].y = t * t;
-    }
-}
-void launch_square_T(float4* rec, int n, cudaStream_t st) {
-    k_square_T<<<std::max(1, std::min(1024, (n + 255) / 256)), 256, 0, st>>>(rec, n);
-}
-void launch_sum_T(const float4* rec, int n, float* out, cudaStream_t st) {
-    k_sum_T<<<std::max(1, std::min(1024, (n + 255) / 256)), 256, 0, st>>>(rec, n, out);
 }
 
 }  // namespace cpppt_gb300

@@ -70,13 +70,26 @@ void launch_nn_forward_debug(const DevNNJob* nnj, const float* in, int n, float*
                              cudaStream_t st);
 void launch_nn_infer(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, const DevNNJob* nnj,
                      float4* params, int num_sms, cudaStream_t st);
-// grad (kNNWeights floats) receives dL/dW; loss[0] accumulates the batch
-// loss and the word at loss + 2 collects status bits (kStatusTensorTimeout);
-// apply: also take one Adam step (step counts from 1).
-// tsum: device pointer to the batch's sum of targets T.
-void launch_nn_train_step(const NNWeights& W, const NNNorm& N, const float4* rec, int n, const float* tsum,
-                          const NNTrainBuf& TB, float* grad, float* loss, const NNAdam& opt, int step, int num_sms,
-                          cudaStream_t st, bool apply);
+// One network's part of a fused training step (device table; one launch
+// per stage covers every task: several scenes' guides train together).
+struct NNTrainTask {
+    NNWeights W;
+    NNNorm N;
+    float4* rec;  // this step's records (T squared in place for chi-square)
+    int32_t n;
+    int32_t chi2;
+    float* scal;  // [0] batch loss, [1] sum of T, [2] status bits (kStatusTensorTimeout; accumulate)
+    NNTrainBuf TB;
+    float* grad;  // kNNWeights floats: dL/dW of this step
+    float lr, bc1, bc2;  // Adam learning rate and bias corrections 1 - b^step
+};
+
+// One training step of n_tasks networks (max_n: the largest task's record
+// count).  prep: zero and compute each task's sum of T (squaring T first
+// for chi-square); otherwise scal[1] holds it already.  apply: take the
+// Adam step (else only the gradient).
+void launch_nn_train_tasks(const NNTrainTask* tasks, int n_tasks, int max_n, int num_sms, cudaStream_t st, bool prep,
+                           bool apply);
 
 // The slot wavefront's stages.  jobs: the render jobs (DevBatchJob, as the
 // plain wavefront; one entry for a single render); P carries the flags and
@@ -92,8 +105,5 @@ void launch_nn_generate(const DevScene& S, const PathBuffers& B, int cur, WaveCo
 // the shadow stage, so their last NEE is counted) and frees their slots.
 void launch_nn_finish(const NNPathData& PD, WaveCounters* ctr, const DevNNJob* nnj, int max_depth, int capacity,
                       cudaStream_t st);
-// T -> T^2 for every record (chi-square training)
-void launch_square_T(float4* rec, int n, cudaStream_t st);
-void launch_sum_T(const float4* rec, int n, float* out, cudaStream_t st);
 
 }  // namespace cpppt_gb300
