@@ -4,6 +4,11 @@
     python -m cpppt.profile_cases nn [R]   # 200k-tri slit room, 640x360, learned guide: R renders of 4 spp
     python -m cpppt.profile_cases slit [R] # the same renders with plain PT (PT_FLAG_UNBIASED_MIS)
     python -m cpppt.profile_cases batch    # 8 soup scenes (10k-160k tris) in one batched wavefront
+    python -m cpppt.profile_cases batchnn [R]    # 8 slit rooms (50k-430k tris), 640x360, one learned
+                                                 # guide each, trained online: R batched renders of 2 spp
+    python -m cpppt.profile_cases batchslit [R]  # the same batches with plain PT (PT_FLAG_UNBIASED_MIS)
+    python -m cpppt.profile_cases c5 [R] [plain|train|frozen]  # the eight 1080p rooms of
+                                                 # batch_guiding_eval (11.4M tris): R batched renders of 2 spp
 
 Each case renders once to warm up (graph capture, allocation), then once
 more: the second render is the one to capture.  Device memory stays at a
@@ -16,7 +21,7 @@ import sys
 import time
 
 from . import scenes
-from .lib import FLAG_UNBIASED_MIS, MODE_MIS, MODE_NN, GpuBatch, GpuScene
+from .lib import FLAG_NN_FREEZE, FLAG_UNBIASED_MIS, MODE_MIS, MODE_NN, GpuBatch, GpuScene
 
 
 def case_extend():
@@ -51,11 +56,56 @@ def case_batch():
     return b.stats()
 
 
+def _rooms():
+    members = [GpuScene(scenes.slit_room(seed=5 + k, n_boxes=1000, box_subdiv=2 + k % 5, width=640, height=360))
+               for k in range(8)]
+    return members, GpuBatch(members)
+
+
+def case_batchnn(renders: int = 3):
+    members, b = _rooms()
+    for k, g in enumerate(members):
+        g.nn_reset(2024 + k)
+    for r in range(renders):
+        b.render([dict(scene=k, spp=2, max_depth=12, seed=100 * r + k) for k in range(8)], outputs=False,
+                 mode=MODE_NN)
+    return {**b.stats(), "steps": sum(g.nn_stats()["steps"] for g in members)}
+
+
+def case_batchslit(renders: int = 3):
+    members, b = _rooms()
+    for r in range(renders):
+        b.render([dict(scene=k, spp=2, max_depth=12, seed=100 * r + k) for k in range(8)], outputs=False,
+                 mode=MODE_MIS, flags=FLAG_UNBIASED_MIS)
+    return b.stats()
+
+
+def case_c5(renders: int = 2, what: str = "train"):
+    from .batch_guiding_eval import plan
+    members = [GpuScene(scenes.slit_room(seed=q["scene_seed"], n_boxes=1000, box_subdiv=q["box_subdiv"], width=1920,
+                                         height=1080)) for q in plan(8, 5, 5e5, 4e6)]
+    b = GpuBatch(members)
+    for k, g in enumerate(members):
+        g.nn_reset(2024 + k)
+    mode, flags = (MODE_MIS, FLAG_UNBIASED_MIS) if what == "plain" else (MODE_NN, FLAG_NN_FREEZE if what == "frozen"
+                                                                         else 0)
+    out = []
+    for r in range(renders):
+        b.render([dict(scene=k, spp=2, max_depth=12, seed=100 * r + k) for k in range(8)], outputs=False,
+                 mode=mode, flags=flags)
+        st = b.stats()
+        out.append(round(st["paths"] / (st["render_ms"] * 1e3), 1))
+    return {**b.stats(), "mpaths_s_per_render": out, "steps": sum(g.nn_stats()["steps"] for g in members)}
+
+
 def main():
     name = sys.argv[1] if len(sys.argv) > 1 else "extend"
-    fn = {"extend": case_extend, "nn": case_nn, "slit": case_slit, "batch": case_batch}[name]
+    fn = {"extend": case_extend, "nn": case_nn, "slit": case_slit, "batch": case_batch, "batchnn": case_batchnn,
+          "batchslit": case_batchslit, "c5": case_c5}[name]
     t0 = time.perf_counter()
-    st = fn(int(sys.argv[2])) if name in ("nn", "slit") and len(sys.argv) > 2 else fn()
+    args = [int(sys.argv[2])] if len(sys.argv) > 2 else []
+    args += sys.argv[3:4]
+    st = fn(*args) if name in ("nn", "slit", "batchnn", "batchslit", "c5") else fn()
     print(name, {k: v for k, v in st.items() if v}, f"{time.perf_counter() - t0:.1f}s")
 
 
