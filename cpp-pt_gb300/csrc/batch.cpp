@@ -383,7 +383,7 @@ NNPathData slot_buffers(pt_batch* b, int capacity, int depth, bool params) {
         b->pd.slot_stack = dalloc<int>(b->pd_owned, cap);
         b->pd.slot_job = dalloc<int>(b->pd_owned, cap);
         b->pd.fin = dalloc<int4>(b->pd_owned, cap);
-        if (params) b->nn_params = dalloc<float4>(b->pd_owned, (size_t)cap * 11);
+        if (params) b->nn_params = dalloc<float4>(b->pd_owned, (size_t)cap * kNNMixF4);
     }
     return b->pd;
 }

@@ -492,7 +492,7 @@ NNPathData nn_path_buffers(pt_scene* s, int capacity, int depth) {
         s->nnpd.slot_stack = dalloc<int>(s->nnpd_owned, cap);
         s->nnpd.slot_job = dalloc<int>(s->nnpd_owned, cap);
         s->nnpd.fin = dalloc<int4>(s->nnpd_owned, cap);
-        s->nn_params = dalloc<float4>(s->nnpd_owned, (size_t)cap * 11);
+        s->nn_params = dalloc<float4>(s->nnpd_owned, (size_t)cap * kNNMixF4);
     }
     return s->nnpd;
 }

@@ -247,11 +247,7 @@ __global__ void __launch_bounds__(kTcInferThreads) k_nn_infer(DevScene S, PathBu
             job = (int)((uint32_t)B.info[cur][i].z >> kNNJobShift);
             return true;
         },
-        [&](int i, const float* prm) {
-            float4* o = params + 11 * (size_t)i;
-            for (int k = 0; k < 10; k++) o[k] = make_float4(prm[4 * k], prm[4 * k + 1], prm[4 * k + 2], prm[4 * k + 3]);
-            o[10] = make_float4(prm[40], 0.f, 0.f, 0.f);
-        });
+        [&](int i, const float* prm) { nn_pack_mixture(prm, params + kNNMixF4 * (size_t)i); });
 }
 
 // ---------------------------------------------------------------------------
@@ -669,7 +665,7 @@ __device__ __forceinline__ int warp_append_nn(int* counter, bool pred) {
 // 4: film total after the vertex's own NEE (rgb), wi valid (non-delta)
 // 5: film total before the NEE (rgb), p_bsdf(wi_nee)  6: wi_nee xyz, NEE valid.
 constexpr int kNNVert = kNNVertFloat4;
-__global__ void __launch_bounds__(256) k_shade_nn(DevScene S, PathBuffers B, int cur, RenderParams P,
+__global__ void __launch_bounds__(256, 2) k_shade_nn(DevScene S, PathBuffers B, int cur, RenderParams P,
                                                   WaveCounters* ctr, unsigned long long* __restrict__ film,
                                                   const float4* __restrict__ params, NNPathData PD, int guided,
                                                   const DevBatchJob* __restrict__ jobs) {
@@ -730,28 +726,22 @@ __global__ void __launch_bounds__(256) k_shade_nn(DevScene S, PathBuffers B, int
                 const Rng4 r0 = rng4(seed, sample, pixel, bounce, 0);
                 const Rng4 r1 = rng4(seed, sample, pixel, bounce, 1);
                 const bool delta_mat = (m.kind == PT_MAT_DIELECTRIC_) || (m.kind == PT_MAT_GGX_ && m.delta);
-                float prm[kNNParams];
+                NNMixture mix;
                 float c = 1.0f;
                 if (guided && !delta_mat) {
-                    const float4* pp = params + 11 * (size_t)i;
-#pragma unroll
-                    for (int k = 0; k < 10; k++) {
-                        const float4 q = pp[k];
-                        prm[4 * k] = q.x; prm[4 * k + 1] = q.y; prm[4 * k + 2] = q.z; prm[4 * k + 3] = q.w;
-                    }
-                    prm[40] = pp[10].x;
-                    c = prm[40];
+                    nn_unpack_mixture(params + kNNMixF4 * (size_t)i, mix);
+                    c = mix.c;
                 }
                 BSample bs;
                 float pmix;
                 if (r1.v[3] < c) {
                     bs = bsdf_sample(m, s, wo, r0.v[0], r0.v[1]);
-                    pmix = (bs.delta || c >= 1.0f) ? bs.pdf : c * bs.pdf + (1.0f - c) * nn_mix_pdf(prm, bs.wi);
+                    pmix = (bs.delta || c >= 1.0f) ? bs.pdf : c * bs.pdf + (1.0f - c) * nn_mixture_pdf(mix, bs.wi);
                 } else {
-                    bs.wi = nn_mix_sample(prm, r0.v[0], r0.v[1], r1.v[2]);
+                    bs.wi = nn_mixture_sample(mix, r0.v[0], r0.v[1], r1.v[2]);
                     bs.delta = false;
                     bs.pdf = bsdf_pdf(m, s, wo, bs.wi);
-                    pmix = c * bs.pdf + (1.0f - c) * nn_mix_pdf(prm, bs.wi);
+                    pmix = c * bs.pdf + (1.0f - c) * nn_mixture_pdf(mix, bs.wi);
                 }
                 f3 nee_wi = mk(0.f, 0.f, 0.f);
                 float nee_pb = 0.f, nee_ok = 0.f;
@@ -765,7 +755,7 @@ __global__ void __launch_bounds__(256) k_shade_nn(DevScene S, PathBuffers B, int
                         nee_wi = sd;
                         nee_pb = pb;
                         nee_ok = 1.f;
-                        if (c < 1.0f) pb = c * pb + (1.0f - c) * nn_mix_pdf(prm, sd);
+                        if (c < 1.0f) pb = c * pb + (1.0f - c) * nn_mixture_pdf(mix, sd);
                         const float pn = ls.pdf * len * len / (fabsf(dot(ls.n, sd)) + kEps);
                         // at the last vertex no sampled direction follows, so NEE takes the full
                         // weight (the two estimators then converge to the same depth-limited image)

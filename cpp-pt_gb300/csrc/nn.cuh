@@ -19,7 +19,9 @@
 // is non-zero.
 #pragma once
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
+#include "nn.h"
 #include "shade.cuh"
 
 namespace cpppt_gb300 {
@@ -107,21 +109,94 @@ __device__ __forceinline__ void nn_postprocess(const float* raw, float* out /*41
     out[40] = c_lo + (c_hi - c_lo) / (1.0f + __expf(-raw[40]));
 }
 
-__device__ __forceinline__ float nn_mix_pdf(const float* p /*41*/, f3 w) {
+// ---- the mixture as the shading stage reads it ----
+// Per path vertex, 8 x 16 B: halves 0..39 = lobe j's mean direction xyz,
+// concentration and selection probability (fp16, at 5 j .. 5 j + 4), then
+// eight floats a_j = (selection probability) x (vMF normaliser), then c.
+// Sampling and the pdf use the same stored values: the probability of
+// choosing lobe j is its stored fp16 value (the last lobe takes the rest,
+// as nn_mixture_sample picks it), the normaliser is computed from the
+// stored fp16 concentration, and the mean direction is renormalised after
+// unpacking, so the pdf is the density of the sampler up to FP32 rounding.
+struct NNMixture {
+    f3 mu[kNNLobes];
+    float kappa[kNNLobes];
+    float w[kNNLobes];  // lobe selection probabilities (cumulated by the sampler)
+    float a[kNNLobes];  // w x kappa / (2 pi (1 - e^{-2 kappa}))
+    float c;            // probability of sampling the BSDF
+};
+
+__device__ __forceinline__ float vmf_norm(float kappa) { return kappa / (2.0f * kPi * (-expm1f(-2.0f * kappa))); }
+
+// prm: the 41 post-processed parameters (nn_postprocess).
+__device__ __forceinline__ void nn_pack_mixture(const float* prm, float4* out /*kNNMixF4*/) {
+    __half h[40];
+    float acc = 0.f, a[kNNLobes];
+#pragma unroll
+    for (int j = 0; j < kNNLobes; j++) {
+        h[5 * j] = __float2half_rn(prm[5 * j]);
+        h[5 * j + 1] = __float2half_rn(prm[5 * j + 1]);
+        h[5 * j + 2] = __float2half_rn(prm[5 * j + 2]);
+        h[5 * j + 3] = __float2half_rn(prm[5 * j + 3]);
+        h[5 * j + 4] = __float2half_rn(prm[5 * j + 4]);
+        const float wj = j < kNNLobes - 1 ? __half2float(h[5 * j + 4]) : fmaxf(0.0f, 1.0f - acc);
+        acc += __half2float(h[5 * j + 4]);
+        a[j] = wj * vmf_norm(__half2float(h[5 * j + 3]));
+    }
+    const uint32_t* hw = reinterpret_cast<const uint32_t*>(h);
+#pragma unroll
+    for (int k = 0; k < 5; k++)
+        out[k] = make_float4(__uint_as_float(hw[4 * k]), __uint_as_float(hw[4 * k + 1]), __uint_as_float(hw[4 * k + 2]),
+                             __uint_as_float(hw[4 * k + 3]));
+    out[5] = make_float4(a[0], a[1], a[2], a[3]);
+    out[6] = make_float4(a[4], a[5], a[6], a[7]);
+    out[7] = make_float4(prm[40], 0.f, 0.f, 0.f);
+}
+
+__device__ __forceinline__ void nn_unpack_mixture(const float4* __restrict__ p, NNMixture& M) {
+    uint32_t hw[20];
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        const float4 q = p[k];
+        hw[4 * k] = __float_as_uint(q.x);
+        hw[4 * k + 1] = __float_as_uint(q.y);
+        hw[4 * k + 2] = __float_as_uint(q.z);
+        hw[4 * k + 3] = __float_as_uint(q.w);
+    }
+    const __half* h = reinterpret_cast<const __half*>(hw);
+#pragma unroll
+    for (int j = 0; j < kNNLobes; j++) {
+        M.mu[j] = normalized(mk(__half2float(h[5 * j]), __half2float(h[5 * j + 1]), __half2float(h[5 * j + 2])));
+        M.kappa[j] = __half2float(h[5 * j + 3]);
+        M.w[j] = __half2float(h[5 * j + 4]);
+    }
+    const float4 a0 = p[5], a1 = p[6];
+    M.a[0] = a0.x; M.a[1] = a0.y; M.a[2] = a0.z; M.a[3] = a0.w;
+    M.a[4] = a1.x; M.a[5] = a1.y; M.a[6] = a1.z; M.a[7] = a1.w;
+    M.c = p[7].x;
+}
+
+__device__ __forceinline__ float nn_mixture_pdf(const NNMixture& M, f3 w) {
     float pdf = 0.f;
-    for (int j = 0; j < kNNLobes; j++)
-        pdf += p[5 * j + 4] * vmf_pdf(mk(p[5 * j], p[5 * j + 1], p[5 * j + 2]), p[5 * j + 3], w);
+#pragma unroll
+    for (int j = 0; j < kNNLobes; j++) pdf += M.a[j] * __expf(M.kappa[j] * (dot(M.mu[j], w) - 1.0f));
     return pdf;
 }
 
-__device__ __forceinline__ f3 nn_mix_sample(const float* p /*41*/, float u0, float u1, float u2) {
+__device__ __forceinline__ f3 nn_mixture_sample(const NNMixture& M, float u0, float u1, float u2) {
     int j = kNNLobes - 1;
     float acc = 0.f;
-    for (int k = 0; k < kNNLobes; k++) {
-        acc += p[5 * k + 4];
-        if (u0 < acc) { j = k; break; }
+#pragma unroll
+    for (int k = 0; k < kNNLobes - 1; k++) {
+        acc += M.w[k];
+        if (u0 < acc && j == kNNLobes - 1) j = k;
     }
-    return vmf_sample(mk(p[5 * j], p[5 * j + 1], p[5 * j + 2]), p[5 * j + 3], u1, u2);
+    f3 mu = M.mu[0];
+    float kappa = M.kappa[0];
+#pragma unroll
+    for (int k = 1; k < kNNLobes; k++)
+        if (k == j) { mu = M.mu[k]; kappa = M.kappa[k]; }
+    return vmf_sample(mu, kappa, u1, u2);
 }
 
 // ---- bf16 tensor-core helpers (mma.sync m16n8k16, row.col, f32 accumulate) ----
