@@ -64,7 +64,7 @@ struct pt_batch {
     int nnjobs_cap = 0;
     int* d_nrec = nullptr;  // one per member scene (in `owned`)
     int* h_nrec = nullptr;  // pinned
-    NNTrainTask* d_tasks = nullptr;  // fused training steps: 16 per member scene (in `owned`)
+    NNTrainTask* d_tasks = nullptr;  // fused training steps: kNNMaxStepsPerRound per member scene (in `owned`)
     NNTrainTask* h_tasks = nullptr;  // pinned
 
     ~pt_batch() {
@@ -187,8 +187,8 @@ void create_batch(pt_scene* const* scenes, int n, pt_batch* b) {
     ck(cudaMallocHost(&b->h_ctr, sizeof(WaveCounters)), "cudaMallocHost");
     b->d_nrec = dalloc<int>(b->owned, n);
     ck(cudaMallocHost(&b->h_nrec, sizeof(int) * n), "cudaMallocHost");
-    b->d_tasks = dalloc<NNTrainTask>(b->owned, (size_t)n * 16);
-    ck(cudaMallocHost(&b->h_tasks, sizeof(NNTrainTask) * n * 16), "cudaMallocHost");
+    b->d_tasks = dalloc<NNTrainTask>(b->owned, (size_t)n * kNNMaxStepsPerRound);
+    ck(cudaMallocHost(&b->h_tasks, sizeof(NNTrainTask) * n * kNNMaxStepsPerRound), "cudaMallocHost");
     ck(cudaEventCreate(&b->ev0), "cudaEventCreate");
     ck(cudaEventCreate(&b->ev1), "cudaEventCreate");
     ck(cudaStreamSynchronize(st), "arena merge");

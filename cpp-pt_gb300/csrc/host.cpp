@@ -402,8 +402,7 @@ void render_ppg(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
 // Learned guide: network state and the NN / unbiased-MIS render driver
 // ---------------------------------------------------------------------------
 constexpr int kNNBatch = 1 << 18;               // largest training batch (records per Adam step)
-constexpr int kNNMaxStepsPerRound = 16;
-constexpr int kNNRecordCap = kNNMaxStepsPerRound * kNNBatch;  // record buffer (64 B each, 268 MB)
+constexpr int kNNRecordCap = 16 * kNNBatch;  // record buffer: 2^22 records (64 B each, 268 MB)
 constexpr int kNNWeightCount = 3 * 64 * 64 + 64 * 48;
 static_assert(kNNWeightCount == PT_NN_WEIGHTS, "weight count");
 static_assert(PT_FLAG_THROUGHPUT_RR == 16, "mirrored by PT_FLAG_THROUGHPUT_RR_ in shade.cuh");
@@ -1404,7 +1403,7 @@ pt_status pt_nn_configure(pt_scene* s, const pt_nn_config* c) {
         return PT_ERR_INVALID;
     }
     if (c->steps_per_round < 1 || c->steps_per_round > kNNMaxStepsPerRound) {
-        g_error = "steps_per_round must be in [1, 16]";
+        g_error = "steps_per_round must be in [1, 64]";
         return PT_ERR_INVALID;
     }
     s->nn_cfg = *c;

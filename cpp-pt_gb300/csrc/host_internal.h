@@ -146,7 +146,7 @@ struct pt_scene {
     float4* nn_params = nullptr;
     int nnpd_cap = 0, nnpd_depth = 0;
     std::vector<void*> nnpd_owned;
-    pt_nn_config nn_cfg{3e-3f, 0.3f, 0.9f, 1 << 18, PT_NN_CHI2, 16};
+    pt_nn_config nn_cfg{3e-3f, 0.3f, 0.9f, 1 << 16, PT_NN_CHI2, 16};
 
     ~pt_scene() {
         for (void* p : nn_owned) cudaFree(p);
@@ -174,11 +174,11 @@ namespace hostimpl {
 // Learned-guide state of a scene (host.cpp), for the multi-scene batch.
 void nn_ensure_scene(pt_scene* s);               // network, Adam state, record and training buffers
 NNNorm nn_scene_norm(const pt_scene* s);         // position normalisation and BSDF-fraction range
-int nn_record_cap(const pt_scene* s);            // records collected per round (steps_per_round batches)
+int nn_record_cap(const pt_scene* s);            // records collected per round (steps_per_round batches, <= 2^22)
 // One training round of several scenes' guides.  Scene k counted held[k]
 // records this round (at most caps[k] of them written); it takes as many
 // Adam steps as it holds full batches, the steps of all scenes fused per
-// step (d_tasks / h_tasks: room for n * 16 task entries); records beyond
+// step (d_tasks / h_tasks: room for n * kNNMaxStepsPerRound task entries); records beyond
 // the last full batch move to the front of its buffer and *d_count[k]
 // receives their number, as does left[k] (-1: no full batch, nothing
 // changed).  Synchronises st once.

@@ -29,6 +29,7 @@ struct NNTrainBuf {
 
 constexpr int kNNVertFloat4 = 7;  // float4 per recorded path vertex
 constexpr int kNNMixF4 = 8;       // float4 per path of the packed mixture (inference -> shading)
+constexpr int kNNMaxStepsPerRound = 64;  // Adam steps of one network between two wavefront checks
 
 // Per-path state of the learned-guide integrator (slot = path's free-list entry).
 struct NNPathData {

@@ -121,3 +121,22 @@ def test_trained_guide_lowers_variance(gpu_lib):
     v_nn, m_nn = rel_var(MODE_NN, FLAG_NN_FREEZE, 200)
     assert abs(m_nn - m_plain) < 0.03 * m_plain, (m_nn, m_plain)  # same image
     assert v_nn < 0.85 * v_plain, (v_nn, v_plain)
+
+
+def test_guide_settings_are_checked(gpu_lib):
+    """pt_nn_configure: the defaults, the accepted ranges, and every
+    out-of-range value refused with the previous settings kept."""
+    from cpppt import scenes
+    from cpppt.lib import NN_CHI2, GpuScene, PtError
+    gs = GpuScene(scenes.cornell(8, 8))
+    cfg = gs.nn_config()
+    assert cfg["batch"] == 65536 and cfg["steps_per_round"] == 16 and cfg["divergence"] == NN_CHI2
+    assert abs(cfg["learning_rate"] - 3e-3) < 1e-9 and abs(cfg["bsdf_frac_min"] - 0.3) < 1e-7
+    assert gs.nn_configure(steps_per_round=64, batch=1024)["steps_per_round"] == 64
+    gs.nn_configure(**cfg)
+    for bad in (dict(steps_per_round=65), dict(steps_per_round=0), dict(batch=1023), dict(batch=262145),
+                dict(bsdf_frac_min=0.05), dict(bsdf_frac_min=0.9, bsdf_frac_max=0.8), dict(learning_rate=0.0),
+                dict(divergence=2)):
+        with pytest.raises(PtError):
+            gs.nn_configure(**bad)
+        assert gs.nn_config() == cfg
