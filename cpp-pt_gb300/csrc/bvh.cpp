@@ -49,45 +49,122 @@ void tri_box(const float* v, AB* b) {
 // ---------------------------------------------------------------------------
 // Reference topology (bvh.h:57-216).
 // ---------------------------------------------------------------------------
-struct RefBuilder {
-    const std::vector<AB>& box;
-    const std::vector<V3>& cen;
-    RefTopology& out;
-    std::vector<int32_t> tmp;
-    std::vector<uint8_t> bin_of;
+// A subtree of the reference topology built on its own: node ids are local
+// (pre-order from 0); -1 as a parent means the subtree's parent outside it.
+struct RefFrag {
+    std::vector<Box3> node_box;
+    std::vector<int32_t> node_parent;
+    std::vector<int32_t> leaf_order;   // primitives in DFS order
+    std::vector<int32_t> leaf_parent;  // per entry of leaf_order
+};
 
-    // returns the internal-node id, or -1 when a leaf was emitted
-    void build(int32_t* prims, int n, int parent) {
+// Appends fragment c as the next child subtree of node `id` of f (pre-order
+// keeps: the parent, then its left subtree, then its right subtree).
+void append_frag(RefFrag& f, const RefFrag& c, int32_t id) {
+    const int32_t off = (int32_t)f.node_box.size();
+    f.node_box.insert(f.node_box.end(), c.node_box.begin(), c.node_box.end());
+    for (int32_t p : c.node_parent) f.node_parent.push_back(p < 0 ? id : p + off);
+    f.leaf_order.insert(f.leaf_order.end(), c.leaf_order.begin(), c.leaf_order.end());
+    for (int32_t p : c.leaf_parent) f.leaf_parent.push_back(p < 0 ? id : p + off);
+}
+
+constexpr int kRefParallelMin = 16384;   // subtrees below this size are built by the thread that reaches them
+constexpr int kRefChunkMin = 1 << 18;     // nodes of at least this many primitives bin and partition in chunks
+
+// f(chunk, begin, end) over [0, n) in T contiguous chunks, chunk 0 on the caller.
+template <class F>
+void par_chunks(int T, int n, F f) {
+    std::vector<std::thread> th;
+    for (int c = 1; c < T; c++) th.emplace_back(f, c, (int)((long long)n * c / T), (int)((long long)n * (c + 1) / T));
+    f(0, 0, (int)((long long)n / T));
+    for (std::thread& t : th) t.join();
+}
+
+// A primitive as the reference-topology build reads it: bounds, centroid,
+// insertion index (moved as a whole by each partition).
+struct PrimRec {
+    AB b;
+    V3 c;
+    int32_t id;
+};
+
+struct RefBuilder {
+    std::vector<PrimRec> tmp;
+    std::vector<uint8_t> bin_of;
+    int threads = 1;  // for the chunked passes of large nodes
+
+    void leaf(const PrimRec* prims, int n, int parent, RefFrag& f) {
+        for (int i = 0; i < n; i++) {
+            f.leaf_order.push_back(prims[i].id);
+            f.leaf_parent.push_back(parent);
+        }
+    }
+
+    // bvh.h:151-216 for prims[0..n) under `parent` (a local id of f, or -1);
+    // the partition is written back into prims (records move with it, so
+    // every pass reads them in sequence).  spawn: levels on which the
+    // left subtree may go to a new thread.
+    void build(PrimRec* prims, int n, int parent, RefFrag& f, int spawn) {
         if (n < 4) {  // bvh.h:152-158: SimpleGroup of < 4 primitives
-            for (int i = 0; i < n; i++) {
-                out.prim_parent[prims[i]] = parent;
-                out.leaf_order.push_back(prims[i]);
-            }
+            leaf(prims, n, parent, f);
             return;
         }
+        // large nodes: passes over the primitives in T chunks; boxes are
+        // united with min / max and counts added, so the result does not
+        // depend on the chunking
+        const int T = (n >= kRefChunkMin && threads > 1) ? threads : 1;
         AB bounds, cb;
-        for (int i = 0; i < n; i++) {
-            bounds.unite(box[prims[i]]);
-            cb.unite(cen[prims[i]]);
+        {
+            std::vector<AB> pb(T), pcb(T);
+            par_chunks(T, n, [&](int c, int b, int e) {
+                for (int i = b; i < e; i++) {
+                    pb[c].unite(prims[i].b);
+                    pcb[c].unite(prims[i].c);
+                }
+            });
+            for (int c = 0; c < T; c++) {
+                bounds.unite(pb[c]);
+                cb.unite(pcb[c]);
+            }
         }
-        // compute_split for x, y, z
+        // compute_split for x, y, z (bvh.h:57-149): 5 equal-width bins over
+        // the centroid bounds, a primitive joins the first bin j with
+        // center < min + (max - min) * (j + 1) / 5
+        const int P = 5;
         float cost[3];
         int best_split[3];
+        float thr_axis[3][4];
         for (int axis = 0; axis < 3; axis++) {
-            const int P = 5;
             float lo = cb.lo[axis], hi = cb.hi[axis];
-            float thr[4];
-            for (int j = 0; j < P - 1; j++) thr[j] = lo + (hi - lo) * float(j + 1) / float(P);
+            for (int j = 0; j < P - 1; j++) thr_axis[axis][j] = lo + (hi - lo) * float(j + 1) / float(P);
+        }
+        std::vector<AB> pbin(T * 15);
+        std::vector<int> pcnt(T * 15, 0);
+        par_chunks(T, n, [&](int ch, int b0, int e0) {
+            AB* bb = pbin.data() + 15 * ch;
+            int* cc = pcnt.data() + 15 * ch;
+            for (int i = b0; i < e0; i++) {
+                const AB& pbx = prims[i].b;
+                const V3& pc = prims[i].c;
+                for (int axis = 0; axis < 3; axis++) {
+                    const float* thr = thr_axis[axis];
+                    float c = pc[axis];
+                    int b = P - 1;
+                    for (int j = 0; j < P - 1; j++)
+                        if (c < thr[j]) { b = j; break; }
+                    cc[5 * axis + b]++;
+                    bb[5 * axis + b].unite(pbx);
+                }
+            }
+        });
+        for (int axis = 0; axis < 3; axis++) {
             AB bin_box[5];
             int cnt[5] = {0, 0, 0, 0, 0};
-            for (int i = 0; i < n; i++) {
-                float c = cen[prims[i]][axis];
-                int b = P - 1;
-                for (int j = 0; j < P - 1; j++)
-                    if (c < thr[j]) { b = j; break; }
-                cnt[b]++;
-                bin_box[b].unite(box[prims[i]]);
-            }
+            for (int ch = 0; ch < T; ch++)
+                for (int b = 0; b < P; b++) {
+                    cnt[b] += pcnt[15 * ch + 5 * axis + b];
+                    bin_box[b].unite(pbin[15 * ch + 5 * axis + b]);
+                }
             float pc[4];
             for (int i = 0; i < P - 1; i++) {
                 AB l, r;
@@ -110,53 +187,76 @@ struct RefBuilder {
         int axis;
         if (c1 < c2) axis = (c1 < c3) ? 0 : (c2 < c3 ? 1 : 2);
         else axis = (c2 < c3) ? 1 : 2;
-        int split = best_split[axis];
-        // stable partition: bins 0..split, then split+1..4, each in input order
-        {
-            const int P = 5;
-            float lo = cb.lo[axis], hi = cb.hi[axis];
-            float thr[4];
-            for (int j = 0; j < P - 1; j++) thr[j] = lo + (hi - lo) * float(j + 1) / float(P);
-            if ((int)tmp.size() < n) tmp.resize(n);
-            int nl = 0;
-            for (int i = 0; i < n; i++) {
-                float c = cen[prims[i]][axis];
+        const int split = best_split[axis];
+        // stable partition: bins 0..split, then split+1..4, each in input
+        // order (one counting pass, one scatter)
+        const float* thr = thr_axis[axis];
+        if ((int)tmp.size() < n) tmp.resize(n);
+        if ((int)bin_of.size() < n) bin_of.resize(n);
+        std::vector<int> ccnt(T * 5, 0);
+        par_chunks(T, n, [&](int ch, int b0, int e0) {
+            int* cc = ccnt.data() + 5 * ch;
+            for (int i = b0; i < e0; i++) {
+                float c = prims[i].c[axis];
                 int b = P - 1;
                 for (int j = 0; j < P - 1; j++)
                     if (c < thr[j]) { b = j; break; }
                 bin_of[i] = (uint8_t)b;
+                cc[b]++;
             }
-            int k = 0;
-            for (int b = 0; b < P; b++) {
-                for (int i = 0; i < n; i++)
-                    if (bin_of[i] == b) tmp[k++] = prims[i];
-                if (b == split) nl = k;
+        });
+        // chunk ch's bin b starts after all of bin b's earlier chunks
+        std::vector<int> cstart(T * 5);
+        int nl = 0;
+        for (int b = 0, k = 0; b < P; b++) {
+            for (int ch = 0; ch < T; ch++) {
+                cstart[5 * ch + b] = k;
+                k += ccnt[5 * ch + b];
             }
-            if (nl == 0 || nl == n) {
-                // The reference recurses without end here (bvh.h:200, TODO);
-                // emit one leaf holding every primitive instead.
-                for (int i = 0; i < n; i++) {
-                    out.prim_parent[prims[i]] = parent;
-                    out.leaf_order.push_back(prims[i]);
-                }
-                return;
-            }
-            std::memcpy(prims, tmp.data(), sizeof(int32_t) * n);
-            int id = (int)out.node_box.size();
-            Box3 bx;
-            bx.lo[0] = bounds.lo.x; bx.lo[1] = bounds.lo.y; bx.lo[2] = bounds.lo.z;
-            bx.hi[0] = bounds.hi.x; bx.hi[1] = bounds.hi.y; bx.hi[2] = bounds.hi.z;
-            out.node_box.push_back(bx);
-            out.node_parent.push_back(parent);
-            build(prims, nl, id);
-            build(prims + nl, n - nl, id);
+            if (b == split) nl = k;
         }
+        if (nl == 0 || nl == n) {
+            // The reference recurses without end here (bvh.h:200, TODO);
+            // emit one leaf holding every primitive instead.
+            leaf(prims, n, parent, f);
+            return;
+        }
+        par_chunks(T, n, [&](int ch, int b0, int e0) {
+            int* st = cstart.data() + 5 * ch;
+            for (int i = b0; i < e0; i++) tmp[st[bin_of[i]]++] = prims[i];
+        });
+        par_chunks(T, n, [&](int, int b0, int e0) {
+            std::memcpy(prims + b0, tmp.data() + b0, sizeof(PrimRec) * (e0 - b0));
+        });
+        const int32_t id = (int32_t)f.node_box.size();
+        Box3 bx;
+        bx.lo[0] = bounds.lo.x; bx.lo[1] = bounds.lo.y; bx.lo[2] = bounds.lo.z;
+        bx.hi[0] = bounds.hi.x; bx.hi[1] = bounds.hi.y; bx.hi[2] = bounds.hi.z;
+        f.node_box.push_back(bx);
+        f.node_parent.push_back(parent);
+        if (spawn > 0 && nl >= kRefParallelMin && n - nl >= kRefParallelMin) {
+            // the two subtrees are independent: the left one on a new thread,
+            // each into its own fragment, stitched in pre-order afterwards
+            RefFrag lf, rf;
+            std::thread th([&] {
+                RefBuilder lb{{}, {}, std::max(1, threads / 2)};
+                lb.build(prims, nl, -1, lf, spawn - 1);
+            });
+            threads = std::max(1, threads - threads / 2);
+            build(prims + nl, n - nl, -1, rf, spawn - 1);
+            th.join();
+            append_frag(f, lf, id);
+            append_frag(f, rf, id);
+            return;
+        }
+        build(prims, nl, id, f, spawn);
+        build(prims + nl, n - nl, id, f, spawn);
     }
 };
 
 }  // namespace
 
-RefTopology build_ref_topology(const float* tri_v, int n) {
+RefTopology build_ref_topology(const float* tri_v, int n, int n_threads) {
     RefTopology t;
     t.rank.assign(n, 0);
     t.prim_parent.assign(n, -1);
@@ -169,11 +269,21 @@ RefTopology build_ref_topology(const float* tri_v, int n) {
         cen[i] = {(box[i].lo.x + box[i].hi.x) * 0.5f, (box[i].lo.y + box[i].hi.y) * 0.5f,
                   (box[i].lo.z + box[i].hi.z) * 0.5f};
     }
-    std::vector<int32_t> prims(n);
-    for (int i = 0; i < n; i++) prims[i] = i;
-    RefBuilder b{box, cen, t, {}, {}};
-    b.bin_of.resize(n > 0 ? n : 1);
-    if (n > 0) b.build(prims.data(), n, -1);
+    std::vector<PrimRec> prims(n);
+    for (int i = 0; i < n; i++) prims[i] = PrimRec{box[i], cen[i], i};
+    if (n_threads <= 0) n_threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    int spawn = 0;
+    while ((1 << spawn) < 2 * n_threads && spawn < 12) spawn++;
+    if (n_threads == 1) spawn = 0;
+    RefFrag f;
+    f.leaf_order.reserve(n);
+    f.leaf_parent.reserve(n);
+    RefBuilder b{{}, {}, n_threads};
+    if (n > 0) b.build(prims.data(), n, -1, f, spawn);
+    t.leaf_order = std::move(f.leaf_order);
+    for (int r = 0; r < n; r++) t.prim_parent[t.leaf_order[r]] = f.leaf_parent[r];
+    t.node_box = std::move(f.node_box);
+    t.node_parent = std::move(f.node_parent);
     for (int r = 0; r < n; r++) t.rank[t.leaf_order[r]] = r;
     return t;
 }

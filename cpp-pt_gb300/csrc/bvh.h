@@ -42,7 +42,10 @@ struct RefTopology {
 
 // Builds the reference topology from per-triangle vertex positions.
 // tri_v: 9 floats per triangle (a, b, c).
-RefTopology build_ref_topology(const float* tri_v, int n_tris);
+// n_threads: 0 = all hardware threads, 1 = sequential; the result does not
+// depend on it (independent subtrees are built in parallel and joined in
+// the reference's pre-order).
+RefTopology build_ref_topology(const float* tri_v, int n_tris, int n_threads = 0);
 
 // Compressed 4-wide node, 64 bytes (4 x uint4 on the device):
 //   w[0..2] origin p (float bits); w[3] = ex | ey<<8 | ez<<16  (biased float exponents of the

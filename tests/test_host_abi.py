@@ -55,3 +55,20 @@ def test_errors_are_status_codes():
     nn = C.c_int32()
     assert L.pt_debug_ref_topology(None, -1, None, None, None, 0, C.byref(nn)) == 1
     assert b"bad argument" in L.pt_last_error()
+
+
+def test_parallel_ref_topology_matches_oracle():
+    """Above 2 x 16384 primitives per side the library builds independent
+    subtrees on separate threads and joins them in pre-order: the tree must
+    stay the reference's, here on 320k triangles plus a block of coincident
+    copies (the reference's endless-recursion case becomes one leaf)."""
+    from cpppt import lib, scenes
+    from oracle.oracle import Oracle
+    sc = scenes.soup(seed=9, n_spheres=1000, freq=4, width=8, height=8)
+    sc.triangles[1000:41000] = sc.triangles[7]  # 40000 coincident copies of one triangle
+    order, boxes, pparent = lib.ref_topology(sc)
+    o_order, o_boxes, _, o_pparent = Oracle("port").scene(sc).bvh_dump()
+    assert len(order) > 300_000
+    assert np.array_equal(order, o_order)
+    assert np.array_equal(boxes.view(np.uint32), o_boxes.view(np.uint32))
+    assert np.array_equal(pparent, o_pparent)
