@@ -10,6 +10,7 @@ Translation units, compiled in parallel, CUDA for sm_103a only:
   csrc/host.cpp   -- C ABI, render drivers, loader, image output
   csrc/bvh.cpp    -- BVH builders
   csrc/sdtree.cpp -- SD-tree structure and update
+  csrc/image_io.cpp -- PNG / Radiance RGBE texture decoding
 Host files use -ffp-contract=off: the reference-topology BVH and the SD-tree
 update must round like the reference.
 """
@@ -51,7 +52,8 @@ def _commands(extra_cuda: list[str] | None = None):
     nvcc = _nvcc()
     common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
     jobs = []
-    for name in ("render.cu", "guide.cu", "nn.cu", "batch.cu", "host.cpp", "batch.cpp", "bvh.cpp", "sdtree.cpp"):
+    for name in ("render.cu", "guide.cu", "nn.cu", "batch.cu", "host.cpp", "batch.cpp", "bvh.cpp", "sdtree.cpp",
+                 "image_io.cpp"):
         src = os.path.join(CSRC, name)
         out = os.path.join(OBJ, name + ".o")
         cmd = [nvcc, "-c", src, "-o", out] + common

@@ -30,7 +30,7 @@ EXPORTS = ["pt_scene_create", "pt_scene_load", "pt_scene_destroy", "pt_scene_inf
            "pt_debug_nn_forward", "pt_debug_nn_grad", "pt_nn_configure", "pt_nn_config_get",
            "pt_batch_create", "pt_batch_destroy", "pt_batch_render", "pt_batch_render_device", "pt_batch_set_tuning",
            "pt_batch_get_tuning", "pt_batch_stats", "pt_batch_autotune", "pt_set_mesh_cache",
-           "pt_batch_render_ex", "pt_batch_render_ex_device"]
+           "pt_batch_render_ex", "pt_batch_render_ex_device", "pt_debug_image_load"]
 
 
 class PtMaterial(C.Structure):
@@ -111,6 +111,7 @@ def load(path: str = LIB_PATH):
     lib.pt_last_error.restype = C.c_char_p
     lib.pt_last_error.argtypes = []
     lib.pt_debug_ref_topology.argtypes = [P, C.c_int32, P, P, P, C.c_int32, P]
+    lib.pt_debug_image_load.argtypes = [C.c_char_p, C.c_int32, C.c_int32, P, P, P, C.c_int64]
     lib.pt_nn_get_weights.argtypes = [P, P]
     lib.pt_nn_set_weights.argtypes = [P, P]
     lib.pt_nn_reset.argtypes = [P, C.c_uint32]
@@ -377,6 +378,17 @@ def save_image(prefix: str, rgb: np.ndarray):
     load()
     rgb = np.ascontiguousarray(rgb, np.float32)
     _check(_lib.pt_image_save(prefix.encode(), _ptr(rgb), rgb.shape[1], rgb.shape[0]))
+
+
+def image_load(path: str, rgb: bool = True, srgb: bool = True) -> np.ndarray:
+    """A texture file's pixels as the library decodes them (host only):
+    (H, W, 3) for rgb, (H, W) otherwise."""
+    lib = load()
+    w, h = C.c_int32(), C.c_int32()
+    _check(lib.pt_debug_image_load(path.encode(), int(rgb), int(srgb), C.byref(w), C.byref(h), None, 0))
+    out = np.zeros((h.value, w.value, 3) if rgb else (h.value, w.value), np.float32)
+    _check(lib.pt_debug_image_load(path.encode(), int(rgb), int(srgb), C.byref(w), C.byref(h), _ptr(out), out.size))
+    return out
 
 
 def ref_topology(sc):

@@ -4,6 +4,7 @@
 // that replays wavefront iterations.  No call throws across the ABI; errors
 // are status codes plus a thread-local message.
 #include "host_internal.h"
+#include "image_io.h"
 
 #include <charconv>
 #include <iterator>
@@ -1582,6 +1583,26 @@ pt_status pt_debug_sdtree_run(const float* lo, const float* hi, int32_t n_iters,
             if (out_counts) out_counts[i] = cnt[i];
             if (out_flux) out_flux[i] = flux[i];
         }
+    });
+}
+
+pt_status pt_debug_image_load(const char* path, int32_t rgb, int32_t srgb, int32_t* w, int32_t* h, float* out,
+                              int64_t cap) {
+    if (!path || !w || !h) { g_error = "null argument"; return PT_ERR_INVALID; }
+    return guarded([&] {
+        DecodedImage im;
+        try {
+            im = decode_image_file(path);
+        } catch (std::runtime_error& e) {
+            throw Fail(PT_ERR_IO, e.what());
+        }
+        *w = im.w;
+        *h = im.h;
+        if (!out) return;
+        std::vector<float> px;
+        texture_pixels(im, rgb != 0, srgb != 0, px);
+        if ((int64_t)px.size() > cap) throw Fail(PT_ERR_LIMIT, "output buffer too small");
+        std::memcpy(out, px.data(), sizeof(float) * px.size());
     });
 }
 

@@ -345,6 +345,14 @@ pt_status pt_debug_sdtree_run(const float* lo, const float* hi, int32_t n_iters,
                               int32_t* out_counts, float* out_flux, int32_t n_queries, const float* queries,
                               float* out_pdf, int32_t* n_spatial);
 
+/* Texture decoding as a material's image(...) texture sees it (host only):
+ * the file's pixels as the reference's Image<Vec3> (rgb = 1) or
+ * Image<float> (rgb = 0) holds them after loading (rgb_image.h:160-205),
+ * sRGB-converted when srgb = 1.  PNG and Radiance .hdr files.  out: w * h *
+ * (rgb ? 3 : 1) floats, top row first; with out = NULL (or cap too small)
+ * only *w and *h are set (PT_ERR_LIMIT when out is given but too small). */
+pt_status pt_debug_image_load(const char* path, int32_t rgb, int32_t srgb, int32_t* w, int32_t* h, float* out,
+                              int64_t cap);
 pt_status pt_debug_ref_topology(const float* tri_v, int32_t n, int32_t* leaf_order, int32_t* prim_parent,
                                 float* node_boxes, int32_t max_nodes, int32_t* n_nodes);
 

@@ -103,6 +103,9 @@ class Oracle:
                 lib.ref_sdtree_run.restype = C.c_int
                 lib.ref_sdtree_run.argtypes = [C.c_void_p] * 2 + [C.c_int] + [C.c_void_p] * 2 + [C.c_int] + \
                     [C.c_void_p] * 4 + [C.c_int] + [C.c_void_p] * 3
+                lib.ref_image_load.restype = C.c_int
+                lib.ref_image_load.argtypes = [C.c_char_p, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                               C.c_void_p, C.c_longlong]
                 lib.ref_scene_load.restype = _P
                 lib.ref_scene_load.argtypes = [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                                C.POINTER(C.c_int)]
@@ -112,6 +115,18 @@ class Oracle:
 
     def scene(self, sc) -> "OracleScene":
         return OracleScene(self, sc)
+
+    def image_load(self, path: str, rgb: bool = True, srgb: bool = True) -> np.ndarray:
+        """An image file as the reference's Image<Vec3> / Image<float> holds
+        it (rgb_image.h:160-205)."""
+        assert self.kind == "reference"
+        w, h = C.c_int(), C.c_int()
+        self.lib.ref_image_load(path.encode(), int(rgb), int(srgb), C.byref(w), C.byref(h), None, 0)
+        out = np.zeros((h.value, w.value, 3) if rgb else (h.value, w.value), np.float32)
+        rc = self.lib.ref_image_load(path.encode(), int(rgb), int(srgb), C.byref(w), C.byref(h), out.ctypes.data,
+                                     out.size)
+        assert rc == 0
+        return out
 
     def load_files(self, settings_file: str) -> "OracleScene":
         """The reference's own Loader (loader.h:256-374) on scene files."""

@@ -402,6 +402,35 @@ double ref_render_ppg(void* h, int spp_axis, int seed_offset, int threads, const
 
 int ref_max_threads(void) { return omp_get_max_threads(); }
 
+// An image file through the reference's own Image<Vec3> (rgb = 1) or
+// Image<float> (rgb = 0) with the colour space a material would give it
+// (rgb_image.h:160-205, stb_image).  out (nullable) receives w * h * (rgb ?
+// 3 : 1) floats.  Returns 0, or 2 when cap is too small.  Only call it on
+// files stb can read: the reference does not check stbi_load's result.
+int ref_image_load(const char* path, int rgb, int srgb, int* w, int* h, float* out, long long cap) {
+    const auto cs = srgb ? ImageDef::SRGB : ImageDef::LINEAR;
+    if (rgb) {
+        Image<Vec3> im(path, cs);
+        *w = im.res.x;
+        *h = im.res.y;
+        if (!out) return 0;
+        if (cap < 3LL * im.res.x * im.res.y) return 2;
+        for (size_t i = 0; i < im.pixels.size(); i++) {
+            out[3 * i] = im.pixels[i].x;
+            out[3 * i + 1] = im.pixels[i].y;
+            out[3 * i + 2] = im.pixels[i].z;
+        }
+    } else {
+        Image<float> im(path, cs);
+        *w = im.res.x;
+        *h = im.res.y;
+        if (!out) return 0;
+        if (cap < 1LL * im.res.x * im.res.y) return 2;
+        for (size_t i = 0; i < im.pixels.size(); i++) out[i] = im.pixels[i];
+    }
+    return 0;
+}
+
 // Runs the reference's SDTree (src/algorithms/sdtree.h:268-674) through
 // n_iters rounds of {splat the round's records, update()}.  splats: 7 floats
 // each {radiance, pos xyz, dir xyz}.  Then dumps, for every spatial leaf in
