@@ -111,7 +111,7 @@ void create_batch(pt_scene* const* scenes, int n, pt_batch* b) {
     if (cur != b->device) throw std::invalid_argument("the current device is not the scenes' device");
     ck(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "cudaStreamCreate");
     // arena sizes and offsets
-    unsigned long long nn = 0, nt = 0, nr = 0, nv = 0, nm = 0, nl = 0;
+    unsigned long long nn = 0, nt = 0, nr = 0, nv = 0, nm = 0, nl = 0, ntex = 0, npx = 0;
     for (int i = 0; i < n; i++) {
         const pt_scene* s = scenes[i];
         nn += s->dev.n_nodes;
@@ -120,7 +120,10 @@ void create_batch(pt_scene* const* scenes, int n, pt_batch* b) {
         nv += s->n_verts;
         nm += s->n_mats;
         nl += s->dev.n_lights;
+        ntex += s->h_tex_info.size();
+        npx += s->n_tex_px;
     }
+    if (ntex >= kNoTex) throw Fail(PT_ERR_LIMIT, "a batch holds at most 254 image textures");
     if (nt >= (1ull << 27)) throw Fail(PT_ERR_LIMIT, "batch exceeds 2^27 - 1 triangles (leaf reference range)");
     if (nn >= (1ull << 31) || nr >= (1ull << 31) || nv >= (1ull << 31) || nm >= (1ull << 31))
         throw Fail(PT_ERR_LIMIT, "batch arena exceeds 32-bit indices");
@@ -133,6 +136,12 @@ void create_batch(pt_scene* const* scenes, int n, pt_batch* b) {
     float4* vnrm = dalloc<float4>(b->owned, nv);
     float4* vbt = dalloc<float4>(b->owned, nv);
     DevMaterial* mats = dalloc<DevMaterial>(b->owned, nm);
+    float2* vuv = dalloc<float2>(b->owned, std::max<unsigned long long>(1, nv));
+    float* tpx = dalloc<float>(b->owned, std::max<unsigned long long>(1, npx));
+    std::vector<int4> tinfo;
+    std::vector<DevMaterial> hmats;
+    tinfo.reserve(ntex + 1);
+    hmats.reserve(nm);
     int32_t* lprim = dalloc<int32_t>(b->owned, nl);
     float* larea = dalloc<float>(b->owned, nl);
     cudaStream_t st = b->stream;
@@ -149,7 +158,24 @@ void create_batch(pt_scene* const* scenes, int n, pt_batch* b) {
         d2d(vpos + ov, S.v_pos, s->n_verts, st);
         d2d(vnrm + ov, S.v_nrm, s->n_verts, st);
         d2d(vbt + ov, S.v_btan, s->n_verts, st);
-        d2d(mats + om, S.mats, s->n_mats, st);
+        d2d(vuv + ov, S.v_uv, s->n_verts, st);
+        // textures: pixels appended, offsets and material slots rebased
+        const int tex_base = (int)tinfo.size();
+        size_t px_off = 0;
+        for (const int4& t : tinfo) px_off = std::max(px_off, (size_t)t.x + (size_t)t.y * t.z * t.w);
+        if (s->n_tex_px) d2d(tpx + px_off, S.tex_px, s->n_tex_px, st);
+        for (int4 t : s->h_tex_info) {
+            t.x += (int)px_off;
+            tinfo.push_back(t);
+        }
+        for (DevMaterial m : s->h_mats) {
+            if (m.tex != kNoTextures)
+                for (int k = 0; k < 4; k++) {
+                    const uint32_t id = (m.tex >> (8 * k)) & 0xffu;
+                    if (id != kNoTex) m.tex = (m.tex & ~(0xffu << (8 * k))) | ((id + (uint32_t)tex_base) << (8 * k));
+                }
+            hmats.push_back(m);
+        }
         launch_offset_i32(lprim + ol, S.light_prim, S.n_lights, ot, st);
         d2d(larea + ol, S.light_area, S.n_lights, st);
         pt_batch::Member m;
@@ -182,6 +208,16 @@ void create_batch(pt_scene* const* scenes, int n, pt_batch* b) {
     A.light_prim = lprim;
     A.light_area = larea;
     A.n_lights = ol;
+    if (!hmats.empty())
+        ck(cudaMemcpyAsync(mats, hmats.data(), sizeof(DevMaterial) * hmats.size(), cudaMemcpyHostToDevice, st),
+           "arena materials");
+    if (tinfo.empty()) tinfo.push_back(make_int4(0, 1, 1, 1));
+    int4* dinfo = dalloc<int4>(b->owned, tinfo.size());
+    ck(cudaMemcpyAsync(dinfo, tinfo.data(), sizeof(int4) * tinfo.size(), cudaMemcpyHostToDevice, st), "arena textures");
+    A.v_uv = vuv;
+    A.tex_px = tpx;
+    A.tex_info = dinfo;
+    A.n_tex = (int)ntex;
     A.cam = b->members[0].cam;  // unused by the batch kernels
     b->d_ctr = dalloc<WaveCounters>(b->pb_owned, 1);
     ck(cudaMallocHost(&b->h_ctr, sizeof(WaveCounters)), "cudaMallocHost");

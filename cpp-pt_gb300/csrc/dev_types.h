@@ -6,15 +6,20 @@
 namespace cpppt_gb300 {
 
 // Device material; for emitters rgb holds rgb * intensity (EmissiveMaterial::get_bxdf,
-// src/bxdf/emissive_material.h:28-30).
+// src/bxdf/emissive_material.h:28-30), and alpha the intensity alone when the
+// colour is an image texture.
 struct DevMaterial {
     int32_t kind;     // PT_MAT_*
     float r, g, b;
     float alpha;      // GGX: max(roughness^2, 0.01) (glossy_bxdf.h:77-79)
     int32_t delta;    // GGX: roughness < 0.01 (glossy_bxdf.h:23)
     float ior;
-    float pad;
+    uint32_t tex;     // image textures, one byte each (kNoTex: constant): albedo / emission colour
+                      // (bits 0-7), roughness (8-15), metal (16-23), normal map (24-31)
 };
+
+constexpr uint32_t kNoTex = 0xffu;
+constexpr uint32_t kNoTextures = 0xffffffffu;
 
 // CameraPerspective (src/camera/camera_perspective.h:19-39): origin and the
 // column basis (x, y, z) of `coords`, stored row-major like Mat3.
@@ -42,6 +47,12 @@ struct DevScene {
     const float* light_area;    // Triangle::area (triangle.h:197-207)
     int32_t n_lights;
     DevCamera cam;
+    // image textures (file scenes): per-vertex uv, pixels of every texture,
+    // {first float, width, height, channels} per texture
+    const float2* v_uv;
+    const float* tex_px;
+    const int4* tex_info;
+    int32_t n_tex;
 };
 
 // One render job of a multi-scene batch (the scenes' geometry is merged into

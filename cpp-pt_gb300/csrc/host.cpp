@@ -29,7 +29,7 @@ void check_device(pt_scene* s) {
     s->num_sms = prop.multiProcessorCount;
 }
 
-void create_scene(const pt_scene_desc* d, pt_scene* s) {
+void create_scene(const pt_scene_desc* d, pt_scene* s, const SceneTextures* tx = nullptr) {
     if (!d) throw std::invalid_argument("null scene description");
     const int nv = d->n_vertices, nt = d->n_triangles, nm = d->n_materials;
     if (nv < 0 || nt < 0 || nm < 0) throw std::invalid_argument("negative count");
@@ -129,6 +129,11 @@ void create_scene(const pt_scene_desc* d, pt_scene* s) {
         dm.alpha = std::max(r2, 0.01f);
         dm.delta = (double)m.roughness < 0.01 ? 1 : 0;
         dm.ior = m.ior;
+        dm.tex = kNoTextures;
+        if (tx && i < (int)tx->mat_tex.size()) {
+            dm.tex = tx->mat_tex[i];
+            if (m.kind == PT_MAT_EMISSIVE && (dm.tex & 0xffu) != kNoTex) dm.alpha = tx->emit_intensity[i];
+        }
         mats[i] = dm;
     }
     std::vector<int32_t> lprim;
@@ -158,9 +163,22 @@ void create_scene(const pt_scene_desc* d, pt_scene* s) {
     S.v_nrm = dupload(s->owned, vnrm, s->stream);
     S.v_btan = dupload(s->owned, vbt, s->stream);
     S.mats = dupload(s->owned, mats, s->stream);
+    s->h_mats = mats;
     S.light_prim = dupload(s->owned, lprim, s->stream);
     S.light_area = dupload(s->owned, larea, s->stream);
     S.n_lights = (int)lprim.size();
+    // image textures and uv (zero uv and an empty texture table without them)
+    std::vector<float2> uv(std::max(1, nv), make_float2(0.f, 0.f));
+    if (tx && tx->uv.size() >= 2 * (size_t)nv)
+        for (int v = 0; v < nv; v++) uv[v] = make_float2(tx->uv[2 * (size_t)v], tx->uv[2 * (size_t)v + 1]);
+    S.v_uv = dupload(s->owned, uv, s->stream);
+    std::vector<float> px = (tx && !tx->px.empty()) ? tx->px : std::vector<float>(1, 0.f);
+    std::vector<int4> info = (tx && !tx->info.empty()) ? tx->info : std::vector<int4>(1, make_int4(0, 1, 1, 1));
+    S.tex_px = dupload(s->owned, px, s->stream);
+    S.tex_info = dupload(s->owned, info, s->stream);
+    S.n_tex = tx ? (int)tx->info.size() : 0;
+    s->h_tex_info.assign(info.begin(), info.begin() + S.n_tex);
+    s->n_tex_px = tx ? tx->px.size() : 0;
     // camera: CameraPerspective(res, tan_fovy, origin, normalized(at - origin), up)
     const pt_camera& c = d->camera;
     float fwd[3] = {c.at[0] - c.origin[0], c.at[1] - c.origin[1], c.at[2] - c.origin[2]};
@@ -831,7 +849,6 @@ void parse_tex(const std::string& tex, bool bw, bool srgb, float out[3]) {
         out[0] = out[1] = out[2] = r;
         return;
     }
-    if (tex.rfind("image", 0) == 0) throw Fail(PT_ERR_IO, "image textures are not supported: " + tex);
     throw Fail(PT_ERR_IO, "Unknown type of tex: " + tex);
 }
 
@@ -841,7 +858,35 @@ struct LoadedScene {
     std::vector<pt_material> mats;
     pt_camera cam{};
     bool has_camera = false;
+    SceneTextures tx;                                // uv, image textures, material slots
+    std::unordered_map<std::string, int> tex_cache;  // path | rgb | srgb -> texture id
 };
+
+// An image(...) texture: the file decoded (image_io.cpp) into the pixels
+// Image<Vec3> (rgb) or Image<float> holds (loader.h:78-92: the colour space
+// is sRGB for albedo and emission, linear for roughness, metal and normal
+// maps); identical requests share one texture.  Returns its id.
+int load_image_texture(LoadedScene& L, const std::string& dir, const std::string& tex, bool rgb, bool srgb) {
+    if (tex.size() < 8 || tex.back() != ')') throw Fail(PT_ERR_IO, "bad texture: " + tex);
+    const std::string path = dir + tex.substr(6, tex.size() - 7);
+    const std::string key = path + (rgb ? "|rgb" : "|bw") + (srgb ? "|srgb" : "|lin");
+    auto it = L.tex_cache.find(key);
+    if (it != L.tex_cache.end()) return it->second;
+    if (L.tx.info.size() >= kNoTex) throw Fail(PT_ERR_LIMIT, "more than 254 image textures");
+    DecodedImage im;
+    try {
+        im = decode_image_file(path);
+    } catch (std::runtime_error& e) {
+        throw Fail(PT_ERR_IO, e.what());
+    }
+    std::vector<float> px;
+    texture_pixels(im, rgb, srgb, px);
+    const int id = (int)L.tx.info.size();
+    L.tx.info.push_back(make_int4((int)L.tx.px.size(), im.w, im.h, rgb ? 3 : 1));
+    L.tx.px.insert(L.tx.px.end(), px.begin(), px.end());
+    L.tex_cache[key] = id;
+    return id;
+}
 
 std::string dir_of(const std::string& f) {
     size_t i = f.find_last_of("/\\");
@@ -858,10 +903,11 @@ std::string dir_of(const std::string& f) {
 // time; a stale or unreadable cache is ignored and rewritten.
 struct MeshArrays {
     std::vector<float> v, n, t;  // 3 per vertex
+    std::vector<float> uv;       // 2 per vertex
     std::vector<int32_t> f;      // 3 per face
 };
 
-const char kMeshCacheMagic[8] = {'G', 'B', 'P', 'T', 'O', 'B', 'J', '1'};
+const char kMeshCacheMagic[8] = {'G', 'B', 'P', 'T', 'O', 'B', 'J', '2'};
 bool g_mesh_cache = true;
 
 struct FileStamp {
@@ -893,10 +939,12 @@ bool read_mesh_cache(const std::string& cpath, const FileStamp& src, MeshArrays&
     M.v.resize(3 * (size_t)nv);
     M.n.resize(3 * (size_t)nv);
     M.t.resize(3 * (size_t)nv);
+    M.uv.resize(2 * (size_t)nv);
     M.f.resize(3 * (size_t)nf);
     f.read(reinterpret_cast<char*>(M.v.data()), sizeof(float) * M.v.size());
     f.read(reinterpret_cast<char*>(M.n.data()), sizeof(float) * M.n.size());
     f.read(reinterpret_cast<char*>(M.t.data()), sizeof(float) * M.t.size());
+    f.read(reinterpret_cast<char*>(M.uv.data()), sizeof(float) * M.uv.size());
     f.read(reinterpret_cast<char*>(M.f.data()), sizeof(int32_t) * M.f.size());
     return (bool)f;
 }
@@ -915,6 +963,7 @@ void write_mesh_cache(const std::string& cpath, const FileStamp& src, const Mesh
         f.write(reinterpret_cast<const char*>(M.v.data()), sizeof(float) * M.v.size());
         f.write(reinterpret_cast<const char*>(M.n.data()), sizeof(float) * M.n.size());
         f.write(reinterpret_cast<const char*>(M.t.data()), sizeof(float) * M.t.size());
+        f.write(reinterpret_cast<const char*>(M.uv.data()), sizeof(float) * M.uv.size());
         f.write(reinterpret_cast<const char*>(M.f.data()), sizeof(int32_t) * M.f.size());
         if (!f) {
             f.close();
@@ -964,12 +1013,14 @@ void parse_ptobj_text(const std::string& path, MeshArrays& M) {
     M.v.resize(3 * (size_t)nv);
     M.n.resize(3 * (size_t)nv);
     M.t.resize(3 * (size_t)nv);
+    M.uv.resize(2 * (size_t)nv);
     M.f.resize(3 * (size_t)nf);
     for (int i = 0; i < nv; i++) {
         LineCursor c = next_line("verts");
         float x[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
         for (int k = 0; k < 11 && c.next(tb, te); k++) std::from_chars(tb, te, x[k]);
         std::memcpy(&M.v[3 * (size_t)i], x, 12);
+        std::memcpy(&M.uv[2 * (size_t)i], x + 3, 8);
         std::memcpy(&M.n[3 * (size_t)i], x + 5, 12);
         std::memcpy(&M.t[3 * (size_t)i], x + 8, 12);
     }
@@ -995,6 +1046,7 @@ void parse_ptobj(const std::string& path, LoadedScene& L, int mat) {
     L.v.insert(L.v.end(), M.v.begin(), M.v.end());
     L.n.insert(L.n.end(), M.n.begin(), M.n.end());
     L.t.insert(L.t.end(), M.t.begin(), M.t.end());
+    L.tx.uv.insert(L.tx.uv.end(), M.uv.begin(), M.uv.end());
     for (int32_t ix : M.f) L.tri.push_back(base + ix);
     L.tri_mat.insert(L.tri_mat.end(), M.f.size() / 3, mat);
 }
@@ -1007,14 +1059,25 @@ int parse_ptmat(const std::string& path, LoadedScene& L, std::unordered_map<std:
     std::string word;
     f >> word;
     pt_material m{};
+    const std::string dir = dir_of(path);
+    uint32_t tex = kNoTextures;  // DevMaterial::tex
+    float emit_intensity = 0.f;
+    // an image(...) texture goes to the slot `shift`; returns whether it was one
+    auto image = [&](const std::string& t, bool rgb, bool srgb, int shift) {
+        if (t.rfind("image", 0) != 0) return false;
+        const uint32_t id = (uint32_t)load_image_texture(L, dir, t, rgb, srgb);
+        tex = (tex & ~(0xffu << shift)) | (id << shift);
+        return true;
+    };
     if (word == "DISNEY") {  // loader.h:154-180
         std::string albedo, spec, rough, metal, transp, ior, normal, alpha;
         f >> albedo >> spec >> rough >> metal >> transp >> ior >> normal >> alpha;
-        float a[3], r[3], me[3], io[3];
-        parse_tex(albedo, false, true, a);
-        parse_tex(rough, true, false, r);
-        parse_tex(metal, true, false, me);
-        parse_tex(ior, true, true, io);
+        float a[3] = {0.f, 0.f, 0.f}, r[3] = {0.f, 0.f, 0.f}, me[3] = {0.f, 0.f, 0.f}, io[3] = {0.f, 0.f, 0.f};
+        if (!image(albedo, true, true, 0)) parse_tex(albedo, false, true, a);
+        if (!image(rough, false, false, 8)) parse_tex(rough, true, false, r);
+        if (!image(metal, false, false, 16)) parse_tex(metal, true, false, me);
+        image(normal, true, false, 24);  // a constant normal map is the identity here
+        if (ior.rfind("image", 0) != 0) parse_tex(ior, true, true, io);  // unused by the BxDFs
         // standard_material.h:46-61: Diffuse when metal < 0.1, else Glossy(roughness)
         m.kind = (double)me[0] < 0.1 ? PT_MAT_DIFFUSE : PT_MAT_GGX;
         std::memcpy(m.rgb, a, 12);
@@ -1023,11 +1086,14 @@ int parse_ptmat(const std::string& path, LoadedScene& L, std::unordered_map<std:
     } else if (word == "EMISSION") {  // loader.h:181-201
         std::string col, inten;
         f >> col >> inten;
-        float c[3];
-        parse_tex(col, false, true, c);
+        float c[3] = {0.f, 0.f, 0.f};
+        const bool textured = image(col, true, true, 0);
+        if (!textured) parse_tex(col, false, true, c);
         m.kind = PT_MAT_EMISSIVE;
         std::memcpy(m.rgb, c, 12);
         m.intensity = (float)std::atof(inten.substr(6, inten.size() - 7).c_str());
+        emit_intensity = m.intensity;
+        if (textured) m.rgb[0] = m.rgb[1] = m.rgb[2] = 1.0f;  // a lit placeholder; the texture decides
     } else if (word == "DIELECTRIC") {  // extension: RefractionBxDF(ior)
         std::string ior;
         f >> ior;
@@ -1040,6 +1106,8 @@ int parse_ptmat(const std::string& path, LoadedScene& L, std::unordered_map<std:
         throw Fail(PT_ERR_IO, "Wrong bsdf type: " + word);
     }
     L.mats.push_back(m);
+    L.tx.mat_tex.push_back(tex);
+    L.tx.emit_intensity.push_back(emit_intensity);
     int id = (int)L.mats.size() - 1;
     cache[path] = id;
     return id;
@@ -1231,16 +1299,18 @@ void scene_check_status(pt_scene* s, uint32_t status) { check_status(s, status);
 
 extern "C" {
 
-pt_status pt_scene_create(const pt_scene_desc* desc, pt_scene** out) {
+pt_status scene_create_with(const pt_scene_desc* desc, const SceneTextures* tx, pt_scene** out) {
     if (!out) { g_error = "null output pointer"; return PT_ERR_INVALID; }
     *out = nullptr;
     pt_scene* s = new (std::nothrow) pt_scene();
     if (!s) { g_error = "host allocation failed"; return PT_ERR_MEMORY; }
-    pt_status st = guarded([&] { create_scene(desc, s); });
+    pt_status st = guarded([&] { create_scene(desc, s, tx); });
     if (st != PT_OK) { delete s; return st; }
     *out = s;
     return PT_OK;
 }
+
+pt_status pt_scene_create(const pt_scene_desc* desc, pt_scene** out) { return scene_create_with(desc, nullptr, out); }
 
 pt_status pt_scene_load(const char* settings_file, pt_scene** out, pt_render_desc* settings, char* output_name,
                         int32_t output_name_len) {
@@ -1262,7 +1332,7 @@ pt_status pt_scene_load(const char* settings_file, pt_scene** out, pt_render_des
     d.n_materials = (int32_t)L.mats.size();
     d.materials = L.mats.data();
     d.camera = L.cam;
-    st = pt_scene_create(&d, out);
+    st = scene_create_with(&d, &L.tx, out);
     if (st != PT_OK) return st;
     if (settings) *settings = rs;
     if (output_name && output_name_len > 0) {

@@ -92,9 +92,23 @@ inline void fcross(const float* a, const float* b, float* o) {
 
 using namespace cpppt_gb300;  // internal header of the ABI's own translation units
 
+// Image textures of a file scene (the loader's image(...) textures): pixels
+// of every texture back to back, {first float, width, height, channels} per
+// texture, per-vertex uv, and each material's texture slots (DevMaterial::tex).
+struct SceneTextures {
+    std::vector<float> px;
+    std::vector<int4> info;
+    std::vector<float> uv;         // 2 per vertex (empty: all zero)
+    std::vector<uint32_t> mat_tex;  // per material (empty: no textures)
+    std::vector<float> emit_intensity;  // per material: intensity of a textured emitter
+};
+
 struct pt_scene {
     // counts of the device arrays (a multi-scene batch copies them)
     int n_verts = 0, n_mats = 0, n_rbox = 0;
+    std::vector<int4> h_tex_info;  // host copy of dev.tex_info (batch arena merge)
+    std::vector<DevMaterial> h_mats;  // host copy of dev.mats (batch arena merge)
+    size_t n_tex_px = 0;           // floats in dev.tex_px
     int device = 0;
     int num_sms = 0;
     cudaStream_t stream = nullptr;

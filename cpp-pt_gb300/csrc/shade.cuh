@@ -70,6 +70,73 @@ struct Surf {
     int32_t mat;
 };
 
+// ---------------------------------------------------------------------------
+// Image textures (ImageTexture::sample, src/texture/image_texture.h:24-41,
+// on Image::get_pixel with the default REPEAT border, src/image/rgb_image.h:
+// 210-250).  The reference leaves ImageTexture::filtering uninitialised; the
+// bilinear branch is used here.  Where the reference's wrap of a negative
+// multiple of the size yields the size itself (i % n + n), the pixel index
+// runs on into the next row as there, and is clamped to the image.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int tex_wrap(int i, int n) {
+    if (i >= n) return i % n;
+    if (i < 0) return i % n + n;
+    return i;
+}
+
+__device__ __forceinline__ f3 tex_pixel(const DevScene& S, int4 info, int i, int j) {
+    const int w = info.y, h = info.z;
+    int idx = tex_wrap(i, w) + tex_wrap(j, h) * w;
+    idx = min(max(idx, 0), w * h - 1);
+    const float* p = S.tex_px + info.x + (size_t)idx * info.w;
+    if (info.w == 1) {
+        const float v = __ldg(p);
+        return mk(v, v, v);
+    }
+    return mk(__ldg(p), __ldg(p + 1), __ldg(p + 2));
+}
+
+__device__ __forceinline__ f3 tex_sample(const DevScene& S, uint32_t t, float u, float v) {
+    const int4 info = __ldg(S.tex_info + t);
+    float x = u * (float)info.y;
+    float y = (float)((1.0 - (double)v) * (double)info.z);
+    x = (float)((double)x - 0.5);
+    y = (float)((double)y - 0.5);
+    const int i = (int)floorf(x), j = (int)floorf(y);
+    x = x - (float)i;
+    y = y - (float)j;
+    const f3 p00 = tex_pixel(S, info, i, j), p10 = tex_pixel(S, info, i + 1, j);
+    const f3 p01 = tex_pixel(S, info, i, j + 1), p11 = tex_pixel(S, info, i + 1, j + 1);
+    return (p00 * (1.0f - x) + p10 * x) * (1.0f - y) + (p01 * (1.0f - x) + p11 * x) * y;
+}
+
+// StandardMaterial::get_bxdf / EmissiveMaterial::get_bxdf at uv
+// (standard_material.h:46-61, emissive_material.h:28-30): the textured
+// albedo or emission colour, the BxDF picked by the metal value and the
+// GGX parameters from the roughness value.
+__device__ __forceinline__ void apply_textures(const DevScene& S, DevMaterial& m, float u, float v) {
+    const uint32_t ta = m.tex & 0xffu, tr = (m.tex >> 8) & 0xffu, tm = (m.tex >> 16) & 0xffu;
+    if (m.kind == PT_MAT_EMISSIVE_) {
+        if (ta != kNoTex) {
+            const f3 c = tex_sample(S, ta, u, v);
+            m.r = c.x * m.alpha;
+            m.g = c.y * m.alpha;
+            m.b = c.z * m.alpha;
+        }
+        return;
+    }
+    if (ta != kNoTex) {
+        const f3 c = tex_sample(S, ta, u, v);
+        m.r = c.x; m.g = c.y; m.b = c.z;
+    }
+    if (tm != kNoTex) m.kind = (double)tex_sample(S, tm, u, v).x < 0.1 ? PT_MAT_DIFFUSE_ : PT_MAT_GGX_;
+    if (tr != kNoTex) {
+        const float r = tex_sample(S, tr, u, v).x;
+        m.alpha = fmaxf(r * r, 0.01f);  // glossy_bxdf.h:23, 77-79
+        m.delta = (double)r < 0.01 ? 1 : 0;
+    }
+}
+
 __device__ __forceinline__ Surf make_surf(const DevScene& S, int32_t prim, f3 o, f3 d, float t, float beta, float gamma,
                                           bool first_hit, int32_t* kind_out, DevMaterial* mat_out) {
     const int4 vi = __ldg(S.tri_vidx + prim);
@@ -86,15 +153,28 @@ __device__ __forceinline__ Surf make_surf(const DevScene& S, int32_t prim, f3 o,
     s.b = bt;
     s.t = normalized(cross(bt, n));
     s.mat = vi.w;
-    const DevMaterial m = S.mats[vi.w];
+    DevMaterial m = S.mats[vi.w];
+    f3 nmap = mk(0.f, 0.f, 1.f);  // tangent-space normal (identity for the constant map rgb(0.5,0.5,1))
+    if (m.tex != kNoTextures) {
+        // triangle.h:91-94: uv1 * alpha + uv2 * beta + uv3 * gamma
+        const float2 t0 = __ldg(S.v_uv + vi.x), t1 = __ldg(S.v_uv + vi.y), t2 = __ldg(S.v_uv + vi.z);
+        const float u = t0.x * alpha + t1.x * beta + t2.x * gamma;
+        const float v = t0.y * alpha + t1.y * beta + t2.y * gamma;
+        const uint32_t tn = m.tex >> 24;
+        if (first_hit && tn != kNoTex && (m.kind == PT_MAT_DIFFUSE_ || m.kind == PT_MAT_GGX_)) {
+            const f3 c = tex_sample(S, tn, u, v);  // standard_material.h:64-71
+            nmap = mk(c.x * 2.0f - 1.0f, c.y * 2.0f - 1.0f, c.z);
+        }
+        apply_textures(S, m, u, v);
+    }
     *mat_out = m;
     *kind_out = m.kind;
     // The reference's Intersection is reused for all bounces of a path and
-    // its computed_normal flag is never reset, so normal mapping (identity
-    // for the constant map rgb(0.5,0.5,1), standard_material.h:64-71) and
-    // the re-orthogonalisation only run at the first hit.
+    // its computed_normal flag is never reset, so normal mapping
+    // (standard_material.h:64-71: Mat3(tangent, bitangent, normal) times the
+    // map's value) and the re-orthogonalisation only run at the first hit.
     if (first_hit) {
-        if (m.kind == PT_MAT_DIFFUSE_ || m.kind == PT_MAT_GGX_) s.n = normalized(s.n);
+        if (m.kind == PT_MAT_DIFFUSE_ || m.kind == PT_MAT_GGX_) s.n = normalized(s.t * nmap.x + s.b * nmap.y + s.n * nmap.z);
         s.b = normalized(cross(s.n, s.t));
         s.t = normalized(cross(s.b, s.n));
     }
@@ -303,7 +383,13 @@ __device__ __forceinline__ LSample sample_light(const DevScene& S, f3 from, floa
     ls.pos = a * al + b * be + c * ga;
     ls.n = normalized(f3of(__ldg(S.v_nrm + vi.x)) * al + f3of(__ldg(S.v_nrm + vi.y)) * be +
                       f3of(__ldg(S.v_nrm + vi.z)) * ga);
-    const DevMaterial m = S.mats[vi.w];
+    DevMaterial m = S.mats[vi.w];
+    if (m.tex != kNoTextures) {
+        // triangle.h:244-249 interpolates the sampled point's uv as
+        // uv1 * alpha + uv2 * beta + uv2 * gamma (the second vertex twice)
+        const float2 t0 = __ldg(S.v_uv + vi.x), t1 = __ldg(S.v_uv + vi.y);
+        apply_textures(S, m, t0.x * al + t1.x * be + t1.x * ga, t0.y * al + t1.y * be + t1.y * ga);
+    }
     const float cosl = fabsf(dot(ls.n, normalized(from - ls.pos)));
     ls.le = mk(m.r * cosl, m.g * cosl, m.b * cosl);
     ls.pdf = (1.0f / __ldg(S.light_area + k)) * (1.0f / (float)nl);

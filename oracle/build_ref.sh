@@ -42,6 +42,11 @@ if [ -d "$REF/src" ]; then
     sed -i 's/for(int i = 0; i<32; i++){/for(int i = 0; i<cpppt_harness_max_depth; i++){/; s/RandomSampler s(i);/RandomSampler s(i + cpppt_harness_seed_offset);/; s/if(i%50==0)/if(cpppt_harness_verbose \&\& i%50==0)/' "$S/renderer/$f"
     grep -q 'cpppt_harness_max_depth' "$S/renderer/$f"
   done
+  # (9) texture/image_texture.h:21  ImageTexture::filtering is never initialised (the image-texture
+  #     path reads an indeterminate value); the harness pins it to the bilinear branch, which the
+  #     GPU texture sampler implements
+  sed -i 's/^    Filtering filtering;/    Filtering filtering = BILINEAR;/' "$S/texture/image_texture.h"
+  grep -q 'Filtering filtering = BILINEAR;' "$S/texture/image_texture.h"
   grep -q 'cpppt_harness_max_depth' "$S/renderer/pathtracerMIS.h"
   grep -q 'unique_ptr<Primitive>&& right' "$S/primitive/bvh.h"
 fi

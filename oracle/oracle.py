@@ -196,9 +196,13 @@ class OracleScene:
         nn = getattr(self.o.lib, self.o.p + "bvh_dump")(self.h, order, boxes, parent, pparent, cap)
         return order, boxes[:6 * nn].reshape(nn, 6), parent[:nn], pparent
 
+    def _dims(self):
+        """Image size: the scene's, or the settings file's for a loaded scene."""
+        return (self.sc.width, self.sc.height) if self.sc is not None else (self.width, self.height)
+
     def render_mis(self, spp_axis: int, max_depth: int, seed_offset: int = 0, threads: int = 0):
         """Returns (image HxWx3 float32, seconds).  spp_axis^2 samples per pixel."""
-        W, H = self.sc.width, self.sc.height
+        W, H = self._dims()
         out = np.zeros(W * H * 3, np.float32)
         if self.o.kind == "port":
             import time
@@ -215,7 +219,7 @@ class OracleScene:
                        threads: int = 0):
         """integrator 1: Pathtracer (PT + NEE, no MIS); 2: PurePt (no NEE).
         Returns (image HxWx3 float32, seconds)."""
-        W, H = self.sc.width, self.sc.height
+        W, H = self._dims()
         out = np.zeros(W * H * 3, np.float32)
         if self.o.kind == "port":
             import time
@@ -229,7 +233,7 @@ class OracleScene:
         return out.reshape(H, W, 3), sec
 
     def render_ppg(self, spp_axis: int, seed_offset: int = 0, threads: int = 0):
-        W, H = self.sc.width, self.sc.height
+        W, H = self._dims()
         out = np.zeros(W * H * 3, np.float32)
         with tempfile.TemporaryDirectory() as d:
             sec = self.o.lib.ref_render_ppg(self.h, spp_axis, seed_offset, threads, os.path.join(d, "img").encode(), out)

@@ -6,6 +6,7 @@ oracle/build_ref.sh):
 
     python tests/golden/make_golden.py            # small fixtures (seconds)
     python tests/golden/make_golden.py --c1-16k   # 16k-spp Cornell reference (~15 min on 8 cores)
+    python tests/golden/make_golden.py --textures # textured room (tests/texscene.py), 16 x 64 spp
 
 Every array stored here is an output of the reference's own code
 (BVH::build, BVH::intersect / intersect_any, PathtracerMIS::render,
@@ -89,11 +90,40 @@ def c1_16k(replicas: int = 16, spp_axis: int = 32, depth: int = 8, tile: int = 1
     print("done", time.time() - t0)
 
 
+def textured(replicas: int = 16, spp_axis: int = 8, depth: int = 8, tile: int = 8):
+    """The textured room of tests/texscene.py (image textures: tiled albedo,
+    metal and roughness maps, normal map, emission texture), loaded by the
+    reference's own Loader and rendered by its PathtracerMIS: replicas of
+    spp_axis^2 spp, replica r seeding column i with i + 500 * (r + 1).
+    Stores the mean image and the per-tile means of every replica."""
+    import tempfile
+    from tests import texscene
+    orc.build_reference()
+    d = tempfile.mkdtemp()
+    rs = orc.Oracle("reference").load_files(texscene.write(d))
+    imgs = []
+    t0 = time.time()
+    for r in range(replicas):
+        img, _ = rs.render_mis(spp_axis, depth, 500 * (r + 1))
+        imgs.append(img)
+    imgs = np.stack(imgs)
+    H, W = texscene.H, texscene.W
+    tiles = imgs.reshape(replicas, H // tile, tile, W // tile, tile, 3).mean(axis=(2, 4))
+    np.savez_compressed(
+        os.path.join(HERE, "texroom_ref.npz"),
+        mean=imgs.mean(0).astype(np.float32), tile_means=tiles.astype(np.float32),
+        replicas=replicas, spp_per_replica=spp_axis * spp_axis, depth=depth, tile=tile)
+    print("textured room", time.time() - t0, "s; mean", float(imgs.mean()))
+
+
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--c1-16k", action="store_true")
+    ap.add_argument("--textures", action="store_true")
     a = ap.parse_args()
     if a.c1_16k:
         c1_16k()
+    elif a.textures:
+        textured()
     else:
         small()

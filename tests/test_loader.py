@@ -76,11 +76,12 @@ def test_cli_renders_files(gpu_lib, tmp_path):
 
 def _read_cache(path):
     raw = open(path, "rb").read()
-    assert raw[:8] == b"GBPTOBJ1"
+    assert raw[:8] == b"GBPTOBJ2"
     nv, nf = np.frombuffer(raw[24:32], np.int32)
     f32 = np.frombuffer(raw[32:32 + 36 * nv], np.float32).reshape(3, nv, 3)
-    faces = np.frombuffer(raw[32 + 36 * nv:], np.int32).reshape(nf, 3)
-    return f32[0], f32[1], f32[2], faces
+    uv = np.frombuffer(raw[32 + 36 * nv:32 + 44 * nv], np.float32).reshape(nv, 2)
+    faces = np.frombuffer(raw[32 + 44 * nv:], np.int32).reshape(nf, 3)
+    return f32[0], f32[1], f32[2], uv, faces
 
 
 def test_mesh_cache_holds_the_parsed_mesh(tmp_path):
@@ -111,8 +112,9 @@ def test_mesh_cache_holds_the_parsed_mesh(tmp_path):
         nv, nf = int(head[0]), int(head[1])
         rows = [list(map(float, l.split())) for l in open(o).read().splitlines()[1:1 + nv]]
         faces = [list(map(int, l.split())) for l in open(o).read().splitlines()[1 + nv:1 + nv + nf]]
-        v, n, t, f = _read_cache(o + ".gbbin")
+        v, n, t, uv, f = _read_cache(o + ".gbbin")
         assert np.array_equal(v, np.float32(np.array(rows)[:, 0:3]))
+        assert np.array_equal(uv, np.float32(np.array(rows)[:, 3:5]))
         assert np.array_equal(n, np.float32(np.array(rows)[:, 5:8]))
         assert np.array_equal(t, np.float32(np.array(rows)[:, 8:11]))
         assert np.array_equal(f, np.array(faces, np.int32))
@@ -125,5 +127,5 @@ def test_mesh_cache_holds_the_parsed_mesh(tmp_path):
     open(o, "w").write("\n".join(text) + "\n")
     os.utime(o, ns=(os.stat(o).st_atime_ns, os.stat(o).st_mtime_ns + 10 ** 9))
     load()
-    v, _, _, _ = _read_cache(o + ".gbbin")
+    v, _, _, _, _ = _read_cache(o + ".gbbin")
     assert v[0, 0] == np.float32(float(vals[0]))
