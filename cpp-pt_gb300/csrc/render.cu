@@ -178,7 +178,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_shadow(DevScene S, PathBuffer
 // the scene's light list inside the arena and the job's film offset.  A
 // single-scene render is a table of one job (so batched and single renders
 // run the same instructions and give bit-identical images).
-__global__ void __launch_bounds__(256) k_shade(DevScene S, PathBuffers B, int cur, WaveCounters* ctr,
+__global__ void __launch_bounds__(256, 3) k_shade(DevScene S, PathBuffers B, int cur, WaveCounters* ctr,
                                                unsigned long long* __restrict__ film,
                                                const DevBatchJob* __restrict__ jobs) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;

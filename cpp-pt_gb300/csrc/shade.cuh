@@ -154,7 +154,8 @@ __device__ __forceinline__ Surf make_surf(const DevScene& S, int32_t prim, f3 o,
     s.t = normalized(cross(bt, n));
     s.mat = vi.w;
     DevMaterial m = S.mats[vi.w];
-    f3 nmap = mk(0.f, 0.f, 1.f);  // tangent-space normal (identity for the constant map rgb(0.5,0.5,1))
+    f3 nmap = mk(0.f, 0.f, 1.f);  // tangent-space normal of a normal-map texture
+    bool mapped = false;          // the constant map rgb(0.5,0.5,1) is the identity
     if (m.tex != kNoTextures) {
         // triangle.h:91-94: uv1 * alpha + uv2 * beta + uv3 * gamma
         const float2 t0 = __ldg(S.v_uv + vi.x), t1 = __ldg(S.v_uv + vi.y), t2 = __ldg(S.v_uv + vi.z);
@@ -164,6 +165,7 @@ __device__ __forceinline__ Surf make_surf(const DevScene& S, int32_t prim, f3 o,
         if (first_hit && tn != kNoTex && (m.kind == PT_MAT_DIFFUSE_ || m.kind == PT_MAT_GGX_)) {
             const f3 c = tex_sample(S, tn, u, v);  // standard_material.h:64-71
             nmap = mk(c.x * 2.0f - 1.0f, c.y * 2.0f - 1.0f, c.z);
+            mapped = true;
         }
         apply_textures(S, m, u, v);
     }
@@ -174,7 +176,8 @@ __device__ __forceinline__ Surf make_surf(const DevScene& S, int32_t prim, f3 o,
     // (standard_material.h:64-71: Mat3(tangent, bitangent, normal) times the
     // map's value) and the re-orthogonalisation only run at the first hit.
     if (first_hit) {
-        if (m.kind == PT_MAT_DIFFUSE_ || m.kind == PT_MAT_GGX_) s.n = normalized(s.t * nmap.x + s.b * nmap.y + s.n * nmap.z);
+        if (m.kind == PT_MAT_DIFFUSE_ || m.kind == PT_MAT_GGX_)
+            s.n = normalized(mapped ? s.t * nmap.x + s.b * nmap.y + s.n * nmap.z : s.n);
         s.b = normalized(cross(s.n, s.t));
         s.t = normalized(cross(s.b, s.n));
     }
