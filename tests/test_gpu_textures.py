@@ -50,3 +50,23 @@ def test_textures_in_every_mode_and_batched(gpu_lib, tmp_path):
     for j, img in zip(jobs, imgs):
         ref = gs.render(j["spp"], max_depth=j["max_depth"], seed=j["seed"])
         assert np.array_equal(img.view(np.uint32), ref.view(np.uint32))
+
+
+def test_batch_of_textured_and_plain_scenes(gpu_lib, tmp_path):
+    """The batch arena appends every scene's textures and rebases the
+    materials' texture slots: a batch of a plain scene and two textured
+    rooms (one with its own copies of the files, one sharing none) gives
+    each job its single render, bit for bit."""
+    from cpppt import scenes
+    from cpppt.lib import GpuBatch, GpuScene
+    from tests import texscene
+    a = GpuScene(scenes.cornell(24, 16))
+    b = GpuScene(settings_file=texscene.write(str(tmp_path / "b")))
+    c = GpuScene(settings_file=texscene.write(str(tmp_path / "c")))
+    batch = GpuBatch([a, b, c])
+    jobs = [dict(scene=1, spp=9, max_depth=6, seed=1), dict(scene=0, spp=4, max_depth=6, seed=2),
+            dict(scene=2, spp=16, max_depth=8, seed=3), dict(scene=1, spp=4, max_depth=3, seed=4)]
+    imgs = batch.render(jobs)
+    for j, img in zip(jobs, imgs):
+        ref = [a, b, c][j["scene"]].render(j["spp"], max_depth=j["max_depth"], seed=j["seed"])
+        assert np.array_equal(img.view(np.uint32), ref.view(np.uint32)), j
