@@ -66,6 +66,8 @@ struct pt_batch {
     int* h_nrec = nullptr;  // pinned
     NNTrainTask* d_tasks = nullptr;  // fused training steps: kNNMaxStepsPerRound per member scene (in `owned`)
     NNTrainTask* h_tasks = nullptr;  // pinned
+    cudaStream_t nn_tst = nullptr;       // training stream (overlaps the wavefront)
+    cudaEvent_t nn_ev_records = nullptr;  // a round's records are complete
 
     ~pt_batch() {
         if (stream) cudaStreamSynchronize(stream);
@@ -82,6 +84,8 @@ struct pt_batch {
         if (h_nnjobs) cudaFreeHost(h_nnjobs);
         if (h_nrec) cudaFreeHost(h_nrec);
         if (h_tasks) cudaFreeHost(h_tasks);
+        if (nn_tst) { cudaStreamSynchronize(nn_tst); cudaStreamDestroy(nn_tst); }
+        if (nn_ev_records) cudaEventDestroy(nn_ev_records);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (stream) cudaStreamDestroy(stream);
@@ -225,6 +229,8 @@ void create_batch(pt_scene* const* scenes, int n, pt_batch* b) {
     ck(cudaMallocHost(&b->h_nrec, sizeof(int) * n), "cudaMallocHost");
     b->d_tasks = dalloc<NNTrainTask>(b->owned, (size_t)n * kNNMaxStepsPerRound);
     ck(cudaMallocHost(&b->h_tasks, sizeof(NNTrainTask) * n * kNNMaxStepsPerRound), "cudaMallocHost");
+    ck(cudaStreamCreateWithFlags(&b->nn_tst, cudaStreamNonBlocking), "cudaStreamCreate");
+    ck(cudaEventCreateWithFlags(&b->nn_ev_records, cudaEventDisableTiming), "cudaEventCreate");
     ck(cudaEventCreate(&b->ev0), "cudaEventCreate");
     ck(cudaEventCreate(&b->ev1), "cudaEventCreate");
     ck(cudaStreamSynchronize(st), "arena merge");
@@ -507,6 +513,8 @@ void render_batch_slot(pt_batch* b, const pt_batch_job* jobs, int n_jobs, float*
         64 + (total / (unsigned long long)capacity + 2 + (unsigned long long)n_jobs) *
                  (unsigned long long)(max_depth + 2) * 4 / (unsigned long long)t.iters_per_graph;
     std::vector<int> left(n_members, -1);  // records kept after a scene's last training round (-1: none)
+    NNTrainPending pending;
+    ck(cudaStreamSynchronize(b->nn_tst), "train");  // nothing of an earlier call is left queued
     double launches = 5;
     unsigned long long rounds = 0;
     while (true) {
@@ -532,15 +540,24 @@ void render_batch_slot(pt_batch* b, const pt_batch_job* jobs, int n_jobs, float*
         if (status & kStatusTensorTimeout) throw Fail(PT_ERR_CUDA, "tensor-core completion wait timed out");
         if (status) throw Fail(PT_ERR_CUDA, "batch render reported an error status");
         if (train) {
-            // every scene with a full batch of records trains, all in the same fused steps
+            // every scene with a full batch of records trains, all in the same
+            // fused steps on the training stream, while the next round fills
+            // the scenes' other record buffers
             std::vector<pt_scene*> sc(n_members, nullptr);
             std::vector<int*> d_count(n_members);
             for (int m = 0; m < n_members; m++) {
                 if (used[m]) sc[m] = b->members[m].scene;
                 d_count[m] = b->d_nrec + m;
             }
-            nn_train_scenes(sc.data(), b->h_nrec, cap.data(), d_count.data(), n_members, b->d_tasks, b->h_tasks,
-                            b->num_sms, st, &launches, left.data());
+            nn_train_enqueue(sc.data(), b->h_nrec, cap.data(), d_count.data(), n_members, b->d_tasks, b->h_tasks,
+                             b->num_sms, st, b->nn_tst, b->nn_ev_records, &launches, left.data(), pending);
+            bool moved = false;
+            for (int m = 0; m < n_members; m++) moved = moved || left[m] >= 0;
+            if (moved) {
+                for (int i = 0; i < n_jobs; i++) b->h_nnjobs[i].rec = b->members[jobs[i].scene].scene->nn_rec;
+                ck(cudaMemcpyAsync(b->d_nnjobs, b->h_nnjobs, sizeof(DevNNJob) * n_jobs, cudaMemcpyHostToDevice, st),
+                   "guide jobs");
+            }
         }
         rounds++;
         if (b->h_ctr->n_cur == 0 && b->h_ctr->work_next >= b->h_ctr->work_total) break;
@@ -550,6 +567,7 @@ void render_batch_slot(pt_batch* b, const pt_batch_job* jobs, int n_jobs, float*
         for (int m = 0; m < n_members; m++)
             if (used[m])
                 b->members[m].scene->nn_rec_count = left[m] >= 0 ? left[m] : std::min(b->h_nrec[m], cap[m]);
+    nn_train_finish(pending);  // the networks are complete before the render returns
     for (int i = 0; i < n_jobs; i++) {
         const pt_batch::Member& m = b->members[jobs[i].scene];
         const size_t off = 3 * (size_t)table[i].film_off;

@@ -486,7 +486,15 @@ void nn_upload(const NNWeights& W, const float* host, cudaStream_t st) {
 void nn_ensure(pt_scene* s) {
     if (s->nn_ready) return;
     nn_alloc(s->nn_owned, &s->nnw, &s->nn_tb, &s->nn_grad, &s->nn_scalars, kNNBatch);
-    s->nn_rec = dalloc<float4>(s->nn_owned, (size_t)kNNRecordCap * 4);
+    for (int k = 0; k < 2; k++) {
+        s->nn_rec_buf[k] = dalloc<float4>(s->nn_owned, (size_t)kNNRecordCap * 4);
+        if (!s->nn_read_done[k])
+            ck(cudaEventCreateWithFlags(&s->nn_read_done[k], cudaEventDisableTiming), "cudaEventCreate");
+    }
+    s->nn_rec_cur = 0;
+    s->nn_rec = s->nn_rec_buf[0];
+    if (!s->nn_tst) ck(cudaStreamCreateWithFlags(&s->nn_tst, cudaStreamNonBlocking), "cudaStreamCreate");
+    if (!s->nn_ev_records) ck(cudaEventCreateWithFlags(&s->nn_ev_records, cudaEventDisableTiming), "cudaEventCreate");
     s->nn_rec_count = 0;
     if (!s->h_rec_left) ck(cudaMallocHost(&s->h_rec_left, sizeof(int)), "cudaMallocHost");
     if (!s->h_scal) ck(cudaMallocHost(&s->h_scal, sizeof(float) * 4), "cudaMallocHost");
@@ -534,11 +542,27 @@ NNPathData nn_path_buffers(pt_scene* s, int capacity, int depth) {
     return s->nnpd;
 }
 
-// Training rounds of one or several scenes' guides (declared in
-// host_internal.h): every scene's step j runs in the same fused launch.
-void train_scenes(pt_scene* const* sc, const int* held, const int* caps, int* const* d_count, int n,
-                  NNTrainTask* d_tasks, NNTrainTask* h_tasks, int num_sms, cudaStream_t st, double* launches,
-                  int* left) {
+// Overlapped training rounds of one or several scenes' guides (declared
+// in host_internal.h): every scene's step j runs in the same fused launch.
+void train_finish(NNTrainPending& P) {
+    if (P.sc.empty()) return;
+    ck(cudaStreamSynchronize(P.tst), "train");
+    for (size_t k = 0; k < P.sc.size(); k++) {
+        pt_scene* s = P.sc[k];
+        uint32_t tstat;
+        std::memcpy(&tstat, &s->h_scal[2], sizeof(tstat));
+        check_status(s, tstat);
+        s->nn_last_loss = s->h_scal[0];
+        s->nn_records += (double)P.steps[k] * s->nn_cfg.batch;
+    }
+    P.sc.clear();
+    P.steps.clear();
+}
+
+void train_enqueue(pt_scene* const* sc, const int* held, const int* caps, int* const* d_count, int n,
+                   NNTrainTask* d_tasks, NNTrainTask* h_tasks, int num_sms, cudaStream_t st, cudaStream_t tst,
+                   cudaEvent_t ev_records, double* launches, int* left, NNTrainPending& P) {
+    train_finish(P);  // h_tasks, h_scal and the pinned counts are free again
     const NNAdam opt;
     std::vector<int> steps(n, 0);
     int max_steps = 0;
@@ -549,7 +573,8 @@ void train_scenes(pt_scene* const* sc, const int* held, const int* caps, int* co
         max_steps = std::max(max_steps, steps[k]);
     }
     if (max_steps == 0) return;
-    // task table: step level j holds the scenes with more than j steps
+    // task table on the buffers the records are in now: step level j holds
+    // the scenes with more than j steps
     std::vector<int> off(max_steps + 1, 0), max_n(max_steps, 0);
     int t = 0;
     for (int j = 0; j < max_steps; j++) {
@@ -575,36 +600,39 @@ void train_scenes(pt_scene* const* sc, const int* held, const int* caps, int* co
         }
     }
     off[max_steps] = t;
-    ck(cudaMemcpyAsync(d_tasks, h_tasks, sizeof(NNTrainTask) * t, cudaMemcpyHostToDevice, st), "training tasks");
+    // training waits for the round's records
+    ck(cudaEventRecord(ev_records, st), "event");
+    ck(cudaStreamWaitEvent(tst, ev_records, 0), "wait records");
+    ck(cudaMemcpyAsync(d_tasks, h_tasks, sizeof(NNTrainTask) * t, cudaMemcpyHostToDevice, tst), "training tasks");
     for (int k = 0; k < n; k++)
-        if (steps[k] > 0) ck(cudaMemsetAsync(sc[k]->nn_scalars + 2, 0, sizeof(float), st), "memset status");
+        if (steps[k] > 0) ck(cudaMemsetAsync(sc[k]->nn_scalars + 2, 0, sizeof(float), tst), "memset status");
     for (int j = 0; j < max_steps; j++) {
-        launch_nn_train_tasks(d_tasks + off[j], off[j + 1] - off[j], max_n[j], num_sms, st, true, true);
+        launch_nn_train_tasks(d_tasks + off[j], off[j + 1] - off[j], max_n[j], num_sms, tst, true, true);
         if (launches) *launches += 5;
     }
+    P.tst = tst;
     for (int k = 0; k < n; k++) {
         if (steps[k] == 0) continue;
         pt_scene* s = sc[k];
-        const int batch = s->nn_cfg.batch;
+        const int batch = s->nn_cfg.batch, cur = s->nn_rec_cur, nxt = 1 - cur;
+        ck(cudaMemcpyAsync(s->h_scal, s->nn_scalars, sizeof(float) * 4, cudaMemcpyDeviceToHost, tst), "copy");
+        ck(cudaEventRecord(s->nn_read_done[cur], tst), "event");
+        // the render stream continues in the other buffer once the training
+        // that last read it has finished; the records after the last full
+        // batch go to its front (this round's training does not read them)
         const int kept = std::min(held[k], caps[k]) - steps[k] * batch;
+        ck(cudaStreamWaitEvent(st, s->nn_read_done[nxt], 0), "wait training");
         if (kept > 0)
-            ck(cudaMemcpyAsync(s->nn_rec, s->nn_rec + (size_t)4 * steps[k] * batch, sizeof(float4) * 4 * kept,
-                               cudaMemcpyDeviceToDevice, st), "keep records");
+            ck(cudaMemcpyAsync(s->nn_rec_buf[nxt], s->nn_rec_buf[cur] + (size_t)4 * steps[k] * batch,
+                               sizeof(float4) * 4 * kept, cudaMemcpyDeviceToDevice, st), "keep records");
         *s->h_rec_left = kept;
         ck(cudaMemcpyAsync(d_count[k], s->h_rec_left, sizeof(int), cudaMemcpyHostToDevice, st), "records");
-        ck(cudaMemcpyAsync(s->h_scal, s->nn_scalars, sizeof(float) * 4, cudaMemcpyDeviceToHost, st), "copy");
-        left[k] = kept;
-    }
-    ck(cudaStreamSynchronize(st), "train");
-    for (int k = 0; k < n; k++) {
-        if (steps[k] == 0) continue;
-        pt_scene* s = sc[k];
-        uint32_t tstat;
-        std::memcpy(&tstat, &s->h_scal[2], sizeof(tstat));
-        check_status(s, tstat);
+        s->nn_rec_cur = nxt;
+        s->nn_rec = s->nn_rec_buf[nxt];
         s->nn_steps += steps[k];
-        s->nn_last_loss = s->h_scal[0];
-        s->nn_records += (double)steps[k] * s->nn_cfg.batch;
+        left[k] = kept;
+        P.sc.push_back(s);
+        P.steps.push_back(steps[k]);
     }
 }
 
@@ -615,6 +643,7 @@ void render_nn(pt_scene* s, const pt_render_desc* desc, float* d_dst, bool guide
     cudaStream_t st = s->stream;
     const bool train = guided && !(desc->flags & PT_FLAG_NN_FREEZE);
     if (guided) nn_ensure(s);
+    if (s->nn_tst) ck(cudaStreamSynchronize(s->nn_tst), "train");  // nothing of an earlier call is left queued
     RenderParams P{};
     P.spp = desc->spp;
     int ax = (int)std::lround(std::sqrt((double)desc->spp));
@@ -663,6 +692,7 @@ void render_nn(pt_scene* s, const pt_render_desc* desc, float* d_dst, bool guide
         64 + (total / (unsigned long long)capacity + 2) * (unsigned long long)(desc->max_depth + 2) * 4 / kItersPerGraph;
     double records = 0;
     int rec_left = -1;  // records kept after the last round's training (-1: that round did not train)
+    NNTrainPending pending;
     for (unsigned long long round = 0;; round++) {
         for (int k = 0; k < kItersPerGraph; k++) {
             const int cur = k & 1;
@@ -679,15 +709,21 @@ void render_nn(pt_scene* s, const pt_render_desc* desc, float* d_dst, bool guide
         check_status(s, s->h_ctr->status);
         rec_left = -1;
         if (train && s->h_ctr->n_rec >= batch) {
+            // this round's full batches train on the training stream while
+            // the next round fills the other record buffer
             int* d_count = &s->d_ctr->n_rec;
-            train_scenes(&s, &s->h_ctr->n_rec, &rec_cap, &d_count, 1, s->d_tasks, s->h_tasks, s->num_sms, st,
-                         &launches, &rec_left);
+            train_enqueue(&s, &s->h_ctr->n_rec, &rec_cap, &d_count, 1, s->d_tasks, s->h_tasks, s->num_sms, st,
+                          s->nn_tst, s->nn_ev_records, &launches, &rec_left, pending);
             records += (double)(std::min(s->h_ctr->n_rec, rec_cap) - rec_left);
+            nj.rec = s->nn_rec;
+            ck(cudaMemcpyAsync(s->d_nnjob, s->h_nnjob, sizeof(DevNNJob), cudaMemcpyHostToDevice, st),
+               "guide job table");
         }
         if (s->h_ctr->n_cur == 0 && s->h_ctr->work_next >= s->h_ctr->work_total) break;
         if (round > max_rounds) throw Fail(PT_ERR_LIMIT, "render did not converge within the iteration bound");
     }
     if (train) s->nn_rec_count = rec_left >= 0 ? rec_left : std::min(s->h_ctr->n_rec, rec_cap);
+    train_finish(pending);  // the network is complete before the render returns
     launch_film_resolve(s->film, d_dst ? d_dst : s->d_out, film_n, 1.0 / (double)desc->spp, st);
     ck(cudaEventRecord(s->ev1, st), "event");
     ck(cudaStreamSynchronize(st), "render");
@@ -1306,11 +1342,13 @@ namespace hostimpl {
 void nn_ensure_scene(pt_scene* s) { nn_ensure(s); }
 NNNorm nn_scene_norm(const pt_scene* s) { return scene_norm(s); }
 int nn_record_cap(const pt_scene* s) { return std::min(kNNRecordCap, s->nn_cfg.steps_per_round * s->nn_cfg.batch); }
-void nn_train_scenes(pt_scene* const* scenes, const int* held, const int* caps, int* const* d_count, int n,
-                     NNTrainTask* d_tasks, NNTrainTask* h_tasks, int num_sms, cudaStream_t st, double* launches,
-                     int* left) {
-    train_scenes(scenes, held, caps, d_count, n, d_tasks, h_tasks, num_sms, st, launches, left);
+void nn_train_enqueue(pt_scene* const* scenes, const int* held, const int* caps, int* const* d_count, int n,
+                      NNTrainTask* d_tasks, NNTrainTask* h_tasks, int num_sms, cudaStream_t st, cudaStream_t tst,
+                      cudaEvent_t ev_records, double* launches, int* left, NNTrainPending& pending) {
+    train_enqueue(scenes, held, caps, d_count, n, d_tasks, h_tasks, num_sms, st, tst, ev_records, launches, left,
+                  pending);
 }
+void nn_train_finish(NNTrainPending& pending) { train_finish(pending); }
 void scene_check_status(pt_scene* s, uint32_t status) { check_status(s, status); }
 }  // namespace hostimpl
 }  // namespace cpppt_gb300

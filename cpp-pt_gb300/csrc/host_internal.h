@@ -153,7 +153,12 @@ struct pt_scene {
     NNTrainTask* h_tasks = nullptr;  // pinned
     int nn_steps = 0;
     double nn_last_loss = 0, nn_records = 0;
-    float4* nn_rec = nullptr;  // training records carried across renders
+    float4* nn_rec = nullptr;  // training records being collected (one of nn_rec_buf)
+    float4* nn_rec_buf[2] = {nullptr, nullptr};  // double buffer: one collects while the other trains
+    int nn_rec_cur = 0;
+    cudaStream_t nn_tst = nullptr;                   // training stream (overlaps the wavefront)
+    cudaEvent_t nn_read_done[2] = {nullptr, nullptr};  // last training that read nn_rec_buf[k] completed
+    cudaEvent_t nn_ev_records = nullptr;             // a round's records are complete (render stream)
     int nn_rec_count = 0;
     int* h_rec_left = nullptr;  // pinned staging word for the kept-record count
     NNPathData nnpd{};          // per-path buffers of the slot-based wavefront (grown on demand)
@@ -177,6 +182,9 @@ struct pt_scene {
         if (h_rec_left) cudaFreeHost(h_rec_left);
         if (h_scal) cudaFreeHost(h_scal);
         if (h_tasks) cudaFreeHost(h_tasks);
+        if (nn_tst) { cudaStreamSynchronize(nn_tst); cudaStreamDestroy(nn_tst); }
+        for (cudaEvent_t e : nn_read_done) if (e) cudaEventDestroy(e);
+        if (nn_ev_records) cudaEventDestroy(nn_ev_records);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (stream) cudaStreamDestroy(stream);
@@ -189,16 +197,26 @@ namespace hostimpl {
 void nn_ensure_scene(pt_scene* s);               // network, Adam state, record and training buffers
 NNNorm nn_scene_norm(const pt_scene* s);         // position normalisation and BSDF-fraction range
 int nn_record_cap(const pt_scene* s);            // records collected per round (steps_per_round batches, <= 2^22)
-// One training round of several scenes' guides.  Scene k counted held[k]
-// records this round (at most caps[k] of them written); it takes as many
-// Adam steps as it holds full batches, the steps of all scenes fused per
-// step (d_tasks / h_tasks: room for n * kNNMaxStepsPerRound task entries); records beyond
-// the last full batch move to the front of its buffer and *d_count[k]
-// receives their number, as does left[k] (-1: no full batch, nothing
-// changed).  Synchronises st once.
-void nn_train_scenes(pt_scene* const* scenes, const int* held, const int* caps, int* const* d_count, int n,
-                     NNTrainTask* d_tasks, NNTrainTask* h_tasks, int num_sms, cudaStream_t st, double* launches,
-                     int* left);
+// Training of the learned guides overlaps the wavefront.  After a round,
+// nn_train_enqueue queues on the training stream `tst` (after the records
+// the render stream `st` has produced so far) as many Adam steps per scene
+// as it holds full batches (held[k] counted, at most caps[k] written), the
+// steps of all scenes fused per step level; it moves each trained scene's
+// records beyond its last full batch to the front of its other record
+// buffer (on `st`, after the training that last read that buffer),
+// switches the scene to that buffer and sets *d_count[k] and left[k] to the
+// records kept (-1: no full batch, nothing changed).  It returns at once;
+// nn_train_finish waits for the queued steps and takes their status and
+// loss (done at the start of the next enqueue and at the end of a render).
+struct NNTrainPending {
+    std::vector<pt_scene*> sc;
+    std::vector<int> steps;
+    cudaStream_t tst = nullptr;
+};
+void nn_train_enqueue(pt_scene* const* scenes, const int* held, const int* caps, int* const* d_count, int n,
+                      NNTrainTask* d_tasks, NNTrainTask* h_tasks, int num_sms, cudaStream_t st, cudaStream_t tst,
+                      cudaEvent_t ev_records, double* launches, int* left, NNTrainPending& pending);
+void nn_train_finish(NNTrainPending& pending);
 void scene_check_status(pt_scene* s, uint32_t status);  // throws on kernel status bits
 }  // namespace hostimpl
 }  // namespace cpppt_gb300
