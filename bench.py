@@ -3,8 +3,11 @@
 Default workload: the 1M-triangle seeded soup -- 2000 geodesic spheres of
 500 triangles in a closed room, Lambert / GGX / dielectric materials, four
 unit emitters of radiance 20 -- rendered at 1920x1080, max depth 10.  One
-step = `--spp-per-step` samples per pixel over the full frame (a full
-256-spp render is 256 / spp-per-step steps).
+step = `--spp-per-step` samples per pixel over the full frame in one
+pt_render call (default 64: a full 256-spp render is four steps).  Each call
+ends with the wavefront draining its last paths over about ten iterations
+at low occupancy; 64 spp per call amortise that like a full render does (4
+spp per call measured 245 Mpaths/s, 16 spp 272, 64 spp 279).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -42,7 +45,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--spp-per-step", type=int, default=4)
+    ap.add_argument("--spp-per-step", type=int, default=64)
     ap.add_argument("--spheres", type=int, default=2000)
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
