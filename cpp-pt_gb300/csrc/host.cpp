@@ -1349,7 +1349,6 @@ void nn_train_enqueue(pt_scene* const* scenes, const int* held, const int* caps,
                   pending);
 }
 void nn_train_finish(NNTrainPending& pending) { train_finish(pending); }
-void scene_check_status(pt_scene* s, uint32_t status) { check_status(s, status); }
 }  // namespace hostimpl
 }  // namespace cpppt_gb300
 

@@ -217,6 +217,5 @@ void nn_train_enqueue(pt_scene* const* scenes, const int* held, const int* caps,
                       NNTrainTask* d_tasks, NNTrainTask* h_tasks, int num_sms, cudaStream_t st, cudaStream_t tst,
                       cudaEvent_t ev_records, double* launches, int* left, NNTrainPending& pending);
 void nn_train_finish(NNTrainPending& pending);
-void scene_check_status(pt_scene* s, uint32_t status);  // throws on kernel status bits
 }  // namespace hostimpl
 }  // namespace cpppt_gb300

@@ -86,3 +86,30 @@ def test_unreadable_images_are_errors(tmp_path):
         lib.image_load(str(q))
     with pytest.raises(PtError):
         lib.image_load(str(tmp_path / "missing.png"))
+
+
+def test_loader_reads_image_textures(tmp_path):
+    """pt_scene_load decodes a scene's image(...) textures while parsing
+    (before any device work, so this runs anywhere); a missing or
+    undecodable texture file is a PT_ERR_IO."""
+    import ctypes as C
+    from cpppt import lib
+    from tests import texscene
+    L = lib.load()
+
+    def load(settings):
+        h = C.c_void_p()
+        rs = lib.PtRenderDesc()
+        st = L.pt_scene_load(settings.encode(), C.byref(h), C.byref(rs), None, 0)
+        if st == 0:
+            L.pt_scene_destroy(h)
+        return st
+
+    settings = texscene.write(str(tmp_path / "ok"))
+    assert load(settings) in (0, 2, 6), L.pt_last_error()  # 2 or 6: no usable sm_103 device here
+    bad = texscene.write(str(tmp_path / "missing"))
+    (tmp_path / "missing" / "checker.png").unlink()
+    assert load(bad) == 5 and b"checker.png" in L.pt_last_error()
+    broken = texscene.write(str(tmp_path / "broken"))
+    (tmp_path / "broken" / "rough.png").write_bytes(b"\x89PNG\r\n\x1a\n broken")
+    assert load(broken) == 5
