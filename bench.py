@@ -192,6 +192,20 @@ def run_reference(a):
     print(json.dumps(out))
 
 
+def aggregate(dist, paths: float, rays: float, ms: float, device: str = "cpu"):
+    """Whole-job throughput over the ranks (replicas): every rank's paths
+    and rays summed, over the slowest rank's time.  Returns (Mpaths/s,
+    Mrays/s, slowest ms).  dist: torch.distributed after init, or None."""
+    if dist is not None:
+        import torch
+        t = torch.tensor([paths, rays], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        m = torch.tensor([ms], dtype=torch.float64, device=device)
+        dist.all_reduce(m, op=dist.ReduceOp.MAX)
+        paths, rays, ms = float(t[0]), float(t[1]), float(m[0])
+    return paths / (ms / 1000.0) / 1e6, rays / (ms / 1000.0) / 1e6, ms
+
+
 def run_ours(a):
     import torch
     from cpppt.lib import GpuScene, FLAG_TIME_KERNELS, FLAG_COUNT
@@ -236,13 +250,7 @@ def run_ours(a):
             shadow += st["shadow_rays"]
         torch.cuda.synchronize()
         wall = time.time() - t_wall
-    step_ms = float(np.sum(ms))
-    if dist:
-        t = torch.tensor([step_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        step_ms = float(t.item())
-    value = paths * world / (step_ms / 1000.0) / 1e6
-    mrays = (closest + shadow) * world / (step_ms / 1000.0) / 1e6
+    value, mrays, step_ms = aggregate(dist, paths, closest + shadow, float(np.sum(ms)), "cuda")
 
     # end to end through pt_render: image copied to a pinned host buffer each step
     host = torch.empty((a.height, a.width, 3), dtype=torch.float32).pin_memory().numpy()
@@ -257,7 +265,7 @@ def run_ours(a):
         h2d += st["h2d_bytes"]
         d2h += st["d2h_bytes"]
     n_e2e = len(e2e_ms)
-    e2e_val = paths / a.steps * world / (float(np.mean(e2e_ms)) / 1000.0) / 1e6
+    e2e_val, _, _ = aggregate(dist, paths / a.steps, 0.0, float(np.mean(e2e_ms)), "cuda")
 
     # roofline of the dominant kernel (closest-hit extension): algorithmic
     # bytes from a counting render, duration from an event-timed render of
