@@ -1397,7 +1397,14 @@ pt_status pt_scene_load(const char* settings_file, pt_scene** out, pt_render_des
     return PT_OK;
 }
 
-void pt_scene_destroy(pt_scene* s) { delete s; }
+void pt_scene_destroy(pt_scene* s) {
+    if (!s) return;
+    if (s->batch_refs > 0) {  // the last batch holding the scene deletes it
+        s->destroy_pending = true;
+        return;
+    }
+    delete s;
+}
 
 pt_status pt_scene_info(pt_scene* s, int32_t* width, int32_t* height, int32_t* n_triangles, int32_t* n_lights) {
     if (!s) { g_error = "null scene"; return PT_ERR_INVALID; }

@@ -106,6 +106,8 @@ struct SceneTextures {
 struct pt_scene {
     // counts of the device arrays (a multi-scene batch copies them)
     int n_verts = 0, n_mats = 0, n_rbox = 0;
+    int batch_refs = 0;           // batches made from this scene (they use its learned guide)
+    bool destroy_pending = false;  // pt_scene_destroy came while batches still held the scene
     std::vector<int4> h_tex_info;  // host copy of dev.tex_info (batch arena merge)
     std::vector<DevMaterial> h_mats;  // host copy of dev.mats (batch arena merge)
     size_t n_tex_px = 0;           // floats in dev.tex_px

@@ -155,6 +155,8 @@ pt_status pt_scene_create(const pt_scene_desc* desc, pt_scene** scene);
 pt_status pt_scene_load(const char* settings_file, pt_scene** scene, pt_render_desc* settings,
                         char* output_name, int32_t output_name_len);
 
+/* Frees the scene; for a member of a live batch (pt_batch_create) the
+ * release waits until the last such batch is destroyed. */
 void pt_scene_destroy(pt_scene* scene);
 
 /* Image resolution of the scene's camera, its triangle and light counts. */
@@ -243,8 +245,8 @@ pt_status pt_batch_render_device(pt_batch* batch, const pt_batch_job* jobs, int3
  * scene's paths unless PT_FLAG_NN_FREEZE; PT_MODE_MIS with
  * PT_FLAG_UNBIASED_MIS: the same estimator with BSDF sampling only.  With
  * frozen guides each job's image is bit-identical to pt_render of the same
- * scene, mode and flags.  PT_MODE_NN needs the scenes the batch was made
- * from to be alive (the guides live in them).  Replaces nothing in the
+ * scene, mode and flags.  The guides live in the member scenes, which the
+ * batch keeps alive (see pt_scene_destroy).  Replaces nothing in the
  * reference (it renders one scene at a time). */
 pt_status pt_batch_render_ex(pt_batch* batch, const pt_batch_job* jobs, int32_t n_jobs, int32_t mode, uint32_t flags,
                              float* const* rgb_out);

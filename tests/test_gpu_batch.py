@@ -174,3 +174,21 @@ def test_batch_errors(members):
     with pytest.raises(PtError):
         b.render([dict(scene=0, spp=1)], mode=99)
     b.render([dict(scene=0, spp=1)])  # still usable
+
+
+def test_batch_keeps_member_scenes_alive(gpu_lib):
+    """pt_scene_destroy on a member of a live batch is deferred: the batch
+    still renders with that scene's learned guide, and destroying the batch
+    releases the scene."""
+    import ctypes as C
+    from cpppt import scenes
+    from cpppt.lib import FLAG_NN_FREEZE, MODE_NN, GpuBatch, GpuScene
+    gs = GpuScene(scenes.cornell(16, 16))
+    ref = gs.render(4, max_depth=4, seed=2, mode=MODE_NN, flags=FLAG_NN_FREEZE)
+    from cpppt import lib
+    b = GpuBatch([gs])
+    lib._lib.pt_scene_destroy(gs.h)  # destroyed through the C ABI while the batch lives
+    gs.h = C.c_void_p()
+    img = b.render([dict(scene=0, spp=4, max_depth=4, seed=2)], mode=MODE_NN, flags=FLAG_NN_FREEZE)[0]
+    assert np.array_equal(img.view(np.uint32), ref.view(np.uint32))
+    b.close()  # releases the scene
