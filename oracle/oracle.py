@@ -90,6 +90,7 @@ class Oracle:
                 lib.or_render_mis_cols.argtypes = [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _FP]
                 lib.or_render_variant.argtypes = [_P, C.c_int, C.c_int, C.c_int, C.c_int, _FP]
                 lib.or_bsdf_eval.argtypes = [C.c_int, _FP, _FP, _FP, _FP, _FP, _FP, _FP, _IP]
+                lib.or_scene_set_textures.argtypes = [_P, _FP, C.c_int, _IP, _FP, C.c_long, _IP, _FP]
             else:
                 lib.ref_render_mis.restype = C.c_double
                 lib.ref_render_mis.argtypes = [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_char_p, _FP]
@@ -195,6 +196,17 @@ class OracleScene:
         pparent = np.zeros(n, np.int32)
         nn = getattr(self.o.lib, self.o.p + "bvh_dump")(self.h, order, boxes, parent, pparent, cap)
         return order, boxes[:6 * nn].reshape(nn, 6), parent[:nn], pparent
+
+    def set_textures(self, uv, tex_info, tex_px, mat_tex, mat_emit):
+        """Image textures (port only): uv per vertex, {first float, w, h,
+        channels} per texture, the pixels, four texture indices per material
+        (albedo or emission colour, roughness, metal, normal map; -1:
+        constant) and the intensity of textured emitters."""
+        assert self.o.kind == "port"
+        k = [np.ascontiguousarray(a) for a in (uv, tex_info, tex_px, mat_tex, mat_emit)]
+        self._keep += k
+        self.o.lib.or_scene_set_textures(self.h, k[0], len(k[1]) // 4, k[1], k[2], len(k[2]), k[3], k[4])
+        return self
 
     def _dims(self):
         """Image size: the scene's, or the settings file's for a loaded scene."""

@@ -134,6 +134,17 @@ typedef struct {
     int* leaf_prims; /* DFS order of primitives */
     int* prim_parent;
     int root; /* >=0 internal node, <0 leaf, or 0x7fffffff when empty */
+    /* image textures (loader.h:78-92, image_texture.h, rgb_image.h): uv per
+     * vertex (2 floats), texture pixels as the reference's Image holds them,
+     * {first float, width, height, channels} per texture, and per material
+     * the texture of albedo / emission colour, roughness, metal, normal map
+     * (-1: constant) and the intensity of a textured emitter */
+    float* uv;
+    int n_tex;
+    int* tex_info;
+    float* tex_px;
+    int* mat_tex;
+    float* mat_emit;
     /* camera (camera_perspective.h:19-39) */
     v3 cam_origin;
     m3 cam_coords;
@@ -394,7 +405,50 @@ static int any_hit(const or_scene* s, ray_t* r) {
 typedef struct {
     v3 normal, g_normal, tangent, bitangent, hit;
     int prim;
+    float u, v; /* texture coordinates (triangle.h:91-94) */
 } isect;
+
+/* ImageTexture::sample, bilinear branch (image_texture.h:24-41; the harness
+ * pins the uninitialised filtering member to it), over Image::get_pixel with
+ * the REPEAT border (rgb_image.h:210-250).  Vec3 images compute in float with
+ * each (1.0 - x) rounded to float (Vector3<float>::operator*(float)); float
+ * images sum in double (pixel * (1.0 - x) promotes) and round once. */
+static int tex_wrap(int i, int n) {
+    if (i >= n) return i % n;
+    if (i < 0) return i % n + n;
+    return i;
+}
+static const float* tex_px(const or_scene* s, int t, int i, int j) {
+    const int* info = s->tex_info + 4 * t;
+    int w = info[1], h = info[2];
+    long idx = (long)tex_wrap(i, w) + (long)tex_wrap(j, h) * w;
+    if (idx > (long)w * h - 1) idx = (long)w * h - 1; /* the reference reads past the image here */
+    if (idx < 0) idx = 0;
+    return s->tex_px + info[0] + idx * info[3];
+}
+static v3 tex_sample(const or_scene* s, int t, float u, float v) {
+    const int* info = s->tex_info + 4 * t;
+    float x = u * (float)info[1];
+    float y = (float)((1.0 - (double)v) * (double)info[2]);
+    x = (float)((double)x - 0.5);
+    y = (float)((double)y - 0.5);
+    int i = (int)floorf(x), j = (int)floorf(y);
+    x = x - (float)i;
+    y = y - (float)j;
+    const float *p00 = tex_px(s, t, i, j), *p10 = tex_px(s, t, i + 1, j);
+    const float *p01 = tex_px(s, t, i, j + 1), *p11 = tex_px(s, t, i + 1, j + 1);
+    if (info[3] == 1) { /* pixel * (1.0 - x) is double, pixel * x a float product */
+        double r = ((double)p00[0] * (1.0 - (double)x) + (double)(p10[0] * x)) * (1.0 - (double)y) +
+                   ((double)p01[0] * (1.0 - (double)x) + (double)(p11[0] * x)) * (double)y;
+        float f = (float)r;
+        return V(f, f, f);
+    }
+    float omx = (float)(1.0 - (double)x), omy = (float)(1.0 - (double)y);
+    v3 a = vadd(vscale(V(p00[0], p00[1], p00[2]), omx), vscale(V(p10[0], p10[1], p10[2]), x));
+    v3 b = vadd(vscale(V(p01[0], p01[1], p01[2]), omx), vscale(V(p11[0], p11[1], p11[2]), x));
+    return vadd(vscale(a, omy), vscale(b, y));
+}
+static int mat_tex(const or_scene* s, int m, int slot) { return s->mat_tex ? s->mat_tex[4 * m + slot] : -1; }
 
 /* triangle.h:83-114 then Intersection::get_bxdf (intersection.h:25-33).
  * `first`: the Intersection object of PathtracerMIS::integrate is reused for
@@ -413,15 +467,24 @@ static void fill_isect(const or_scene* s, int p, const ray_t* r, const tri_hit* 
     it->tangent = vnorm(vcross(bt, normal));
     it->hit = vadd(r->o, vscale(r->d, h->t));
     it->prim = p;
+    it->u = it->v = 0.0f;
+    if (s->uv) { /* triangle.h:91-94: uv1 * alpha + uv2 * beta + uv3 * gamma */
+        it->u = s->uv[2 * i0] * h->alpha + s->uv[2 * i1] * h->beta + s->uv[2 * i2] * h->gamma;
+        it->v = s->uv[2 * i0 + 1] * h->alpha + s->uv[2 * i1 + 1] * h->beta + s->uv[2 * i2 + 1] * h->gamma;
+    }
     if (!first) return;
-    /* get_normal_mapped: StandardMaterial maps rgb(0.5,0.5,1) to (0,0,1)
-     * through Mat3(tangent, bitangent, normal) (standard_material.h:64-71);
-     * the emissive and dielectric materials keep the normal. */
-    int kind = s->mat_kind[s->tri_mat[p]];
+    /* get_normal_mapped: StandardMaterial maps the normal-map value through
+     * Mat3(tangent, bitangent, normal) (standard_material.h:64-71), the
+     * constant rgb(0.5,0.5,1) to (0,0,1); the emissive and dielectric
+     * materials keep the normal. */
+    int m = s->tri_mat[p], kind = s->mat_kind[m];
     if (kind == MAT_DIFFUSE || kind == MAT_GGX) {
         m3 M = mcols(it->tangent, it->bitangent, it->normal);
-        float nx = (float)(0.5 * 2.0 - 1.0), ny = (float)(0.5 * 2.0 - 1.0);
-        it->normal = vnorm(mmul(&M, V(nx, ny, 1.0f)));
+        v3 c = V(0.5f, 0.5f, 1.0f);
+        int tn = mat_tex(s, m, 3);
+        if (tn >= 0) c = tex_sample(s, tn, it->u, it->v);
+        float nx = (float)((double)c.x * 2.0 - 1.0), ny = (float)((double)c.y * 2.0 - 1.0);
+        it->normal = vnorm(mmul(&M, V(nx, ny, c.z)));
     }
     it->bitangent = vnorm(vcross(it->normal, it->tangent));
     it->tangent = vnorm(vcross(it->bitangent, it->normal));
@@ -543,15 +606,26 @@ typedef struct {
     float ior;
 } bsdf_t;
 
-static bsdf_t make_bsdf(const or_scene* s, int prim) {
-    const float* p = s->mat_params + 8 * s->tri_mat[prim];
+/* Material::get_bxdf at texture coordinates (u, v): StandardMaterial
+ * (standard_material.h:46-61: Diffuse(albedo) when metal < 0.1, else
+ * Glossy(roughness)), EmissiveMaterial (emissive_material.h:28-30: colour x
+ * intensity), from constants or image textures. */
+static bsdf_t make_bsdf(const or_scene* s, int prim, float u, float v) {
+    int m = s->tri_mat[prim];
+    const float* p = s->mat_params + 8 * m;
     bsdf_t b;
     memset(&b, 0, sizeof(b));
-    b.kind = s->mat_kind[s->tri_mat[prim]];
-    if (b.kind == MAT_EMISSIVE) b.col = vscale(V(p[0], p[1], p[2]), p[5]);
-    else b.col = V(p[0], p[1], p[2]);
+    b.kind = s->mat_kind[m];
+    int ta = mat_tex(s, m, 0), tr = mat_tex(s, m, 1), tm = mat_tex(s, m, 2);
+    if (b.kind == MAT_EMISSIVE) {
+        if (ta >= 0) b.col = vscale(tex_sample(s, ta, u, v), s->mat_emit[m]);
+        else b.col = vscale(V(p[0], p[1], p[2]), p[5]);
+    } else {
+        b.col = ta >= 0 ? tex_sample(s, ta, u, v) : V(p[0], p[1], p[2]);
+        if (tm >= 0) b.kind = (double)tex_sample(s, tm, u, v).x < 0.1 ? MAT_DIFFUSE : MAT_GGX;
+    }
     if (b.kind == MAT_GGX) {
-        float r = p[3];
+        float r = tr >= 0 ? tex_sample(s, tr, u, v).x : p[3];
         float a2 = r * r;
         b.alpha = a2 > 0.01f ? a2 : 0.01f; /* std::max(r*r, 0.01f) */
         b.delta = (double)r < 0.01;
@@ -629,7 +703,7 @@ static dsample bsdf_sample(const bsdf_t* b, mt19937* g, v3 wo, const isect* it) 
 }
 
 /* Triangle::sample (triangle.h:209-269): position and interpolated normal */
-static void tri_sample(const or_scene* s, int p, mt19937* g, v3* pos, v3* normal) {
+static void tri_sample(const or_scene* s, int p, mt19937* g, v3* pos, v3* normal, float* u, float* v) {
     float r1 = mt_float(g), r2 = mt_float(g);
     float al = r1, be = r2;
     if ((double)(al + be) > 1.0) { al = (float)(1.0 - (double)al); be = (float)(1.0 - (double)be); }
@@ -637,6 +711,11 @@ static void tri_sample(const or_scene* s, int p, mt19937* g, v3* pos, v3* normal
     int i0 = s->tri[3 * p], i1 = s->tri[3 * p + 1], i2 = s->tri[3 * p + 2];
     *pos = vadd(vadd(vscale(s->pos[i0], al), vscale(s->pos[i1], be)), vscale(s->pos[i2], ga));
     *normal = vnorm(vadd(vadd(vscale(s->nrm[i0], al), vscale(s->nrm[i1], be)), vscale(s->nrm[i2], ga)));
+    *u = *v = 0.0f;
+    if (s->uv) { /* triangle.h:244-249: uv1 * alpha + uv2 * beta + uv2 * gamma (the second vertex twice) */
+        *u = s->uv[2 * i0] * al + s->uv[2 * i1] * be + s->uv[2 * i1] * ga;
+        *v = s->uv[2 * i0 + 1] * al + s->uv[2 * i1 + 1] * be + s->uv[2 * i1 + 1] * ga;
+    }
 }
 
 static float tri_area(const or_scene* s, int p) { /* triangle.h:197-207 */
@@ -653,8 +732,9 @@ static light_sample light_connect(const or_scene* s, mt19937* g, const isect* fr
     int p = s->light_tri[k];
     light_sample ls;
     v3 normal;
-    tri_sample(s, p, g, &ls.position, &normal);
-    bsdf_t e = make_bsdf(s, p);
+    float su, sv;
+    tri_sample(s, p, g, &ls.position, &normal, &su, &sv);
+    bsdf_t e = make_bsdf(s, p, su, sv);
     v3 dir = vnorm(vsub(from->hit, ls.position));
     ls.intensity = vscale(e.col, fabsf(vdot(normal, dir)));
     ls.pdf = (float)(1.0 / (double)tri_area(s, p));
@@ -699,7 +779,7 @@ static v3 integrate(const or_scene* s, float cx, float cy, mt19937* g, int max_d
         ray.max_t = h.t;
         isect it;
         fill_isect(s, prim, &ray, &h, i == 0, &it);
-        bsdf_t b = make_bsdf(s, prim);
+        bsdf_t b = make_bsdf(s, prim, it.u, it.v);
         v3 wo = vneg(ray.d);
         if (b.kind == MAT_EMISSIVE) {
             if (sampled_delta || integrator == 2) {
@@ -811,11 +891,34 @@ void* or_scene_create(int n_meshes, const int* mesh_vert_offset, const int* mesh
     return s;
 }
 
+/* Image textures of a scene read from the reference's files: uv (2 per
+ * vertex), n_tex textures ({first float, width, height, channels} each,
+ * pixels as the reference's Image<Vec3> / Image<float> holds them, n_px
+ * floats in all), per material four texture indices (albedo or emission
+ * colour, roughness, metal, normal map; -1: constant) and the intensity of
+ * a textured emitter. */
+void or_scene_set_textures(void* h, const float* uv, int n_tex, const int* tex_info, const float* tex_px, long n_px,
+                           const int* mat_tex, const float* mat_emit) {
+    or_scene* s = (or_scene*)h;
+    s->uv = malloc(sizeof(float) * 2 * (s->n_verts ? s->n_verts : 1));
+    memcpy(s->uv, uv, sizeof(float) * 2 * s->n_verts);
+    s->n_tex = n_tex;
+    s->tex_info = malloc(sizeof(int) * 4 * (n_tex ? n_tex : 1));
+    memcpy(s->tex_info, tex_info, sizeof(int) * 4 * n_tex);
+    s->tex_px = malloc(sizeof(float) * (n_px ? n_px : 1));
+    memcpy(s->tex_px, tex_px, sizeof(float) * n_px);
+    s->mat_tex = malloc(sizeof(int) * 4 * (s->n_mats ? s->n_mats : 1));
+    memcpy(s->mat_tex, mat_tex, sizeof(int) * 4 * s->n_mats);
+    s->mat_emit = malloc(sizeof(float) * (s->n_mats ? s->n_mats : 1));
+    memcpy(s->mat_emit, mat_emit, sizeof(float) * s->n_mats);
+}
+
 void or_scene_destroy(void* h) {
     or_scene* s = h;
     if (!s) return;
     free(s->pos); free(s->nrm); free(s->btan); free(s->tri); free(s->tri_mat);
     free(s->mat_kind); free(s->mat_params); free(s->tri_light); free(s->light_tri);
+    free(s->uv); free(s->tex_info); free(s->tex_px); free(s->mat_tex); free(s->mat_emit);
     free(s->node_box); free(s->node_child); free(s->node_parent);
     free(s->leaf_start); free(s->leaf_count); free(s->leaf_prims); free(s->prim_parent);
     free(s);
@@ -934,7 +1037,7 @@ void or_bsdf_eval(int n, const float* params, const float* normal, const float* 
         fake.tri_mat = &tm;
         fake.mat_kind = &kind;
         fake.mat_params = mp;
-        bsdf_t b = make_bsdf(&fake, 0);
+        bsdf_t b = make_bsdf(&fake, 0, 0.0f, 0.0f);
         v3 o = V(wo[3 * i], wo[3 * i + 1], wo[3 * i + 2]), w = V(wi[3 * i], wi[3 * i + 1], wi[3 * i + 2]);
         v3 e = bsdf_eval(&b, o, w, &it);
         out_eval[3 * i] = e.x; out_eval[3 * i + 1] = e.y; out_eval[3 * i + 2] = e.z;

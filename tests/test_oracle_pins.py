@@ -66,3 +66,25 @@ def test_reference_harness_matches_fixture(golden):
     s = orc.Oracle("reference").scene(SMALL_SCENES["cornell"]())
     idx, t = s.trace_closest(g["rays"])
     assert np.array_equal(idx, g["hit_index"])
+
+
+@pytest.mark.parametrize("spp_axis,depth,seed", [(2, 8, 3), (1, 12, 40), (3, 4, 7)])
+def test_textured_room_port_matches_reference(tmp_path, spp_axis, depth, seed):
+    """The port's image textures (bilinear sampling, REPEAT wrap, per-hit
+    metal / roughness / albedo, normal map at the first hit, emission texture
+    also at the light sample) give the reference's own render of the
+    textured room's files bit for bit; the texture pixels come from the
+    reference's Image loader."""
+    from oracle import oracle as orc
+    from tests import texscene
+    if not orc.reference_available():
+        pytest.skip("reference harness not built here")
+    ref = orc.Oracle("reference")
+    settings = texscene.write(str(tmp_path))
+    rs = ref.load_files(settings)
+    sc, uv, tex_info, tex_px, mat_tex, mat_emit = texscene.port_inputs(str(tmp_path), ref.image_load)
+    ps = orc.Oracle("port").scene(sc).set_textures(uv, tex_info, tex_px, mat_tex, mat_emit)
+    want, _ = rs.render_mis(spp_axis, depth, seed, threads=1)
+    got, _ = ps.render_mis(spp_axis, depth, seed)
+    assert want.mean() > 0
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
