@@ -120,6 +120,11 @@ __device__ __forceinline__ void tc_end(bool ok, uint32_t tmem, uint32_t bar, uin
 // networks): each tile runs once per distinct job among its rows, staging
 // that job's weights when they differ from the staged ones.  Jobs are
 // rendered in order, so nearly every tile holds one job and runs once.
+// Training runs on its own stream, so an Adam step may rewrite the BF16
+// weights while a tile stages them; the tile then holds a mix of two
+// consecutive networks, which is still one fixed network for all its paths:
+// their mixtures are written once here and both sampled and evaluated from
+// that copy, so the estimator stays unbiased.
 constexpr int kTcInferThreads = kTcRows;
 constexpr int kTcInferSmem = kNNLayers * kTcWLayerBytes + kTcABytes + 64;
 
