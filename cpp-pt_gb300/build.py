@@ -11,6 +11,7 @@ Translation units, compiled in parallel, CUDA for sm_103a only:
   csrc/bvh.cpp    -- BVH builders
   csrc/sdtree.cpp -- SD-tree structure and update
   csrc/image_io.cpp -- PNG / Radiance RGBE texture decoding
+  csrc/loader.cpp -- the reference's scene file formats, mesh cache
 Host files use -ffp-contract=off: the reference-topology BVH and the SD-tree
 update must round like the reference.
 """
@@ -53,7 +54,7 @@ def _commands(extra_cuda: list[str] | None = None):
     common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
     jobs = []
     for name in ("render.cu", "guide.cu", "nn.cu", "batch.cu", "host.cpp", "batch.cpp", "bvh.cpp", "sdtree.cpp",
-                 "image_io.cpp"):
+                 "image_io.cpp", "loader.cpp"):
         src = os.path.join(CSRC, name)
         out = os.path.join(OBJ, name + ".o")
         cmd = [nvcc, "-c", src, "-o", out] + common
