@@ -643,7 +643,10 @@ pt_status pt_batch_create(pt_scene* const* scenes, int32_t n_scenes, pt_batch** 
     if (!b) { g_error = "host allocation failed"; return PT_ERR_MEMORY; }
     const pt_status r = guarded([&] { create_batch(scenes, n_scenes, b); });
     if (r != PT_OK) { delete b; return r; }
-    for (const pt_batch::Member& m : b->members) m.scene->batch_refs++;  // kept alive until the batch goes
+    {
+        std::lock_guard<std::mutex> lock(lifetime_mutex());
+        for (const pt_batch::Member& m : b->members) m.scene->batch_refs++;  // kept alive until the batch goes
+    }
     *out = b;
     return PT_OK;
 }
@@ -653,8 +656,13 @@ void pt_batch_destroy(pt_batch* b) {
     std::vector<pt_scene*> held;
     for (const pt_batch::Member& m : b->members) held.push_back(m.scene);
     delete b;
-    for (pt_scene* s : held)
-        if (--s->batch_refs == 0 && s->destroy_pending) delete s;
+    std::vector<pt_scene*> dead;
+    {
+        std::lock_guard<std::mutex> lock(lifetime_mutex());
+        for (pt_scene* s : held)
+            if (--s->batch_refs == 0 && s->destroy_pending) dead.push_back(s);
+    }
+    for (pt_scene* s : dead) delete s;
 }
 
 pt_status pt_batch_render_device(pt_batch* b, const pt_batch_job* jobs, int32_t n_jobs, float* const* d_rgb_out) {

@@ -1033,9 +1033,12 @@ pt_status pt_scene_load(const char* settings_file, pt_scene** out, pt_render_des
 
 void pt_scene_destroy(pt_scene* s) {
     if (!s) return;
-    if (s->batch_refs > 0) {  // the last batch holding the scene deletes it
-        s->destroy_pending = true;
-        return;
+    {
+        std::lock_guard<std::mutex> lock(lifetime_mutex());
+        if (s->batch_refs > 0) {  // the last batch holding the scene deletes it
+            s->destroy_pending = true;
+            return;
+        }
     }
     delete s;
 }
@@ -1096,6 +1099,11 @@ pt_status pt_render_device_noalloc(pt_scene* s, const pt_render_desc* desc, floa
             throw std::invalid_argument("max_depth must be in [1, 65535]");
         if (desc->mode != PT_MODE_MIS) throw Fail(PT_ERR_INVALID, "the allocation-free render supports PT_MODE_MIS only");
         if (desc->flags != 0) throw Fail(PT_ERR_INVALID, "the allocation-free render takes no flags");
+        int cur_dev = -1;
+        ck(cudaGetDevice(&cur_dev), "cudaGetDevice");
+        if (cur_dev != s->device)
+            throw Fail(PT_ERR_INVALID, "the scene was created on device " + std::to_string(s->device) +
+                                       " but device " + std::to_string(cur_dev) + " is current");
         const long long pixels = (long long)s->width * s->height;
         if (pixels > noalloc_max_pixels())
             throw Fail(PT_ERR_LIMIT, "image of " + std::to_string(pixels) + " pixels exceeds the allocation-free render's "
@@ -1114,6 +1122,13 @@ pt_status pt_render_device_noalloc(pt_scene* s, const pt_render_desc* desc, floa
         ck(render_noalloc(s->dev, P, s->num_sms, desc->max_depth, d_rgb_out, static_cast<cudaStream_t>(stream), &h,
                           &limit),
            "allocation-free render");
+        pt_render_stats R{};
+        R.paths = (double)h.stat_paths;
+        R.closest_rays = (double)h.stat_closest;
+        R.shadow_rays = (double)h.stat_shadow;
+        R.iterations = (double)h.stat_iters;
+        R.nonfinite = (double)h.stat_nonfinite;
+        s->stats = R;
         check_status(s, h.status);
         if (limit) throw Fail(PT_ERR_LIMIT, "render did not converge within the iteration bound");
     });

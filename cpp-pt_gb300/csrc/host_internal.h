@@ -2,6 +2,7 @@
 // batch.cpp): error plumbing, device allocation helpers and the scene object.
 #pragma once
 #include <algorithm>
+#include <mutex>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -106,7 +107,8 @@ struct SceneTextures {
 struct pt_scene {
     // counts of the device arrays (a multi-scene batch copies them)
     int n_verts = 0, n_mats = 0, n_rbox = 0;
-    int batch_refs = 0;           // batches made from this scene (they use its learned guide)
+    int batch_refs = 0;           // batches made from this scene (they use its learned guide);
+                                  // read and changed under lifetime_mutex() only
     bool destroy_pending = false;  // pt_scene_destroy came while batches still held the scene
     std::vector<int4> h_tex_info;  // host copy of dev.tex_info (batch arena merge)
     std::vector<DevMaterial> h_mats;  // host copy of dev.mats (batch arena merge)

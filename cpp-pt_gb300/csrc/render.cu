@@ -418,9 +418,9 @@ void launch_film_resolve(const unsigned long long* film, float* out, int n, doub
 //
 // For callers that cannot allocate device memory at render time: a host
 // whose device memory is reserved up front by another allocator (a caching
-// allocator or an engine's memory budget), a process that is inside CUDA
-// stream capture (cudaMalloc is not allowed there), or a frame loop that
-// must not enter the driver's allocation path.  The wavefront's scratch --
+// allocator or an engine's memory budget), or a frame loop that must not
+// enter the driver's allocation path.  The host still polls the wavefront's
+// counters between rounds of iterations.  The wavefront's scratch --
 // path state, queues, film and counters -- lives in one file-scope
 // __device__ array instead of per-scene buffers.  The array is part of this
 // module, so every GPU that loads the library holds it until the process

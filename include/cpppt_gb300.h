@@ -108,7 +108,7 @@ typedef struct {
     int32_t rr_start;   /* Russian roulette from this bounce index; reference: 3 (i > 2, :118) */
     uint32_t seed;      /* random stream of this render */
     int32_t mode;       /* PT_MODE_* */
-    int32_t flags;      /* reserved, 0 */
+    int32_t flags;      /* PT_FLAG_* bits (below); 0 = the reference's estimator */
 } pt_render_desc;
 
 /* Counters of the last render on a scene. */
@@ -190,18 +190,21 @@ pt_status pt_render_device(pt_scene* scene, const pt_render_desc* desc, float* d
 /* Allocation-free render; it has no counterpart in the reference (whose
  * renderer runs on the CPU).  For callers that cannot allocate device memory
  * when they render: a host whose GPU memory is reserved up front by another
- * allocator or an engine's budget, code running inside CUDA stream capture
- * (where cudaMalloc is not permitted), or a frame loop that must stay off
- * the driver's allocation path.  Same arguments, algorithm and image as
- * pt_render_device (bit-identical for the same desc), enqueued on `stream`
- * and synchronised before return, but it calls no cudaMalloc/cudaFree: its
- * scratch (path state, queues, film, counters) is one fixed array of about
- * 19 MB in the library's device memory, which every GPU that loads the
- * library holds until the process exits.  Limits: at most 262144 pixels
- * (e.g. 512 x 512), PT_MODE_MIS, flags 0; larger images return PT_ERR_LIMIT.
- * The first call on a device looks up the array's device address; make that
- * first call before any stream capture begins.  All calls share the array:
- * calls that overlap on the GPU (other threads or streams) race on it. */
+ * allocator or an engine's budget (a further cudaMalloc would fail or evict
+ * its pools), or a frame loop that must stay off the driver's allocation
+ * path.  Same arguments, algorithm and image as pt_render_device
+ * (bit-identical for the same desc), enqueued on `stream` and synchronised
+ * before return (the host polls the wavefront's counters between rounds of
+ * iterations), but it calls no cudaMalloc/cudaFree: its scratch (path state,
+ * queues, film, counters) is one fixed array of about 19 MB in the library's
+ * device memory, which every GPU that loads the library holds until the
+ * process exits.  Limits: at most 262144 pixels (e.g. 512 x 512),
+ * PT_MODE_MIS, flags 0; larger images return PT_ERR_LIMIT.  The scene must
+ * belong to the current device (PT_ERR_INVALID otherwise).  The first call on
+ * a device looks up the array's device address; make that first call before
+ * any stream capture begins.  All calls share the array: calls that overlap
+ * on the GPU (other threads or streams) race on it.  The call fills the
+ * scene's pt_render_stats (paths, rays, iterations) like pt_render. */
 pt_status pt_render_device_noalloc(pt_scene* scene, const pt_render_desc* desc, float* d_rgb_out, void* stream);
 
 pt_status pt_render_stats_get(pt_scene* scene, pt_render_stats* stats);

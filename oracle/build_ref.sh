@@ -2,7 +2,7 @@
 # Builds the reference renderer's own code (drcd1/cpp-pt, header-only C++) as a
 # shared library for the oracle harness.  Test infrastructure only.
 #
-#   oracle/build_ref.sh [REFERENCE_ROOT]
+#   oracle/build_ref.sh [REFERENCE_ROOT]   (default: $CPPPT_REFERENCE_ROOT, else /root/reference)
 #
 # Step 1 (only where REFERENCE_ROOT exists): copy REFERENCE_ROOT/src and the
 #   vendored stb headers into oracle/_ref/src and apply the compat patches below
@@ -13,7 +13,7 @@
 #   oracle/_ref/libref_harness.so with -O2 -fopenmp -ffp-contract=off.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${1:-/root/reference}"
+REF="${1:-${CPPPT_REFERENCE_ROOT:-/root/reference}}"
 OUT="$HERE/_ref"
 mkdir -p "$OUT"
 if [ -d "$REF/src" ]; then

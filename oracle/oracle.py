@@ -23,7 +23,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libpt_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libref_harness.so")
-REFERENCE_ROOT = "/root/reference"
+# Root of the reference checkout (drcd1/cpp-pt); only the harness build reads it.
+REFERENCE_ROOT = os.environ.get("CPPPT_REFERENCE_ROOT", "/root/reference")
 
 
 def build(force: bool = False) -> str:

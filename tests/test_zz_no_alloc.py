@@ -1,7 +1,7 @@
 """pt_render_device_noalloc: the render entry point for callers that cannot
 allocate device memory while they render (memory reserved up front by
-another allocator, code inside CUDA stream capture, frame loops that must
-stay off the driver's allocation path).  Its scratch is a fixed array inside
+another allocator or an engine's budget, frame loops that must stay off the
+driver's allocation path).  Its scratch is a fixed array inside
 the library, so it must give the same image as pt_render_device and leave
 the device's free memory unchanged.
 
@@ -46,6 +46,8 @@ def test_noalloc_render_matches_allocating_render_twice(gpu_lib):
     got_a = _render(lib_mod, L, gs, "noalloc", 11, out)  # first call on this device: address lookup
     got_b = _render(lib_mod, L, gs, "noalloc", 12, out)  # second call reuses the same scratch
     free1, _ = torch.cuda.mem_get_info()
+    st = gs.stats()  # the allocation-free call fills the scene's counters like pt_render
+    assert st["paths"] == gs.width * gs.height * 64 and st["closest_rays"] >= st["paths"]
     # Same paths, same counter-based random numbers, order-independent
     # fixed-point film: the images are equal to the last bit (tolerance 0).
     np.testing.assert_array_equal(got_a, ref_a)
