@@ -29,6 +29,13 @@ namespace cpppt_gb300 {
 namespace hostimpl {
 extern thread_local std::string g_error;
 
+// Serialises the scene/batch lifetime bookkeeping (pt_scene::batch_refs and
+// destroy_pending) across threads.
+inline std::mutex& lifetime_mutex() {
+    static std::mutex m;
+    return m;
+}
+
 struct Fail : std::runtime_error {
     pt_status code;
     Fail(pt_status c, const std::string& m) : std::runtime_error(m), code(c) {}
