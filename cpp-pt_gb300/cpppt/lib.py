@@ -27,10 +27,11 @@ EXPORTS = ["pt_scene_create", "pt_scene_load", "pt_scene_destroy", "pt_scene_inf
            "pt_render_device_noalloc",
            "pt_render_stats_get", "pt_image_save", "pt_last_error", "pt_debug_ref_topology",
            "pt_debug_sdtree_run", "pt_nn_get_weights", "pt_nn_set_weights", "pt_nn_reset", "pt_nn_stats",
-           "pt_debug_nn_forward", "pt_debug_nn_grad", "pt_nn_configure", "pt_nn_config_get",
+           "pt_debug_nn_forward", "pt_debug_nn_grad", "pt_debug_nn_grad_ex", "pt_nn_configure", "pt_nn_config_get",
            "pt_batch_create", "pt_batch_destroy", "pt_batch_render", "pt_batch_render_device", "pt_batch_set_tuning",
            "pt_batch_get_tuning", "pt_batch_stats", "pt_batch_autotune", "pt_set_mesh_cache",
-           "pt_batch_render_ex", "pt_batch_render_ex_device", "pt_debug_image_load"]
+           "pt_batch_render_ex", "pt_batch_render_ex_device", "pt_debug_image_load", "pt_debug_bsdf",
+           "pt_debug_light_sample"]
 
 
 class PtMaterial(C.Structure):
@@ -117,7 +118,10 @@ def load(path: str = LIB_PATH):
     lib.pt_nn_reset.argtypes = [P, C.c_uint32]
     lib.pt_nn_stats.argtypes = [P, P, P, P]
     lib.pt_debug_nn_forward.argtypes = [P, P, P, P, C.c_int32, P]
+    lib.pt_debug_bsdf.argtypes = [C.c_int32, P, P]
+    lib.pt_debug_light_sample.argtypes = [P, C.c_int32, P, P]
     lib.pt_debug_nn_grad.argtypes = [P, P, P, P, C.c_int32, P, P]
+    lib.pt_debug_nn_grad_ex.argtypes = [P, P, P, P, C.c_int32, C.c_int32, C.c_float, C.c_float, P, P]
     lib.pt_nn_configure.argtypes = [P, P]
     lib.pt_nn_config_get.argtypes = [P, P]
     lib.pt_set_mesh_cache.argtypes = [C.c_int32]
@@ -437,6 +441,26 @@ def sdtree_run(lo, hi, rounds, queries, max_leaves=1 << 20, fn=None, lib=None):
             "flux": flux[:n], "pdf": pdf}
 
 
+def debug_bsdf(cases: np.ndarray) -> np.ndarray:
+    """The integrator's BxDF eval / pdf / sample on the device (pt_debug_bsdf):
+    cases n x 20 -> n x 10 (see the header)."""
+    L = load()
+    c = np.ascontiguousarray(cases, np.float32).reshape(-1, 20)
+    out = np.zeros((len(c), 10), np.float32)
+    _check(L.pt_debug_bsdf(len(c), _ptr(c), _ptr(out)))
+    return out
+
+
+def debug_light_sample(scene: "GpuScene", cases: np.ndarray) -> np.ndarray:
+    """The integrator's light sampling on the device (pt_debug_light_sample):
+    cases n x 6 (point, u0, u1, u2) -> n x 10 (position, normal, Le |cos|, pdf)."""
+    L = load()
+    c = np.ascontiguousarray(cases, np.float32).reshape(-1, 6)
+    out = np.zeros((len(c), 10), np.float32)
+    _check(L.pt_debug_light_sample(scene.h, len(c), _ptr(c), _ptr(out)))
+    return out
+
+
 def nn_forward(weights, lo, hi, inputs):
     """Debug forward pass of the learned guide on the GPU: (n,9) -> (n,41)."""
     L = load()
@@ -459,4 +483,19 @@ def nn_grad(weights, lo, hi, records):
     lo = np.ascontiguousarray(lo, np.float32)
     hi = np.ascontiguousarray(hi, np.float32)
     _check(L.pt_debug_nn_grad(_ptr(w), _ptr(lo), _ptr(hi), _ptr(r), len(r), _ptr(g), C.byref(loss)))
+    return loss.value, g
+
+
+def nn_grad_step(weights, lo, hi, records, divergence=NN_CHI2, c_lo=0.3, c_hi=0.9):
+    """The renderer's training-step gradient on the GPU (device T sum, KL or
+    chi-square weights, BSDF fraction in [c_lo, c_hi]): (loss, dL/dW)."""
+    L = load()
+    w = np.ascontiguousarray(weights, np.float32)
+    r = np.ascontiguousarray(records, np.float32)
+    g = np.zeros(NN_WEIGHTS, np.float32)
+    loss = C.c_float()
+    lo = np.ascontiguousarray(lo, np.float32)
+    hi = np.ascontiguousarray(hi, np.float32)
+    _check(L.pt_debug_nn_grad_ex(_ptr(w), _ptr(lo), _ptr(hi), _ptr(r), len(r), int(divergence), float(c_lo),
+                                 float(c_hi), _ptr(g), C.byref(loss)))
     return loss.value, g

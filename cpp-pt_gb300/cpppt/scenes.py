@@ -220,14 +220,16 @@ def _geodesic_sphere(freq: int):
 
 
 def soup(seed: int = 2, n_spheres: int = 2000, freq: int = 5, width: int = 1920, height: int = 1080,
-         extent: float = 20.0) -> Scene:
+         extent: float = 20.0, only: int | None = None, rough_range: tuple = (0.05, 0.5)) -> Scene:
     """Seeded triangle soup of geodesic spheres (20*freq^2 triangles each;
     freq 5 gives 500) with centres uniform in [0, extent]^3 and radii
     log-uniform in [0.05, 1], inside a closed box room.  One material per
     sphere, uniform among Lambert (albedo U[0.1,0.9]), GGX conductor
     (roughness U[0.05,0.5]) and smooth dielectric (IOR 1.5).  Four emissive
     unit quads with radiance 20 under the ceiling.  2000 spheres x 500 gives
-    the 1M-triangle configuration."""
+    the 1M-triangle configuration.  `only` (DIFFUSE, GGX or DIELECTRIC)
+    gives every sphere that material kind, with the same random draws
+    otherwise; `rough_range` is the GGX roughness interval."""
     rng = np.random.default_rng(seed)
     b = _Builder()
     lo, hi = -2.0, extent + 2.0
@@ -250,10 +252,10 @@ def soup(seed: int = 2, n_spheres: int = 2000, freq: int = 5, width: int = 1920,
     radii = np.exp(rng.uniform(math.log(0.05), math.log(1.0), size=n_spheres))
     kinds = rng.integers(0, 3, size=n_spheres)
     albedo = rng.uniform(0.1, 0.9, size=(n_spheres, 3))
-    rough = rng.uniform(0.05, 0.5, size=n_spheres)
+    rough = rng.uniform(rough_range[0], rough_range[1], size=n_spheres)
     tang = _perp(V)
     for i in range(n_spheres):
-        k = int(kinds[i])
+        k = int(kinds[i]) if only is None else int(only)
         if k == 0:
             m = b.material(DIFFUSE, tuple(albedo[i]))
         elif k == 1:

@@ -1272,43 +1272,102 @@ pt_status pt_debug_nn_forward(const float* weights, const float* lo, const float
     });
 }
 
+pt_status pt_debug_bsdf(int32_t n, const float* cases, float* out) {
+    if (n < 0 || (n > 0 && (!cases || !out))) { g_error = "bad argument"; return PT_ERR_INVALID; }
+    return guarded([&] {
+        if (n == 0) return;
+        for (int32_t i = 0; i < n; i++) {
+            const float k = cases[(size_t)kDebugBsdfIn * i];
+            if (!(k == 0.f || k == 1.f || k == 2.f || k == 3.f)) throw std::invalid_argument("unknown material kind");
+        }
+        DebugCtx c;
+        float* din = dalloc<float>(c.owned, (size_t)kDebugBsdfIn * n);
+        float* dout = dalloc<float>(c.owned, (size_t)kDebugBsdfOut * n);
+        ck(cudaMemcpyAsync(din, cases, sizeof(float) * kDebugBsdfIn * n, cudaMemcpyHostToDevice, c.st), "copy");
+        launch_debug_bsdf(din, dout, n, c.st);
+        ck(cudaGetLastError(), "debug bsdf launch");
+        ck(cudaMemcpyAsync(out, dout, sizeof(float) * kDebugBsdfOut * n, cudaMemcpyDeviceToHost, c.st), "copy");
+        ck(cudaStreamSynchronize(c.st), "debug bsdf");
+    });
+}
+
+pt_status pt_debug_light_sample(pt_scene* s, int32_t n, const float* cases, float* out) {
+    if (!s || n < 0 || (n > 0 && (!cases || !out))) { g_error = "bad argument"; return PT_ERR_INVALID; }
+    return guarded([&] {
+        if (n == 0) return;
+        if (s->dev.n_lights <= 0) throw std::invalid_argument("the scene has no emissive triangles");
+        std::vector<void*> owned;
+        struct Free {
+            std::vector<void*>& v;
+            ~Free() { for (void* p : v) cudaFree(p); }
+        } guard{owned};
+        float* din = dalloc<float>(owned, (size_t)kDebugLightIn * n);
+        float* dout = dalloc<float>(owned, (size_t)kDebugLightOut * n);
+        ck(cudaMemcpyAsync(din, cases, sizeof(float) * kDebugLightIn * n, cudaMemcpyHostToDevice, s->stream), "copy");
+        launch_debug_light(s->dev, din, dout, n, s->stream);
+        ck(cudaGetLastError(), "debug light launch");
+        ck(cudaMemcpyAsync(out, dout, sizeof(float) * kDebugLightOut * n, cudaMemcpyDeviceToHost, s->stream), "copy");
+        ck(cudaStreamSynchronize(s->stream), "debug light");
+    });
+}
+
+namespace {
+// One gradient evaluation of the training kernels on a host batch.  prep:
+// the renderer's own step (T summed, and squared for chi-square, on the
+// device); otherwise the host sums T and the KL weights are used.
+void nn_grad_debug(const float* weights, const float* lo, const float* hi, const float* records, int32_t n, bool prep,
+                   int divergence, float c_lo, float c_hi, float* out_grad, float* out_loss) {
+    DebugCtx c;
+    NNWeights W;
+    NNTrainBuf TB;
+    float *grad, *scal;
+    nn_alloc(c.owned, &W, &TB, &grad, &scal, n);
+    nn_upload(W, weights, c.st);
+    float4* drec = dalloc<float4>(c.owned, (size_t)4 * n);
+    ck(cudaMemcpyAsync(drec, records, sizeof(float) * 16 * n, cudaMemcpyHostToDevice, c.st), "copy");
+    double tsum = 0;
+    if (!prep)
+        for (int i = 0; i < n; i++) tsum += records[16 * i + 13];
+    const float sc0[4] = {0.f, (float)tsum, 0.f, 0.f};
+    ck(cudaMemcpyAsync(scal, sc0, sizeof(sc0), cudaMemcpyHostToDevice, c.st), "copy");
+    NNTrainTask task{};
+    task.W = W;
+    task.N = norm_from(lo, hi);
+    task.N.c_lo = c_lo;
+    task.N.c_hi = c_hi;
+    task.rec = drec;
+    task.n = n;
+    task.chi2 = divergence == PT_NN_CHI2 ? 1 : 0;
+    task.scal = scal;
+    task.TB = TB;
+    task.grad = grad;
+    NNTrainTask* dtask = dalloc<NNTrainTask>(c.owned, 1);
+    ck(cudaMemcpyAsync(dtask, &task, sizeof(task), cudaMemcpyHostToDevice, c.st), "copy");
+    launch_nn_train_tasks(dtask, 1, n, c.sms, c.st, prep, false);
+    ck(cudaMemcpyAsync(out_grad, grad, sizeof(float) * kNNWeightCount, cudaMemcpyDeviceToHost, c.st), "copy");
+    float sc[4] = {0.f, 0.f, 0.f, 0.f};
+    ck(cudaMemcpyAsync(sc, scal, sizeof(sc), cudaMemcpyDeviceToHost, c.st), "copy");
+    ck(cudaStreamSynchronize(c.st), "grad");
+    ck(cudaGetLastError(), "grad");
+    uint32_t tstat;
+    std::memcpy(&tstat, &sc[2], sizeof(tstat));
+    if (tstat & kStatusTensorTimeout) throw Fail(PT_ERR_CUDA, "tensor-core completion wait timed out");
+    if (out_loss) *out_loss = sc[0];
+}
+}  // namespace
+
+pt_status pt_debug_nn_grad_ex(const float* weights, const float* lo, const float* hi, const float* records, int32_t n,
+                              int32_t divergence, float c_lo, float c_hi, float* out_grad, float* out_loss) {
+    if (!weights || !lo || !hi || n <= 0 || !records || !out_grad) { g_error = "bad argument"; return PT_ERR_INVALID; }
+    if (divergence != PT_NN_KL && divergence != PT_NN_CHI2) { g_error = "unknown divergence"; return PT_ERR_INVALID; }
+    if (!(c_lo >= 0.1f && c_lo <= c_hi && c_hi <= 1.0f)) { g_error = "need 0.1 <= c_lo <= c_hi <= 1"; return PT_ERR_INVALID; }
+    return guarded([&] { nn_grad_debug(weights, lo, hi, records, n, true, divergence, c_lo, c_hi, out_grad, out_loss); });
+}
+
 pt_status pt_debug_nn_grad(const float* weights, const float* lo, const float* hi, const float* records, int32_t n,
                            float* out_grad, float* out_loss) {
     if (!weights || !lo || !hi || n <= 0 || !records || !out_grad) { g_error = "bad argument"; return PT_ERR_INVALID; }
-    return guarded([&] {
-        DebugCtx c;
-        NNWeights W;
-        NNTrainBuf TB;
-        float *grad, *scal;
-        nn_alloc(c.owned, &W, &TB, &grad, &scal, n);
-        nn_upload(W, weights, c.st);
-        float4* drec = dalloc<float4>(c.owned, (size_t)4 * n);
-        ck(cudaMemcpyAsync(drec, records, sizeof(float) * 16 * n, cudaMemcpyHostToDevice, c.st), "copy");
-        double tsum = 0;
-        for (int i = 0; i < n; i++) tsum += records[16 * i + 13];
-        const float sc0[4] = {0.f, (float)tsum, 0.f, 0.f};
-        ck(cudaMemcpyAsync(scal, sc0, sizeof(sc0), cudaMemcpyHostToDevice, c.st), "copy");
-        NNTrainTask task{};
-        task.W = W;
-        task.N = norm_from(lo, hi);
-        task.rec = drec;
-        task.n = n;
-        task.scal = scal;
-        task.TB = TB;
-        task.grad = grad;
-        NNTrainTask* dtask = dalloc<NNTrainTask>(c.owned, 1);
-        ck(cudaMemcpyAsync(dtask, &task, sizeof(task), cudaMemcpyHostToDevice, c.st), "copy");
-        launch_nn_train_tasks(dtask, 1, n, c.sms, c.st, false, false);
-        ck(cudaMemcpyAsync(out_grad, grad, sizeof(float) * kNNWeightCount, cudaMemcpyDeviceToHost, c.st), "copy");
-        float sc[4] = {0.f, 0.f, 0.f, 0.f};
-        ck(cudaMemcpyAsync(sc, scal, sizeof(sc), cudaMemcpyDeviceToHost, c.st), "copy");
-        ck(cudaStreamSynchronize(c.st), "grad");
-        ck(cudaGetLastError(), "grad");
-        uint32_t tstat;
-        std::memcpy(&tstat, &sc[2], sizeof(tstat));
-        if (tstat & kStatusTensorTimeout) throw Fail(PT_ERR_CUDA, "tensor-core completion wait timed out");
-        if (out_loss) *out_loss = sc[0];
-    });
+    return guarded([&] { nn_grad_debug(weights, lo, hi, records, n, false, PT_NN_KL, 0.1f, 0.9f, out_grad, out_loss); });
 }
 
 pt_status pt_render_stats_get(pt_scene* s, pt_render_stats* out) {

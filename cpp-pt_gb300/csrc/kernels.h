@@ -63,6 +63,11 @@ cudaError_t render_noalloc(const DevScene& S, const RenderParams& P, int num_sms
 size_t noalloc_scratch_bytes();
 int noalloc_max_pixels();
 int noalloc_paths();
+// Unit-test launches of the integrator's BxDF and light sampling
+// (pt_debug_bsdf / pt_debug_light_sample): floats per case in and out.
+constexpr int kDebugBsdfIn = 20, kDebugBsdfOut = 10, kDebugLightIn = 6, kDebugLightOut = 10;
+void launch_debug_bsdf(const float* in, float* out, int n, cudaStream_t st);
+void launch_debug_light(const DevScene& S, const float* in, float* out, int n, cudaStream_t st);
 // film: 32.32 fixed point per pixel and channel; out = film * scale / 2^32
 void launch_film_resolve(const unsigned long long* film, float* out, int n, double scale, cudaStream_t st);
 

@@ -414,6 +414,72 @@ void launch_film_resolve(const unsigned long long* film, float* out, int n, doub
 }
 
 // ---------------------------------------------------------------------------
+// Unit-test kernels: the integrator's own BxDF and light-sampling functions
+// (shade.cuh) on cases given by the host, one case per thread
+// (pt_debug_bsdf, pt_debug_light_sample).
+// ---------------------------------------------------------------------------
+__global__ void k_debug_bsdf(const float* __restrict__ in, float* __restrict__ out, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* c = in + (size_t)kDebugBsdfIn * i;
+    DevMaterial m{};
+    m.kind = (int32_t)c[0];
+    m.r = c[1];
+    m.g = c[2];
+    m.b = c[3];
+    m.alpha = fmaxf(c[4] * c[4], 0.01f);  // glossy_bxdf.h:77-79, as the scene upload sets it
+    m.delta = (double)c[4] < 0.01 ? 1 : 0;
+    m.ior = c[5];
+    m.tex = kNoTextures;
+    // The frame make_surf builds at a path's first hit on a flat triangle
+    // whose vertices carry normal N and tangent T (bitangent N x T,
+    // loader.h:237), then re-orthogonalised (standard_material.h:64-71).
+    Surf s;
+    s.p = mk(0.f, 0.f, 0.f);
+    s.mat = 0;
+    s.n = normalized(mk(c[6], c[7], c[8]));
+    s.ng = s.n;
+    s.b = normalized(cross(s.n, mk(c[9], c[10], c[11])));
+    s.t = normalized(cross(s.b, s.n));
+    if (m.kind == PT_MAT_DIFFUSE_ || m.kind == PT_MAT_GGX_) s.n = normalized(s.n);
+    s.b = normalized(cross(s.n, s.t));
+    s.t = normalized(cross(s.b, s.n));
+    const f3 wo = mk(c[12], c[13], c[14]), wi = mk(c[15], c[16], c[17]);
+    const f3 ev = bsdf_eval(m, s, wo, wi);
+    const BSample b = bsdf_sample(m, s, wo, c[18], c[19]);
+    float* o = out + (size_t)kDebugBsdfOut * i;
+    o[0] = ev.x;
+    o[1] = ev.y;
+    o[2] = ev.z;
+    o[3] = bsdf_pdf(m, s, wo, wi);
+    o[4] = same_hemisphere(s, wo, wi) ? 1.f : 0.f;
+    o[5] = b.wi.x;
+    o[6] = b.wi.y;
+    o[7] = b.wi.z;
+    o[8] = b.pdf;
+    o[9] = b.delta ? 1.f : 0.f;
+}
+
+__global__ void k_debug_light(DevScene S, const float* __restrict__ in, float* __restrict__ out, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* c = in + (size_t)kDebugLightIn * i;
+    const LSample l = sample_light(S, mk(c[0], c[1], c[2]), c[3], c[4], c[5]);
+    float* o = out + (size_t)kDebugLightOut * i;
+    o[0] = l.pos.x; o[1] = l.pos.y; o[2] = l.pos.z;
+    o[3] = l.n.x; o[4] = l.n.y; o[5] = l.n.z;
+    o[6] = l.le.x; o[7] = l.le.y; o[8] = l.le.z;
+    o[9] = l.pdf;
+}
+
+void launch_debug_bsdf(const float* in, float* out, int n, cudaStream_t st) {
+    if (n > 0) k_debug_bsdf<<<(n + 127) / 128, 128, 0, st>>>(in, out, n);
+}
+void launch_debug_light(const DevScene& S, const float* in, float* out, int n, cudaStream_t st) {
+    if (n > 0) k_debug_light<<<(n + 127) / 128, 128, 0, st>>>(S, in, out, n);
+}
+
+// ---------------------------------------------------------------------------
 // Allocation-free render (pt_render_device_noalloc)
 //
 // For callers that cannot allocate device memory at render time: a host

@@ -2,6 +2,12 @@
 // integrator.  Each function names the reference code it follows; the
 // arithmetic is single precision (the reference's double-literal steps are
 // evaluated in float here, which changes results only in the last bits).
+// Vector arithmetic and the BxDF formulas round every product and sum
+// separately (__fmul_rn / __fadd_rn), in the reference's order: the
+// reference's float code has no fused multiply-adds, and a contracted
+// 1 - z*z near the normal (sin theta of GGX, the cosine-weighted
+// hemisphere) would round differently from its own where the subtraction
+// cancels.
 #pragma once
 #include "dev_types.h"
 
@@ -20,15 +26,20 @@ constexpr float kEps = 1e-4f;  // EPS, src/math/math.h:11
 struct f3 {
     float x, y, z;
 };
+// unfused single-precision steps
+__device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fa(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fs(float a, float b) { return __fsub_rn(a, b); }
+
 __device__ __forceinline__ f3 mk(float x, float y, float z) { return {x, y, z}; }
-__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
-__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
-__device__ __forceinline__ f3 operator*(f3 a, f3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
-__device__ __forceinline__ f3 operator*(f3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return {fa(a.x, b.x), fa(a.y, b.y), fa(a.z, b.z)}; }
+__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return {fs(a.x, b.x), fs(a.y, b.y), fs(a.z, b.z)}; }
+__device__ __forceinline__ f3 operator*(f3 a, f3 b) { return {fm(a.x, b.x), fm(a.y, b.y), fm(a.z, b.z)}; }
+__device__ __forceinline__ f3 operator*(f3 a, float s) { return {fm(a.x, s), fm(a.y, s), fm(a.z, s)}; }
 __device__ __forceinline__ f3 operator-(f3 a) { return {-a.x, -a.y, -a.z}; }
-__device__ __forceinline__ float dot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float dot(f3 a, f3 b) { return fa(fa(fm(a.x, b.x), fm(a.y, b.y)), fm(a.z, b.z)); }
 __device__ __forceinline__ f3 cross(f3 a, f3 b) {
-    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+    return {fs(fm(a.y, b.z), fm(a.z, b.y)), fs(fm(a.z, b.x), fm(a.x, b.z)), fs(fm(a.x, b.y), fm(a.y, b.x))};
 }
 __device__ __forceinline__ float length(f3 a) { return sqrtf(dot(a, a)); }
 __device__ __forceinline__ f3 normalized(f3 a) { return a * (1.0f / length(a)); }
@@ -159,8 +170,8 @@ __device__ __forceinline__ Surf make_surf(const DevScene& S, int32_t prim, f3 o,
     if (m.tex != kNoTextures) {
         // triangle.h:91-94: uv1 * alpha + uv2 * beta + uv3 * gamma
         const float2 t0 = __ldg(S.v_uv + vi.x), t1 = __ldg(S.v_uv + vi.y), t2 = __ldg(S.v_uv + vi.z);
-        const float u = t0.x * alpha + t1.x * beta + t2.x * gamma;
-        const float v = t0.y * alpha + t1.y * beta + t2.y * gamma;
+        const float u = fa(fa(fm(t0.x, alpha), fm(t1.x, beta)), fm(t2.x, gamma));
+        const float v = fa(fa(fm(t0.y, alpha), fm(t1.y, beta)), fm(t2.y, gamma));
         const uint32_t tn = m.tex >> 24;
         if (first_hit && tn != kNoTex && (m.kind == PT_MAT_DIFFUSE_ || m.kind == PT_MAT_GGX_)) {
             const f3 c = tex_sample(S, tn, u, v);  // standard_material.h:64-71
@@ -193,74 +204,81 @@ __device__ __forceinline__ bool same_hemisphere(const Surf& s, f3 wo, f3 wi) {
 // ---------------------------------------------------------------------------
 // GGX (MicrofacetDistribution, microfacet_distribution.h:9-168), isotropic.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float sin_t(f3 w) { return sqrtf(fmaxf(0.0f, 1.0f - w.z * w.z)); }
+__device__ __forceinline__ float sin_t(f3 w) { return sqrtf(fmaxf(0.0f, fs(1.0f, fm(w.z, w.z)))); }
 __device__ __forceinline__ float cos_p(f3 w) { const float s = sin_t(w); return s == 0.f ? 1.f : w.x / s; }
 __device__ __forceinline__ float sin_p(f3 w) { const float s = sin_t(w); return s == 0.f ? 1.f : w.y / s; }
 
 __device__ __forceinline__ float ggx_d(float a, f3 wh) {
     float tan2 = sin_t(wh) / wh.z;
-    tan2 = tan2 * tan2;
+    tan2 = fm(tan2, tan2);
     if (isinf(tan2)) return 0.f;
-    const float cos4 = (wh.z * wh.z) * (wh.z * wh.z);
+    const float cos4 = fm(fm(wh.z, wh.z), fm(wh.z, wh.z));
     const float cp = cos_p(wh), sp = sin_p(wh);
-    const float e = (cp * cp / (a * a) + sp * sp / (a * a)) * tan2;
-    return 1.0f / (kPi * a * a * cos4 * (1.f + e) * (1.f + e));
+    const float a2 = fm(a, a);
+    const float e = fm(fa(fm(cp, cp) / a2, fm(sp, sp) / a2), tan2);
+    const float e1 = fa(1.f, e);
+    return 1.0f / fm(fm(fm(fm(fm(kPi, a), a), cos4), e1), e1);
 }
 // |cos(theta)/sin(theta)| as written at microfacet_distribution.h:138
+// The reference evaluates (-1 + sqrt(1 + x)) / 2 in double; the same value
+// in float without the cancellation is x / (2 (1 + sqrt(1 + x))).
 __device__ __forceinline__ float ggx_lambda(float a, f3 w) {
     const float abs_tan = fabsf(w.z / sin_t(w));
     if (isinf(abs_tan)) return 0.f;
     const float cp = cos_p(w), sp = sin_p(w);
-    const float al = sqrtf(cp * cp * a * a + sp * sp * a * a);
-    const float a2t2 = (al * abs_tan) * (al * abs_tan);
-    return (-1.0f + sqrtf(1.0f + a2t2)) * 0.5f;
+    const float al = sqrtf(fa(fm(fm(fm(cp, cp), a), a), fm(fm(fm(sp, sp), a), a)));
+    const float at = fm(al, abs_tan);
+    const float a2t2 = fm(at, at);
+    return a2t2 / fm(2.0f, fa(1.0f, sqrtf(fa(1.0f, a2t2))));
 }
-__device__ __forceinline__ float ggx_g(float a, f3 wo, f3 wi) { return 1.0f / (1.0f + ggx_lambda(a, wo) + ggx_lambda(a, wi)); }
-__device__ __forceinline__ float ggx_g1(float a, f3 w) { return 1.0f / (1.0f + ggx_lambda(a, w)); }
+__device__ __forceinline__ float ggx_g(float a, f3 wo, f3 wi) {
+    return 1.0f / fa(fa(1.0f, ggx_lambda(a, wo)), ggx_lambda(a, wi));
+}
+__device__ __forceinline__ float ggx_g1(float a, f3 w) { return 1.0f / fa(1.0f, ggx_lambda(a, w)); }
 __device__ __forceinline__ float ggx_pdf_h(float a, f3 wo, f3 wh) {
-    return ggx_d(a, wh) * ggx_g1(a, wo) * fabsf(dot(wo, wh)) / fabsf(wo.z);
+    return fm(fm(ggx_d(a, wh), ggx_g1(a, wo)), fabsf(dot(wo, wh))) / fabsf(wo.z);
 }
 
 // sample11 (microfacet_distribution.h:13-58), PBRT-3 visible-normal sampling
 __device__ __forceinline__ void ggx_sample11(float cos_theta, float U1, float U2, float& sx, float& sy) {
     if (cos_theta > .9999f) {
-        const float r = sqrtf(U1 / (1.f - U1));
-        const float phi = 6.28318530718f * U2;
+        const float r = sqrtf(U1 / fs(1.f, U1));
+        const float phi = fm(6.28318530718f, U2);
         float sn, cs;
         sincosf(phi, &sn, &cs);
-        sx = r * cs;
-        sy = r * sn;
+        sx = fm(r, cs);
+        sy = fm(r, sn);
         return;
     }
-    const float sin_theta = sqrtf(fmaxf(0.f, 1.f - cos_theta * cos_theta));
+    const float sin_theta = sqrtf(fmaxf(0.f, fs(1.f, fm(cos_theta, cos_theta))));
     const float tan_theta = sin_theta / cos_theta;
     const float a = 1.f / tan_theta;
-    const float G1 = 2.f / (1.f + sqrtf(1.f + 1.f / (a * a)));
-    const float A = 2.f * U1 / G1 - 1.f;
-    float tmp = 1.f / (A * A - 1.f);
+    const float G1 = 2.f / fa(1.f, sqrtf(fa(1.f, 1.f / fm(a, a))));
+    const float A = fs(fm(2.f, U1) / G1, 1.f);
+    float tmp = 1.f / fs(fm(A, A), 1.f);
     if (tmp > 1e10f) tmp = 1e10f;
     const float B = tan_theta;
-    const float D = sqrtf(fmaxf(B * B * tmp * tmp - (A * A - B * B) * tmp, 0.f));
-    const float s1 = B * tmp - D, s2 = B * tmp + D;
+    const float D = sqrtf(fmaxf(fs(fm(fm(fm(B, B), tmp), tmp), fm(fs(fm(A, A), fm(B, B)), tmp)), 0.f));
+    const float s1 = fs(fm(B, tmp), D), s2 = fa(fm(B, tmp), D);
     sx = (A < 0.f || s2 > 1.f / tan_theta) ? s1 : s2;
     float S;
-    if (U2 > 0.5f) { S = 1.f; U2 = 2.f * (U2 - .5f); }
-    else { S = -1.f; U2 = 2.f * (.5f - U2); }
-    const float z = (U2 * (U2 * (U2 * 0.27385f - 0.73369f) + 0.46341f)) /
-                    (U2 * (U2 * (U2 * 0.093073f + 0.309420f) - 1.000000f) + 0.597999f);
-    sy = S * z * sqrtf(1.f + sx * sx);
+    if (U2 > 0.5f) { S = 1.f; U2 = fm(2.f, fs(U2, .5f)); }
+    else { S = -1.f; U2 = fm(2.f, fs(.5f, U2)); }
+    const float z = fm(U2, fa(fm(U2, fs(fm(U2, 0.27385f), 0.73369f)), 0.46341f)) /
+                    fa(fm(U2, fs(fm(U2, fa(fm(U2, 0.093073f), 0.309420f)), 1.000000f)), 0.597999f);
+    sy = fm(fm(S, z), sqrtf(fa(1.f, fm(sx, sx))));
     if (isinf(sy) || isnan(sy)) sy = 0.f;
 }
 
 __device__ __forceinline__ f3 ggx_sample_wh(float a, f3 wi, float U1, float U2) {
-    const f3 ws = normalized(mk(a * wi.x, a * wi.y, wi.z));
+    const f3 ws = normalized(mk(fm(a, wi.x), fm(a, wi.y), wi.z));
     float sx, sy;
     ggx_sample11(ws.z, U1, U2, sx, sy);
     const float cp = cos_p(ws), sp = sin_p(ws);
-    const float tmp = cp * sx - sp * sy;
-    sy = sp * sx + cp * sy;
+    const float tmp = fs(fm(cp, sx), fm(sp, sy));
+    sy = fa(fm(sp, sx), fm(cp, sy));
     sx = tmp;
-    return normalized(mk(-a * sx, -a * sy, 1.f));
+    return normalized(mk(-fm(a, sx), -fm(a, sy), 1.f));
 }
 
 // frame helpers: Mat3(tangent, bitangent, normal) and its transpose
@@ -272,14 +290,14 @@ __device__ __forceinline__ f3 reflect(f3 wo, f3 wh) { return normalized(-wo + wh
 // BxDF dispatch: eval includes the cosine (diffuse_bxdf.h:25-27).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ f3 bsdf_eval(const DevMaterial& m, const Surf& s, f3 wo, f3 wi) {
-    if (m.kind == PT_MAT_DIFFUSE_) {
-        const float c = fabsf(dot(s.n, wi)) * kInvPi;
-        return mk(m.r * c, m.g * c, m.b * c);
+    if (m.kind == PT_MAT_DIFFUSE_) {  // albedo * |n.wi| divided by pi (a product with 1/pi, as vdivs)
+        const float c = fabsf(dot(s.n, wi));
+        return mk(fm(m.r, c), fm(m.g, c), fm(m.b, c)) * kInvPi;
     }
     if (m.kind == PT_MAT_GGX_) {  // glossy_bxdf.h:23-33: white, no Fresnel, signed cos
         const f3 wol = normalized(to_local(s, wo)), wil = normalized(to_local(s, wi));
         const f3 wh = normalized(wol + wil);
-        const float v = ggx_g(m.alpha, wol, wil) * ggx_d(m.alpha, wh) / (4.0f * dot(wo, s.n));
+        const float v = fm(ggx_g(m.alpha, wol, wil), ggx_d(m.alpha, wh)) / fm(4.0f, dot(wo, s.n));
         return mk(v, v, v);
     }
     if (m.kind == PT_MAT_DIELECTRIC_) return mk(1.f, 1.f, 1.f);
@@ -291,7 +309,7 @@ __device__ __forceinline__ float bsdf_pdf(const DevMaterial& m, const Surf& s, f
     if (m.kind == PT_MAT_GGX_) {  // glossy_bxdf.h:55-72
         const f3 wol = normalized(to_local(s, wo));
         const f3 wh = normalized(to_local(s, wo + wi));
-        return ggx_pdf_h(m.alpha, wol, wh) / (4.0f * fabsf(dot(wol, wh)));
+        return ggx_pdf_h(m.alpha, wol, wh) / fm(4.0f, fabsf(dot(wol, wh)));
     }
     return 1.0f;
 }
@@ -317,18 +335,18 @@ __device__ __forceinline__ void orthogonal(f3 v1, f3& x, f3& y, f3& z) {
 __device__ __forceinline__ BSample bsdf_sample(const DevMaterial& m, const Surf& s, f3 wo, float u1, float u2) {
     BSample r;
     if (m.kind == PT_MAT_DIFFUSE_) {  // diffuse_bxdf.h:28-41 + sample_hemisphere_cos (math.h:647-653)
-        const float theta = u1 * 2.0f * kPi;
+        const float theta = fm(fm(u1, 2.0f), kPi);
         const float sin_phi = sqrtf(u2);
-        const float cos_phi = sqrtf(fmaxf(0.f, 1.0f - sin_phi * sin_phi));
+        const float cos_phi = sqrtf(fmaxf(0.f, fs(1.0f, fm(sin_phi, sin_phi))));
         float sn, cs;
         sincosf(theta, &sn, &cs);
-        const f3 sm = mk(cs * sin_phi, sn * sin_phi, cos_phi);
+        const f3 sm = mk(fm(cs, sin_phi), fm(sn, sin_phi), cos_phi);
         f3 n = s.n;
         if (dot(n, wo) < 0.f) n = -n;  // correct_normal, bxdf.h:52-57
         f3 x, y, z;
         orthogonal(n, x, y, z);
         r.wi = y * sm.x + z * sm.y + x * sm.z;  // Mat3(y, z, x) * sample
-        r.pdf = sm.z * kInvPi;
+        r.pdf = fm(sm.z, kInvPi);
         r.delta = false;
         return r;
     }
@@ -352,10 +370,10 @@ __device__ __forceinline__ BSample bsdf_sample(const DevMaterial& m, const Surf&
     float n2 = 1.0f / m.ior;
     if (dot(n, wo) < 0.f) { n2 = 1.0f / n2; n = -n; }
     const float ci = dot(wo, n);
-    const float ct2 = 1.0f - n2 * n2 * (1.0f - ci * ci);
+    const float ct2 = fs(1.0f, fm(fm(n2, n2), fs(1.0f, fm(ci, ci))));
     f3 w;
-    if (ct2 < 0.f) w = normalized(-wo + s.n * (dot(s.n, wo) * 2.0f));
-    else w = normalized((-wo) * n2 + n * (n2 * ci - sqrtf(ct2)));
+    if (ct2 < 0.f) w = normalized(-wo + s.n * fm(dot(s.n, wo), 2.0f));
+    else w = normalized((-wo) * n2 + n * fs(fm(n2, ci), sqrtf(ct2)));
     r.wi = w;
     r.pdf = 1.0f;
     r.delta = true;
@@ -381,7 +399,7 @@ __device__ __forceinline__ LSample sample_light(const DevScene& S, f3 from, floa
     const int4 vi = __ldg(S.tri_vidx + prim);
     float al = u1, be = u2;
     if (al + be > 1.0f) { al = 1.0f - al; be = 1.0f - be; }
-    const float ga = 1.0f - al - be;
+    const float ga = fs(fs(1.0f, al), be);
     const f3 a = f3of(__ldg(S.v_pos + vi.x)), b = f3of(__ldg(S.v_pos + vi.y)), c = f3of(__ldg(S.v_pos + vi.z));
     ls.pos = a * al + b * be + c * ga;
     ls.n = normalized(f3of(__ldg(S.v_nrm + vi.x)) * al + f3of(__ldg(S.v_nrm + vi.y)) * be +
@@ -391,11 +409,12 @@ __device__ __forceinline__ LSample sample_light(const DevScene& S, f3 from, floa
         // triangle.h:244-249 interpolates the sampled point's uv as
         // uv1 * alpha + uv2 * beta + uv2 * gamma (the second vertex twice)
         const float2 t0 = __ldg(S.v_uv + vi.x), t1 = __ldg(S.v_uv + vi.y);
-        apply_textures(S, m, t0.x * al + t1.x * be + t1.x * ga, t0.y * al + t1.y * be + t1.y * ga);
+        apply_textures(S, m, fa(fa(fm(t0.x, al), fm(t1.x, be)), fm(t1.x, ga)),
+                       fa(fa(fm(t0.y, al), fm(t1.y, be)), fm(t1.y, ga)));
     }
     const float cosl = fabsf(dot(ls.n, normalized(from - ls.pos)));
-    ls.le = mk(m.r * cosl, m.g * cosl, m.b * cosl);
-    ls.pdf = (1.0f / __ldg(S.light_area + k)) * (1.0f / (float)nl);
+    ls.le = mk(fm(m.r, cosl), fm(m.g, cosl), fm(m.b, cosl));
+    ls.pdf = fm(1.0f / __ldg(S.light_area + k), 1.0f / (float)nl);
     return ls;
 }
 

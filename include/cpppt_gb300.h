@@ -325,6 +325,30 @@ pt_status pt_debug_nn_forward(const float* weights, const float* lo, const float
                               float* out);
 pt_status pt_debug_nn_grad(const float* weights, const float* lo, const float* hi, const float* records, int32_t n,
                            float* out_grad, float* out_loss);
+/* The renderer's own training step on a host batch (without the Adam
+ * update): T summed on the device and, for PT_NN_CHI2, squared first
+ * (records weighted by T^2), with the BSDF selection probability in
+ * [c_lo, c_hi] (pt_nn_configure's range; 0.1 <= c_lo <= c_hi <= 1). */
+pt_status pt_debug_nn_grad_ex(const float* weights, const float* lo, const float* hi, const float* records, int32_t n,
+                              int32_t divergence, float c_lo, float c_hi, float* out_grad, float* out_loss);
+
+/* Unit-test hooks of the integrator's own device functions, checked against
+ * the oracle on the same numbers.  pt_debug_bsdf runs BxDF::eval, ::pdf,
+ * ::sample and BxDF::same_hemisphere (diffuse_bxdf.h:25-49,
+ * glossy_bxdf.h:23-79, microfacet_distribution.h:9-168,
+ * refraction_bxdf.h:17-61, bxdf.h:42-57) on the current device.  Per case,
+ * 20 floats: kind (PT_MAT_*), rgb, roughness, ior, the vertex normal and
+ * tangent of a flat triangle (the shading frame of a path's first hit),
+ * wo, wi, and the two uniform numbers of the sample.  Per case out, 10
+ * floats: eval(wo, wi) (3, the cosine included), pdf(wo, wi),
+ * same_hemisphere(wo, wi) (0/1), the sampled wi (3), its pdf, delta (0/1).
+ * pt_debug_light_sample runs LightGroup::connect_eye_path
+ * (light_group.h:25-30, shape_light.h:24-44, triangle.h:209-269) on the
+ * scene's emitters: 6 floats per case in (the shaded point, then the
+ * numbers picking the light and the point on it), 10 out (position,
+ * normal, Le |n_l . w|, pdf). */
+pt_status pt_debug_bsdf(int32_t n, const float* cases, float* out);
+pt_status pt_debug_light_sample(pt_scene* scene, int32_t n, const float* cases, float* out);
 
 /* Message of the last failed call on this thread ("" when none). */
 const char* pt_last_error(void);

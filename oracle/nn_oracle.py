@@ -5,8 +5,12 @@ The learned guide has no counterpart in the reference renderer, so its
 oracle is this restatement of the network the GPU runs (csrc/nn.cuh,
 csrc/nn.cu): input encoding, 64-64-64-64-48 ReLU MLP without biases, the
 post-processing into an 8-lobe von Mises-Fisher mixture plus a BSDF
-selection probability, and the training loss
-    L = -sum_r T_r log(c_r p_bsdf,r + (1 - c_r) q_r(wi_r)) / sum_r T_r.
+selection probability c = c_lo + (c_hi - c_lo) sigmoid(logit), and the
+training loss
+    L = -sum_r W_r log(c_r p_bsdf,r + (1 - c_r) q_r(wi_r)) / sum_r W_r
+with W = T (the KL divergence) or W = T^2 (the chi-square divergence, the
+renderer's default: its gradient is the gradient of the estimator's second
+moment up to a positive factor).
 Rounding to bfloat16 happens where the GPU rounds (weights, input features,
 hidden activations); everything else is float64.  Gradients come from
 autograd with the rounding treated as the identity.
@@ -60,12 +64,12 @@ def forward_raw(weights: np.ndarray, pos_n, n, wo):
     return x @ Ws[3]
 
 
-def postprocess(raw: torch.Tensor):
+def postprocess(raw: torch.Tensor, c_lo: float = 0.1, c_hi: float = 0.9):
     mu = raw[:, 0:24].reshape(-1, LOBES, 3)
     mu = mu / mu.norm(dim=2, keepdim=True).clamp_min(1e-20)
     kappa = (torch.nn.functional.softplus(raw[:, 24:32]) + 0.1).clamp(max=5000.0)
     w = torch.softmax(raw[:, 32:40], dim=1)
-    c = 0.1 + 0.8 * torch.sigmoid(raw[:, 40])
+    c = c_lo + (c_hi - c_lo) * torch.sigmoid(raw[:, 40])
     return mu, kappa, w, c
 
 
@@ -94,8 +98,10 @@ def forward(weights: np.ndarray, lo, hi, inputs: np.ndarray) -> np.ndarray:
     return params41(raw).numpy()
 
 
-def loss_and_grad(weights: np.ndarray, lo, hi, records: np.ndarray):
-    """records (n, 16): pos, normal, wo, wi, p_bsdf, T, 0, 0."""
+def loss_and_grad(weights: np.ndarray, lo, hi, records: np.ndarray, divergence: str = "kl",
+                  c_lo: float = 0.1, c_hi: float = 0.9):
+    """records (n, 16): pos, normal, wo, wi, p_bsdf, T, 0, 0.  divergence
+    "kl" weighs a record by T, "chi2" by T^2; c in [c_lo, c_hi]."""
     r = torch.tensor(records, dtype=torch.float64)
     W = torch.tensor(weights, dtype=torch.float64, requires_grad=True)
     Ws, off = [], 0
@@ -106,11 +112,12 @@ def loss_and_grad(weights: np.ndarray, lo, hi, records: np.ndarray):
     for l in range(3):
         x = bf16(torch.relu(x @ Ws[l]))
     raw = x @ Ws[3]
-    mu, kappa, w, c = postprocess(raw)
+    mu, kappa, w, c = postprocess(raw, c_lo, c_hi)
     wi = r[:, 9:12]
     q = (w * vmf_pdf(mu, kappa, wi)).sum(1)
     m = (c * r[:, 12] + (1 - c) * q).clamp_min(1e-20)
-    T = r[:, 13] / r[:, 13].sum()
+    T = r[:, 13] ** 2 if divergence == "chi2" else r[:, 13]
+    T = T / T.sum()
     loss = -(T * torch.log(m)).sum()
     loss.backward()
     return float(loss.detach()), W.grad.numpy()

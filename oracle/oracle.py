@@ -91,6 +91,9 @@ class Oracle:
                 lib.or_render_mis_cols.argtypes = [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _FP]
                 lib.or_render_variant.argtypes = [_P, C.c_int, C.c_int, C.c_int, C.c_int, _FP]
                 lib.or_bsdf_eval.argtypes = [C.c_int, _FP, _FP, _FP, _FP, _FP, _FP, _FP, _IP]
+                lib.or_bsdf_sample.argtypes = [C.c_int, _FP, _FP, _FP, _FP, _FP, _FP, _FP, _IP]
+                lib.or_light_sample.argtypes = [_P, C.c_int, _FP, _FP]
+                lib.or_scene_set_fast.argtypes = [_P, C.c_int]
                 lib.or_scene_set_textures.argtypes = [_P, _FP, C.c_int, _IP, _FP, C.c_long, _IP, _FP]
             else:
                 lib.ref_render_mis.restype = C.c_double
@@ -245,6 +248,25 @@ class OracleScene:
                                                     os.path.join(d, "img").encode(), out)
         return out.reshape(H, W, 3), sec
 
+    def set_fast(self, fast: bool = True):
+        """Port only: queries by the culling traversal, which gives the
+        exhaustive recursion's answers (checked by test_oracle_pins.py) at a
+        cost that scales with log(triangles) instead of with the tree."""
+        assert self.o.kind == "port"
+        self.o.lib.or_scene_set_fast(self.h, int(fast))
+        return self
+
+    def light_sample(self, cases):
+        """LightGroup::connect_eye_path on given numbers (port only): cases =
+        n x 6 (from xyz, u0, u1, u2) -> n x 10 (position, normal, Le |cos|,
+        pdf)."""
+        assert self.o.kind == "port"
+        c = np.ascontiguousarray(np.asarray(cases, np.float32).reshape(-1))
+        n = c.size // 6
+        out = np.zeros(10 * n, np.float32)
+        self.o.lib.or_light_sample(self.h, n, c, out)
+        return out.reshape(n, 10)
+
     def render_ppg(self, spp_axis: int, seed_offset: int = 0, threads: int = 0):
         W, H = self._dims()
         out = np.zeros(W * H * 3, np.float32)
@@ -263,3 +285,15 @@ def bsdf_eval(params, normal, tangent, wo, wi):
     nz = np.zeros(n, np.int32)
     lib.or_bsdf_eval(n, f(params), f(normal), f(tangent), f(wo), f(wi), ev, pdf, nz)
     return ev.reshape(n, 3), pdf, nz
+
+
+def bsdf_sample(params, normal, tangent, wo, u):
+    """Oracle BxDF::sample on given uniform numbers u (n x 2): (wi, pdf, delta)."""
+    lib = Oracle("port").lib
+    n = len(params)
+    f = lambda a: np.ascontiguousarray(np.asarray(a, np.float32).reshape(-1))
+    wi = np.zeros(3 * n, np.float32)
+    pdf = np.zeros(n, np.float32)
+    delta = np.zeros(n, np.int32)
+    lib.or_bsdf_sample(n, f(params), f(normal), f(tangent), f(wo), f(u), wi, pdf, delta)
+    return wi.reshape(n, 3), pdf, delta

@@ -134,6 +134,8 @@ typedef struct {
     int* leaf_prims; /* DFS order of primitives */
     int* prim_parent;
     int root; /* >=0 internal node, <0 leaf, or 0x7fffffff when empty */
+    int fast;       /* queries by the culling traversal (closest_fast / any_fast) */
+    float fast_pad; /* box inflation of the culling test */
     /* image textures (loader.h:78-92, image_texture.h, rgb_image.h): uv per
      * vertex (2 floats), texture pixels as the reference's Image holds them,
      * {first float, width, height, channels} per texture, and per material
@@ -389,14 +391,103 @@ static int any_rec(const or_scene* s, int node, ray_t* r) {
     return 0;
 }
 
+/* Culling traversal with the same answers (test infrastructure: it lets the
+ * oracle render million-triangle scenes in seconds; the reference's
+ * exhaustive recursion would take hours).  The reference's closest hit is
+ * the smallest t among the triangles it tests -- those whose ancestor boxes
+ * all pass box_hit -- and on equal t the one visited last, i.e. the larger
+ * position in leaf_prims (leaves are numbered in the recursion's order).
+ * A subtree whose entry distance (boxes inflated by fast_pad) exceeds the
+ * best t so far by more than 2^-8 relative cannot hold a better candidate,
+ * so skipping it, and visiting the nearer child first, changes nothing.
+ * test_oracle_pins.py checks the two traversals against each other. */
+#define OR_FAST_STACK 4096
+static float box_entry(const float* bx, const ray_t* r, float pad) {
+    float t0 = 0.0f;
+    for (int k = 0; k < 3; k++) {
+        float o = vget(r->o, k), d = vget(r->d, k);
+        float a = (bx[k] - pad - o) / d, b = (bx[3 + k] + pad - o) / d; /* d == 0: +-inf or NaN */
+        float near = fminf(a, b);                                      /* fminf drops a NaN */
+        if (near > t0) t0 = near;
+    }
+    return t0;
+}
+
+static int closest_fast(const or_scene* s, ray_t* r, tri_hit* h) {
+    int stack[OR_FAST_STACK];
+    int sp = 0, best = -1, best_rank = -1;
+    float best_t = INFINITY;
+    const float slack = 1.0f + 1.0f / 256.0f;
+    stack[sp++] = s->root;
+    while (sp > 0) {
+        int node = stack[--sp];
+        if (node >= 0) {
+            const float* bx = s->node_box + 6 * node;
+            if (!box_hit(bx, r)) continue;
+            if (best >= 0 && box_entry(bx, r, s->fast_pad) > best_t * slack) continue;
+            int c0 = s->node_child[2 * node], c1 = s->node_child[2 * node + 1];
+            float e0 = c0 >= 0 ? box_entry(s->node_box + 6 * c0, r, s->fast_pad) : 0.0f;
+            float e1 = c1 >= 0 ? box_entry(s->node_box + 6 * c1, r, s->fast_pad) : 0.0f;
+            if (sp + 2 > OR_FAST_STACK) { /* deeper than the stack: the exhaustive recursion */
+                best = -1;
+                closest_rec(s, s->root, r, &best, h);
+                return best;
+            }
+            if (e0 <= e1) { stack[sp++] = c1; stack[sp++] = c0; }
+            else { stack[sp++] = c0; stack[sp++] = c1; }
+        } else {
+            int leaf = ~node;
+            for (int k = 0; k < s->leaf_count[leaf]; k++) {
+                int rank = s->leaf_start[leaf] + k;
+                int p = s->leaf_prims[rank];
+                tri_hit th;
+                if (!tri_test(s, p, r, &th)) continue;
+                if (th.t < best_t || (th.t == best_t && rank > best_rank)) {
+                    best_t = th.t; best_rank = rank; best = p; *h = th;
+                }
+            }
+        }
+    }
+    if (best >= 0) r->max_t = best_t;
+    return best;
+}
+
+static int any_fast(const or_scene* s, ray_t* r) {
+    int stack[OR_FAST_STACK];
+    int sp = 0;
+    const float limit = r->max_t * (1.0f + 1.0f / 256.0f);
+    stack[sp++] = s->root;
+    while (sp > 0) {
+        int node = stack[--sp];
+        if (node >= 0) {
+            const float* bx = s->node_box + 6 * node;
+            if (!box_hit(bx, r)) continue;
+            if (box_entry(bx, r, s->fast_pad) > limit) continue;
+            if (sp + 2 > OR_FAST_STACK) return any_rec(s, s->root, r);
+            stack[sp++] = s->node_child[2 * node + 1];
+            stack[sp++] = s->node_child[2 * node];
+        } else {
+            int leaf = ~node;
+            for (int k = 0; k < s->leaf_count[leaf]; k++) {
+                tri_hit h;
+                if (tri_test(s, s->leaf_prims[s->leaf_start[leaf] + k], r, &h)) return 1;
+            }
+        }
+    }
+    return 0;
+}
+
 static int closest(const or_scene* s, ray_t* r, tri_hit* h) {
     int best = -1;
-    if (s->n_tris > 0) closest_rec(s, s->root, r, &best, h);
+    if (s->n_tris <= 0) return -1;
+    if (s->fast) return closest_fast(s, r, h);
+    closest_rec(s, s->root, r, &best, h);
     return best;
 }
 
 static int any_hit(const or_scene* s, ray_t* r) {
-    return s->n_tris > 0 ? any_rec(s, s->root, r) : 0;
+    if (s->n_tris <= 0) return 0;
+    return s->fast ? any_fast(s, r) : any_rec(s, s->root, r);
 }
 
 /* ----------------------------------------------------------------------- */
@@ -555,11 +646,9 @@ static void md_sample11(float cosTheta, float U1, float U2, float* slope_x, floa
     if (isinf(*slope_y) || isnan(*slope_y)) *slope_y = 0.0f;
 }
 
-static v3 md_sample(float alpha, v3 wi, mt19937* g) {
+static v3 md_sample(float alpha, v3 wi, float U1, float U2) {
     v3 ws = vnorm(V(alpha * wi.x, alpha * wi.y, wi.z));
     float sx, sy;
-    float U1 = mt_float(g);
-    float U2 = mt_float(g);
     md_sample11(cosT(ws), U1, U2, &sx, &sy);
     float tmp = cosP(ws) * sx - sinP(ws) * sy;
     sy = sinP(ws) * sx + cosP(ws) * sy;
@@ -662,10 +751,12 @@ static float bsdf_pdf(const bsdf_t* b, v3 wo, v3 wi, const isect* it) {
     return 1.0f;
 }
 
-static dsample bsdf_sample(const bsdf_t* b, mt19937* g, v3 wo, const isect* it) {
+/* BxDF::sample on the two uniform numbers it draws (Lambert: r1, r2 of
+ * sample_hemisphere_cos; GGX: U1, U2 of MicrofacetDistribution::sample; the
+ * delta GGX and the dielectric draw none). */
+static dsample bsdf_sample_u(const bsdf_t* b, float r1, float r2, v3 wo, const isect* it) {
     dsample d;
     if (b->kind == MAT_DIFFUSE) { /* diffuse_bxdf.h:28-41 */
-        float r1 = mt_float(g), r2 = mt_float(g);
         v3 sm = sample_hemisphere_cos(r1, r2);
         float p = (float)((double)sm.z / OR_PI);
         v3 n = it->normal;
@@ -683,7 +774,7 @@ static dsample bsdf_sample(const bsdf_t* b, mt19937* g, v3 wo, const isect* it) 
         m3 M = mcols(it->tangent, it->bitangent, it->normal);
         m3 Mt = mtranspose(&M);
         v3 wol = vnorm(mmul(&Mt, wo));
-        v3 whl = vnorm(md_sample(b->alpha, wol, g));
+        v3 whl = vnorm(md_sample(b->alpha, wol, r1, r2));
         v3 wh = vnorm(mmul(&M, whl));
         d.wi = reflect(wo, wh);
         d.pdf = bsdf_pdf(b, wo, d.wi, it);
@@ -702,9 +793,17 @@ static dsample bsdf_sample(const bsdf_t* b, mt19937* g, v3 wo, const isect* it) 
     return d;
 }
 
+static dsample bsdf_sample(const bsdf_t* b, mt19937* g, v3 wo, const isect* it) {
+    float r1 = 0.0f, r2 = 0.0f;
+    if (b->kind == MAT_DIFFUSE || (b->kind == MAT_GGX && !b->delta)) {
+        r1 = mt_float(g);
+        r2 = mt_float(g);
+    }
+    return bsdf_sample_u(b, r1, r2, wo, it);
+}
+
 /* Triangle::sample (triangle.h:209-269): position and interpolated normal */
-static void tri_sample(const or_scene* s, int p, mt19937* g, v3* pos, v3* normal, float* u, float* v) {
-    float r1 = mt_float(g), r2 = mt_float(g);
+static void tri_sample(const or_scene* s, int p, float r1, float r2, v3* pos, v3* normal, float* u, float* v) {
     float al = r1, be = r2;
     if ((double)(al + be) > 1.0) { al = (float)(1.0 - (double)al); be = (float)(1.0 - (double)be); }
     float ga = (float)(1.0 - (double)al - (double)be);
@@ -726,14 +825,14 @@ static float tri_area(const or_scene* s, int p) { /* triangle.h:197-207 */
 typedef struct { float pdf; v3 position, intensity, normal; } light_sample;
 
 /* LightGroup::connect_eye_path (light_group.h:25-30) + ShapeLight (shape_light.h:24-44) */
-static light_sample light_connect(const or_scene* s, mt19937* g, const isect* from) {
+static light_sample light_connect_u(const or_scene* s, float u0, float r1, float r2, const isect* from) {
     size_t n = (size_t)s->n_lights;
-    int k = (int)((size_t)(int)(mt_float(g) * (float)n) % n);
+    int k = (int)((size_t)(int)(u0 * (float)n) % n);
     int p = s->light_tri[k];
     light_sample ls;
     v3 normal;
     float su, sv;
-    tri_sample(s, p, g, &ls.position, &normal, &su, &sv);
+    tri_sample(s, p, r1, r2, &ls.position, &normal, &su, &sv);
     bsdf_t e = make_bsdf(s, p, su, sv);
     v3 dir = vnorm(vsub(from->hit, ls.position));
     ls.intensity = vscale(e.col, fabsf(vdot(normal, dir)));
@@ -741,6 +840,14 @@ static light_sample light_connect(const or_scene* s, mt19937* g, const isect* fr
     ls.normal = normal;
     ls.pdf = (float)((double)ls.pdf * (1.0 / (double)(float)n));
     return ls;
+}
+
+/* draws the light index, then the triangle's two numbers (triangle.h:209-215) */
+static light_sample light_connect(const or_scene* s, mt19937* g, const isect* from) {
+    float u0 = mt_float(g);
+    float r1 = mt_float(g);
+    float r2 = mt_float(g);
+    return light_connect_u(s, u0, r1, r2, from);
 }
 
 static float light_pdf(const or_scene* s, int prim) { /* light_group.h:43-55 */
@@ -888,8 +995,18 @@ void* or_scene_create(int n_meshes, const int* mesh_vert_offset, const int* mesh
     s->height = height;
     s->root = 0x7fffffff;
     if (nt > 0) bvh_build(s);
+    float ext = 0.0f;
+    for (int v = 0; v < nv; v++) {
+        float m = fmaxf(fabsf(s->pos[v].x), fmaxf(fabsf(s->pos[v].y), fabsf(s->pos[v].z)));
+        if (m > ext) ext = m;
+    }
+    s->fast_pad = 1e-5f * (2.0f * ext + 1.0f);
     return s;
 }
+
+/* Switches the scene's queries between the reference's exhaustive recursion
+ * (0, the default) and the culling traversal with the same answers (1). */
+void or_scene_set_fast(void* h, int fast) { ((or_scene*)h)->fast = fast; }
 
 /* Image textures of a scene read from the reference's files: uv (2 per
  * vertex), n_tex textures ({first float, width, height, channels} each,
@@ -1043,5 +1160,49 @@ void or_bsdf_eval(int n, const float* params, const float* normal, const float* 
         out_eval[3 * i] = e.x; out_eval[3 * i + 1] = e.y; out_eval[3 * i + 2] = e.z;
         out_pdf[i] = (kind == MAT_DIELECTRIC) ? 1.0f : bsdf_pdf(&b, o, w, &it);
         out_nonzero[i] = same_hemisphere(&it, o, w);
+    }
+}
+
+/* BxDF::sample for n cases on given uniform numbers u (2 per case): out_wi
+ * (3 floats), out_pdf and out_delta.  Same case layout as or_bsdf_eval. */
+void or_bsdf_sample(int n, const float* params, const float* normal, const float* tangent, const float* wo,
+                    const float* u, float* out_wi, float* out_pdf, int* out_delta) {
+    for (int i = 0; i < n; i++) {
+        const float* pp = params + 6 * i;
+        int kind = (int)pp[0];
+        isect it;
+        frame_from(normal + 3 * i, tangent + 3 * i, kind, &it);
+        float mp[8] = {pp[1], pp[2], pp[3], pp[4], pp[5], 1.0f, 0, 0};
+        or_scene fake;
+        memset(&fake, 0, sizeof(fake));
+        int tm = 0;
+        fake.tri_mat = &tm;
+        fake.mat_kind = &kind;
+        fake.mat_params = mp;
+        bsdf_t b = make_bsdf(&fake, 0, 0.0f, 0.0f);
+        v3 o = V(wo[3 * i], wo[3 * i + 1], wo[3 * i + 2]);
+        dsample d = bsdf_sample_u(&b, u[2 * i], u[2 * i + 1], o, &it);
+        out_wi[3 * i] = d.wi.x; out_wi[3 * i + 1] = d.wi.y; out_wi[3 * i + 2] = d.wi.z;
+        out_pdf[i] = d.pdf;
+        out_delta[i] = d.delta;
+    }
+}
+
+/* LightGroup::connect_eye_path from n points on the scene's lights: in = 6
+ * floats per case (from xyz, u0, u1, u2), out = 10 floats (position, normal,
+ * intensity = Le |n_l . w|, pdf). */
+void or_light_sample(void* h, int n, const float* in, float* out) {
+    const or_scene* s = (const or_scene*)h;
+    for (int i = 0; i < n; i++) {
+        const float* c = in + 6 * i;
+        isect it;
+        memset(&it, 0, sizeof(it));
+        it.hit = V(c[0], c[1], c[2]);
+        light_sample ls = light_connect_u(s, c[3], c[4], c[5], &it);
+        float* o = out + 10 * i;
+        o[0] = ls.position.x; o[1] = ls.position.y; o[2] = ls.position.z;
+        o[3] = ls.normal.x; o[4] = ls.normal.y; o[5] = ls.normal.z;
+        o[6] = ls.intensity.x; o[7] = ls.intensity.y; o[8] = ls.intensity.z;
+        o[9] = ls.pdf;
     }
 }

@@ -44,31 +44,69 @@ def test_forward_matches_oracle(gpu_lib):
     np.testing.assert_allclose(got[:, wcols].sum(1), 1.0, atol=1e-5)
 
 
-def test_gradient_matches_oracle(gpu_lib):
-    from cpppt import lib
-    from oracle import nn_oracle
-    rng = np.random.default_rng(3)
-    w = random_weights(4)
-    n = 4096
-    x = random_inputs(n, 5)
+def _grad_records(n, seed):
+    rng = np.random.default_rng(seed)
+    x = random_inputs(n, seed + 2)
     wi = rng.normal(size=(n, 3)); wi /= np.linalg.norm(wi, axis=1, keepdims=True)
-    pb = rng.uniform(0.05, 0.5, n)
-    T = rng.exponential(1.0, n)
     rec = np.zeros((n, 16), np.float32)
     rec[:, 0:9] = x
     rec[:, 9:12] = wi
-    rec[:, 12] = pb
-    rec[:, 13] = T
-    loss, g = lib.nn_grad(w, LO, HI, rec)
-    rloss, rg = nn_oracle.loss_and_grad(w, LO, HI, rec)
-    assert abs(loss - rloss) < 1e-2 * max(1.0, abs(rloss))
+    rec[:, 12] = rng.uniform(0.05, 0.5, n)
+    rec[:, 13] = rng.exponential(1.0, n)
+    return rec
+
+
+# Per-layer agreement of the GPU weight gradient with the FP64 oracle.  The
+# GPU keeps activations and the gradients of each layer's output in BF16
+# (8-bit mantissa, relative rounding 2^-9) and sums the products over the
+# batch in FP32; the oracle rounds the activations the same way but carries
+# the backward pass in FP64.  Over four layers and 4096 records that leaves a
+# few parts per thousand of relative error per layer (measured on a GB300:
+# at most 1.8e-3 relative, cosine above 0.999998, in the first layer; less
+# in the later ones).
+GRAD_COS = 0.99995
+GRAD_REL = 5e-3
+
+
+@pytest.mark.parametrize("case", ["kl_host", "kl", "chi2"])
+def test_gradient_matches_oracle(gpu_lib, case):
+    """kl_host: pt_debug_nn_grad (T summed on the host, KL weights, c in
+    [0.1, 0.9]).  kl / chi2: pt_debug_nn_grad_ex, the renderer's own step
+    (T summed, and squared for chi-square, on the device) with the renderer's
+    default BSDF-fraction range [0.3, 0.9]; chi2 is the renderer's default
+    divergence."""
+    from cpppt import lib
+    from oracle import nn_oracle
+    w = random_weights(4)
+    rec = _grad_records(4096, 3)
+    if case == "kl_host":
+        loss, g = lib.nn_grad(w, LO, HI, rec)
+        rloss, rg = nn_oracle.loss_and_grad(w, LO, HI, rec)
+    else:
+        div = lib.NN_CHI2 if case == "chi2" else lib.NN_KL
+        loss, g = lib.nn_grad_step(w, LO, HI, rec, divergence=div, c_lo=0.3, c_hi=0.9)
+        rloss, rg = nn_oracle.loss_and_grad(w, LO, HI, rec, divergence=case, c_lo=0.3, c_hi=0.9)
+    assert abs(loss - rloss) < 2e-3 * max(1.0, abs(rloss)), (loss, rloss)
     off = 0
     for i, o in [(64, 64), (64, 64), (64, 64), (64, 48)]:
         a, b = g[off:off + i * o], rg[off:off + i * o]
         cos = float(a @ b / (np.linalg.norm(a) * np.linalg.norm(b) + 1e-30))
         rel = float(np.linalg.norm(a - b) / (np.linalg.norm(b) + 1e-30))
-        assert cos > 0.995 and rel < 0.1, (off, cos, rel)
+        assert cos > GRAD_COS and rel < GRAD_REL, (off, cos, rel)
         off += i * o
+
+
+def test_chi2_differs_from_kl(gpu_lib):
+    """The two divergences weigh the same records differently, so their
+    gradients must differ by far more than the rounding error above (the
+    chi-square path is really taken)."""
+    from cpppt import lib
+    w = random_weights(4)
+    rec = _grad_records(2048, 8)
+    _, gk = lib.nn_grad_step(w, LO, HI, rec, divergence=lib.NN_KL)
+    _, gc = lib.nn_grad_step(w, LO, HI, rec, divergence=lib.NN_CHI2)
+    diff = float(np.linalg.norm(gk / np.linalg.norm(gk) - gc / np.linalg.norm(gc)))
+    assert diff > 10 * GRAD_REL, diff
 
 
 def test_guided_render_converges_to_plain(gpu_lib):

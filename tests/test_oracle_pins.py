@@ -88,3 +88,40 @@ def test_textured_room_port_matches_reference(tmp_path, spp_axis, depth, seed):
     got, _ = ps.render_mis(spp_axis, depth, seed)
     assert want.mean() > 0
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+@pytest.mark.parametrize("name", sorted(SMALL_SCENES))
+def test_culling_traversal_matches_goldens(port, golden, name):
+    """The port's culling traversal (set_fast) gives the reference's answers
+    on the golden ray batches and the bit-identical renders."""
+    g = golden(f"{name}_ref.npz")
+    s = port.scene(SMALL_SCENES[name]()).set_fast()
+    idx, t = s.trace_closest(g["rays"])
+    assert np.array_equal(idx, g["hit_index"])
+    assert np.array_equal(t.view(np.uint32), g["hit_t"].view(np.uint32))
+    assert np.array_equal(s.trace_any(g["shadow_rays"]), g["occluded"])
+    img, _ = s.render_mis(2, 8, 0)
+    assert np.array_equal(img.view(np.uint32), g["render_spp2_d8"].view(np.uint32))
+
+
+@pytest.mark.parametrize("make", [lambda: __import__("cpppt.scenes").scenes.soup(seed=9, n_spheres=400),
+                                  lambda: __import__("cpppt.scenes").scenes.slit_room(seed=4, n_boxes=150,
+                                                                                      box_subdiv=2)],
+                         ids=["soup200k", "slitroom29k"])
+def test_culling_traversal_matches_exhaustive(port, make):
+    """Larger scenes than the goldens: the culling traversal against the
+    exhaustive recursion on 2^14 mixed rays (camera, secondary, edge and
+    vertex aims, axis-parallel), closest and any hit, bit for bit."""
+    from cpppt import scenes
+    sc = make()
+    rays = scenes.hit_ray_batch(sc, 1 << 14, seed=21)
+    slow = port.scene(sc)
+    fast = port.scene(sc).set_fast()
+    i0, t0 = slow.trace_closest(rays)
+    i1, t1 = fast.trace_closest(rays)
+    assert (i0 >= 0).mean() > 0.5
+    assert np.array_equal(i0, i1)
+    assert np.array_equal(t0.view(np.uint32), t1.view(np.uint32))
+    sh = rays.copy()
+    sh[:, 6] = np.where(np.isfinite(t0), t0 * np.float32(0.999), np.float32(3.0))
+    assert np.array_equal(slow.trace_any(sh), fast.trace_any(sh))
