@@ -284,14 +284,17 @@ def run_ours(a):
     except Exception:
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    traffic = None
-    tfile = os.path.join(ROOT, "profiles", "extend_traffic.json")
+    # DRAM (and L2) bytes per extension ray measured by ncu over every bounce
+    # of a render of the same scene (profiles/k_extend_soup1M_720p_bounces.md),
+    # scaled by the rays of one launch here
+    traffic, l2_traffic = None, None
+    tfile = os.path.join(ROOT, "profiles", "k_extend_soup1M_720p_traffic.json")
     if os.path.exists(tfile):
         try:
             tj = json.load(open(tfile))
-            traffic = tj.get("bytes_per_ray", None)
-            if traffic is not None:
-                traffic = traffic * cnt["closest_rays"] / max(1.0, n_launch)
+            per_launch = cnt["closest_rays"] / max(1.0, n_launch)
+            traffic = tj["bytes_per_ray"] * per_launch
+            l2_traffic = tj["l2_bytes_per_ray"] * per_launch
         except Exception:
             traffic = None
 
@@ -309,6 +312,9 @@ def run_ours(a):
                             "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800",
                             "unit": "GB/s", "frac": achieved / peak,
                             "traffic": traffic,
+                            "traffic_source": "ncu dram__bytes_read+write per extension ray, all bounces of the "
+                                              "1280x720 render of this scene, x rays per launch",
+                            "l2_traffic": l2_traffic,
                             "algorithmic_bytes_per_launch": alg_bytes / max(1.0, n_launch),
                             "avg_launch_ms": tim["trace_closest_ms"] / max(1.0, n_launch),
                             "per_ray": {"nodes": cnt["extend_nodes"] / cnt["closest_rays"],

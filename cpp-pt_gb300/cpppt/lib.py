@@ -31,7 +31,7 @@ EXPORTS = ["pt_scene_create", "pt_scene_load", "pt_scene_destroy", "pt_scene_inf
            "pt_batch_create", "pt_batch_destroy", "pt_batch_render", "pt_batch_render_device", "pt_batch_set_tuning",
            "pt_batch_get_tuning", "pt_batch_stats", "pt_batch_autotune", "pt_set_mesh_cache",
            "pt_batch_render_ex", "pt_batch_render_ex_device", "pt_debug_image_load", "pt_debug_bsdf",
-           "pt_debug_light_sample"]
+           "pt_debug_light_sample", "pt_debug_traversal_limits", "pt_debug_tensor_wait_timeout"]
 
 
 class PtMaterial(C.Structure):
@@ -59,7 +59,8 @@ class PtRenderDesc(C.Structure):
 class PtRenderStats(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("paths", "closest_rays", "shadow_rays", "render_ms", "trace_closest_ms",
                                            "trace_shadow_ms", "iterations", "kernel_launches", "extend_nodes",
-                                           "extend_tris", "h2d_bytes", "d2h_bytes", "nonfinite")]
+                                           "extend_tris", "h2d_bytes", "d2h_bytes", "nonfinite",
+                                           "film_overflow")]
 
 
 class PtNNConfig(C.Structure):
@@ -119,6 +120,8 @@ def load(path: str = LIB_PATH):
     lib.pt_nn_stats.argtypes = [P, P, P, P]
     lib.pt_debug_nn_forward.argtypes = [P, P, P, P, C.c_int32, P]
     lib.pt_debug_bsdf.argtypes = [C.c_int32, P, P]
+    lib.pt_debug_traversal_limits.argtypes = [P, C.c_int32, C.c_int32]
+    lib.pt_debug_tensor_wait_timeout.argtypes = []
     lib.pt_debug_light_sample.argtypes = [P, C.c_int32, P, P]
     lib.pt_debug_nn_grad.argtypes = [P, P, P, P, C.c_int32, P, P]
     lib.pt_debug_nn_grad_ex.argtypes = [P, P, P, P, C.c_int32, C.c_int32, C.c_float, C.c_float, P, P]

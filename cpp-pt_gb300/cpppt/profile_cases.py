@@ -1,6 +1,7 @@
 """Small, fixed workloads for profiling single kernels (ncu -k ... -c 1..3).
 
     python -m cpppt.profile_cases extend   # 1M-tri soup, 1280x720, 1 spp, depth 10 (plain PT+NEE+MIS)
+    python -m cpppt.profile_cases raycounts  # extension rays of each bounce of that render
     python -m cpppt.profile_cases nn [R]   # 200k-tri slit room, 640x360, learned guide: R renders of 4 spp
     python -m cpppt.profile_cases slit [R] # the same renders with plain PT (PT_FLAG_UNBIASED_MIS)
     python -m cpppt.profile_cases batch    # 8 soup scenes (10k-160k tris) in one batched wavefront
@@ -29,6 +30,22 @@ def case_extend():
     for _ in range(2):
         gs.render(1, max_depth=10, seed=1, mode=MODE_MIS)
     return gs.stats()
+
+
+def case_raycounts():
+    """Extension rays per bounce of the extend case.  All 921,600 paths start
+    in the first iteration (the wavefront holds 2^21), and a path's random
+    numbers depend only on its pixel, sample and bounce, so a render limited
+    to depth b traces exactly the first b bounces of the depth-10 render:
+    rays of bounce b = closest rays at depth b+1 minus those at depth b."""
+    gs = GpuScene(scenes.soup(seed=2, width=1280, height=720))
+    prev, per = 0.0, []
+    for d in range(1, 11):
+        gs.render(1, max_depth=d, seed=1, mode=MODE_MIS)
+        c = gs.stats()["closest_rays"]
+        per.append(int(c - prev))
+        prev = c
+    return {"rays_per_bounce": per, "total": int(prev)}
 
 
 def case_nn(renders: int = 2):
@@ -100,7 +117,7 @@ def case_c5(renders: int = 2, what: str = "train"):
 
 def main():
     name = sys.argv[1] if len(sys.argv) > 1 else "extend"
-    fn = {"extend": case_extend, "nn": case_nn, "slit": case_slit, "batch": case_batch, "batchnn": case_batchnn,
+    fn = {"extend": case_extend, "raycounts": case_raycounts, "nn": case_nn, "slit": case_slit, "batch": case_batch, "batchnn": case_batchnn,
           "batchslit": case_batchslit, "c5": case_c5}[name]
     t0 = time.perf_counter()
     args = [int(sys.argv[2])] if len(sys.argv) > 2 else []

@@ -362,6 +362,11 @@ void render_batch(pt_batch* b, const pt_batch_job* jobs, int n_jobs, float* cons
     ck(cudaMemsetAsync(b->film, 0, sizeof(unsigned long long) * 3 * pixels, st), "memset film");
     WaveCounters init{};
     init.work_total = total;
+    {
+        double per_pixel = 1.0;
+        for (const DevBatchJob& j : table) per_pixel = std::max(per_pixel, (double)j.spp * (2.0 * j.max_depth + 2.0));
+        init.film_safe = film_safe_bound(per_pixel);
+    }
     *b->h_ctr = init;
     ck(cudaMemcpyAsync(b->d_ctr, b->h_ctr, sizeof(WaveCounters), cudaMemcpyHostToDevice, st), "init counters");
     launch_generate(b->arena, b->pb, 1, b->d_ctr, b->d_jobs, n_jobs, st);  // fills buffer 0
@@ -406,8 +411,10 @@ void render_batch(pt_batch* b, const pt_batch_job* jobs, int n_jobs, float* cons
     R.render_ms = ms;
     R.kernel_launches = launches;
     R.nonfinite = (double)b->h_ctr->stat_nonfinite;
+    R.film_overflow = (double)b->h_ctr->stat_film_overflow;
     R.h2d_bytes = (double)(sizeof(WaveCounters) + sizeof(DevBatchJob) * n_jobs);
     R.d2h_bytes = (double)(rounds * sizeof(WaveCounters));
+    check_film(R.film_overflow);
 }
 
 // Per-path buffers of the slot wavefront, grown on demand.
@@ -506,6 +513,11 @@ void render_batch_slot(pt_batch* b, const pt_batch_job* jobs, int n_jobs, float*
     WaveCounters init{};
     init.work_total = total;
     init.free_top = capacity;
+    {
+        double per_pixel = 1.0;
+        for (int k = 0; k < n_jobs; k++) per_pixel = std::max(per_pixel, (double)jobs[k].spp * (2.0 * jobs[k].max_depth + 2.0));
+        init.film_safe = film_safe_bound(per_pixel);
+    }
     *b->h_ctr = init;
     ck(cudaMemcpyAsync(b->d_ctr, b->h_ctr, sizeof(WaveCounters), cudaMemcpyHostToDevice, st), "init counters");
     launch_nn_generate(b->arena, b->pb, 1, b->d_ctr, PD, b->d_jobs, n_jobs, st);  // fills buffer 0
@@ -592,6 +604,8 @@ void render_batch_slot(pt_batch* b, const pt_batch_job* jobs, int n_jobs, float*
     R.h2d_bytes = (double)(sizeof(WaveCounters) + (sizeof(DevBatchJob) + sizeof(DevNNJob)) * n_jobs +
                            sizeof(int) * n_members);
     R.d2h_bytes = (double)(rounds * (sizeof(WaveCounters) + (train ? sizeof(int) * n_members : 0)));
+    R.film_overflow = (double)b->h_ctr->stat_film_overflow;
+    check_film(R.film_overflow);
 }
 
 // Dispatch on the render mode (as pt_render's modes, without the SD-tree).

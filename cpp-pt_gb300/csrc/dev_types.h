@@ -30,7 +30,16 @@ struct DevCamera {
     int32_t width, height;
 };
 
+// Default bounds of a ray's traversal (kernel-side bounded loops): steps of
+// the persistent loop and entries of the per-lane stack.  A scene may carry
+// lower bounds (pt_debug_traversal_limits), never higher ones.
+constexpr uint32_t kTraversalStepLimit = 1u << 22;
+constexpr int32_t kTraversalStackSize = 64;
+
 struct DevScene {
+    // traversal bounds (see kTraversalStepLimit)
+    uint32_t step_limit = kTraversalStepLimit;
+    int32_t stack_limit = kTraversalStackSize;
     // traversal
     const uint4* nodes;      // 4 per wide node
     int32_t n_nodes;
@@ -87,11 +96,21 @@ constexpr uint32_t kStatusTensorTimeout = 8u;  // a tensor-core completion wait 
 struct WaveCounters {
     int32_t n_cur, n_next, n_shadow, n_fin;  // n_fin: finished paths of the learned-guide integrator
     int32_t fetch_ext, fetch_sh, free_top, n_rec;  // free_top: vertex-slot free list; n_rec: training records
-    uint32_t status, pad3, pad4, pad5;
+    uint32_t status;
+    float film_safe;  // |contribution| below this cannot carry a film sum out of the 32.32 range
+    uint32_t pad4, pad5;
     unsigned long long work_next, work_total;
     unsigned long long stat_closest, stat_shadow, stat_paths, stat_iters;
     unsigned long long stat_nodes, stat_tris;  // counting build of the extend kernel only
     unsigned long long stat_nonfinite;         // contributions dropped because they were inf/NaN
+    unsigned long long stat_film_overflow;     // contributions the 32.32 film could not hold
 };
+
+// film_safe for a render of at most `per_pixel` film contributions per pixel
+// and channel: a sum of contributions below 2^31 / per_pixel stays below
+// 2^31, the largest value the signed 32.32 fixed-point film holds.
+inline float film_safe_bound(double per_pixel) {
+    return (float)(2147483648.0 / (per_pixel > 1.0 ? per_pixel : 1.0));
+}
 
 }  // namespace cpppt_gb300

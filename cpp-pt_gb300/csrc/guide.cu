@@ -174,14 +174,7 @@ __global__ void __launch_bounds__(256) k_shade_ppg(DevScene S, PathBuffers B, in
                 const f3 rad = mk(m.r, m.g, m.b);
                 if (bounce > 0) set_vertex_rad(V, slot, bounce - 1, D_, rad);
                 const f3 c = mul * rad;
-                if (isfinite(c.x) && isfinite(c.y) && isfinite(c.z)) {
-                    const float sc = 4294967296.0f;
-                    if (c.x != 0.f) atomicAdd(film + 3 * pixel, (unsigned long long)__float2ll_rn(c.x * sc));
-                    if (c.y != 0.f) atomicAdd(film + 3 * pixel + 1, (unsigned long long)__float2ll_rn(c.y * sc));
-                    if (c.z != 0.f) atomicAdd(film + 3 * pixel + 2, (unsigned long long)__float2ll_rn(c.z * sc));
-                } else {
-                    atomicAdd(&ctr->stat_nonfinite, 1ull);
-                }
+                film_add_rgb(film, pixel, c.x, c.y, c.z, ctr);
             } else {
                 const Rng4 r0 = rng4(P.seed, sample, pixel, bounce, 0);
                 const Rng4 r1 = rng4(P.seed, sample, pixel, bounce, 1);

@@ -387,6 +387,7 @@ void render_ppg(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
         WaveCounters init{};
         init.work_total = work;
         init.free_top = capacity;
+        init.film_safe = film_safe_bound((double)passes[l] * (2.0 * D + 2.0));
         *s->h_ctr = init;
         ck(cudaMemcpyAsync(s->d_ctr, s->h_ctr, sizeof(WaveCounters), cudaMemcpyHostToDevice, st), "init counters");
         launch_generate_ppg(s->dev, s->pb, 1, P, s->d_ctr, slots, st);
@@ -411,6 +412,7 @@ void render_ppg(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
         total.closest_rays += (double)s->h_ctr->stat_closest;
         total.iterations += (double)s->h_ctr->stat_iters;
         total.nonfinite += (double)s->h_ctr->stat_nonfinite;
+        total.film_overflow += (double)s->h_ctr->stat_film_overflow;
         if (l + 1 == passes.size()) {
             launch_film_resolve(s->film, d_dst ? d_dst : s->d_out, film_n, 1.0 / (double)passes[l], st);
             launches += 1;
@@ -432,6 +434,7 @@ void render_ppg(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
     total.render_ms = ms;
     total.kernel_launches = launches;
     s->stats = total;
+    check_film(total.film_overflow);
 }
 
 // ---------------------------------------------------------------------------
@@ -682,6 +685,7 @@ void render_nn(pt_scene* s, const pt_render_desc* desc, float* d_dst, bool guide
     init.work_total = total;
     init.free_top = capacity;
     init.n_rec = train ? s->nn_rec_count : 0;
+    init.film_safe = film_safe_bound((double)desc->spp * (2.0 * desc->max_depth + 2.0));
     *s->h_ctr = init;
     ck(cudaMemcpyAsync(s->d_ctr, s->h_ctr, sizeof(WaveCounters), cudaMemcpyHostToDevice, st), "init counters");
     launch_nn_generate(s->dev, s->pb, 1, s->d_ctr, PD, s->d_job, 1, st);
@@ -737,7 +741,9 @@ void render_nn(pt_scene* s, const pt_render_desc* desc, float* d_dst, bool guide
     R.render_ms = ms;
     R.kernel_launches = launches + 1;
     R.nonfinite = (double)s->h_ctr->stat_nonfinite;
+    R.film_overflow = (double)s->h_ctr->stat_film_overflow;
     (void)records;
+    check_film(R.film_overflow);
 }
 
 void render_impl(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
@@ -794,6 +800,7 @@ void render_impl(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
     ck(cudaMemsetAsync(s->film, 0, sizeof(unsigned long long) * film_n, st), "memset film");
     WaveCounters init{};
     init.work_total = total;
+    init.film_safe = film_safe_bound((double)desc->spp * (2.0 * desc->max_depth + 2.0));
     *s->h_ctr = init;
     ck(cudaMemcpyAsync(s->d_ctr, s->h_ctr, sizeof(WaveCounters), cudaMemcpyHostToDevice, st), "init counters");
     *s->h_job = single_job(s->dev, P);
@@ -866,6 +873,8 @@ void render_impl(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
         R.trace_closest_ms = ext;
         R.trace_shadow_ms = sh;
     }
+    R.film_overflow = (double)s->h_ctr->stat_film_overflow;
+    check_film(R.film_overflow);
 }
 
 
@@ -1128,7 +1137,9 @@ pt_status pt_render_device_noalloc(pt_scene* s, const pt_render_desc* desc, floa
         R.shadow_rays = (double)h.stat_shadow;
         R.iterations = (double)h.stat_iters;
         R.nonfinite = (double)h.stat_nonfinite;
+        R.film_overflow = (double)h.stat_film_overflow;
         s->stats = R;
+        check_film(R.film_overflow);
         check_status(s, h.status);
         if (limit) throw Fail(PT_ERR_LIMIT, "render did not converge within the iteration bound");
     });
@@ -1269,6 +1280,36 @@ pt_status pt_debug_nn_forward(const float* weights, const float* lo, const float
         ck(cudaStreamSynchronize(c.st), "forward");
         ck(cudaGetLastError(), "forward");
         if (hstat & kStatusTensorTimeout) throw Fail(PT_ERR_CUDA, "tensor-core completion wait timed out");
+    });
+}
+
+pt_status pt_debug_traversal_limits(pt_scene* s, int32_t step_limit, int32_t stack_limit) {
+    if (!s) { g_error = "null scene"; return PT_ERR_INVALID; }
+    if (step_limit < 0 || (uint32_t)step_limit > kTraversalStepLimit || stack_limit < 0 ||
+        stack_limit > kTraversalStackSize) {
+        g_error = "limits must lie in [0, default] (0: the default)";
+        return PT_ERR_INVALID;
+    }
+    return guarded([&] {
+        ck(cudaStreamSynchronize(s->stream), "sync");
+        s->dev.step_limit = step_limit ? (uint32_t)step_limit : kTraversalStepLimit;
+        s->dev.stack_limit = stack_limit ? stack_limit : kTraversalStackSize;
+        // the captured iteration graph holds the scene description by value
+        if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
+    });
+}
+
+pt_status pt_debug_tensor_wait_timeout(void) {
+    return guarded([&] {
+        DebugCtx c;
+        uint32_t* dstat = dalloc<uint32_t>(c.owned, 1);
+        ck(cudaMemsetAsync(dstat, 0, sizeof(uint32_t), c.st), "memset");
+        launch_debug_tc_timeout(dstat, c.st);
+        ck(cudaGetLastError(), "launch");
+        uint32_t h = 0;
+        ck(cudaMemcpyAsync(&h, dstat, sizeof(h), cudaMemcpyDeviceToHost, c.st), "copy");
+        ck(cudaStreamSynchronize(c.st), "timeout kernel");
+        if (h & kStatusTensorTimeout) throw Fail(PT_ERR_CUDA, "tensor-core completion wait timed out");
     });
 }
 

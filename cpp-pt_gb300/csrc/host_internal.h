@@ -41,6 +41,15 @@ struct Fail : std::runtime_error {
     Fail(pt_status c, const std::string& m) : std::runtime_error(m), code(c) {}
 };
 
+// A render whose film could not hold a contribution (stat_film_overflow) has
+// a wrong image: fail it (the counter stays in the render's statistics).
+inline void check_film(double overflow) {
+    if (overflow > 0)
+        throw Fail(PT_ERR_LIMIT, "film overflow: " + std::to_string((long long)overflow) +
+                                     " contributions did not fit the film's 32.32 fixed-point range "
+                                     "(a pixel's sum must stay below 2^31)");
+}
+
 inline void ck(cudaError_t e, const char* what) {
     if (e != cudaSuccess) {
         cudaGetLastError();

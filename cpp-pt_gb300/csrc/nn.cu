@@ -116,6 +116,22 @@ __device__ __forceinline__ void tc_end(bool ok, uint32_t tmem, uint32_t bar, uin
     }
 }
 
+// Unit test of the bounded completion wait: the CTA allocates its tensor
+// memory, waits on a completion barrier that nothing arrives on, and takes
+// the timeout path of the tensor-core kernels (status bit, the second bounded
+// wait, tensor memory freed).  No tensor-core instruction is ever in flight.
+__global__ void __launch_bounds__(kTcRows) k_debug_tc_timeout(uint32_t* status) {
+    __shared__ uint64_t s_bar;
+    __shared__ uint32_t s_tmem;
+    const uint32_t tmem = tc_begin(&s_bar, &s_tmem);
+    uint32_t phase = 0;
+    const bool ok = __syncthreads_and(mbar_wait_bounded(smem_u32(&s_bar), phase)) != 0;
+    phase ^= 1u;
+    tc_end(ok, tmem, smem_u32(&s_bar), phase, status);
+}
+
+void launch_debug_tc_timeout(uint32_t* status, cudaStream_t st) { k_debug_tc_timeout<<<1, kTcRows, 0, st>>>(status); }
+
 // Inference over the paths of several render jobs (scenes with their own
 // networks): each tile runs once per distinct job among its rows, staging
 // that job's weights when they differ from the staged ones.  Jobs are
@@ -644,14 +660,7 @@ void launch_nn_train_tasks(const NNTrainTask* tasks, int n_tasks, int max_n, int
 __device__ __forceinline__ float luminance(f3 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
 
 __device__ __forceinline__ void film_add_nn(unsigned long long* film, size_t pix, f3 c, WaveCounters* ctr) {
-    if (!isfinite(c.x) || !isfinite(c.y) || !isfinite(c.z)) {
-        atomicAdd(&ctr->stat_nonfinite, 1ull);
-        return;
-    }
-    const float s = 4294967296.0f;
-    if (c.x != 0.f) atomicAdd(film + 3 * pix, (unsigned long long)__float2ll_rn(c.x * s));
-    if (c.y != 0.f) atomicAdd(film + 3 * pix + 1, (unsigned long long)__float2ll_rn(c.y * s));
-    if (c.z != 0.f) atomicAdd(film + 3 * pix + 2, (unsigned long long)__float2ll_rn(c.z * s));
+    film_add_rgb(film, pix, c.x, c.y, c.z, ctr);
 }
 
 __device__ __forceinline__ int warp_append_nn(int* counter, bool pred) {

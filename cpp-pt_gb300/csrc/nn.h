@@ -92,6 +92,10 @@ struct NNTrainTask {
 // Adam step (else only the gradient).
 void launch_nn_train_tasks(const NNTrainTask* tasks, int n_tasks, int max_n, int num_sms, cudaStream_t st, bool prep,
                            bool apply);
+// One CTA that waits on a completion barrier nothing arrives on (bounded)
+// and sets kStatusTensorTimeout in *status: the tensor-core kernels' timeout
+// path, exercised without a tensor-core instruction.
+void launch_debug_tc_timeout(uint32_t* status, cudaStream_t st);
 
 // The slot wavefront's stages.  jobs: the render jobs (DevBatchJob, as the
 // plain wavefront; one entry for a single render); P carries the flags and

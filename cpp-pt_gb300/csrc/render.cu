@@ -104,20 +104,12 @@ void launch_trace_any(const DevScene& S, const float* rays, int n, uint8_t* occ,
 // ---------------------------------------------------------------------------
 // Wavefront integrator
 // ---------------------------------------------------------------------------
-// Film: signed 32.32 fixed point, one 64-bit integer per pixel and channel.
-// Integer addition is associative, so a render's image does not depend on
-// the order in which contributions arrive (bit-identical across schedules,
-// batch sizes and launch shapes).  The final division by spp happens in FP64.
+// Film (film_add_rgb, shade.cuh): the image does not depend on the order in
+// which contributions arrive (bit-identical across schedules, batch sizes and
+// launch shapes).  The final division by spp happens in FP64.
 __device__ __forceinline__ void film_add(unsigned long long* film, size_t pix, float r, float g, float b,
                                          WaveCounters* ctr) {
-    if (!isfinite(r) || !isfinite(g) || !isfinite(b)) {
-        atomicAdd(&ctr->stat_nonfinite, 1ull);
-        return;
-    }
-    const float s = 4294967296.0f;
-    if (r != 0.f) atomicAdd(film + 3 * pix, (unsigned long long)__float2ll_rn(r * s));
-    if (g != 0.f) atomicAdd(film + 3 * pix + 1, (unsigned long long)__float2ll_rn(g * s));
-    if (b != 0.f) atomicAdd(film + 3 * pix + 2, (unsigned long long)__float2ll_rn(b * s));
+    film_add_rgb(film, pix, r, g, b, ctr);
 }
 
 template <bool COUNT>
@@ -561,6 +553,7 @@ cudaError_t render_noalloc(const DevScene& S, const RenderParams& P, int num_sms
     if (e != cudaSuccess) return e;
     WaveCounters init{};
     init.work_total = total;
+    init.film_safe = film_safe_bound((double)P.spp * (2.0 * max_depth + 2.0));
     e = cudaMemcpyAsync(ctr, &init, sizeof(init), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return e;
     const DevBatchJob hjob = single_job(S, P);

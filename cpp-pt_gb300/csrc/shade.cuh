@@ -63,6 +63,46 @@ __device__ __forceinline__ uint4 philox4x32(uint4 c, uint2 k) {
 }
 __device__ __forceinline__ float u01(uint32_t x) { return (float)(x >> 8) * (1.0f / 16777216.0f); }
 
+// ---------------------------------------------------------------------------
+// Film: signed 32.32 fixed point, one 64-bit integer per pixel and channel.
+// Integer addition is associative, so a render's image does not depend on
+// the order in which contributions arrive.  A contribution below
+// ctr->film_safe cannot carry the sum out of range (fire-and-forget add);
+// a larger one adds with the returned old value and counts a sum that left
+// the range (and one that cannot be represented at all is dropped and
+// counted); the host then fails the render.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void film_add1(unsigned long long* cell, float v, float safe, WaveCounters* ctr) {
+    if (v == 0.f) return;
+    const float a = fabsf(v);
+    const float s = 4294967296.0f;
+    if (a < safe) {
+        atomicAdd(cell, (unsigned long long)__float2ll_rn(v * s));
+        return;
+    }
+    if (a >= 2147483648.0f) {  // the contribution alone exceeds the range
+        atomicAdd(&ctr->stat_film_overflow, 1ull);
+        return;
+    }
+    const long long q = __float2ll_rn(v * s);
+    const long long old = (long long)atomicAdd(cell, (unsigned long long)q);
+    const long long sum = (long long)((unsigned long long)old + (unsigned long long)q);
+    if ((q > 0 && sum < old) || (q < 0 && sum > old)) atomicAdd(&ctr->stat_film_overflow, 1ull);
+}
+
+// One pixel's contribution (r, g, b); inf / NaN ones are dropped and counted.
+__device__ __forceinline__ void film_add_rgb(unsigned long long* film, size_t pix, float r, float g, float b,
+                                             WaveCounters* ctr) {
+    if (!isfinite(r) || !isfinite(g) || !isfinite(b)) {
+        atomicAdd(&ctr->stat_nonfinite, 1ull);
+        return;
+    }
+    const float safe = ctr->film_safe;
+    film_add1(film + 3 * pix, r, safe, ctr);
+    film_add1(film + 3 * pix + 1, g, safe, ctr);
+    film_add1(film + 3 * pix + 2, b, safe, ctr);
+}
+
 struct Rng4 {
     float v[4];
 };

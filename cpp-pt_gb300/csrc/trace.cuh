@@ -6,8 +6,7 @@
 namespace cpppt_gb300 {
 
 constexpr int kSmemNodes = 256;       // top of the wide BVH staged in shared memory (16 KB)
-constexpr int kStackSize = 64;
-constexpr int kMaxTraversalSteps = 1 << 22;
+constexpr int kStackSize = kTraversalStackSize;
 // Nodes whose entry distance exceeds best_t * (1 + 2^-8) are skipped.  The
 // margin covers the rounding of the reference's Cramer-rule t (triangle.h:41-57)
 // for every hit that is not within ~1e-4 rad of grazing the triangle.
@@ -251,7 +250,7 @@ __device__ __forceinline__ void trav_node(Trav& T, TravStack& K, const DevScene&
         trav_pop(T, K);
         return;
     }
-    if (T.sp + 3 > kStackSize) {
+    if (T.sp + 3 > S.stack_limit) {
         trav_abort(T, status, kStatusStackOverflow);
         return;
     }
@@ -362,7 +361,7 @@ __device__ __forceinline__ void persistent_trace(const DevScene& S, const uint4*
         unsigned wait, inner;
         do {
             if (active && is_inner(T.cur)) {
-                if (++T.steps > kMaxTraversalSteps) trav_abort(T, status, kStatusIterLimit);
+                if (++T.steps > S.step_limit) trav_abort(T, status, kStatusIterLimit);
                 else if (T.cur_t > cull_dist(T)) trav_pop(T, K);
                 else trav_node<ANY, COUNT>(T, K, S, snodes, status, cnt);
             }

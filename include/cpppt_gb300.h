@@ -126,6 +126,9 @@ typedef struct {
     double h2d_bytes;        /* host-to-device bytes copied by the call */
     double d2h_bytes;        /* device-to-host bytes copied by the call */
     double nonfinite;        /* contributions dropped because they were inf or NaN */
+    double film_overflow;    /* contributions the film could not hold: the film keeps signed 32.32
+                                fixed-point sums (a pixel's sum below 2^31); when non-zero the
+                                render returned PT_ERR_LIMIT */
 } pt_render_stats;
 
 /* pt_render_desc.flags */
@@ -348,6 +351,17 @@ pt_status pt_debug_nn_grad_ex(const float* weights, const float* lo, const float
  * numbers picking the light and the point on it), 10 out (position,
  * normal, Le |n_l . w|, pdf). */
 pt_status pt_debug_bsdf(int32_t n, const float* cases, float* out);
+
+/* Error-path hooks.  pt_debug_traversal_limits lowers the scene's kernel-side
+ * traversal bounds (steps of a ray's loop, default 2^22; entries of its
+ * stack, default 64; 0 restores a default): a query or render that runs out
+ * returns PT_ERR_LIMIT and leaves the context usable.
+ * pt_debug_tensor_wait_timeout runs one CTA that waits, bounded, on a
+ * tensor-core completion barrier nothing arrives on, through the timeout
+ * path of the learned guide's kernels: it returns PT_ERR_CUDA ("tensor-core
+ * completion wait timed out") and leaves the context usable. */
+pt_status pt_debug_traversal_limits(pt_scene* scene, int32_t step_limit, int32_t stack_limit);
+pt_status pt_debug_tensor_wait_timeout(void);
 pt_status pt_debug_light_sample(pt_scene* scene, int32_t n, const float* cases, float* out);
 
 /* Message of the last failed call on this thread ("" when none). */
