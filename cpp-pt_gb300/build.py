@@ -6,6 +6,7 @@
 Translation units, compiled in parallel, CUDA for sm_103a only:
   csrc/render.cu  -- traversal and PT+NEE+MIS wavefront kernels (nvcc -gencode arch=compute_103a,code=sm_103a)
   csrc/guide.cu   -- SD-tree guided (PPG) wavefront kernels
+  csrc/gpu_bvh.cu -- device build of the reference-topology BVH
   csrc/nn.cu      -- learned guide: MLP on the tensor cores, training, guided wavefront
   csrc/host.cpp   -- C ABI, render drivers, loader, image output
   csrc/bvh.cpp    -- BVH builders
@@ -53,7 +54,7 @@ def _commands(extra_cuda: list[str] | None = None):
     nvcc = _nvcc()
     common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
     jobs = []
-    for name in ("render.cu", "guide.cu", "nn.cu", "batch.cu", "host.cpp", "batch.cpp", "bvh.cpp", "sdtree.cpp",
+    for name in ("render.cu", "guide.cu", "nn.cu", "batch.cu", "gpu_bvh.cu", "host.cpp", "batch.cpp", "bvh.cpp", "sdtree.cpp",
                  "image_io.cpp", "loader.cpp"):
         src = os.path.join(CSRC, name)
         out = os.path.join(OBJ, name + ".o")

@@ -30,7 +30,7 @@ EXPORTS = ["pt_scene_create", "pt_scene_load", "pt_scene_destroy", "pt_scene_inf
            "pt_debug_nn_forward", "pt_debug_nn_grad", "pt_debug_nn_grad_ex", "pt_nn_configure", "pt_nn_config_get",
            "pt_batch_create", "pt_batch_destroy", "pt_batch_render", "pt_batch_render_device", "pt_batch_set_tuning",
            "pt_batch_get_tuning", "pt_batch_stats", "pt_batch_autotune", "pt_set_mesh_cache",
-           "pt_batch_render_ex", "pt_batch_render_ex_device", "pt_debug_image_load", "pt_debug_bsdf",
+           "pt_batch_render_ex", "pt_batch_render_ex_device", "pt_debug_image_load", "pt_debug_ref_topology_device", "pt_debug_bsdf",
            "pt_debug_light_sample", "pt_debug_traversal_limits", "pt_debug_tensor_wait_timeout"]
 
 
@@ -113,6 +113,7 @@ def load(path: str = LIB_PATH):
     lib.pt_last_error.restype = C.c_char_p
     lib.pt_last_error.argtypes = []
     lib.pt_debug_ref_topology.argtypes = [P, C.c_int32, P, P, P, C.c_int32, P]
+    lib.pt_debug_ref_topology_device.argtypes = [P, C.c_int32, P, P, P, C.c_int32, P, P]
     lib.pt_debug_image_load.argtypes = [C.c_char_p, C.c_int32, C.c_int32, P, P, P, C.c_int64]
     lib.pt_nn_get_weights.argtypes = [P, P]
     lib.pt_nn_set_weights.argtypes = [P, P]
@@ -410,6 +411,21 @@ def ref_topology(sc):
     nn = C.c_int32()
     _check(lib.pt_debug_ref_topology(_ptr(tv), n, _ptr(order), _ptr(pparent), _ptr(boxes), cap, C.byref(nn)))
     return order, boxes[:6 * nn.value].reshape(-1, 6), pparent
+
+
+def ref_topology_device(sc):
+    """The same topology built on the GPU: (leaf order, node boxes, prim parents, levels)."""
+    lib = load()
+    tv = np.ascontiguousarray(sc.vertices[sc.triangles].reshape(-1), np.float32)
+    n = sc.n_triangles
+    cap = max(2 * n, 16)
+    order = np.zeros(n, np.int32)
+    pparent = np.zeros(n, np.int32)
+    boxes = np.zeros(6 * cap, np.float32)
+    nn, lv = C.c_int32(), C.c_int32()
+    _check(lib.pt_debug_ref_topology_device(_ptr(tv), n, _ptr(order), _ptr(pparent), _ptr(boxes), cap, C.byref(nn),
+                                            C.byref(lv)))
+    return order, boxes[:6 * nn.value].reshape(-1, 6), pparent, lv.value
 
 
 def sdtree_run(lo, hi, rounds, queries, max_leaves=1 << 20, fn=None, lib=None):

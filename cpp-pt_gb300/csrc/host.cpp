@@ -3,6 +3,7 @@
 // Owns the device copy of a scene, the wavefront buffers and the CUDA graph
 // that replays wavefront iterations.  No call throws across the ABI; errors
 // are status codes plus a thread-local message.
+#include "gpu_bvh.h"
 #include "host_internal.h"
 #include "image_io.h"
 #include "loader.h"
@@ -71,7 +72,7 @@ void create_scene(const pt_scene_desc* d, pt_scene* s, const SceneTextures* tx =
     });
     RefTopology ref;
     try {
-        ref = build_ref_topology(tv.data(), nt);
+        ref = build_ref_topology_device(tv.data(), nt, s->stream);
     } catch (...) {
         wide_th.join();
         throw;
@@ -1485,6 +1486,30 @@ pt_status pt_debug_image_load(const char* path, int32_t rgb, int32_t srgb, int32
         texture_pixels(im, rgb != 0, srgb != 0, px);
         if ((int64_t)px.size() > cap) throw Fail(PT_ERR_LIMIT, "output buffer too small");
         std::memcpy(out, px.data(), sizeof(float) * px.size());
+    });
+}
+
+pt_status pt_debug_ref_topology_device(const float* tri_v, int32_t n, int32_t* leaf_order, int32_t* prim_parent,
+                                       float* node_boxes, int32_t max_nodes, int32_t* n_nodes, int32_t* levels) {
+    if (n < 0 || (n > 0 && (!tri_v || !leaf_order || !prim_parent)) || !n_nodes) {
+        g_error = "bad argument";
+        return PT_ERR_INVALID;
+    }
+    return guarded([&] {
+        DebugCtx c;
+        RefBuildStats rs;
+        RefTopology t = build_ref_topology_device(tri_v, n, c.st, &rs);
+        if (levels) *levels = rs.levels;
+        *n_nodes = (int32_t)t.node_box.size();
+        if ((int32_t)t.node_box.size() > max_nodes) throw Fail(PT_ERR_LIMIT, "node buffer too small");
+        for (int i = 0; i < n; i++) {
+            leaf_order[i] = t.leaf_order[i];
+            prim_parent[i] = t.prim_parent[i];
+        }
+        for (size_t i = 0; i < t.node_box.size(); i++) {
+            std::memcpy(node_boxes + 6 * i, t.node_box[i].lo, 12);
+            std::memcpy(node_boxes + 6 * i + 3, t.node_box[i].hi, 12);
+        }
     });
 }
 

@@ -147,8 +147,9 @@ typedef struct {
 
 /* Replaces: Loader::load_scene + BVH::add/build (loader.h:314-374,
  * bvh.h:205-216) for a scene given as flat arrays.  Builds the
- * reference-topology BVH (for tie-breaks) and the wide traversal BVH, and
- * uploads the scene to the current CUDA device. */
+ * reference-topology BVH (for tie-breaks; on the device, bit-identical to
+ * BVH::build) and the wide traversal BVH, and uploads the scene to the
+ * current CUDA device. */
 pt_status pt_scene_create(const pt_scene_desc* desc, pt_scene** scene);
 
 /* Replaces: Loader::load_render_settings + Loader::load_scene
@@ -398,6 +399,11 @@ pt_status pt_debug_image_load(const char* path, int32_t rgb, int32_t srgb, int32
                               int64_t cap);
 pt_status pt_debug_ref_topology(const float* tri_v, int32_t n, int32_t* leaf_order, int32_t* prim_parent,
                                 float* node_boxes, int32_t max_nodes, int32_t* n_nodes);
+/* The same topology built on the current device (level-synchronous binning
+ * kernels, bit-identical to the host build and to BVH::build); *levels
+ * receives the number of tree levels. */
+pt_status pt_debug_ref_topology_device(const float* tri_v, int32_t n, int32_t* leaf_order, int32_t* prim_parent,
+                                       float* node_boxes, int32_t max_nodes, int32_t* n_nodes, int32_t* levels);
 
 #ifdef __cplusplus
 }
