@@ -27,6 +27,7 @@ void check_device(pt_scene* s) {
         throw Fail(PT_ERR_NO_DEVICE, "device " + std::string(prop.name) + " is not compute capability 10.3 (sm_103a)");
     s->device = dev;
     s->num_sms = prop.multiProcessorCount;
+    ck(trace_kernels_setup(), "traversal shared memory limits");
 }
 
 void create_scene(const pt_scene_desc* d, pt_scene* s, const SceneTextures* tx = nullptr) {

@@ -68,6 +68,9 @@ int noalloc_paths();
 constexpr int kDebugBsdfIn = 20, kDebugBsdfOut = 10, kDebugLightIn = 6, kDebugLightOut = 10;
 void launch_debug_bsdf(const float* in, float* out, int n, cudaStream_t st);
 void launch_debug_light(const DevScene& S, const float* in, float* out, int n, cudaStream_t st);
+// Shared-memory limits of the traversal kernels (their top-node staging may
+// exceed the default 48 KB); call on each device before the first launch.
+cudaError_t trace_kernels_setup();
 // film: 32.32 fixed point per pixel and channel; out = film * scale / 2^32
 void launch_film_resolve(const unsigned long long* film, float* out, int n, double scale, cudaStream_t st);
 

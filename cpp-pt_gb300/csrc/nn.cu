@@ -574,7 +574,11 @@ size_t nn_smem_infer() { return (size_t)kTcInferSmem; }
 size_t nn_smem_train() { return (size_t)kTcTrainSmem; }
 size_t nn_wcopy_elems() { return (size_t)kNNLayers * kWLayer; }
 
+cudaError_t nn_shadow_smem_limit();  // after k_shadow_nn below
+
 cudaError_t nn_set_smem_limits() {
+    cudaError_t es = nn_shadow_smem_limit();
+    if (es != cudaSuccess) return es;
     cudaError_t e = cudaFuncSetAttribute(k_nn_forward_debug, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)nn_smem_infer());
     if (e != cudaSuccess) return e;
@@ -936,10 +940,10 @@ __global__ void __launch_bounds__(256) k_finish_nn(NNPathData PD, WaveCounters* 
 // NEE shadow rays of the learned-guide integrator: unoccluded contributions
 // go to the film and to the owning path's running total (for its training
 // targets).
-__global__ void __launch_bounds__(256) k_shadow_nn(DevScene S, PathBuffers B, WaveCounters* ctr,
+__global__ void __launch_bounds__(kTraceThreads) k_shadow_nn(DevScene S, PathBuffers B, WaveCounters* ctr,
                                                    unsigned long long* __restrict__ film, NNPathData PD,
                                                    const DevBatchJob* __restrict__ jobs) {
-    __shared__ uint4 snodes[kSmemNodes * 4];
+    extern __shared__ uint4 snodes[];
     const int n = ctr->n_shadow;
     if (n == 0) return;
     const int nn = min(S.n_nodes, kSmemNodes) * 4;
@@ -967,6 +971,10 @@ __global__ void __launch_bounds__(256) k_shadow_nn(DevScene S, PathBuffers B, Wa
                 }
             }
         });
+}
+
+cudaError_t nn_shadow_smem_limit() {
+    return cudaFuncSetAttribute(k_shadow_nn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemNodeBytes);
 }
 
 // Camera paths (stratified like pathtracerMIS.h:148-153) with a vertex slot.
@@ -1056,7 +1064,7 @@ void launch_nn_shade(const DevScene& S, const PathBuffers& B, int cur, const Ren
 }
 void launch_nn_shadow(const DevScene& S, const PathBuffers& B, WaveCounters* ctr, unsigned long long* film,
                       const NNPathData& PD, const DevBatchJob* jobs, int num_sms, cudaStream_t st) {
-    k_shadow_nn<<<num_sms * 4, 256, 0, st>>>(S, B, ctr, film, PD, jobs);
+    k_shadow_nn<<<num_sms * kTraceBlocksPerSM, kTraceThreads, kSmemNodeBytes, st>>>(S, B, ctr, film, PD, jobs);
 }
 void launch_nn_generate(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, const NNPathData& PD,
                         const DevBatchJob* jobs, int n_jobs, cudaStream_t st) {

@@ -20,8 +20,6 @@
 
 namespace cpppt_gb300 {
 
-constexpr int kTraceThreads = 256;
-constexpr int kTraceBlocksPerSM = 4;
 
 __device__ __forceinline__ void stage_top_nodes(const DevScene& S, uint4* snodes) {
     const int n = min(S.n_nodes, kSmemNodes) * 4;
@@ -53,10 +51,10 @@ __device__ __forceinline__ int warp_append(int* counter, bool pred) {
 // ---------------------------------------------------------------------------
 // Ray batches (BVH::intersect / intersect_any on arrays of rays)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kTraceThreads) k_trace_closest(DevScene S, const float* __restrict__ rays, int n,
+__global__ void __launch_bounds__(kTraceThreads, kTraceBlocksPerSM) k_trace_closest(DevScene S, const float* __restrict__ rays, int n,
                                                                  float4* __restrict__ hits, int* counter,
                                                                  uint32_t* status) {
-    __shared__ uint4 snodes[kSmemNodes * 4];
+    extern __shared__ uint4 snodes[];
     stage_top_nodes(S, snodes);
     TraceCount cnt{0u, 0u};
     persistent_trace<false, false>(
@@ -70,10 +68,10 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_closest(DevScene S, con
         [&](int i, const HitRec& h) { hits[i] = make_float4(h.t, __int_as_float(h.prim), h.beta, h.gamma); });
 }
 
-__global__ void __launch_bounds__(kTraceThreads) k_trace_any(DevScene S, const float* __restrict__ rays, int n,
+__global__ void __launch_bounds__(kTraceThreads, kTraceBlocksPerSM) k_trace_any(DevScene S, const float* __restrict__ rays, int n,
                                                              uint8_t* __restrict__ occ, int* counter,
                                                              uint32_t* status) {
-    __shared__ uint4 snodes[kSmemNodes * 4];
+    extern __shared__ uint4 snodes[];
     stage_top_nodes(S, snodes);
     TraceCount cnt{0u, 0u};
     persistent_trace<true, false>(
@@ -91,14 +89,14 @@ void launch_trace_closest(const DevScene& S, const float* rays, int n, float4* h
                           int num_sms, cudaStream_t st) {
     if (n <= 0) return;
     const int blocks = min(num_sms * kTraceBlocksPerSM, (n + kTraceThreads - 1) / kTraceThreads);
-    k_trace_closest<<<blocks, kTraceThreads, 0, st>>>(S, rays, n, hits, counter, status);
+    k_trace_closest<<<blocks, kTraceThreads, kSmemNodeBytes, st>>>(S, rays, n, hits, counter, status);
 }
 
 void launch_trace_any(const DevScene& S, const float* rays, int n, uint8_t* occ, int* counter, uint32_t* status,
                       int num_sms, cudaStream_t st) {
     if (n <= 0) return;
     const int blocks = min(num_sms * kTraceBlocksPerSM, (n + kTraceThreads - 1) / kTraceThreads);
-    k_trace_any<<<blocks, kTraceThreads, 0, st>>>(S, rays, n, occ, counter, status);
+    k_trace_any<<<blocks, kTraceThreads, kSmemNodeBytes, st>>>(S, rays, n, occ, counter, status);
 }
 
 // ---------------------------------------------------------------------------
@@ -113,8 +111,8 @@ __device__ __forceinline__ void film_add(unsigned long long* film, size_t pix, f
 }
 
 template <bool COUNT>
-__global__ void __launch_bounds__(kTraceThreads) k_extend(DevScene S, PathBuffers B, int cur, WaveCounters* ctr) {
-    __shared__ uint4 snodes[kSmemNodes * 4];
+__global__ void __launch_bounds__(kTraceThreads, kTraceBlocksPerSM) k_extend(DevScene S, PathBuffers B, int cur, WaveCounters* ctr) {
+    extern __shared__ uint4 snodes[];
     const int n = ctr->n_cur;
     if (n == 0) return;  // drained wavefront: skip staging
     stage_top_nodes(S, snodes);
@@ -142,9 +140,9 @@ __global__ void __launch_bounds__(kTraceThreads) k_extend(DevScene S, PathBuffer
     }
 }
 
-__global__ void __launch_bounds__(kTraceThreads) k_shadow(DevScene S, PathBuffers B, WaveCounters* ctr,
+__global__ void __launch_bounds__(kTraceThreads, kTraceBlocksPerSM) k_shadow(DevScene S, PathBuffers B, WaveCounters* ctr,
                                                           unsigned long long* __restrict__ film) {
-    __shared__ uint4 snodes[kSmemNodes * 4];
+    extern __shared__ uint4 snodes[];
     const int n = ctr->n_shadow;
     if (n == 0) return;
     stage_top_nodes(S, snodes);
@@ -366,16 +364,26 @@ __global__ void k_resolve(const unsigned long long* __restrict__ film, float* __
 
 void launch_extend(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, int num_sms, cudaStream_t st,
                    bool count) {
-    if (count) k_extend<true><<<num_sms * kTraceBlocksPerSM, kTraceThreads, 0, st>>>(S, B, cur, ctr);
-    else k_extend<false><<<num_sms * kTraceBlocksPerSM, kTraceThreads, 0, st>>>(S, B, cur, ctr);
+    if (count) k_extend<true><<<num_sms * kTraceBlocksPerSM, kTraceThreads, kSmemNodeBytes, st>>>(S, B, cur, ctr);
+    else k_extend<false><<<num_sms * kTraceBlocksPerSM, kTraceThreads, kSmemNodeBytes, st>>>(S, B, cur, ctr);
 }
+cudaError_t trace_kernels_setup() {
+    const int bytes = (int)kSmemNodeBytes;
+    cudaError_t e = cudaFuncSetAttribute(k_trace_closest, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_any, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_extend<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_extend<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_shadow, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    return e;
+}
+
 void launch_shade(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, unsigned long long* film,
                   const DevBatchJob* jobs, cudaStream_t st) {
     k_shade<<<(B.capacity + 255) / 256, 256, 0, st>>>(S, B, cur, ctr, film, jobs);
 }
 void launch_shadow(const DevScene& S, const PathBuffers& B, WaveCounters* ctr, unsigned long long* film, int num_sms,
                    cudaStream_t st) {
-    k_shadow<<<num_sms * kTraceBlocksPerSM, kTraceThreads, 0, st>>>(S, B, ctr, film);
+    k_shadow<<<num_sms * kTraceBlocksPerSM, kTraceThreads, kSmemNodeBytes, st>>>(S, B, ctr, film);
 }
 void launch_generate(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, const DevBatchJob* jobs,
                      int n_jobs, cudaStream_t st) {

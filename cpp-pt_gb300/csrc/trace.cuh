@@ -5,7 +5,29 @@
 
 namespace cpppt_gb300 {
 
-constexpr int kSmemNodes = 256;       // top of the wide BVH staged in shared memory (16 KB)
+// Launch shape of the traversal kernels (threads per CTA, resident CTAs per
+// SM; the grid is the latter times the SM count) and the number of top wide
+// nodes (breadth-first, so the top levels) each CTA stages in shared memory.
+// One CTA of 1024 threads per SM stages 2048 nodes (128 KB, the top five
+// levels and part of the sixth) once per SM instead of four 256-thread CTAs
+// staging 256 nodes each.  Measured on the 1M-triangle soup at 1080p (same
+// 64 registers, no spills): 256x4 with 256 nodes 273.0 Mpaths/s, 512 nodes
+// 273.4, 512x2 with 1024 nodes 275.2, 1024x1 with 2048 nodes 277.3, with
+// 3072 nodes 256.7 (L1 squeezed); 5 and 6 CTAs of 256 threads (48 and 40
+// registers, spilling) 264.9 and 234.5.
+#ifndef CPPPT_TRACE_THREADS
+#define CPPPT_TRACE_THREADS 1024
+#endif
+#ifndef CPPPT_TRACE_BLOCKS_PER_SM
+#define CPPPT_TRACE_BLOCKS_PER_SM 1
+#endif
+#ifndef CPPPT_SMEM_NODES
+#define CPPPT_SMEM_NODES 2048
+#endif
+constexpr int kTraceThreads = CPPPT_TRACE_THREADS;
+constexpr int kTraceBlocksPerSM = CPPPT_TRACE_BLOCKS_PER_SM;
+constexpr int kSmemNodes = CPPPT_SMEM_NODES;
+constexpr size_t kSmemNodeBytes = (size_t)kSmemNodes * 64;  // dynamic shared memory of a traversal CTA
 constexpr int kStackSize = kTraversalStackSize;
 // Nodes whose entry distance exceeds best_t * (1 + 2^-8) are skipped.  The
 // margin covers the rounding of the reference's Cramer-rule t (triangle.h:41-57)
