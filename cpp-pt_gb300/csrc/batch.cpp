@@ -344,24 +344,21 @@ void render_batch(pt_batch* b, const pt_batch_job* jobs, int n_jobs, float* cons
     const pt_batch::GraphKey key{b->film, n_jobs, capacity, t.iters_per_graph};
     if (!b->graph || !(b->graph_key == key)) {
         if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
-        cudaGraph_t g;
-        ck(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
-        for (int k = 0; k < t.iters_per_graph; k++) {
-            const int cur = k & 1;
-            launch_extend(b->arena, b->pb, cur, b->d_ctr, b->num_sms, st);
-            launch_shade(b->arena, b->pb, cur, b->d_ctr, b->film, b->d_jobs, st);
-            launch_shadow(b->arena, b->pb, b->d_ctr, b->film, b->num_sms, st);
-            launch_generate(b->arena, b->pb, cur, b->d_ctr, b->d_jobs, n_jobs, st);
-        }
-        ck(cudaStreamEndCapture(st, &g), "end capture");
-        ck(cudaGraphInstantiate(&b->graph, g, 0), "graph instantiate");
-        cudaGraphDestroy(g);
+        ck(build_render_graph(b->arena, b->pb, b->d_ctr, b->film, b->d_jobs, n_jobs, t.iters_per_graph, b->num_sms, st,
+                              &b->graph),
+           "render graph");
         b->graph_key = key;
     }
     ck(cudaEventRecord(b->ev0, st), "event");
     ck(cudaMemsetAsync(b->film, 0, sizeof(unsigned long long) * 3 * pixels, st), "memset film");
+    int max_depth = 1;
+    for (const DevBatchJob& j : table) max_depth = std::max(max_depth, j.max_depth);
+    const unsigned long long max_rounds =
+        64 + (total / (unsigned long long)capacity + 2 + (unsigned long long)n_jobs) *
+                 (unsigned long long)(max_depth + 2) * 4 / (unsigned long long)t.iters_per_graph;
     WaveCounters init{};
     init.work_total = total;
+    init.max_rounds = (uint32_t)std::min<unsigned long long>(max_rounds, 0xffffffffull);
     {
         double per_pixel = 1.0;
         for (const DevBatchJob& j : table) per_pixel = std::max(per_pixel, (double)j.spp * (2.0 * j.max_depth + 2.0));
@@ -370,26 +367,19 @@ void render_batch(pt_batch* b, const pt_batch_job* jobs, int n_jobs, float* cons
     *b->h_ctr = init;
     ck(cudaMemcpyAsync(b->d_ctr, b->h_ctr, sizeof(WaveCounters), cudaMemcpyHostToDevice, st), "init counters");
     launch_generate(b->arena, b->pb, 1, b->d_ctr, b->d_jobs, n_jobs, st);  // fills buffer 0
-    int max_depth = 1;
-    for (const DevBatchJob& j : table) max_depth = std::max(max_depth, j.max_depth);
-    const unsigned long long max_rounds =
-        64 + (total / (unsigned long long)capacity + 2 + (unsigned long long)n_jobs) *
-                 (unsigned long long)(max_depth + 2) * 4 / (unsigned long long)t.iters_per_graph;
-    unsigned long long rounds = 0;
-    double launches = 2;
-    while (true) {
-        ck(cudaGraphLaunch(b->graph, st), "graph launch");
-        launches += kKernelsPerIteration * t.iters_per_graph;
-        ck(cudaMemcpyAsync(b->h_ctr, b->d_ctr, sizeof(WaveCounters), cudaMemcpyDeviceToHost, st), "read counters");
-        ck(cudaStreamSynchronize(st), "batch render");
+    // the whole loop on the device: one graph launch, one read of the counters
+    ck(cudaGraphLaunch(b->graph, st), "graph launch");
+    ck(cudaMemcpyAsync(b->h_ctr, b->d_ctr, sizeof(WaveCounters), cudaMemcpyDeviceToHost, st), "read counters");
+    ck(cudaStreamSynchronize(st), "batch render");
+    {
         const uint32_t status = b->h_ctr->status;
         if (status & kStatusStackOverflow) throw Fail(PT_ERR_LIMIT, "traversal stack overflow");
         if (status & kStatusIterLimit) throw Fail(PT_ERR_LIMIT, "traversal step limit reached");
         if (status & kStatusQueueOverflow) throw Fail(PT_ERR_LIMIT, "wavefront queue overflow");
-        rounds++;
-        if (b->h_ctr->n_cur == 0 && b->h_ctr->work_next >= b->h_ctr->work_total) break;
-        if (rounds > max_rounds) throw Fail(PT_ERR_LIMIT, "batch render did not converge within the iteration bound");
+        if (status & kStatusRoundLimit) throw Fail(PT_ERR_LIMIT, "batch render did not converge within the iteration bound");
     }
+    const unsigned long long rounds = b->h_ctr->rounds;
+    double launches = 2 + (double)rounds * (kKernelsPerIteration * t.iters_per_graph + 1);
     for (int i = 0; i < n_jobs; i++) {
         const pt_batch::Member& m = b->members[jobs[i].scene];
         const size_t off = 3 * (size_t)table[i].film_off;
@@ -413,7 +403,7 @@ void render_batch(pt_batch* b, const pt_batch_job* jobs, int n_jobs, float* cons
     R.nonfinite = (double)b->h_ctr->stat_nonfinite;
     R.film_overflow = (double)b->h_ctr->stat_film_overflow;
     R.h2d_bytes = (double)(sizeof(WaveCounters) + sizeof(DevBatchJob) * n_jobs);
-    R.d2h_bytes = (double)(rounds * sizeof(WaveCounters));
+    R.d2h_bytes = (double)sizeof(WaveCounters);
     check_film(R.film_overflow);
 }
 
@@ -729,8 +719,12 @@ pt_status pt_batch_stats(pt_batch* b, pt_render_stats* out) {
 
 // Autotuner: renders a reduced copy of the job list (spp divided by
 // spp_divisor, at least 1) once per candidate setting and keeps the one with
-// the highest paths per second.  Candidates: wavefront capacity 2^19..2^22,
-// 8/16/32 iterations per graph, and scanline or 8x4 / 4x8 / 16x2 pixel tiles.
+// the highest paths per second.  Candidates: wavefront capacity 2^21 or 2^22
+// (scanline order), then scanline or 8x4 / 4x8 / 16x2 pixel tiles at the
+// better capacity: five settings.  The render loop runs on the device
+// (build_render_graph), so the iterations per loop body only set how often
+// its control kernel runs and are kept (16); smaller capacities are clamped
+// to the work anyway and never won on the batches measured.
 pt_status pt_batch_autotune(pt_batch* b, const pt_batch_job* jobs, int32_t n_jobs, int32_t spp_divisor,
                             pt_batch_tuning* best_out, double* best_mpaths) {
     if (!b) { g_error = "null batch"; return PT_ERR_INVALID; }
@@ -739,9 +733,9 @@ pt_status pt_batch_autotune(pt_batch* b, const pt_batch_job* jobs, int32_t n_job
         if (spp_divisor < 1) throw std::invalid_argument("spp_divisor must be >= 1");
         std::vector<pt_batch_job> sample(jobs, jobs + n_jobs);
         for (pt_batch_job& j : sample) j.spp = std::max(1, j.spp / spp_divisor);
-        const int caps[] = {1 << 19, 1 << 20, 1 << 21, 1 << 22};
-        const int iters[] = {8, 16, 32};
+        const int caps[] = {1 << 21, 1 << 22};
         const int tiles[][2] = {{1, 1}, {8, 4}, {4, 8}, {16, 2}};
+        const int iters = b->tuning.iters_per_graph;
         pt_batch_tuning best = b->tuning;
         double best_rate = -1.0;
         auto trial = [&](const pt_batch_tuning& t) {
@@ -750,9 +744,8 @@ pt_status pt_batch_autotune(pt_batch* b, const pt_batch_job* jobs, int32_t n_job
             const double rate = b->stats.paths / (b->stats.render_ms * 1e3);
             if (rate > best_rate) { best_rate = rate; best = t; }
         };
-        // capacity and graph length first (scanline order), then the tile shape
-        for (int c : caps)
-            for (int it : iters) trial(pt_batch_tuning{c, it, 1, 1});
+        // capacity first (scanline order), then the tile shape
+        for (int c : caps) trial(pt_batch_tuning{c, iters, 1, 1});
         const pt_batch_tuning base = best;
         for (const auto& tl : tiles) {
             if (tl[0] == 1 && tl[1] == 1) continue;

@@ -91,6 +91,7 @@ constexpr uint32_t kStatusIterLimit = 1u;
 constexpr uint32_t kStatusStackOverflow = 2u;
 constexpr uint32_t kStatusQueueOverflow = 4u;
 constexpr uint32_t kStatusTensorTimeout = 8u;  // a tensor-core completion wait ran out (bounded spin)
+constexpr uint32_t kStatusRoundLimit = 16u;    // a device-driven render loop reached its round bound
 
 // Wavefront counters, one block of device memory per scene.
 struct WaveCounters {
@@ -98,7 +99,8 @@ struct WaveCounters {
     int32_t fetch_ext, fetch_sh, free_top, n_rec;  // free_top: vertex-slot free list; n_rec: training records
     uint32_t status;
     float film_safe;  // |contribution| below this cannot carry a film sum out of the 32.32 range
-    uint32_t pad4, pad5;
+    uint32_t rounds;      // loop bodies run by a device-driven render (k_round_control)
+    uint32_t max_rounds;  // its bound
     unsigned long long work_next, work_total;
     unsigned long long stat_closest, stat_shadow, stat_paths, stat_iters;
     unsigned long long stat_nodes, stat_tris;  // counting build of the extend kernel only

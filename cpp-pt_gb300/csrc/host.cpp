@@ -28,6 +28,7 @@ void check_device(pt_scene* s) {
     s->device = dev;
     s->num_sms = prop.multiProcessorCount;
     ck(trace_kernels_setup(), "traversal shared memory limits");
+    ck(nn_set_smem_limits(), "guided wavefront shared memory limits");
 }
 
 void create_scene(const pt_scene_desc* d, pt_scene* s, const SceneTextures* tx = nullptr) {
@@ -244,6 +245,7 @@ void check_status(pt_scene* s, uint32_t status) {
     if (status & kStatusStackOverflow) throw Fail(PT_ERR_LIMIT, "traversal stack overflow");
     if (status & kStatusQueueOverflow) throw Fail(PT_ERR_LIMIT, "wavefront queue overflow");
     if (status & kStatusTensorTimeout) throw Fail(PT_ERR_CUDA, "tensor-core completion wait timed out");
+    if (status & kStatusRoundLimit) throw Fail(PT_ERR_LIMIT, "render did not converge within the iteration bound");
 }
 
 void trace_device(pt_scene* s, const pt_ray* rays, int n, void* out, bool any, cudaStream_t st) {
@@ -307,18 +309,6 @@ void ensure_wave(pt_scene* s, int capacity, int film_n) {
         ck(cudaMalloc(&s->d_out, sizeof(float) * film_n), "cudaMalloc film");
         s->film_n = film_n;
         if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
-    }
-}
-
-// The render parameters live in the scene's one-entry job table, so the
-// captured iterations stay valid across renders.
-void enqueue_iterations(pt_scene* s, int iters) {
-    for (int k = 0; k < iters; k++) {
-        const int cur = k & 1;
-        launch_extend(s->dev, s->pb, cur, s->d_ctr, s->num_sms, s->stream);
-        launch_shade(s->dev, s->pb, cur, s->d_ctr, s->film, s->d_job, s->stream);
-        launch_shadow(s->dev, s->pb, s->d_ctr, s->film, s->num_sms, s->stream);
-        launch_generate(s->dev, s->pb, cur, s->d_ctr, s->d_job, 1, s->stream);
     }
 }
 
@@ -790,19 +780,20 @@ void render_impl(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
     const bool timed = (desc->flags & PT_FLAG_TIME_KERNELS) != 0;
     const bool count = (desc->flags & PT_FLAG_COUNT) != 0;
     const bool direct = timed || count;
-    if (!direct && !s->graph) {
-        cudaGraph_t g;
-        ck(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
-        enqueue_iterations(s, kItersPerGraph);
-        ck(cudaStreamEndCapture(st, &g), "end capture");
-        ck(cudaGraphInstantiate(&s->graph, g, 0), "graph instantiate");
-        cudaGraphDestroy(g);
-    }
+    // the render parameters live in the scene's one-entry job table and the
+    // counters, so the graph stays valid across renders
+    if (!direct && !s->graph)
+        ck(build_render_graph(s->dev, s->pb, s->d_ctr, s->film, s->d_job, 1, kItersPerGraph, s->num_sms, st,
+                              &s->graph),
+           "render graph");
     ck(cudaEventRecord(s->ev0, st), "event");
     ck(cudaMemsetAsync(s->film, 0, sizeof(unsigned long long) * film_n, st), "memset film");
+    const unsigned long long max_rounds = 64 + (total / (unsigned long long)capacity + 2) *
+                                                   (unsigned long long)(desc->max_depth + 2) * 4 / kItersPerGraph;
     WaveCounters init{};
     init.work_total = total;
     init.film_safe = film_safe_bound((double)desc->spp * (2.0 * desc->max_depth + 2.0));
+    init.max_rounds = (uint32_t)std::min<unsigned long long>(max_rounds, 0xffffffffull);
     *s->h_ctr = init;
     ck(cudaMemcpyAsync(s->d_ctr, s->h_ctr, sizeof(WaveCounters), cudaMemcpyHostToDevice, st), "init counters");
     *s->h_job = single_job(s->dev, P);
@@ -811,12 +802,19 @@ void render_impl(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
     ck(cudaMemcpyAsync(s->d_job, s->h_job, sizeof(DevBatchJob), cudaMemcpyHostToDevice, st), "job table");
     launch_generate(s->dev, s->pb, 1, s->d_ctr, s->d_job, 1, st);  // fills buffer 0
     double launches = 2;
-    const unsigned long long max_rounds = 64 + (total / (unsigned long long)capacity + 2) *
-                                                   (unsigned long long)(desc->max_depth + 2) * 4 / kItersPerGraph;
     std::vector<cudaEvent_t> tev;
     unsigned long long rounds = 0;
-    while (true) {
-        if (direct) {
+    if (!direct) {
+        // the whole loop on the device: one graph launch, one read of the counters
+        ck(cudaGraphLaunch(s->graph, st), "graph launch");
+        ck(cudaMemcpyAsync(s->h_ctr, s->d_ctr, sizeof(WaveCounters), cudaMemcpyDeviceToHost, st), "read counters");
+        ck(cudaStreamSynchronize(st), "render");
+        check_status(s, s->h_ctr->status);
+        rounds = s->h_ctr->rounds;
+        launches += (double)rounds * (kKernelsPerIteration * kItersPerGraph + 1);
+    }
+    while (direct) {
+        {
             // the graph's work, launched one kernel at a time
             for (int k = 0; k < kItersPerGraph; k++) {
                 const int cur = k & 1;
@@ -832,8 +830,6 @@ void render_impl(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
                 if (timed) ck(cudaEventRecord(e[3], st), "event");
                 launch_generate(s->dev, s->pb, cur, s->d_ctr, s->d_job, 1, st);
             }
-        } else {
-            ck(cudaGraphLaunch(s->graph, st), "graph launch");
         }
         launches += kKernelsPerIteration * kItersPerGraph;
         ck(cudaMemcpyAsync(s->h_ctr, s->d_ctr, sizeof(WaveCounters), cudaMemcpyDeviceToHost, st), "read counters");
@@ -861,7 +857,7 @@ void render_impl(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
     R.extend_tris = (double)s->h_ctr->stat_tris;
     R.nonfinite = (double)s->h_ctr->stat_nonfinite;
     R.h2d_bytes = (double)sizeof(WaveCounters);
-    R.d2h_bytes = (double)(rounds * sizeof(WaveCounters));
+    R.d2h_bytes = (double)((direct ? rounds : 1) * sizeof(WaveCounters));
     if (timed) {
         double ext = 0, sh = 0;
         for (size_t q = 0; q + 3 < tev.size(); q += 4) {

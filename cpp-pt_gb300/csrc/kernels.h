@@ -51,6 +51,16 @@ void launch_shadow(const DevScene& S, const PathBuffers& B, WaveCounters* ctr, u
                    cudaStream_t st);
 void launch_generate(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, const DevBatchJob* jobs,
                      int n_jobs, cudaStream_t st);
+// The whole wavefront loop of a plain render (PT_MODE_MIS / NEE / PT, single
+// scene or batch) as one executable graph: a conditional WHILE node whose
+// body runs `iters` (even) iterations and then a round-control kernel that
+// ends the loop when no path is left and no work waits, or when a kernel set
+// a status bit, or at ctr->max_rounds bodies (kStatusRoundLimit).  One graph
+// launch renders everything after the first generate; the host reads the
+// counters once, at the end.
+cudaError_t build_render_graph(const DevScene& S, const PathBuffers& B, WaveCounters* ctr, unsigned long long* film,
+                               const DevBatchJob* jobs, int n_jobs, int iters, int num_sms, cudaStream_t st,
+                               cudaGraphExec_t* out);
 // The job-table entry of a single-scene render of S with parameters P.
 DevBatchJob single_job(const DevScene& S, const RenderParams& P);
 constexpr int kKernelsPerIteration = 5;

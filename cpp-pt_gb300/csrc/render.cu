@@ -391,6 +391,58 @@ void launch_generate(const DevScene& S, const PathBuffers& B, int cur, WaveCount
     k_advance<<<1, 32, 0, st>>>(ctr, B.capacity);
 }
 
+// Body end of a device-driven render loop (build_render_graph).  One thread.
+__global__ void k_round_control(WaveCounters* ctr, cudaGraphConditionalHandle h) {
+    const uint32_t r = ctr->rounds + 1u;
+    ctr->rounds = r;
+    bool more = !(ctr->n_cur == 0 && ctr->work_next >= ctr->work_total) && ctr->status == 0u;
+    if (more && r >= ctr->max_rounds) {
+        ctr->status |= kStatusRoundLimit;
+        more = false;
+    }
+    cudaGraphSetConditional(h, more ? 1u : 0u);
+}
+
+cudaError_t build_render_graph(const DevScene& S, const PathBuffers& B, WaveCounters* ctr, unsigned long long* film,
+                               const DevBatchJob* jobs, int n_jobs, int iters, int num_sms, cudaStream_t st,
+                               cudaGraphExec_t* out) {
+    *out = nullptr;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaGraphCreate(&g, 0);
+    if (e != cudaSuccess) return e;
+    cudaGraphConditionalHandle h;
+    e = cudaGraphConditionalHandleCreate(&h, g, 1u, cudaGraphCondAssignDefault);
+    cudaGraphNodeParams cp = {};
+    if (e == cudaSuccess) {
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t node;
+        e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp);
+    }
+    if (e == cudaSuccess) {
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        e = cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            for (int k = 0; k < iters; k++) {
+                const int cur = k & 1;
+                launch_extend(S, B, cur, ctr, num_sms, st);
+                launch_shade(S, B, cur, ctr, film, jobs, st);
+                launch_shadow(S, B, ctr, film, num_sms, st);
+                launch_generate(S, B, cur, ctr, jobs, n_jobs, st);
+            }
+            k_round_control<<<1, 1, 0, st>>>(ctr, h);
+            cudaGraph_t captured = nullptr;
+            const cudaError_t e2 = cudaStreamEndCapture(st, &captured);
+            e = e2 != cudaSuccess ? e2 : cudaGetLastError();
+        }
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    return e;
+}
+
 DevBatchJob single_job(const DevScene& S, const RenderParams& P) {
     DevBatchJob j{};
     j.cam = S.cam;

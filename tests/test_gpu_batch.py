@@ -74,6 +74,16 @@ def test_autotune_picks_a_valid_shape(members):
         assert np.array_equal(img.view(np.uint32), unbatched(members, j).view(np.uint32))
 
 
+def test_batch_loop_runs_on_the_device(members):
+    """A batch render is one graph launch of the whole loop: one counter read."""
+    from cpppt.lib import GpuBatch
+    b = GpuBatch(members)
+    b.render(JOBS, outputs=False)
+    st = b.stats()
+    assert st["d2h_bytes"] == 128
+    assert st["paths"] == sum(members[j["scene"]].width * members[j["scene"]].height * j["spp"] for j in JOBS)
+
+
 def test_device_outputs(members):
     import torch
     from cpppt.lib import GpuBatch

@@ -185,6 +185,19 @@ def test_render_stats_account_for_every_path(gpu_lib):
     assert st["iterations"] >= 8
 
 
+def test_render_loop_runs_on_the_device(gpu_lib):
+    """The whole wavefront loop is one graph launch (a conditional loop whose
+    control kernel ends it): the host reads the counters once per render,
+    however many loop bodies ran."""
+    from cpppt.lib import GpuScene
+    gs = GpuScene(scenes.cornell(64, 64))
+    gs.render(64, max_depth=8, seed=2)
+    st = gs.stats()
+    assert st["d2h_bytes"] == 128 + 64 * 64 * 3 * 4  # one WaveCounters read and the image
+    assert st["kernel_launches"] > 5 * 16  # more than one loop body ran
+    assert st["paths"] == 64 * 64 * 64
+
+
 def test_render_argument_errors(gpu_lib):
     from cpppt.lib import GpuScene, PtError
     gs = GpuScene(scenes.cornell(8, 8))
