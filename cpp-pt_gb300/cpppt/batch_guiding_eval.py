@@ -42,12 +42,21 @@ from .lib import FLAG_NN_FREEZE, FLAG_THROUGHPUT_RR, FLAG_UNBIASED_MIS, MODE_MIS
 
 def plan(n: int, seed: int, min_tris: float, max_tris: float):
     """Room k: slit room of seed `seed + k`, 1000 boxes whose faces are split
-    s x s with 12000 s^2 + 38 ~ the drawn triangle count."""
+    s x s (12000 s^2 + 38 triangles) with s nearest to the drawn count.  The
+    counts are drawn log-uniform in [min_tris, max_tris], stratified (one
+    draw in each of n equal slices of the log range, in shuffled order) so
+    that a batch of a few rooms spans the range; s is kept to the splits
+    whose count lies inside it (7..18 for [0.5M, 4M]: 588k..3.89M)."""
     rng = np.random.default_rng(seed)
+    lo, hi = math.log(min_tris), math.log(max_tris)
+    s_min = max(1, math.ceil(math.sqrt(max(0.0, min_tris - 38) / 12000.0)))
+    s_max = max(s_min, math.floor(math.sqrt(max(0.0, max_tris - 38) / 12000.0)))
+    slices = rng.permutation(n)
     out = []
     for k in range(n):
-        tris = math.exp(rng.uniform(math.log(min_tris), math.log(max_tris)))
-        out.append(dict(scene_seed=seed + k, box_subdiv=max(1, int(round(math.sqrt(tris / 12000.0))))))
+        tris = math.exp(lo + (hi - lo) * (slices[k] + rng.uniform()) / n)
+        s = min(s_max, max(s_min, int(round(math.sqrt(tris / 12000.0)))))
+        out.append(dict(scene_seed=seed + k, box_subdiv=s))
     return out
 
 

@@ -15,7 +15,13 @@ scored by relMSE = mean over pixels and channels of (x - ref)^2 / (ref^2 +
             online from fresh weights inside the time budget (training time
             counts; optionally frozen after a given number of seconds);
 * sdtree -- the reference's practical path guiding (PPG: SD-tree, no NEE),
-            one render whose spp is sized to the budget.
+            one render whose spp is sized to the budget;
+* mis_default (--mis-default) -- the drop-in default PT_MODE_MIS (the
+            reference's estimator: RR-scaled MIS weights, MIS weight at the
+            last vertex).  It converges to a slightly different image, so it
+            is scored against its own reference (ref_spp / 4 of the same
+            estimator); its distance to the unbiased reference is printed as
+            its bias.
 
 Plain and nn accumulate chunks of spp on the GPU; relMSE is taken at
 checkpoints spaced by sqrt(2) up to the largest budget.  Prints one JSON
@@ -103,6 +109,8 @@ def main():
     ap.add_argument("--no-sdtree", action="store_true")
     ap.add_argument("--plain-trr", action="store_true",
                     help="also run plain PT with Russian roulette on the throughput (method plain_trr)")
+    ap.add_argument("--mis-default", action="store_true",
+                    help="also run the drop-in default PT_MODE_MIS, scored against its own reference")
     ap.add_argument("--save", default="")
     a = ap.parse_args()
     sc = scenes.slit_room(seed=4, n_boxes=a.boxes, box_subdiv=4, width=a.width, height=a.height)
@@ -129,6 +137,23 @@ def main():
     print(json.dumps({"reference": {"spp": a.ref_spp, "seconds": ref_s, "mean": float(ref.mean()),
                                     "relMSE_noise_estimate": ref_noise, "triangles": sc.n_triangles,
                                     "resolution": [W, H], "depth": a.depth}}), flush=True)
+    ref_def = None
+    if a.mis_default:
+        # the default estimator's own reference, also as two halves
+        hd = [torch.zeros((H, W, 3), dtype=torch.float64, device="cuda") for _ in range(2)]
+        nd = max(2, (a.ref_spp // 4) // step)
+        t0 = time.perf_counter()
+        for q in range(nd):
+            gs.render_device(img.data_ptr(), step, max_depth=a.depth, seed=888000 + q * step, mode=MODE_MIS, flags=0)
+            hd[q & 1] += img.double()
+        ref_def = ((hd[0] + hd[1]) / nd).float()
+        da = (hd[0] / ((nd + 1) // 2)).float()
+        db = (hd[1] / max(1, nd // 2)).float()
+        def_noise = float(((da - db) ** 2 / (ref_def ** 2 + 1e-2)).mean()) / 4.0
+        print(json.dumps({"reference_mis_default": {"spp": nd * step, "seconds": time.perf_counter() - t0,
+                                                    "relMSE_noise_estimate": def_noise,
+                                                    "bias_relMSE_vs_unbiased": rel_mse(ref_def, ref),
+                                                    "mean": float(ref_def.mean())}}), flush=True)
     # warm-up (graph capture, allocations, kernel loading)
     gs.render_device(img.data_ptr(), 1, max_depth=a.depth, seed=1, mode=MODE_MIS, flags=FLAG_UNBIASED_MIS)
     gs.render_device(img.data_ptr(), 1, max_depth=a.depth, seed=1, mode=MODE_NN, flags=FLAG_NN_FREEZE)
@@ -137,6 +162,8 @@ def main():
     results = {}
     res_plain, img_plain, _ = progressive(gs, MODE_MIS, FLAG_UNBIASED_MIS, B, a.chunk, a.depth, 10_000, ref, cps)
     results["plain"] = res_plain
+    if ref_def is not None:
+        results["mis_default"], _, _ = progressive(gs, MODE_MIS, 0, B, a.chunk, a.depth, 15_000, ref_def, cps)
     if a.plain_trr:
         results["plain_trr"], _, _ = progressive(gs, MODE_MIS, FLAG_UNBIASED_MIS | FLAG_THROUGHPUT_RR, B, a.chunk,
                                                  a.depth, 10_000, ref, cps)
@@ -189,6 +216,13 @@ def main():
                          "time_fraction": None if t_nn is None else t_nn / bud,
                          "relMSE_noise_corrected": None if not n else n[0] - ref_noise,
                          "time_fraction_noise_corrected": None if t_nc is None else t_nc / bud}
+        if "mis_default" in results:
+            d = [r for t, _, r in results["mis_default"] if t == bud]
+            if d:
+                row["mis_default_relMSE_vs_own_reference"] = d[0]
+                for name in nn_runs:
+                    t_d = time_to_reach(results[name], d[0])
+                    row[name]["time_fraction_vs_mis_default"] = None if t_d is None else t_d / bud
         if "sdtree" in results:
             sd = [r for (el, spp, r), b2 in zip(results["sdtree"], a.budgets) if b2 == bud]
             row["sdtree_relMSE"] = sd[0] if sd else None
