@@ -4,9 +4,9 @@
 //   master  float  [kNNWeights]          layer l at nn_layer_offset(l), row-major [in][out]
 //   wt      bf16   [4 layers][64][72]    transposed [out][in], rows padded to 72
 //   w       bf16   [4 layers][64][72]    row-major  [in][out] padded (backward data pass)
-// Inference and the training forward/backward run on tcgen05 (tiles of 128
-// samples, one sample per thread, accumulators in tensor memory); the
-// weight-gradient reduction over the batch runs on mma.sync fragments.
+// Inference, the training forward/backward and the weight-gradient reduction
+// over the batch run on tcgen05 (MMAs issued by one thread from operands in
+// shared memory, FP32 accumulators in tensor memory).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -464,71 +464,89 @@ __global__ void __launch_bounds__(kTcRows) k_nn_train_fb(const NNTrainTask* __re
     if (lane == 0) atomicAdd(loss_out, ls);
 }
 
-// dW_l = A_l^T dZ_l over the batch: one CTA reduces a slice of rows into a
-// 64 x out_l tile with mma (A^T fragments read transposed from smem), then
-// adds it to the FP32 gradient.  blockIdx.y = layer.
-constexpr int kWGRows = 64;
-// blockIdx.z: the network (task).
-__global__ void __launch_bounds__(kNNThreads) k_nn_wgrad(const NNTrainTask* __restrict__ tasks) {
-    __shared__ __align__(16) __nv_bfloat16 sA[kWGRows][72];
-    __shared__ __align__(16) __nv_bfloat16 sG[kWGRows][72];
+// dW_l = A_l^T dZ_l over the batch on the tensor cores.  blockIdx.y = layer,
+// blockIdx.z = network (task); the CTAs of a (layer, network) share its
+// records in K tiles of kWGK.  Per tile every thread takes one record and
+// writes its activation row and output-gradient row transposed into the
+// canonical K-major layout (A: input x record, B: output x record), then one
+// thread issues the K chain of MMAs, D (+)= A B^T, into an FP32 accumulator
+// in tensor memory that persists over the CTA's tiles.  M = 128 with input
+// rows 64..127 of A kept zero (lane r of the accumulator = input r); N = 64
+// or 48 outputs.  The CTA's sum is read back once (tcgen05.ld, inputs
+// 0..63 = warps 0 and 1) and added to the FP32 gradient.
+constexpr int kWGK = 128;                               // records per K tile
+constexpr uint32_t kWGSbo = (kWGK / 8) * 128;           // K = 128: 16 core matrices per 8-row group
+constexpr int kWGABytes = kTcRows * kWGK * 2;           // A tile: 128 x 128 bf16
+constexpr int kWGBBytes = 64 * kWGK * 2;                // B tile: 64 x 128 bf16
+constexpr size_t kWGSmem = kWGABytes + kWGBBytes + 16;  // + barrier, tensor-memory address
+
+__global__ void __launch_bounds__(kTcRows) k_nn_wgrad(const NNTrainTask* __restrict__ tasks) {
+    extern __shared__ __align__(1024) unsigned char smem[];
     const NNTrainTask& task = tasks[blockIdx.z];
     const NNTrainBuf TB = task.TB;
     const int n = task.n;
-    float* __restrict__ grad = task.grad;
     const int l = blockIdx.y;
     const int nout = nn_layer_out(l);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, g = lane >> 2, t = lane & 3;
-    // warp w computes rows (inputs) 16w .. 16w+15 of dW, all outputs
-    float acc[8][4];
-#pragma unroll
-    for (int nt = 0; nt < 8; nt++) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
+    uint32_t* status = reinterpret_cast<uint32_t*>(task.scal + 2);
+    unsigned char* s_a = smem;
+    unsigned char* s_b = smem + kWGABytes;
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_b + kWGBBytes);
+    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(s_bar + 1);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    // zero both tiles once: A's rows 64..127 and B's rows >= nout stay zero
+    for (int e = tid; e < (kWGABytes + kWGBBytes) / 16; e += blockDim.x)
+        reinterpret_cast<uint4*>(smem)[e] = make_uint4(0u, 0u, 0u, 0u);
+    const uint32_t tmem = tc_begin(s_bar, s_tmem);  // (its barrier also orders the zeroing)
+    const uint32_t bar = smem_u32(s_bar), a_addr = smem_u32(s_a), b_addr = smem_u32(s_b);
     const __nv_bfloat16* A = TB.act + (size_t)l * TB.cap * 64;
     const __nv_bfloat16* G = TB.grad + (size_t)l * TB.cap * 64;
-    for (int r0 = blockIdx.x * kWGRows; r0 < n; r0 += gridDim.x * kWGRows) {
-        __syncthreads();
-        for (int e = threadIdx.x; e < kWGRows * 8; e += blockDim.x) {
-            const int r = e >> 3, c8 = (e & 7) * 8;
+    uint32_t phase = 0;
+    bool ok = true;
+    int tiles = 0;
+    for (int r0 = blockIdx.x * kWGK; r0 < n && ok; r0 += gridDim.x * kWGK, tiles++) {
+        const int r = r0 + tid;  // this thread's record = column k = tid of both tiles
+#pragma unroll
+        for (int g = 0; g < 8; g++) {
             uint4 va = make_uint4(0u, 0u, 0u, 0u), vg = make_uint4(0u, 0u, 0u, 0u);
-            if (r0 + r < n) {
-                va = *reinterpret_cast<const uint4*>(A + (size_t)(r0 + r) * 64 + c8);
-                if (c8 < nout) vg = *reinterpret_cast<const uint4*>(G + (size_t)(r0 + r) * 64 + c8);
+            if (r < n) {
+                va = *reinterpret_cast<const uint4*>(A + (size_t)r * 64 + 8 * g);
+                if (8 * g < nout) vg = *reinterpret_cast<const uint4*>(G + (size_t)r * 64 + 8 * g);
             }
-            *reinterpret_cast<uint4*>(&sA[r][c8]) = va;
-            *reinterpret_cast<uint4*>(&sG[r][c8]) = vg;
+            const uint16_t* ea = reinterpret_cast<const uint16_t*>(&va);
+            const uint16_t* eg = reinterpret_cast<const uint16_t*>(&vg);
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                *reinterpret_cast<uint16_t*>(s_a + umma_offset(8 * g + q, tid, kWGK)) = ea[q];
+                if (8 * g < nout) *reinterpret_cast<uint16_t*>(s_b + umma_offset(8 * g + q, tid, kWGK)) = eg[q];
+            }
         }
+        fence_proxy_async_smem();
+        tc_fence_before_sync();
         __syncthreads();
-        // K = rows of the slice, 4 k-tiles of 16
+        tc_fence_after_sync();
+        if (tid == 0) {
+            const uint32_t idesc = umma_idesc_bf16_f32(kTcRows, nout);
+            for (int ks = 0; ks < kWGK / 16; ks++)
+                umma_bf16(tmem, umma_desc(a_addr + ks * 2 * kUmmaLBO, kWGSbo),
+                          umma_desc(b_addr + ks * 2 * kUmmaLBO, kWGSbo), idesc, (tiles > 0 || ks > 0) ? 1u : 0u);
+            umma_commit(bar);
+        }
+        // the tiles are rewritten only after the MMAs that read them completed
+        ok = __syncthreads_and(mbar_wait_bounded(bar, phase)) != 0;
+        phase ^= 1u;
+        if (ok) tc_fence_after_sync();
+    }
+    if (ok && tiles > 0 && warp < 2) {
+        const uint32_t t_row = tmem + ((uint32_t)(warp * 32) << 16);
+        float* dst = task.grad + nn_layer_offset(l) + (size_t)tid * nout;  // row = input tid
+        for (int c0 = 0; c0 < nout; c0 += 16) {
+            float v[16];
+            tmem_ld16(t_row + (uint32_t)c0, v);
 #pragma unroll
-        for (int kt = 0; kt < kWGRows / 16; kt++) {
-            // A^T fragment: element (m = input 16w+g(+8), k = row 16kt+2t(+1,+8,+9))
-            const int m0 = 16 * warp + g, k0 = 16 * kt + 2 * t;
-            uint32_t a[4];
-            a[0] = pack_bf16(__bfloat162float(sA[k0][m0]), __bfloat162float(sA[k0 + 1][m0]));
-            a[1] = pack_bf16(__bfloat162float(sA[k0][m0 + 8]), __bfloat162float(sA[k0 + 1][m0 + 8]));
-            a[2] = pack_bf16(__bfloat162float(sA[k0 + 8][m0]), __bfloat162float(sA[k0 + 9][m0]));
-            a[3] = pack_bf16(__bfloat162float(sA[k0 + 8][m0 + 8]), __bfloat162float(sA[k0 + 9][m0 + 8]));
-#pragma unroll
-            for (int nt = 0; nt < 8; nt++) {
-                if (nt * 8 >= nout) break;
-                // B fragment: element (k = row 16kt+2t(+1), n = output 8nt+g) from sG[row][out]
-                uint32_t b[2];
-                b[0] = pack_bf16(__bfloat162float(sG[k0][nt * 8 + g]), __bfloat162float(sG[k0 + 1][nt * 8 + g]));
-                b[1] = pack_bf16(__bfloat162float(sG[k0 + 8][nt * 8 + g]), __bfloat162float(sG[k0 + 9][nt * 8 + g]));
-                mma_bf16(acc[nt], a, b);
-            }
+            for (int k = 0; k < 16; k++) atomicAdd(dst + c0 + k, v[k]);
         }
     }
-    float* dst = grad + nn_layer_offset(l);
-#pragma unroll
-    for (int nt = 0; nt < 8; nt++) {
-        if (nt * 8 >= nout) break;
-        const int m0 = 16 * warp + g, c = nt * 8 + 2 * t;
-        atomicAdd(dst + m0 * nout + c, acc[nt][0]);
-        atomicAdd(dst + m0 * nout + c + 1, acc[nt][1]);
-        atomicAdd(dst + (m0 + 8) * nout + c, acc[nt][2]);
-        atomicAdd(dst + (m0 + 8) * nout + c + 1, acc[nt][3]);
-    }
+    tc_end(ok, tmem, bar, phase, status);
 }
 
 // Adam (Kingma & Ba 2015) on the FP32 master weights; refreshes the two
@@ -583,6 +601,8 @@ cudaError_t nn_set_smem_limits() {
                                          (int)nn_smem_infer());
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(k_nn_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nn_smem_infer());
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_nn_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWGSmem);
     if (e != cudaSuccess) return e;
     return cudaFuncSetAttribute(k_nn_train_fb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nn_smem_train());
 }
@@ -643,8 +663,8 @@ void launch_nn_train_tasks(const NNTrainTask* tasks, int n_tasks, int max_n, int
     const dim3 gf(std::max(1, std::min(per_task, (max_n + kTcRows - 1) / kTcRows)), n_tasks);
     k_nn_train_fb<<<gf, kTcRows, nn_smem_train(), st>>>(tasks);
     const int per_task_w = std::max(1, (num_sms + n_tasks - 1) / n_tasks);
-    const dim3 gw(std::max(1, std::min(per_task_w, (max_n + kWGRows - 1) / kWGRows)), kNNLayers, n_tasks);
-    k_nn_wgrad<<<gw, kNNThreads, 0, st>>>(tasks);
+    const dim3 gw(std::max(1, std::min(per_task_w, (max_n + kWGK - 1) / kWGK)), kNNLayers, n_tasks);
+    k_nn_wgrad<<<gw, kTcRows, kWGSmem, st>>>(tasks);
     if (apply) k_nn_adam<<<gz, 256, 0, st>>>(tasks, opt.b1, opt.b2, opt.eps, opt.clip);
 }
 

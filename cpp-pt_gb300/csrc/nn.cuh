@@ -5,7 +5,7 @@
 //
 // Network: 64 inputs -> 64 -> 64 -> 64 (ReLU) -> 48 outputs, no biases
 // (the constant input feature acts as one), BF16 weights and activations,
-// FP32 accumulation (mma.sync m16n8k16 bf16).
+// FP32 accumulation in tensor memory (tcgen05.mma kind::f16, nn.cu).
 // Inputs (64): frequency encoding of the position normalised to the scene
 // box (3 axes x 8 octaves x sin/cos = 48), shading normal (3), direction to
 // the previous vertex wo (3), 1, zero padding.
@@ -199,18 +199,10 @@ __device__ __forceinline__ f3 nn_mixture_sample(const NNMixture& M, float u0, fl
     return vmf_sample(mu, kappa, u1, u2);
 }
 
-// ---- bf16 tensor-core helpers (mma.sync m16n8k16, row.col, f32 accumulate) ----
+// two floats as a bf16 pair (round to nearest even), low half first
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
     return *reinterpret_cast<const uint32_t*>(&v);
-}
-
-__device__ __forceinline__ void mma_bf16(float c[4], const uint32_t a[4], const uint32_t b[2]) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
 }  // namespace cpppt_gb300
