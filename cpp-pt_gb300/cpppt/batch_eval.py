@@ -53,9 +53,16 @@ def main():
     p = plan(a.scenes, a.seed, a.min_tris, a.max_tris, a.spp_scale)
     t0 = time.perf_counter()
 
+    gen_s, create_s = [], []
+
     def make(q):
+        t1 = time.perf_counter()
         sc = scenes.soup(seed=q["scene_seed"], n_spheres=q["n_spheres"], width=q["res"], height=q["res"])
-        return GpuScene(sc)
+        t2 = time.perf_counter()
+        gs = GpuScene(sc)
+        gen_s.append(t2 - t1)
+        create_s.append(time.perf_counter() - t2)
+        return gs
 
     with ThreadPoolExecutor(a.threads) as ex:
         members = list(ex.map(make, p))
@@ -64,7 +71,9 @@ def main():
     jobs = [dict(scene=k, spp=q["spp"], max_depth=a.depth, seed=a.seed * 1000003 + k) for k, q in enumerate(p)]
     paths = sum(q["res"] * q["res"] * q["spp"] for q in p)
     print(json.dumps({"phase": "build", "scenes": a.scenes, "triangles": int(sum(tris)), "min_tris": min(tris),
-                      "max_tris": max(tris), "paths": paths, "seconds": t_build}), flush=True)
+                      "max_tris": max(tris), "paths": paths, "seconds": t_build,
+                      "soup_generation_thread_seconds": sum(gen_s), "scene_create_thread_seconds": sum(create_s)}),
+          flush=True)
 
     t0 = time.perf_counter()
     b = GpuBatch(members)

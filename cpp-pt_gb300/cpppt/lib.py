@@ -20,6 +20,7 @@ MODE_MIS, MODE_SDTREE, MODE_NN, MODE_NEE, MODE_PT = 0, 1, 2, 3, 4
 FLAG_TIME_KERNELS, FLAG_COUNT, FLAG_UNBIASED_MIS, FLAG_NN_FREEZE, FLAG_THROUGHPUT_RR = 1, 2, 4, 8, 16
 NN_WEIGHTS = 15360
 NN_KL, NN_CHI2 = 0, 1
+NN_ENC_FREQ, NN_ENC_ONEBLOB = 0, 1
 
 # every function the header declares
 EXPORTS = ["pt_scene_create", "pt_scene_load", "pt_scene_destroy", "pt_scene_info", "pt_trace_closest", "pt_trace_any",
@@ -27,7 +28,7 @@ EXPORTS = ["pt_scene_create", "pt_scene_load", "pt_scene_destroy", "pt_scene_inf
            "pt_render_device_noalloc",
            "pt_render_stats_get", "pt_image_save", "pt_last_error", "pt_debug_ref_topology",
            "pt_debug_sdtree_run", "pt_nn_get_weights", "pt_nn_set_weights", "pt_nn_reset", "pt_nn_stats",
-           "pt_debug_nn_forward", "pt_debug_nn_grad", "pt_debug_nn_grad_ex", "pt_nn_configure", "pt_nn_config_get",
+           "pt_debug_nn_forward", "pt_debug_nn_forward_ex", "pt_debug_nn_grad", "pt_debug_nn_grad_ex", "pt_nn_configure", "pt_nn_config_get",
            "pt_batch_create", "pt_batch_destroy", "pt_batch_render", "pt_batch_render_device", "pt_batch_set_tuning",
            "pt_batch_get_tuning", "pt_batch_stats", "pt_batch_autotune", "pt_set_mesh_cache",
            "pt_batch_render_ex", "pt_batch_render_ex_device", "pt_debug_image_load", "pt_debug_ref_topology_device", "pt_debug_bsdf",
@@ -65,7 +66,8 @@ class PtRenderStats(C.Structure):
 
 class PtNNConfig(C.Structure):
     _fields_ = [("learning_rate", C.c_float), ("bsdf_frac_min", C.c_float), ("bsdf_frac_max", C.c_float),
-                ("batch", C.c_int32), ("divergence", C.c_int32), ("steps_per_round", C.c_int32)]
+                ("batch", C.c_int32), ("divergence", C.c_int32), ("steps_per_round", C.c_int32),
+                ("encoding", C.c_int32)]
 
 
 class PtBatchJob(C.Structure):
@@ -125,7 +127,8 @@ def load(path: str = LIB_PATH):
     lib.pt_debug_tensor_wait_timeout.argtypes = []
     lib.pt_debug_light_sample.argtypes = [P, C.c_int32, P, P]
     lib.pt_debug_nn_grad.argtypes = [P, P, P, P, C.c_int32, P, P]
-    lib.pt_debug_nn_grad_ex.argtypes = [P, P, P, P, C.c_int32, C.c_int32, C.c_float, C.c_float, P, P]
+    lib.pt_debug_nn_grad_ex.argtypes = [P, P, P, P, C.c_int32, C.c_int32, C.c_float, C.c_float, C.c_int32, P, P]
+    lib.pt_debug_nn_forward_ex.argtypes = [P, P, P, P, C.c_int32, C.c_int32, P]
     lib.pt_nn_configure.argtypes = [P, P]
     lib.pt_nn_config_get.argtypes = [P, P]
     lib.pt_set_mesh_cache.argtypes = [C.c_int32]
@@ -275,7 +278,8 @@ class GpuScene:
 
     def nn_configure(self, **kw):
         """Updates the learned guide's settings (learning_rate, bsdf_frac_min,
-        bsdf_frac_max, batch, divergence: NN_KL / NN_CHI2, steps_per_round);
+        bsdf_frac_max, batch, divergence: NN_KL / NN_CHI2, steps_per_round,
+        encoding: NN_ENC_FREQ / NN_ENC_ONEBLOB);
         returns the new settings."""
         c = PtNNConfig()
         _check(_lib.pt_nn_config_get(self.h, C.byref(c)))
@@ -480,7 +484,7 @@ def debug_light_sample(scene: "GpuScene", cases: np.ndarray) -> np.ndarray:
     return out
 
 
-def nn_forward(weights, lo, hi, inputs):
+def nn_forward(weights, lo, hi, inputs, encoding=NN_ENC_FREQ):
     """Debug forward pass of the learned guide on the GPU: (n,9) -> (n,41)."""
     L = load()
     w = np.ascontiguousarray(weights, np.float32)
@@ -488,7 +492,7 @@ def nn_forward(weights, lo, hi, inputs):
     out = np.zeros((len(x), 41), np.float32)
     lo = np.ascontiguousarray(lo, np.float32)
     hi = np.ascontiguousarray(hi, np.float32)
-    _check(L.pt_debug_nn_forward(_ptr(w), _ptr(lo), _ptr(hi), _ptr(x), len(x), _ptr(out)))
+    _check(L.pt_debug_nn_forward_ex(_ptr(w), _ptr(lo), _ptr(hi), _ptr(x), len(x), int(encoding), _ptr(out)))
     return out
 
 
@@ -505,7 +509,7 @@ def nn_grad(weights, lo, hi, records):
     return loss.value, g
 
 
-def nn_grad_step(weights, lo, hi, records, divergence=NN_CHI2, c_lo=0.3, c_hi=0.9):
+def nn_grad_step(weights, lo, hi, records, divergence=NN_CHI2, c_lo=0.3, c_hi=0.9, encoding=NN_ENC_FREQ):
     """The renderer's training-step gradient on the GPU (device T sum, KL or
     chi-square weights, BSDF fraction in [c_lo, c_hi]): (loss, dL/dW)."""
     L = load()
@@ -516,5 +520,5 @@ def nn_grad_step(weights, lo, hi, records, divergence=NN_CHI2, c_lo=0.3, c_hi=0.
     lo = np.ascontiguousarray(lo, np.float32)
     hi = np.ascontiguousarray(hi, np.float32)
     _check(L.pt_debug_nn_grad_ex(_ptr(w), _ptr(lo), _ptr(hi), _ptr(r), len(r), int(divergence), float(c_lo),
-                                 float(c_hi), _ptr(g), C.byref(loss)))
+                                 float(c_hi), int(encoding), _ptr(g), C.byref(loss)))
     return loss.value, g

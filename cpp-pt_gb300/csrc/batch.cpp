@@ -485,6 +485,7 @@ void render_batch_slot(pt_batch* b, const pt_batch_job* jobs, int n_jobs, float*
         }
         nj.c_lo = N.c_lo;
         nj.c_hi = N.c_hi;
+        nj.encoding = N.encoding;
         nj.rec = train ? s->nn_rec : nullptr;
         nj.rec_cap = cap[m];
     }

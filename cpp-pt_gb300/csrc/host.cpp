@@ -509,6 +509,7 @@ NNNorm scene_norm(const pt_scene* s) {
     }
     N.c_lo = s->nn_cfg.bsdf_frac_min;
     N.c_hi = s->nn_cfg.bsdf_frac_max;
+    N.encoding = s->nn_cfg.encoding;
     return N;
 }
 
@@ -665,6 +666,7 @@ void render_nn(pt_scene* s, const pt_render_desc* desc, float* d_dst, bool guide
     for (int k = 0; k < 3; k++) { nj.lo[k] = N.lo[k]; nj.inv_ext[k] = N.inv_ext[k]; }
     nj.c_lo = N.c_lo;
     nj.c_hi = N.c_hi;
+    nj.encoding = N.encoding;
     nj.rec = train ? s->nn_rec : nullptr;
     nj.rec_cap = train ? rec_cap : 0;
     nj.n_rec = &s->d_ctr->n_rec;
@@ -1198,6 +1200,10 @@ pt_status pt_nn_configure(pt_scene* s, const pt_nn_config* c) {
         g_error = "steps_per_round must be in [1, 64]";
         return PT_ERR_INVALID;
     }
+    if (c->encoding != PT_NN_ENC_FREQ && c->encoding != PT_NN_ENC_ONEBLOB) {
+        g_error = "encoding must be PT_NN_ENC_FREQ or PT_NN_ENC_ONEBLOB";
+        return PT_ERR_INVALID;
+    }
     s->nn_cfg = *c;
     s->nn_rec_count = 0;  // records of the previous batch size are dropped
     return PT_OK;
@@ -1247,9 +1253,10 @@ NNNorm norm_from(const float* lo, const float* hi) {
 }
 }  // namespace
 
-pt_status pt_debug_nn_forward(const float* weights, const float* lo, const float* hi, const float* inputs, int32_t n,
-                              float* out) {
+pt_status pt_debug_nn_forward_ex(const float* weights, const float* lo, const float* hi, const float* inputs,
+                                 int32_t n, int32_t encoding, float* out) {
     if (!weights || !lo || !hi || n < 0 || (n > 0 && (!inputs || !out))) { g_error = "bad argument"; return PT_ERR_INVALID; }
+    if (encoding != PT_NN_ENC_FREQ && encoding != PT_NN_ENC_ONEBLOB) { g_error = "unknown encoding"; return PT_ERR_INVALID; }
     return guarded([&] {
         if (n == 0) return;
         DebugCtx c;
@@ -1269,6 +1276,7 @@ pt_status pt_debug_nn_forward(const float* weights, const float* lo, const float
         for (int k = 0; k < 3; k++) { hj.lo[k] = N.lo[k]; hj.inv_ext[k] = N.inv_ext[k]; }
         hj.c_lo = N.c_lo;
         hj.c_hi = N.c_hi;
+        hj.encoding = encoding;
         DevNNJob* dj = dalloc<DevNNJob>(c.owned, 1);
         ck(cudaMemcpyAsync(dj, &hj, sizeof(hj), cudaMemcpyHostToDevice, c.st), "copy");
         launch_nn_forward_debug(dj, din, n, dout, dstat, c.sms, c.st);
@@ -1350,12 +1358,17 @@ pt_status pt_debug_light_sample(pt_scene* s, int32_t n, const float* cases, floa
     });
 }
 
+pt_status pt_debug_nn_forward(const float* weights, const float* lo, const float* hi, const float* inputs, int32_t n,
+                              float* out) {
+    return pt_debug_nn_forward_ex(weights, lo, hi, inputs, n, PT_NN_ENC_FREQ, out);
+}
+
 namespace {
 // One gradient evaluation of the training kernels on a host batch.  prep:
 // the renderer's own step (T summed, and squared for chi-square, on the
 // device); otherwise the host sums T and the KL weights are used.
 void nn_grad_debug(const float* weights, const float* lo, const float* hi, const float* records, int32_t n, bool prep,
-                   int divergence, float c_lo, float c_hi, float* out_grad, float* out_loss) {
+                   int divergence, float c_lo, float c_hi, int encoding, float* out_grad, float* out_loss) {
     DebugCtx c;
     NNWeights W;
     NNTrainBuf TB;
@@ -1374,6 +1387,7 @@ void nn_grad_debug(const float* weights, const float* lo, const float* hi, const
     task.N = norm_from(lo, hi);
     task.N.c_lo = c_lo;
     task.N.c_hi = c_hi;
+    task.N.encoding = encoding;
     task.rec = drec;
     task.n = n;
     task.chi2 = divergence == PT_NN_CHI2 ? 1 : 0;
@@ -1396,17 +1410,23 @@ void nn_grad_debug(const float* weights, const float* lo, const float* hi, const
 }  // namespace
 
 pt_status pt_debug_nn_grad_ex(const float* weights, const float* lo, const float* hi, const float* records, int32_t n,
-                              int32_t divergence, float c_lo, float c_hi, float* out_grad, float* out_loss) {
+                              int32_t divergence, float c_lo, float c_hi, int32_t encoding, float* out_grad,
+                              float* out_loss) {
     if (!weights || !lo || !hi || n <= 0 || !records || !out_grad) { g_error = "bad argument"; return PT_ERR_INVALID; }
     if (divergence != PT_NN_KL && divergence != PT_NN_CHI2) { g_error = "unknown divergence"; return PT_ERR_INVALID; }
     if (!(c_lo >= 0.1f && c_lo <= c_hi && c_hi <= 1.0f)) { g_error = "need 0.1 <= c_lo <= c_hi <= 1"; return PT_ERR_INVALID; }
-    return guarded([&] { nn_grad_debug(weights, lo, hi, records, n, true, divergence, c_lo, c_hi, out_grad, out_loss); });
+    if (encoding != PT_NN_ENC_FREQ && encoding != PT_NN_ENC_ONEBLOB) { g_error = "unknown encoding"; return PT_ERR_INVALID; }
+    return guarded([&] {
+        nn_grad_debug(weights, lo, hi, records, n, true, divergence, c_lo, c_hi, encoding, out_grad, out_loss);
+    });
 }
 
 pt_status pt_debug_nn_grad(const float* weights, const float* lo, const float* hi, const float* records, int32_t n,
                            float* out_grad, float* out_loss) {
     if (!weights || !lo || !hi || n <= 0 || !records || !out_grad) { g_error = "bad argument"; return PT_ERR_INVALID; }
-    return guarded([&] { nn_grad_debug(weights, lo, hi, records, n, false, PT_NN_KL, 0.1f, 0.9f, out_grad, out_loss); });
+    return guarded([&] {
+        nn_grad_debug(weights, lo, hi, records, n, false, PT_NN_KL, 0.1f, 0.9f, PT_NN_ENC_FREQ, out_grad, out_loss);
+    });
 }
 
 pt_status pt_render_stats_get(pt_scene* s, pt_render_stats* out) {

@@ -38,8 +38,40 @@ constexpr int kNNParams = 41;  // post-processed mixture per sample: 8 x (mu xyz
 __host__ __device__ constexpr int nn_layer_out(int l) { return l == kNNLayers - 1 ? kNNOut : kNNHidden; }
 __host__ __device__ constexpr int nn_layer_offset(int l) { return l * 64 * 64; }
 
+// One-blob encoding (Mueller et al. 2019, "Neural importance sampling"):
+// a scalar s in [0, 1] spread over kNNBlobBins Gaussian bins of width
+// sigma = 1 / kNNBlobBins centred at (b + 1/2) / kNNBlobBins; `wrap`: s is
+// periodic (an azimuth), distances are taken around the circle.
+constexpr int kNNBlobBins = 6;
+__device__ __forceinline__ float one_blob(float s, int b, bool wrap) {
+    float d = fabsf(s - ((float)b + 0.5f) * (1.0f / kNNBlobBins));
+    if (wrap) d = fminf(d, 1.0f - d);
+    const float z = d * (float)kNNBlobBins;  // distance in units of sigma
+    return __expf(-0.5f * z * z);
+}
+
+// Input feature j of a sample (pos already normalised to [0,1]^3) under
+// encoding 1 (PT_NN_ENC_ONEBLOB): position at 6 octaves (36), one-blob
+// cos theta and phi of the normal and of wo (4 x 6), 1.
+__device__ __forceinline__ float nn_feature_oneblob(int j, f3 pn, f3 n, f3 wo) {
+    if (j < 36) {
+        const int c = j / 12, k = (j % 12) >> 1;
+        const float x = c == 0 ? pn.x : (c == 1 ? pn.y : pn.z);
+        const float a = x * (float)(1 << k) * kPi;
+        return (j & 1) ? __cosf(a) : __sinf(a);
+    }
+    if (j < 36 + 4 * kNNBlobBins) {
+        const int q = (j - 36) / kNNBlobBins, b = (j - 36) % kNNBlobBins;
+        const f3 v = q < 2 ? n : wo;
+        const float s = (q & 1) ? atan2f(v.y, v.x) * (0.5f * kInvPi) + 0.5f : 0.5f * (v.z + 1.0f);
+        return one_blob(s, b, (q & 1) != 0);
+    }
+    return j == 36 + 4 * kNNBlobBins ? 1.0f : 0.0f;
+}
+
 // Input feature j of a sample (pos already normalised to [0,1]^3).
-__device__ __forceinline__ float nn_feature(int j, f3 pn, f3 n, f3 wo) {
+__device__ __forceinline__ float nn_feature(int j, f3 pn, f3 n, f3 wo, int encoding = 0) {
+    if (encoding == 1) return nn_feature_oneblob(j, pn, n, wo);
     if (j < 48) {
         const int c = j >> 4, k = (j >> 1) & 7;
         const float x = c == 0 ? pn.x : (c == 1 ? pn.y : pn.z);

@@ -19,6 +19,7 @@ struct NNWeights {
 struct NNNorm {
     float lo[3], inv_ext[3];  // position normalisation to the scene box
     float c_lo = 0.1f, c_hi = 0.9f;  // range of the BSDF selection probability
+    int32_t encoding = 0;            // PT_NN_ENC_* (input encoding)
 };
 
 struct NNTrainBuf {
@@ -48,6 +49,7 @@ struct DevNNJob {
     const __nv_bfloat16* wt;  // forward weights of the job's scene (W_l^T, rows padded to 72)
     float lo[3], inv_ext[3];  // position normalisation to the scene box
     float c_lo, c_hi;         // range of the BSDF selection probability
+    int32_t encoding;         // PT_NN_ENC_* of the job's network
     float4* rec;              // training records of the job's scene (4 float4 each)
     int32_t rec_cap;          // capacity of rec (0: no records)
     int32_t* n_rec;           // record counter of the job's scene

@@ -314,7 +314,17 @@ typedef struct pt_nn_config {
     int32_t batch;
     int32_t divergence;
     int32_t steps_per_round; /* Adam steps at most per wavefront round (16 iterations), 1..64 */
+    int32_t encoding;        /* PT_NN_ENC_FREQ (default) or PT_NN_ENC_ONEBLOB; reset the weights
+                                (pt_nn_reset) after changing it */
 } pt_nn_config;
+/* Input encodings of the learned guide (64 inputs, the last constant 1):
+ * FREQ: sin / cos of the position normalised to the scene box at 8
+ *   octaves per axis (48), then the shading normal and wo as they are;
+ * ONEBLOB: the position at 6 octaves per axis (36), then the normal's and
+ *   wo's cos theta and phi, each mapped to [0, 1] and spread over 6
+ *   Gaussian bins (one-blob encoding, sigma = 1/6; phi wraps around). */
+#define PT_NN_ENC_FREQ 0
+#define PT_NN_ENC_ONEBLOB 1
 pt_status pt_nn_configure(pt_scene* scene, const pt_nn_config* config);
 pt_status pt_nn_config_get(pt_scene* scene, pt_nn_config* config);
 
@@ -334,7 +344,11 @@ pt_status pt_debug_nn_grad(const float* weights, const float* lo, const float* h
  * (records weighted by T^2), with the BSDF selection probability in
  * [c_lo, c_hi] (pt_nn_configure's range; 0.1 <= c_lo <= c_hi <= 1). */
 pt_status pt_debug_nn_grad_ex(const float* weights, const float* lo, const float* hi, const float* records, int32_t n,
-                              int32_t divergence, float c_lo, float c_hi, float* out_grad, float* out_loss);
+                              int32_t divergence, float c_lo, float c_hi, int32_t encoding, float* out_grad,
+                              float* out_loss);
+/* pt_debug_nn_forward with the input encoding (PT_NN_ENC_*). */
+pt_status pt_debug_nn_forward_ex(const float* weights, const float* lo, const float* hi, const float* inputs,
+                                 int32_t n, int32_t encoding, float* out);
 
 /* Unit-test hooks of the integrator's own device functions, checked against
  * the oracle on the same numbers.  pt_debug_bsdf runs BxDF::eval, ::pdf,

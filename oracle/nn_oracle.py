@@ -40,11 +40,42 @@ def bf16(x: torch.Tensor) -> torch.Tensor:
     return x + (r - x).detach()
 
 
-def features(pos_n: torch.Tensor, n: torch.Tensor, wo: torch.Tensor) -> torch.Tensor:
-    """64 inputs: sin/cos(2^k pi x) for the 3 normalised coordinates and
-    8 octaves (feature j < 48: axis j // 16, octave (j // 2) % 8, cos when j
-    is odd), normal, wo, 1, zeros."""
+BLOB_BINS = 6
+
+
+def one_blob(s: torch.Tensor, wrap: bool) -> torch.Tensor:
+    """s in [0, 1] over BLOB_BINS Gaussian bins (sigma = 1 / BLOB_BINS,
+    centres (b + 1/2) / BLOB_BINS); wrap: periodic s (an azimuth)."""
+    c = (torch.arange(BLOB_BINS, dtype=torch.float64) + 0.5) / BLOB_BINS
+    d = (s[:, None] - c[None, :]).abs()
+    if wrap:
+        d = torch.minimum(d, 1.0 - d)
+    z = d * BLOB_BINS
+    return torch.exp(-0.5 * z * z)
+
+
+def features(pos_n: torch.Tensor, n: torch.Tensor, wo: torch.Tensor, encoding: int = 0) -> torch.Tensor:
+    """64 inputs.  encoding 0: sin/cos(2^k pi x) for the 3 normalised
+    coordinates and 8 octaves (feature j < 48: axis j // 16, octave
+    (j // 2) % 8, cos when j is odd), normal, wo, 1, zeros.  encoding 1: the
+    same at 6 octaves (j < 36: axis j // 12, octave (j % 12) // 2), then the
+    one-blob encodings of the normal's cos theta ((z + 1) / 2) and phi
+    (atan2(y, x) / 2 pi + 1/2, periodic) and of wo's, 6 bins each, then 1."""
     B = pos_n.shape[0]
+    if encoding == 1:
+        f = torch.zeros(B, 64, dtype=torch.float64)
+        for j in range(36):
+            c, k = j // 12, (j % 12) >> 1
+            a = pos_n[:, c] * (2 ** k) * math.pi
+            f[:, j] = torch.cos(a) if (j & 1) else torch.sin(a)
+        col = 36
+        for v in (n, wo):
+            f[:, col:col + BLOB_BINS] = one_blob(0.5 * (v[:, 2] + 1.0), False)
+            col += BLOB_BINS
+            f[:, col:col + BLOB_BINS] = one_blob(torch.atan2(v[:, 1], v[:, 0]) / (2 * math.pi) + 0.5, True)
+            col += BLOB_BINS
+        f[:, col] = 1.0
+        return f
     f = torch.zeros(B, 64, dtype=torch.float64)
     for j in range(48):
         c, k = j >> 4, (j >> 1) & 7
@@ -56,9 +87,9 @@ def features(pos_n: torch.Tensor, n: torch.Tensor, wo: torch.Tensor) -> torch.Te
     return f
 
 
-def forward_raw(weights: np.ndarray, pos_n, n, wo):
+def forward_raw(weights: np.ndarray, pos_n, n, wo, encoding: int = 0):
     Ws = [bf16(torch.tensor(w, dtype=torch.float64)) for w in split_weights(weights)]
-    x = bf16(features(pos_n, n, wo))
+    x = bf16(features(pos_n, n, wo, encoding))
     for l in range(3):
         x = bf16(torch.relu(x @ Ws[l]))
     return x @ Ws[3]
@@ -91,15 +122,15 @@ def normalise(pos, lo, hi):
     return (pos - lo) / (hi - lo).clamp_min(1e-6)
 
 
-def forward(weights: np.ndarray, lo, hi, inputs: np.ndarray) -> np.ndarray:
+def forward(weights: np.ndarray, lo, hi, inputs: np.ndarray, encoding: int = 0) -> np.ndarray:
     """inputs (n, 9): position, normal, wo -> (n, 41) mixture parameters."""
     x = torch.tensor(inputs, dtype=torch.float64)
-    raw = forward_raw(weights, normalise(x[:, 0:3], lo, hi), x[:, 3:6], x[:, 6:9])
+    raw = forward_raw(weights, normalise(x[:, 0:3], lo, hi), x[:, 3:6], x[:, 6:9], encoding)
     return params41(raw).numpy()
 
 
 def loss_and_grad(weights: np.ndarray, lo, hi, records: np.ndarray, divergence: str = "kl",
-                  c_lo: float = 0.1, c_hi: float = 0.9):
+                  c_lo: float = 0.1, c_hi: float = 0.9, encoding: int = 0):
     """records (n, 16): pos, normal, wo, wi, p_bsdf, T, 0, 0.  divergence
     "kl" weighs a record by T, "chi2" by T^2; c in [c_lo, c_hi]."""
     r = torch.tensor(records, dtype=torch.float64)
@@ -108,7 +139,7 @@ def loss_and_grad(weights: np.ndarray, lo, hi, records: np.ndarray, divergence: 
     for i, o in SHAPES:
         Ws.append(bf16(W[off:off + i * o].reshape(i, o)))
         off += i * o
-    x = bf16(features(normalise(r[:, 0:3], lo, hi), r[:, 3:6], r[:, 6:9]))
+    x = bf16(features(normalise(r[:, 0:3], lo, hi), r[:, 3:6], r[:, 6:9], encoding))
     for l in range(3):
         x = bf16(torch.relu(x @ Ws[l]))
     raw = x @ Ws[3]

@@ -25,13 +25,14 @@ def random_weights(seed):
     return np.concatenate(w).astype(np.float32)
 
 
-def test_forward_matches_oracle(gpu_lib):
+@pytest.mark.parametrize("encoding", [0, 1], ids=["freq", "oneblob"])
+def test_forward_matches_oracle(gpu_lib, encoding):
     from cpppt import lib
     from oracle import nn_oracle
     w = random_weights(1)
     x = random_inputs(1000, 2)
-    got = lib.nn_forward(w, LO, HI, x)
-    ref = nn_oracle.forward(w, LO, HI, x)
+    got = lib.nn_forward(w, LO, HI, x, encoding=encoding)
+    ref = nn_oracle.forward(w, LO, HI, x, encoding=encoding)
     # mixture weights, selection probability and lobe means; bf16 activations
     assert np.abs(got[:, 40] - ref[:, 40]).max() < 2e-2
     wcols = [5 * j + 4 for j in range(8)]
@@ -68,13 +69,13 @@ GRAD_COS = 0.99995
 GRAD_REL = 5e-3
 
 
-@pytest.mark.parametrize("case", ["kl_host", "kl", "chi2"])
+@pytest.mark.parametrize("case", ["kl_host", "kl", "chi2", "chi2_oneblob"])
 def test_gradient_matches_oracle(gpu_lib, case):
     """kl_host: pt_debug_nn_grad (T summed on the host, KL weights, c in
     [0.1, 0.9]).  kl / chi2: pt_debug_nn_grad_ex, the renderer's own step
     (T summed, and squared for chi-square, on the device) with the renderer's
     default BSDF-fraction range [0.3, 0.9]; chi2 is the renderer's default
-    divergence."""
+    divergence.  chi2_oneblob: the same with the one-blob input encoding."""
     from cpppt import lib
     from oracle import nn_oracle
     w = random_weights(4)
@@ -83,9 +84,11 @@ def test_gradient_matches_oracle(gpu_lib, case):
         loss, g = lib.nn_grad(w, LO, HI, rec)
         rloss, rg = nn_oracle.loss_and_grad(w, LO, HI, rec)
     else:
-        div = lib.NN_CHI2 if case == "chi2" else lib.NN_KL
-        loss, g = lib.nn_grad_step(w, LO, HI, rec, divergence=div, c_lo=0.3, c_hi=0.9)
-        rloss, rg = nn_oracle.loss_and_grad(w, LO, HI, rec, divergence=case, c_lo=0.3, c_hi=0.9)
+        enc = 1 if case.endswith("oneblob") else 0
+        dname = case.split("_")[0]
+        div = lib.NN_CHI2 if dname == "chi2" else lib.NN_KL
+        loss, g = lib.nn_grad_step(w, LO, HI, rec, divergence=div, c_lo=0.3, c_hi=0.9, encoding=enc)
+        rloss, rg = nn_oracle.loss_and_grad(w, LO, HI, rec, divergence=dname, c_lo=0.3, c_hi=0.9, encoding=enc)
     assert abs(loss - rloss) < 2e-3 * max(1.0, abs(rloss)), (loss, rloss)
     off = 0
     for i, o in [(64, 64), (64, 64), (64, 64), (64, 48)]:
@@ -109,16 +112,18 @@ def test_chi2_differs_from_kl(gpu_lib):
     assert diff > 10 * GRAD_REL, diff
 
 
-def test_guided_render_converges_to_plain(gpu_lib):
+@pytest.mark.parametrize("encoding", [0, 1], ids=["freq", "oneblob"])
+def test_guided_render_converges_to_plain(gpu_lib, encoding):
     """Both estimators are unbiased (PT_FLAG_UNBIASED_MIS for plain PT), so
-    after training the guided image must match the plain one statistically."""
+    after training the guided image must match the plain one statistically,
+    with either input encoding of the guide."""
     from cpppt import scenes
     from cpppt.lib import FLAG_UNBIASED_MIS, MODE_MIS, MODE_NN, GpuScene
     from tests.test_gpu_render import check_z, tile_means, ztest
     sc = scenes.slit_room(seed=4, n_boxes=60, box_subdiv=2, width=64, height=32)
     gs = GpuScene(sc)
-    cfg = gs.nn_configure(batch=1 << 14)
-    assert cfg["batch"] == 1 << 14
+    cfg = gs.nn_configure(batch=1 << 14, encoding=encoding)
+    assert cfg["batch"] == 1 << 14 and cfg["encoding"] == encoding
     for k in range(6):  # train the guide
         gs.render(256, max_depth=12, seed=1000 + k, mode=MODE_NN)
     st = gs.nn_stats()
@@ -165,16 +170,18 @@ def test_guide_settings_are_checked(gpu_lib):
     """pt_nn_configure: the defaults, the accepted ranges, and every
     out-of-range value refused with the previous settings kept."""
     from cpppt import scenes
-    from cpppt.lib import NN_CHI2, GpuScene, PtError
+    from cpppt.lib import NN_CHI2, NN_ENC_FREQ, NN_ENC_ONEBLOB, GpuScene, PtError
     gs = GpuScene(scenes.cornell(8, 8))
     cfg = gs.nn_config()
     assert cfg["batch"] == 65536 and cfg["steps_per_round"] == 16 and cfg["divergence"] == NN_CHI2
     assert abs(cfg["learning_rate"] - 3e-3) < 1e-9 and abs(cfg["bsdf_frac_min"] - 0.3) < 1e-7
+    assert cfg["encoding"] == NN_ENC_FREQ
     assert gs.nn_configure(steps_per_round=64, batch=1024)["steps_per_round"] == 64
+    assert gs.nn_configure(encoding=NN_ENC_ONEBLOB)["encoding"] == NN_ENC_ONEBLOB
     gs.nn_configure(**cfg)
     for bad in (dict(steps_per_round=65), dict(steps_per_round=0), dict(batch=1023), dict(batch=262145),
                 dict(bsdf_frac_min=0.05), dict(bsdf_frac_min=0.9, bsdf_frac_max=0.8), dict(learning_rate=0.0),
-                dict(divergence=2)):
+                dict(divergence=2), dict(encoding=2), dict(encoding=-1)):
         with pytest.raises(PtError):
             gs.nn_configure(**bad)
         assert gs.nn_config() == cfg
