@@ -7,6 +7,7 @@ Translation units, compiled in parallel, CUDA for sm_103a only:
   csrc/render.cu  -- traversal and PT+NEE+MIS wavefront kernels (nvcc -gencode arch=compute_103a,code=sm_103a)
   csrc/guide.cu   -- SD-tree guided (PPG) wavefront kernels
   csrc/gpu_bvh.cu -- device build of the reference-topology BVH
+  csrc/gpu_sah.cu -- device build of the 4-wide SAH traversal tree
   csrc/nn.cu      -- learned guide: MLP on the tensor cores, training, guided wavefront
   csrc/host.cpp   -- C ABI, render drivers, loader, image output
   csrc/bvh.cpp    -- BVH builders
@@ -54,7 +55,7 @@ def _commands(extra_cuda: list[str] | None = None):
     nvcc = _nvcc()
     common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
     jobs = []
-    for name in ("render.cu", "guide.cu", "nn.cu", "batch.cu", "gpu_bvh.cu", "host.cpp", "batch.cpp", "bvh.cpp", "sdtree.cpp",
+    for name in ("render.cu", "guide.cu", "nn.cu", "batch.cu", "gpu_bvh.cu", "gpu_sah.cu", "host.cpp", "batch.cpp", "bvh.cpp", "sdtree.cpp",
                  "image_io.cpp", "loader.cpp"):
         src = os.path.join(CSRC, name)
         out = os.path.join(OBJ, name + ".o")

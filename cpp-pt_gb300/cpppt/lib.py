@@ -31,7 +31,7 @@ EXPORTS = ["pt_scene_create", "pt_scene_load", "pt_scene_destroy", "pt_scene_inf
            "pt_debug_nn_forward", "pt_debug_nn_forward_ex", "pt_debug_nn_grad", "pt_debug_nn_grad_ex", "pt_nn_configure", "pt_nn_config_get",
            "pt_batch_create", "pt_batch_destroy", "pt_batch_render", "pt_batch_render_device", "pt_batch_set_tuning",
            "pt_batch_get_tuning", "pt_batch_stats", "pt_batch_autotune", "pt_set_mesh_cache",
-           "pt_batch_render_ex", "pt_batch_render_ex_device", "pt_debug_image_load", "pt_debug_ref_topology_device", "pt_debug_bsdf",
+           "pt_batch_render_ex", "pt_batch_render_ex_device", "pt_debug_image_load", "pt_debug_ref_topology_device", "pt_debug_wide_bvh", "pt_debug_bsdf",
            "pt_debug_light_sample", "pt_debug_traversal_limits", "pt_debug_tensor_wait_timeout"]
 
 
@@ -116,6 +116,7 @@ def load(path: str = LIB_PATH):
     lib.pt_last_error.argtypes = []
     lib.pt_debug_ref_topology.argtypes = [P, C.c_int32, P, P, P, C.c_int32, P]
     lib.pt_debug_ref_topology_device.argtypes = [P, C.c_int32, P, P, P, C.c_int32, P, P]
+    lib.pt_debug_wide_bvh.argtypes = [P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P, C.c_int32, P, P, P, P]
     lib.pt_debug_image_load.argtypes = [C.c_char_p, C.c_int32, C.c_int32, P, P, P, C.c_int64]
     lib.pt_nn_get_weights.argtypes = [P, P]
     lib.pt_nn_set_weights.argtypes = [P, P]
@@ -430,6 +431,22 @@ def ref_topology_device(sc):
     _check(lib.pt_debug_ref_topology_device(_ptr(tv), n, _ptr(order), _ptr(pparent), _ptr(boxes), cap, C.byref(nn),
                                             C.byref(lv)))
     return order, boxes[:6 * nn.value].reshape(-1, 6), pparent, lv.value
+
+
+def wide_bvh(sc, on_device=True, host_threads=0, max_leaf=4):
+    """The 4-wide traversal tree the library builds for a scene's triangles:
+    (nodes (m, 16) uint32, leaf order, depth, inflation), built on the GPU
+    (as scenes are) or on the host with host_threads threads."""
+    lib = load()
+    tv = np.ascontiguousarray(sc.vertices[sc.triangles].reshape(-1), np.float32)
+    n = sc.n_triangles
+    cap = max(n, 16)
+    nodes = np.zeros((cap, 16), np.uint32)
+    order = np.zeros(max(n, 1), np.int32)
+    nn, depth, infl = C.c_int32(), C.c_int32(), C.c_float()
+    _check(lib.pt_debug_wide_bvh(_ptr(tv), n, int(max_leaf), int(bool(on_device)), int(host_threads), _ptr(nodes),
+                                 cap, C.byref(nn), _ptr(order), C.byref(depth), C.byref(infl)))
+    return nodes[:nn.value], order[:n], depth.value, infl.value
 
 
 def sdtree_run(lo, hi, rounds, queries, max_leaves=1 << 20, fn=None, lib=None):

@@ -362,10 +362,14 @@ struct SahBuilder {
         float trav = bb.sah_area() * 1.0f;  // traversal cost relative to one triangle test
         bool make_leaf = count <= max_leaf && (best_axis < 0 || best_cost + trav >= leaf_cost);
         if (make_leaf) { nd.start = start; nd.count = count; return; }
+        // Both sides keep their order (a stable partition), so every node's
+        // primitives stay sorted by insertion index and the tree depends
+        // only on which primitives each node holds: the device build
+        // (gpu_sah.cu) reproduces it node for node.
         if (best_axis >= 0) {
             float lo = cb.lo[best_axis], hi = cb.hi[best_axis];
             float scale = kBins / (hi - lo);
-            int32_t* p = std::partition(order + start, order + start + count, [&](int32_t t) {
+            int32_t* p = std::stable_partition(order + start, order + start + count, [&](int32_t t) {
                 int b = (int)((cen[t][best_axis] - lo) * scale);
                 b = b < 0 ? 0 : (b >= kBins ? kBins - 1 : b);
                 return b <= best_bin;
@@ -373,14 +377,9 @@ struct SahBuilder {
             mid = (int)(p - order);
         }
         if (mid <= start || mid >= start + count) {
-            // no useful SAH split (coincident centroids or depth limit): median split
-            int axis = 0;
-            float ext = -1.0f;
-            for (int k = 0; k < 3; k++)
-                if (cb.hi[k] - cb.lo[k] > ext) { ext = cb.hi[k] - cb.lo[k]; axis = k; }
+            // no SAH split (coincident centroids or the depth limit): halve in
+            // insertion order
             mid = start + count / 2;
-            std::nth_element(order + start, order + mid, order + start + count,
-                             [&](int32_t a, int32_t b) { return cen[a][axis] < cen[b][axis]; });
         }
         int32_t l = alloc(), r = alloc();
         nd.left = l;

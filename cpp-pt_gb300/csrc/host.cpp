@@ -59,17 +59,23 @@ void create_scene(const pt_scene_desc* d, pt_scene* s, const SceneTextures* tx =
         for (int k = 0; k < 3; k++)
             std::memcpy(&tv[9 * (size_t)t + 3 * k], d->vertices + 3 * (size_t)d->triangles[3 * t + k], 12);
 
-    // the two builds are independent: the 4-wide SAH tree on a second thread
+    // the two device builds are independent: the 4-wide SAH tree from a
+    // second host thread on a stream of its own
     auto t0 = std::chrono::steady_clock::now();
     WideBVH wide;
     std::exception_ptr wide_err;
     std::chrono::steady_clock::time_point t2;
+    const int dev = s->device;
     std::thread wide_th([&] {
+        cudaStream_t ws = nullptr;
         try {
-            wide = build_wide_bvh(tv.data(), nt, 4);
+            ck(cudaSetDevice(dev), "cudaSetDevice");
+            ck(cudaStreamCreateWithFlags(&ws, cudaStreamNonBlocking), "cudaStreamCreate");
+            wide = build_wide_bvh_device(tv.data(), nt, 4, ws);
         } catch (...) {
             wide_err = std::current_exception();
         }
+        if (ws) cudaStreamDestroy(ws);
         t2 = std::chrono::steady_clock::now();
     });
     RefTopology ref;
@@ -1527,6 +1533,31 @@ pt_status pt_debug_ref_topology_device(const float* tri_v, int32_t n, int32_t* l
             std::memcpy(node_boxes + 6 * i, t.node_box[i].lo, 12);
             std::memcpy(node_boxes + 6 * i + 3, t.node_box[i].hi, 12);
         }
+    });
+}
+
+pt_status pt_debug_wide_bvh(const float* tri_v, int32_t n, int32_t max_leaf, int32_t on_device, int32_t host_threads,
+                            uint32_t* nodes, int32_t max_nodes, int32_t* n_nodes, int32_t* tri_order,
+                            int32_t* max_depth, float* inflate) {
+    if (n < 0 || (n > 0 && (!tri_v || !tri_order)) || !n_nodes || max_leaf < 1 || max_leaf > 16) {
+        g_error = "bad argument";
+        return PT_ERR_INVALID;
+    }
+    return guarded([&] {
+        WideBVH w;
+        if (on_device) {
+            DebugCtx c;
+            w = build_wide_bvh_device(tri_v, n, max_leaf, c.st);
+        } else {
+            w = build_wide_bvh(tri_v, n, max_leaf, host_threads);
+        }
+        *n_nodes = (int32_t)w.nodes.size();
+        if (max_depth) *max_depth = w.max_depth;
+        if (inflate) *inflate = w.inflate;
+        if ((int32_t)w.nodes.size() > max_nodes || (!nodes && !w.nodes.empty()))
+            throw Fail(PT_ERR_LIMIT, "node buffer too small");
+        if (!w.nodes.empty()) std::memcpy(nodes, w.nodes.data(), sizeof(WideNode) * w.nodes.size());
+        if (n > 0) std::memcpy(tri_order, w.tri_order.data(), sizeof(int32_t) * (size_t)n);
     });
 }
 

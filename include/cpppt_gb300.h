@@ -419,6 +419,19 @@ pt_status pt_debug_ref_topology(const float* tri_v, int32_t n, int32_t* leaf_ord
 pt_status pt_debug_ref_topology_device(const float* tri_v, int32_t n, int32_t* leaf_order, int32_t* prim_parent,
                                        float* node_boxes, int32_t max_nodes, int32_t* n_nodes, int32_t* levels);
 
+/* The 4-wide traversal tree the library builds for a triangle list (binned
+ * SAH, 32 bins, leaves of at most max_leaf triangles, collapsed to 64-byte
+ * compressed nodes), built on the current device (on_device = 1, as scenes
+ * are) or on the host with host_threads threads (on_device = 0; 0 = all
+ * hardware threads; no CUDA call).  Both builds give the same bytes.
+ * Outputs: nodes[16 * max_nodes] (16 words per node, breadth first),
+ * *n_nodes, tri_order[n] (leaf order -> insertion index), *max_depth (tree
+ * levels), *inflate (the absolute box inflation).  PT_ERR_LIMIT when the
+ * tree has more than max_nodes nodes (*n_nodes is set). */
+pt_status pt_debug_wide_bvh(const float* tri_v, int32_t n, int32_t max_leaf, int32_t on_device, int32_t host_threads,
+                            uint32_t* nodes, int32_t max_nodes, int32_t* n_nodes, int32_t* tri_order,
+                            int32_t* max_depth, float* inflate);
+
 #ifdef __cplusplus
 }
 #endif

@@ -72,3 +72,27 @@ def test_parallel_ref_topology_matches_oracle():
     assert np.array_equal(order, o_order)
     assert np.array_equal(boxes.view(np.uint32), o_boxes.view(np.uint32))
     assert np.array_equal(pparent, o_pparent)
+
+
+def test_wide_bvh_host_build_is_thread_independent():
+    """The host 4-wide SAH build keeps every node's triangles in insertion
+    order (stable partitions; halving in that order where no SAH split
+    exists), so its bytes do not depend on how many threads build
+    independent subtrees -- the property the device build relies on to
+    reproduce it.  320k triangles (above the 65536-triangle threading
+    threshold) plus a block of coincident copies and a smaller one."""
+    from cpppt import lib, scenes
+    sc = scenes.soup(seed=9, n_spheres=1000, freq=4, width=8, height=8)
+    sc.triangles[1000:41000] = sc.triangles[7]   # 40000 coincident copies
+    sc.triangles[50000:50100] = sc.triangles[9]  # 100 more
+    n1, o1, d1, f1 = lib.wide_bvh(sc, on_device=False, host_threads=1)
+    n16, o16, d16, f16 = lib.wide_bvh(sc, on_device=False, host_threads=16)
+    assert np.array_equal(n1, n16) and np.array_equal(o1, o16) and d1 == d16 and f1 == f16
+    assert np.array_equal(np.sort(o1), np.arange(sc.n_triangles))
+    # every leaf's triangles ascend by insertion index
+    refs = n1[:, 10:14].reshape(-1)
+    leaves = refs[(refs != 0xFFFFFFFF) & (refs >> 31 == 1)]
+    start, count = leaves & 0x7FFFFFF, ((leaves >> 27) & 15) + 1
+    assert count.sum() == sc.n_triangles
+    for s, c in zip(start[:5000], count[:5000]):
+        assert np.all(np.diff(o1[s:s + c]) > 0)
