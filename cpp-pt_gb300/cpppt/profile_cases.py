@@ -1,6 +1,7 @@
 """Small, fixed workloads for profiling single kernels (ncu -k ... -c 1..3).
 
-    python -m cpppt.profile_cases extend   # 1M-tri soup, 1280x720, 1 spp, depth 10 (plain PT+NEE+MIS)
+    python -m cpppt.profile_cases extend   # 1M-tri soup, 1280x720, 1 spp, depth 10 (plain PT+NEE+MIS),
+                                           # kernels launched one by one (ncu-visible)
     python -m cpppt.profile_cases raycounts  # extension rays of each bounce of that render
     python -m cpppt.profile_cases nn [R]   # 200k-tri slit room, 640x360, learned guide: R renders of 4 spp
     python -m cpppt.profile_cases slit [R] # the same renders with plain PT (PT_FLAG_UNBIASED_MIS)
@@ -22,13 +23,18 @@ import sys
 import time
 
 from . import scenes
-from .lib import FLAG_NN_FREEZE, FLAG_UNBIASED_MIS, MODE_MIS, MODE_NN, GpuBatch, GpuScene
+from .lib import FLAG_NN_FREEZE, FLAG_TIME_KERNELS, FLAG_UNBIASED_MIS, MODE_MIS, MODE_NN, GpuBatch, GpuScene
 
 
 def case_extend():
+    """Renders with PT_FLAG_TIME_KERNELS: the same kernels launched one by one
+    (16 iterations per round) instead of inside the device-driven graph,
+    whose kernel nodes ncu cannot capture (a graph with a conditional node);
+    each render here takes one round, so the second render's extension
+    launches start at launch 16."""
     gs = GpuScene(scenes.soup(seed=2, width=1280, height=720))
     for _ in range(2):
-        gs.render(1, max_depth=10, seed=1, mode=MODE_MIS)
+        gs.render(1, max_depth=10, seed=1, mode=MODE_MIS, flags=FLAG_TIME_KERNELS)
     return gs.stats()
 
 
