@@ -24,6 +24,13 @@ namespace cpppt_gb300 {
 #ifndef CPPPT_SMEM_NODES
 #define CPPPT_SMEM_NODES 2048
 #endif
+// Child slab distances two children at a time with the packed f32x2 adds
+// and FMAs of sm_100 and later (1) or one at a time (0); same results
+// (bit-identical images).  Measured on the 1M-triangle soup at 1080p, 64 spp:
+// 280.8 against 277.5 Mpaths/s (closest-hit kernel -0.9 %, shadow -2.4 %).
+#ifndef CPPPT_TRACE_F32X2
+#define CPPPT_TRACE_F32X2 1
+#endif
 constexpr int kTraceThreads = CPPPT_TRACE_THREADS;
 constexpr int kTraceBlocksPerSM = CPPPT_TRACE_BLOCKS_PER_SM;
 constexpr int kSmemNodes = CPPPT_SMEM_NODES;
@@ -122,6 +129,34 @@ __device__ __forceinline__ bool ref_box_exact(float4 lo, float4 hi, float3 o, fl
 // subtraction removes 2^23 (keeps the integer pipe free for the min/max)
 __device__ __forceinline__ float byte_to_float(uint32_t w, int c) {
     return __uint_as_float(__byte_perm(w, 0x4b000000u, 0x7540u | (uint32_t)c)) - 8388608.0f;
+}
+
+// Packed pairs of floats (two children per instruction on sm_100 and later:
+// add.f32x2 / fma.f32x2 round each half exactly as add.f32 / fma.rn.f32).
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 pk2(float a, float b) {
+    f32x2 d;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(a), "f"(b));
+    return d;
+}
+__device__ __forceinline__ void upk2(f32x2 v, float& a, float& b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
+    f32x2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+// slab distances of byte children c and c + 1 of w: q B + A, with q exact
+__device__ __forceinline__ void slab2(uint32_t w, int c, f32x2 B2, f32x2 A2, float& t0, float& t1) {
+    const f32x2 q = pk2(__uint_as_float(__byte_perm(w, 0x4b000000u, 0x7540u | (uint32_t)c)),
+                        __uint_as_float(__byte_perm(w, 0x4b000000u, 0x7540u | (uint32_t)(c + 1))));
+    upk2(fma2(add2(q, pk2(-8388608.0f, -8388608.0f)), B2, A2), t0, t1);
 }
 
 // three-operand min / max (one instruction on sm_100 and later)
@@ -251,6 +286,28 @@ __device__ __forceinline__ void trav_node(Trav& T, TravStack& K, const DevScene&
     const uint32_t ny = nys ? w2.x : w1.y, fy = nys ? w1.y : w2.x;
     const uint32_t nz = nzs ? w2.y : w1.z, fz = nzs ? w1.z : w2.y;
     uint32_t key[4];
+#if CPPPT_TRACE_F32X2
+    // children in pairs: the same roundings as the scalar form below
+    const f32x2 BX = pk2(bx, bx), BY = pk2(by, by), BZ = pk2(bz, bz);
+    const f32x2 AX = pk2(ax, ax), AY = pk2(ay, ay), AZ = pk2(az, az);
+#pragma unroll
+    for (int c = 0; c < 4; c += 2) {
+        float tnx[2], tny[2], tnz[2], tfx[2], tfy[2], tfz[2];
+        slab2(nx, c, BX, AX, tnx[0], tnx[1]);
+        slab2(ny, c, BY, AY, tny[0], tny[1]);
+        slab2(nz, c, BZ, AZ, tnz[0], tnz[1]);
+        slab2(fx, c, BX, AX, tfx[0], tfx[1]);
+        slab2(fy, c, BY, AY, tfy[0], tfy[1]);
+        slab2(fz, c, BZ, AZ, tfz[0], tfz[1]);
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const float tn = fmax3(tnx[h], tny[h], fmaxf(tnz[h], 0.0f));
+            const float tf = fmin3(tfx[h], tfy[h], fminf(tfz[h], cull));
+            const bool hit = tn <= tf * 1.0000005f;
+            key[c + h] = hit ? ((__float_as_uint(tn) & ~3u) | (uint32_t)(c + h)) : 0xffffffffu;
+        }
+    }
+#else
 #pragma unroll
     for (int c = 0; c < 4; c++) {
         const float tnx = fmaf(byte_to_float(nx, c), bx, ax);
@@ -264,6 +321,7 @@ __device__ __forceinline__ void trav_node(Trav& T, TravStack& K, const DevScene&
         const bool hit = tn <= tf * 1.0000005f;
         key[c] = hit ? ((__float_as_uint(tn) & ~3u) | (uint32_t)c) : 0xffffffffu;
     }
+#endif
     const uint32_t refs[4] = {w2.z, w2.w, w3.x, w3.y};
 #define CSWAP(a, b) { uint32_t lo_ = min(key[a], key[b]), hi_ = max(key[a], key[b]); key[a] = lo_; key[b] = hi_; }
     CSWAP(0, 1) CSWAP(2, 3) CSWAP(0, 2) CSWAP(1, 3) CSWAP(1, 2)
