@@ -39,6 +39,19 @@ namespace cpppt_gb300 {
 #ifndef CPPPT_ANY_UNSORTED
 #define CPPPT_ANY_UNSORTED 1
 #endif
+// Closest-hit queries: the nearest child next and the others pushed in slot
+// order (1), or all pushed far to near after a full sort (0).  Measured as
+// above: closest-hit kernel 258.0 -> 250.3 ms, 286.9 -> 291.8 Mpaths/s,
+// bit-identical images (culling compares each popped entry with the best
+// hit, so the push order changes the work, never the answer).
+#ifndef CPPPT_CLOSEST_PARTIAL
+#define CPPPT_CLOSEST_PARTIAL 1
+#endif
+// Any-hit queries keep no entry distances (an occlusion query never culls
+// below its own max_t, so the distances are not needed) (1), or keep them (0).
+#ifndef CPPPT_ANY_LEAN
+#define CPPPT_ANY_LEAN 0
+#endif
 constexpr int kTraceThreads = CPPPT_TRACE_THREADS;
 constexpr int kTraceBlocksPerSM = CPPPT_TRACE_BLOCKS_PER_SM;
 constexpr int kSmemNodes = CPPPT_SMEM_NODES;
@@ -312,7 +325,8 @@ __device__ __forceinline__ void trav_node(Trav& T, TravStack& K, const DevScene&
             const float tn = fmax3(tnx[h], tny[h], fmaxf(tnz[h], 0.0f));
             const float tf = fmin3(tfx[h], tfy[h], fminf(tfz[h], cull));
             const bool hit = tn <= tf * 1.0000005f;
-            key[c + h] = hit ? ((__float_as_uint(tn) & ~3u) | (uint32_t)(c + h)) : 0xffffffffu;
+            if (ANY && CPPPT_ANY_LEAN) key[c + h] = hit ? 0u : 0xffffffffu;
+            else key[c + h] = hit ? ((__float_as_uint(tn) & ~3u) | (uint32_t)(c + h)) : 0xffffffffu;
         }
     }
 #else
@@ -352,6 +366,25 @@ __device__ __forceinline__ void trav_node(Trav& T, TravStack& K, const DevScene&
         }
         T.cur = nxt;
         T.cur_t = __uint_as_float(nxt_t);
+        return;
+    }
+#endif
+#if CPPPT_CLOSEST_PARTIAL
+    if (!ANY) {  // nearest child next, the others pushed in slot order
+        const uint32_t m = min(min(key[0], key[1]), min(key[2], key[3]));
+        if (m == 0xffffffffu) {
+            trav_pop(T, K);
+            return;
+        }
+        if (T.sp + 3 > S.stack_limit) {
+            trav_abort(T, status, kStatusStackOverflow);
+            return;
+        }
+#pragma unroll
+        for (int c = 3; c >= 0; c--)
+            if (key[c] != 0xffffffffu && key[c] != m) K.e[T.sp++] = make_uint2(refs[c], key[c] & ~3u);
+        T.cur = refs[m & 3u];
+        T.cur_t = __uint_as_float(m & ~3u);
         return;
     }
 #endif
