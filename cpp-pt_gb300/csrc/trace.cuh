@@ -49,8 +49,9 @@ namespace cpppt_gb300 {
 #endif
 // Any-hit queries keep no entry distances (an occlusion query never culls
 // below its own max_t, so the distances are not needed) (1), or keep them (0).
+// Measured as above: shadow kernel 137.4 -> 136.4 ms.
 #ifndef CPPPT_ANY_LEAN
-#define CPPPT_ANY_LEAN 0
+#define CPPPT_ANY_LEAN 1
 #endif
 constexpr int kTraceThreads = CPPPT_TRACE_THREADS;
 constexpr int kTraceBlocksPerSM = CPPPT_TRACE_BLOCKS_PER_SM;
