@@ -453,17 +453,32 @@ __device__ __forceinline__ bool trav_leaf(Trav& T, const DevScene& S, TraceCount
 // Every iteration has a node phase and a leaf phase (leaves are postponed
 // as in Aila and Laine 2009, "Understanding the efficiency of ray traversal
 // on GPUs"): a lane that reaches a leaf parks it and keeps descending inner
-// nodes; the node phase repeats until a quarter of the warp's active lanes
+// nodes; the node phase repeats until a third of the warp's active lanes
 // cannot continue without their leaf, or no lane has an inner node left,
 // and then the lanes with a parked leaf test its triangles together.
 // Inner-node and triangle code run with most lanes converged instead of
-// alternating per lane.  Measured on the 1M-triangle soup: the quarter
-// threshold 238.7 Mpaths/s against 232.5 at one half, 232.0 at one eighth
-// and 215 at any waiting lane; repeating the node phase instead of one node
-// step per iteration 247 against 237.  The result does not depend on the visiting order: the closest
+// alternating per lane.  Measured on the 1M-triangle soup with an earlier
+// node phase: a quarter 238.7 Mpaths/s against 232.5 at one half, 232.0 at
+// one eighth and 215 at any waiting lane; repeating the node phase instead
+// of one node step per iteration 247 against 237 (the current figures are
+// below).  The result does not depend on the visiting order: the closest
 // hit is the minimum over the tested triangles of (t, -rank), and a node is
 // culled only when its entry distance lies behind the best hit found so far.
-constexpr int kChunk = 64;
+// Rays a warp takes from the global counter at a time, and the leaf-phase
+// trigger (a leaf phase once 1/CPPPT_LEAF_WAIT_DIV of the active lanes wait
+// on a parked leaf).  Measured on the 1M-triangle soup at 1080p, 64 spp, with
+// the node phase above: chunk 64 / quarter 292.5 Mpaths/s, chunk 128 277.0,
+// chunk 32 300.9, chunk 16 302.0; with a third: chunk 64 294.6, chunk 32
+// 302.8, chunk 16 303.1; with a sixth (chunk 64) 287.7.  Smaller chunks
+// balance the lanes' and warps' uneven ray lengths better, above all at
+// the end of a launch.
+#ifndef CPPPT_RAY_CHUNK
+#define CPPPT_RAY_CHUNK 16
+#endif
+#ifndef CPPPT_LEAF_WAIT_DIV
+#define CPPPT_LEAF_WAIT_DIV 3
+#endif
+constexpr int kChunk = CPPPT_RAY_CHUNK;
 
 template <bool ANY, bool COUNT, class Load, class Store>
 __device__ __forceinline__ void persistent_trace(const DevScene& S, const uint4* __restrict__ snodes, int n,
@@ -518,7 +533,7 @@ __device__ __forceinline__ void persistent_trace(const DevScene& S, const uint4*
             const bool waiting = active && T.leaf != kTravDone && !is_inner(T.cur);
             wait = __ballot_sync(0xffffffffu, waiting);
             inner = __ballot_sync(0xffffffffu, active && is_inner(T.cur));
-        } while (inner != 0 && 4 * __popc(wait) < __popc(act));
+        } while (inner != 0 && CPPPT_LEAF_WAIT_DIV * __popc(wait) < __popc(act));
         // leaf phase (the node phase ended because enough lanes wait or none can descend)
         if (active && T.leaf != kTravDone) {
             ++T.steps;
