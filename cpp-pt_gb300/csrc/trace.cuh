@@ -8,13 +8,15 @@ namespace cpppt_gb300 {
 // Launch shape of the traversal kernels (threads per CTA, resident CTAs per
 // SM; the grid is the latter times the SM count) and the number of top wide
 // nodes (breadth-first, so the top levels) each CTA stages in shared memory.
-// One CTA of 1024 threads per SM stages 2048 nodes (128 KB, the top five
-// levels and part of the sixth) once per SM instead of four 256-thread CTAs
-// staging 256 nodes each.  Measured on the 1M-triangle soup at 1080p (same
-// 64 registers, no spills): 256x4 with 256 nodes 273.0 Mpaths/s, 512 nodes
-// 273.4, 512x2 with 1024 nodes 275.2, 1024x1 with 2048 nodes 277.3, with
-// 3072 nodes 256.7 (L1 squeezed); 5 and 6 CTAs of 256 threads (48 and 40
-// registers, spilling) 264.9 and 234.5.
+// Measured on the 1M-triangle soup at 1080p, 64 spp.  With the earlier node
+// phase (full child sort, 64-ray chunks), staging paid: 256x4 with 256
+// nodes 273.0 Mpaths/s, 512x2 with 1024 nodes 275.2, 1024x1 with 2048
+// nodes 277.3, with 3072 nodes 256.7 (L1 squeezed); 5 and 6 CTAs of 256
+// threads (48 and 40 registers, spilling) 264.9 and 234.5.  With the
+// current node phase the whole L1 serves better: 1024x1 with 2048 nodes
+// 303.1, 1536 306.2, 1024 305.9, 512 308.8, 256 310.1, 128 310.6, none
+// 310.4-310.8; without staging 512x2 310.0 and 256x4 309.4.  So no nodes
+// are staged (the mechanism stays for other scenes and shapes).
 #ifndef CPPPT_TRACE_THREADS
 #define CPPPT_TRACE_THREADS 1024
 #endif
@@ -22,7 +24,7 @@ namespace cpppt_gb300 {
 #define CPPPT_TRACE_BLOCKS_PER_SM 1
 #endif
 #ifndef CPPPT_SMEM_NODES
-#define CPPPT_SMEM_NODES 2048
+#define CPPPT_SMEM_NODES 0
 #endif
 // Child slab distances two children at a time with the packed f32x2 adds
 // and FMAs of sm_100 and later (1) or one at a time (0); same results
