@@ -62,8 +62,8 @@ def _commands(extra_cuda: list[str] | None = None):
         cmd = [nvcc, "-c", src, "-o", out] + common
         if name.endswith(".cu"):
             cmd += ARCH + ["-lineinfo"] + (extra_cuda or [])
-        else:
-            cmd += ["-x", "c++"]
+        else:  # compile-time knobs (-D...) reach the host files too
+            cmd += ["-x", "c++"] + [f for f in (extra_cuda or []) if f.startswith("-D")]
         jobs.append((src, out, cmd))
     return nvcc, jobs
 

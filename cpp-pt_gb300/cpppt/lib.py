@@ -67,7 +67,7 @@ class PtRenderStats(C.Structure):
 class PtNNConfig(C.Structure):
     _fields_ = [("learning_rate", C.c_float), ("bsdf_frac_min", C.c_float), ("bsdf_frac_max", C.c_float),
                 ("batch", C.c_int32), ("divergence", C.c_int32), ("steps_per_round", C.c_int32),
-                ("encoding", C.c_int32)]
+                ("encoding", C.c_int32), ("passes", C.c_int32)]
 
 
 class PtBatchJob(C.Structure):
@@ -279,8 +279,9 @@ class GpuScene:
 
     def nn_configure(self, **kw):
         """Updates the learned guide's settings (learning_rate, bsdf_frac_min,
-        bsdf_frac_max, batch, divergence: NN_KL / NN_CHI2, steps_per_round,
-        encoding: NN_ENC_FREQ / NN_ENC_ONEBLOB);
+        bsdf_frac_max, batch, divergence: NN_KL / NN_CHI2, steps_per_round
+        (batches per round), encoding: NN_ENC_FREQ / NN_ENC_ONEBLOB, passes:
+        Adam steps per batch);
         returns the new settings."""
         c = PtNNConfig()
         _check(_lib.pt_nn_config_get(self.h, C.byref(c)))

@@ -64,7 +64,7 @@ struct pt_batch {
     int nnjobs_cap = 0;
     int* d_nrec = nullptr;  // one per member scene (in `owned`)
     int* h_nrec = nullptr;  // pinned
-    NNTrainTask* d_tasks = nullptr;  // fused training steps: kNNMaxStepsPerRound per member scene (in `owned`)
+    NNTrainTask* d_tasks = nullptr;  // fused training steps: kNNMaxStepsPerRound x kNNMaxPasses per member scene (in `owned`)
     NNTrainTask* h_tasks = nullptr;  // pinned
     cudaStream_t nn_tst = nullptr;       // training stream (overlaps the wavefront)
     cudaEvent_t nn_ev_records = nullptr;  // a round's records are complete
@@ -227,8 +227,8 @@ void create_batch(pt_scene* const* scenes, int n, pt_batch* b) {
     ck(cudaMallocHost(&b->h_ctr, sizeof(WaveCounters)), "cudaMallocHost");
     b->d_nrec = dalloc<int>(b->owned, n);
     ck(cudaMallocHost(&b->h_nrec, sizeof(int) * n), "cudaMallocHost");
-    b->d_tasks = dalloc<NNTrainTask>(b->owned, (size_t)n * kNNMaxStepsPerRound);
-    ck(cudaMallocHost(&b->h_tasks, sizeof(NNTrainTask) * n * kNNMaxStepsPerRound), "cudaMallocHost");
+    b->d_tasks = dalloc<NNTrainTask>(b->owned, (size_t)n * kNNMaxStepsPerRound * kNNMaxPasses);
+    ck(cudaMallocHost(&b->h_tasks, sizeof(NNTrainTask) * n * kNNMaxStepsPerRound * kNNMaxPasses), "cudaMallocHost");
     ck(cudaStreamCreateWithFlags(&b->nn_tst, cudaStreamNonBlocking), "cudaStreamCreate");
     ck(cudaEventCreateWithFlags(&b->nn_ev_records, cudaEventDisableTiming), "cudaEventCreate");
     ck(cudaEventCreate(&b->ev0), "cudaEventCreate");

@@ -286,7 +286,10 @@ void trace_host(pt_scene* s, const pt_ray* rays, int n, void* out, bool any) {
     check_status(s, status);
 }
 
-constexpr int kMaxCapacity = 1 << 21;
+#ifndef CPPPT_MAX_WAVE_LOG2
+#define CPPPT_MAX_WAVE_LOG2 21
+#endif
+constexpr int kMaxCapacity = 1 << CPPPT_MAX_WAVE_LOG2;
 constexpr int kItersPerGraph = 16;  // even: buffers alternate
 
 void ensure_wave(pt_scene* s, int capacity, int film_n) {
@@ -497,8 +500,9 @@ void nn_ensure(pt_scene* s) {
     s->nn_rec_count = 0;
     if (!s->h_rec_left) ck(cudaMallocHost(&s->h_rec_left, sizeof(int)), "cudaMallocHost");
     if (!s->h_scal) ck(cudaMallocHost(&s->h_scal, sizeof(float) * 4), "cudaMallocHost");
-    if (!s->h_tasks) ck(cudaMallocHost(&s->h_tasks, sizeof(NNTrainTask) * kNNMaxStepsPerRound), "cudaMallocHost");
-    s->d_tasks = dalloc<NNTrainTask>(s->nn_owned, kNNMaxStepsPerRound);
+    if (!s->h_tasks)
+        ck(cudaMallocHost(&s->h_tasks, sizeof(NNTrainTask) * kNNMaxStepsPerRound * kNNMaxPasses), "cudaMallocHost");
+    s->d_tasks = dalloc<NNTrainTask>(s->nn_owned, kNNMaxStepsPerRound * kNNMaxPasses);
     std::vector<float> w = nn_random_weights(12345u);
     nn_upload(s->nnw, w.data(), s->stream);
     ck(cudaStreamSynchronize(s->stream), "nn init");
@@ -553,7 +557,7 @@ void train_finish(NNTrainPending& P) {
         std::memcpy(&tstat, &s->h_scal[2], sizeof(tstat));
         check_status(s, tstat);
         s->nn_last_loss = s->h_scal[0];
-        s->nn_records += (double)P.steps[k] * s->nn_cfg.batch;
+        s->nn_records += (double)P.steps[k] * s->nn_cfg.batch;  // P.steps: batches trained on
     }
     P.sc.clear();
     P.steps.clear();
@@ -564,12 +568,14 @@ void train_enqueue(pt_scene* const* sc, const int* held, const int* caps, int* c
                    cudaEvent_t ev_records, double* launches, int* left, NNTrainPending& P) {
     train_finish(P);  // h_tasks, h_scal and the pinned counts are free again
     const NNAdam opt;
-    std::vector<int> steps(n, 0);
+    // steps[k] = full batches x passes; step j of scene k uses batch j / passes
+    std::vector<int> steps(n, 0), batches(n, 0);
     int max_steps = 0;
     for (int k = 0; k < n; k++) {
         left[k] = -1;
         if (!sc[k]) continue;
-        steps[k] = std::min(held[k], caps[k]) / sc[k]->nn_cfg.batch;
+        batches[k] = std::min(held[k], caps[k]) / sc[k]->nn_cfg.batch;
+        steps[k] = batches[k] * sc[k]->nn_cfg.passes;
         max_steps = std::max(max_steps, steps[k]);
     }
     if (max_steps == 0) return;
@@ -586,8 +592,10 @@ void train_enqueue(pt_scene* const* sc, const int* held, const int* caps, int* c
             T = NNTrainTask{};
             T.W = s->nnw;
             T.N = scene_norm(s);
-            T.rec = s->nn_rec + (size_t)4 * j * s->nn_cfg.batch;
+            const int passes = s->nn_cfg.passes;
+            T.rec = s->nn_rec + (size_t)4 * (j / passes) * s->nn_cfg.batch;
             T.n = s->nn_cfg.batch;
+            T.prep = j % passes == 0 ? 1 : 0;  // later passes reuse the batch's prepared T and its sum
             T.chi2 = s->nn_cfg.divergence == PT_NN_CHI2 ? 1 : 0;
             T.scal = s->nn_scalars;
             T.TB = s->nn_tb;
@@ -620,10 +628,10 @@ void train_enqueue(pt_scene* const* sc, const int* held, const int* caps, int* c
         // the render stream continues in the other buffer once the training
         // that last read it has finished; the records after the last full
         // batch go to its front (this round's training does not read them)
-        const int kept = std::min(held[k], caps[k]) - steps[k] * batch;
+        const int kept = std::min(held[k], caps[k]) - batches[k] * batch;
         ck(cudaStreamWaitEvent(st, s->nn_read_done[nxt], 0), "wait training");
         if (kept > 0)
-            ck(cudaMemcpyAsync(s->nn_rec_buf[nxt], s->nn_rec_buf[cur] + (size_t)4 * steps[k] * batch,
+            ck(cudaMemcpyAsync(s->nn_rec_buf[nxt], s->nn_rec_buf[cur] + (size_t)4 * batches[k] * batch,
                                sizeof(float4) * 4 * kept, cudaMemcpyDeviceToDevice, st), "keep records");
         *s->h_rec_left = kept;
         ck(cudaMemcpyAsync(d_count[k], s->h_rec_left, sizeof(int), cudaMemcpyHostToDevice, st), "records");
@@ -632,7 +640,7 @@ void train_enqueue(pt_scene* const* sc, const int* held, const int* caps, int* c
         s->nn_steps += steps[k];
         left[k] = kept;
         P.sc.push_back(s);
-        P.steps.push_back(steps[k]);
+        P.steps.push_back(batches[k]);
     }
 }
 
@@ -1210,6 +1218,10 @@ pt_status pt_nn_configure(pt_scene* s, const pt_nn_config* c) {
         g_error = "encoding must be PT_NN_ENC_FREQ or PT_NN_ENC_ONEBLOB";
         return PT_ERR_INVALID;
     }
+    if (c->passes < 1 || c->passes > kNNMaxPasses) {
+        g_error = "passes must be in [1, 8]";
+        return PT_ERR_INVALID;
+    }
     s->nn_cfg = *c;
     s->nn_rec_count = 0;  // records of the previous batch size are dropped
     return PT_OK;
@@ -1397,6 +1409,7 @@ void nn_grad_debug(const float* weights, const float* lo, const float* hi, const
     task.rec = drec;
     task.n = n;
     task.chi2 = divergence == PT_NN_CHI2 ? 1 : 0;
+    task.prep = 1;
     task.scal = scal;
     task.TB = TB;
     task.grad = grad;

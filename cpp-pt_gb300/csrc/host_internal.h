@@ -185,7 +185,7 @@ struct pt_scene {
     float4* nn_params = nullptr;
     int nnpd_cap = 0, nnpd_depth = 0;
     std::vector<void*> nnpd_owned;
-    pt_nn_config nn_cfg{3e-3f, 0.3f, 0.9f, 1 << 16, PT_NN_CHI2, 16, PT_NN_ENC_FREQ};
+    pt_nn_config nn_cfg{3e-3f, 0.3f, 0.9f, 1 << 16, PT_NN_CHI2, 16, PT_NN_ENC_FREQ, 1};
 
     ~pt_scene() {
         for (void* p : nn_owned) cudaFree(p);

@@ -627,13 +627,14 @@ __global__ void k_nn_task_zero(const NNTrainTask* __restrict__ tasks, int prep) 
     if (i < kNNWeights) task.grad[i] = 0.f;
     if (i == 0) {
         task.scal[0] = 0.f;
-        if (prep) task.scal[1] = 0.f;
+        if (prep && task.prep) task.scal[1] = 0.f;
     }
 }
 
 // Chi-square targets (T squared in place) and the sum of T of each task.
 __global__ void k_nn_task_T(const NNTrainTask* __restrict__ tasks) {
     const NNTrainTask& task = tasks[blockIdx.y];
+    if (!task.prep) return;  // a later pass over a batch already prepared
     float4* __restrict__ rec = task.rec;
     float s = 0.f;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < task.n; i += gridDim.x * blockDim.x) {

@@ -30,7 +30,8 @@ struct NNTrainBuf {
 
 constexpr int kNNVertFloat4 = 7;  // float4 per recorded path vertex
 constexpr int kNNMixF4 = 8;       // float4 per path of the packed mixture (inference -> shading)
-constexpr int kNNMaxStepsPerRound = 64;  // Adam steps of one network between two wavefront checks
+constexpr int kNNMaxStepsPerRound = 64;  // batches of one network between two wavefront checks
+constexpr int kNNMaxPasses = 8;          // Adam steps per batch
 
 // Per-path state of the learned-guide integrator (slot = path's free-list entry).
 struct NNPathData {
@@ -82,6 +83,7 @@ struct NNTrainTask {
     float4* rec;  // this step's records (T squared in place for chi-square)
     int32_t n;
     int32_t chi2;
+    int32_t prep;  // with the launch's prep: square T (chi-square) and sum it; 0: a later pass over the same batch
     float* scal;  // [0] batch loss, [1] sum of T, [2] status bits (kStatusTensorTimeout; accumulate)
     NNTrainBuf TB;
     float* grad;  // kNNWeights floats: dL/dW of this step

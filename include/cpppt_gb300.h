@@ -313,9 +313,11 @@ typedef struct pt_nn_config {
     float bsdf_frac_max;
     int32_t batch;
     int32_t divergence;
-    int32_t steps_per_round; /* Adam steps at most per wavefront round (16 iterations), 1..64 */
+    int32_t steps_per_round; /* batches at most per wavefront round (16 iterations), 1..64 */
     int32_t encoding;        /* PT_NN_ENC_FREQ (default) or PT_NN_ENC_ONEBLOB; reset the weights
                                 (pt_nn_reset) after changing it */
+    int32_t passes;          /* Adam steps taken on each batch of records, 1..8 (default 1);
+                                steps_per_round counts batches */
 } pt_nn_config;
 /* Input encodings of the learned guide (64 inputs, the last constant 1):
  * FREQ: sin / cos of the position normalised to the scene box at 8

@@ -175,13 +175,31 @@ def test_guide_settings_are_checked(gpu_lib):
     cfg = gs.nn_config()
     assert cfg["batch"] == 65536 and cfg["steps_per_round"] == 16 and cfg["divergence"] == NN_CHI2
     assert abs(cfg["learning_rate"] - 3e-3) < 1e-9 and abs(cfg["bsdf_frac_min"] - 0.3) < 1e-7
-    assert cfg["encoding"] == NN_ENC_FREQ
+    assert cfg["encoding"] == NN_ENC_FREQ and cfg["passes"] == 1
     assert gs.nn_configure(steps_per_round=64, batch=1024)["steps_per_round"] == 64
     assert gs.nn_configure(encoding=NN_ENC_ONEBLOB)["encoding"] == NN_ENC_ONEBLOB
+    assert gs.nn_configure(passes=8)["passes"] == 8
     gs.nn_configure(**cfg)
     for bad in (dict(steps_per_round=65), dict(steps_per_round=0), dict(batch=1023), dict(batch=262145),
                 dict(bsdf_frac_min=0.05), dict(bsdf_frac_min=0.9, bsdf_frac_max=0.8), dict(learning_rate=0.0),
-                dict(divergence=2), dict(encoding=2), dict(encoding=-1)):
+                dict(divergence=2), dict(encoding=2), dict(encoding=-1), dict(passes=0), dict(passes=9)):
         with pytest.raises(PtError):
             gs.nn_configure(**bad)
         assert gs.nn_config() == cfg
+
+
+def test_passes_take_several_steps_per_batch(gpu_lib):
+    """passes = 3: every batch of records is used for three Adam steps (the
+    chi-square targets prepared once), so the step count is three times the
+    batches trained on, and the guided image stays finite and lit."""
+    from cpppt import scenes
+    from cpppt.lib import MODE_NN, GpuScene
+    gs = GpuScene(scenes.slit_room(seed=4, n_boxes=60, box_subdiv=2, width=64, height=32))
+    gs.nn_configure(batch=1024, passes=3, steps_per_round=8)
+    for k in range(4):
+        img = gs.render(64, max_depth=12, seed=500 + k, mode=MODE_NN)
+    st = gs.nn_stats()
+    batches = st["records"] / 1024
+    assert batches >= 4 and batches == int(batches), st
+    assert st["steps"] == 3 * batches, st
+    assert np.isfinite(img).all() and img.mean() > 0
