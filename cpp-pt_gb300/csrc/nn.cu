@@ -200,8 +200,10 @@ __device__ __forceinline__ void tc_infer_loop(int n, unsigned char* smem, const 
             float v[64];
             const f3 pn = mk((in.pn.x - nj.lo[0]) * nj.inv_ext[0], (in.pn.y - nj.lo[1]) * nj.inv_ext[1],
                              (in.pn.z - nj.lo[2]) * nj.inv_ext[2]);
+            nn_features(v, pn, in.n, in.wo, nj.encoding);
+            if (!mine)
 #pragma unroll
-            for (int k = 0; k < 64; k++) v[k] = mine ? nn_feature(k, pn, in.n, in.wo, nj.encoding) : 0.f;
+                for (int k = 0; k < 64; k++) v[k] = 0.f;
             tc_store_row(s_a, row, v, false);
             for (int l = 0; l < kNNLayers; l++) {
                 const int nout = nn_layer_out(l);
@@ -409,8 +411,10 @@ __global__ void __launch_bounds__(kTcRows) k_nn_train_fb(const NNTrainTask* __re
             T = r3.y * inv_tsum;
         }
         float v[64];
+        nn_features(v, in.pn, in.n, in.wo, N.encoding);
+        if (!valid)
 #pragma unroll
-        for (int j = 0; j < 64; j++) v[j] = valid ? nn_feature(j, in.pn, in.n, in.wo, N.encoding) : 0.f;
+            for (int j = 0; j < 64; j++) v[j] = 0.f;
         tc_store_row(s_a, row, v, false);
         if (valid) store_row_bf16(TB.act + (size_t)i * 64, v, 64, false);
         for (int l = 0; l < kNNLayers; l++) {

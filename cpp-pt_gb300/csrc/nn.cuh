@@ -90,6 +90,30 @@ __device__ __forceinline__ float nn_feature(int j, f3 pn, f3 n, f3 wo, int encod
     }
 }
 
+// All 64 input features of a sample under encoding (the values of
+// nn_feature, with the branch on the encoding taken once and the one-blob
+// angles computed once per sample).
+#ifndef CPPPT_NN_ONEBLOB
+#define CPPPT_NN_ONEBLOB 1
+#endif
+__device__ __forceinline__ void nn_features(float v[64], f3 pn, f3 n, f3 wo, int encoding) {
+    if (CPPPT_NN_ONEBLOB && encoding == 1) {
+#pragma unroll
+        for (int j = 0; j < 36; j++) v[j] = nn_feature_oneblob(j, pn, n, wo);
+        const float s4[4] = {0.5f * (n.z + 1.0f), atan2f(n.y, n.x) * (0.5f * kInvPi) + 0.5f, 0.5f * (wo.z + 1.0f),
+                             atan2f(wo.y, wo.x) * (0.5f * kInvPi) + 0.5f};
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+#pragma unroll
+            for (int b = 0; b < kNNBlobBins; b++) v[36 + q * kNNBlobBins + b] = one_blob(s4[q], b, (q & 1) != 0);
+#pragma unroll
+        for (int j = 36 + 4 * kNNBlobBins; j < 64; j++) v[j] = j == 36 + 4 * kNNBlobBins ? 1.0f : 0.0f;
+    } else {
+#pragma unroll
+        for (int j = 0; j < 64; j++) v[j] = nn_feature(j, pn, n, wo, 0);
+    }
+}
+
 __device__ __forceinline__ float softplusf(float x) { return x > 15.f ? x : log1pf(__expf(x)); }
 
 // vMF lobe pdf over the sphere: kappa / (2 pi (1 - e^{-2 kappa})) e^{kappa (mu.w - 1)}
