@@ -470,6 +470,7 @@ void render_batch_slot(pt_batch* b, const pt_batch_job* jobs, int n_jobs, float*
         ck(cudaMallocHost(&b->h_nnjobs, sizeof(DevNNJob) * n_jobs), "cudaMallocHost guide jobs");
         b->nnjobs_cap = n_jobs;
     }
+    bool oneblob = false;  // some guide of the batch uses the one-blob encoding
     for (int i = 0; i < n_jobs; i++) {
         const int m = jobs[i].scene;
         DevNNJob& nj = b->h_nnjobs[i];
@@ -486,6 +487,7 @@ void render_batch_slot(pt_batch* b, const pt_batch_job* jobs, int n_jobs, float*
         nj.c_lo = N.c_lo;
         nj.c_hi = N.c_hi;
         nj.encoding = N.encoding;
+        oneblob = oneblob || N.encoding == PT_NN_ENC_ONEBLOB;
         nj.rec = train ? s->nn_rec : nullptr;
         nj.rec_cap = cap[m];
     }
@@ -524,7 +526,8 @@ void render_batch_slot(pt_batch* b, const pt_batch_job* jobs, int n_jobs, float*
         for (int k = 0; k < t.iters_per_graph; k++) {
             const int cur = k & 1;
             launch_extend(b->arena, b->pb, cur, b->d_ctr, b->num_sms, st);
-            if (guided) launch_nn_infer(b->arena, b->pb, cur, b->d_ctr, b->d_nnjobs, b->nn_params, b->num_sms, st);
+            if (guided)
+                launch_nn_infer(b->arena, b->pb, cur, b->d_ctr, b->d_nnjobs, b->nn_params, b->num_sms, st, oneblob);
             launch_nn_shade(b->arena, b->pb, cur, P, b->d_ctr, b->film, b->nn_params, PD, guided, b->d_jobs, st);
             launch_nn_shadow(b->arena, b->pb, b->d_ctr, b->film, PD, b->d_jobs, b->num_sms, st);
             launch_nn_finish(PD, b->d_ctr, b->d_nnjobs, max_depth, capacity, st);

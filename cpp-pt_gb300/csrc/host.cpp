@@ -290,6 +290,11 @@ void trace_host(pt_scene* s, const pt_ray* rays, int n, void* out, bool any) {
 #define CPPPT_MAX_WAVE_LOG2 21
 #endif
 constexpr int kMaxCapacity = 1 << CPPPT_MAX_WAVE_LOG2;
+// paths in flight of the learned-guide (slot) wavefront, each with a vertex
+// record per bounce for training
+#ifndef CPPPT_NN_WAVE_LOG2
+#define CPPPT_NN_WAVE_LOG2 20
+#endif
 constexpr int kItersPerGraph = 16;  // even: buffers alternate
 
 void ensure_wave(pt_scene* s, int capacity, int film_n) {
@@ -614,8 +619,10 @@ void train_enqueue(pt_scene* const* sc, const int* held, const int* caps, int* c
     ck(cudaMemcpyAsync(d_tasks, h_tasks, sizeof(NNTrainTask) * t, cudaMemcpyHostToDevice, tst), "training tasks");
     for (int k = 0; k < n; k++)
         if (steps[k] > 0) ck(cudaMemsetAsync(sc[k]->nn_scalars + 2, 0, sizeof(float), tst), "memset status");
+    bool oneblob = false;
+    for (int k = 0; k < n; k++) oneblob = oneblob || (sc[k] && sc[k]->nn_cfg.encoding == PT_NN_ENC_ONEBLOB);
     for (int j = 0; j < max_steps; j++) {
-        launch_nn_train_tasks(d_tasks + off[j], off[j + 1] - off[j], max_n[j], num_sms, tst, true, true);
+        launch_nn_train_tasks(d_tasks + off[j], off[j + 1] - off[j], max_n[j], num_sms, tst, true, true, oneblob);
         if (launches) *launches += 5;
     }
     P.tst = tst;
@@ -663,7 +670,7 @@ void render_nn(pt_scene* s, const pt_render_desc* desc, float* d_dst, bool guide
     P.height = s->height;
     P.flags = desc->flags;
     const unsigned long long total = (unsigned long long)s->width * s->height * (unsigned long long)desc->spp;
-    const int capacity = (int)std::min<unsigned long long>(1 << 20, (total + 1023) / 1024 * 1024);
+    const int capacity = (int)std::min<unsigned long long>(1 << CPPPT_NN_WAVE_LOG2, (total + 1023) / 1024 * 1024);
     const int film_n = 3 * s->width * s->height;
     ensure_wave(s, capacity, film_n);
     NNPathData PD = nn_path_buffers(s, capacity, train ? P.max_depth : 0);
@@ -707,7 +714,9 @@ void render_nn(pt_scene* s, const pt_render_desc* desc, float* d_dst, bool guide
         for (int k = 0; k < kItersPerGraph; k++) {
             const int cur = k & 1;
             launch_extend(s->dev, s->pb, cur, s->d_ctr, s->num_sms, st);
-            if (guided) launch_nn_infer(s->dev, s->pb, cur, s->d_ctr, s->d_nnjob, params, s->num_sms, st);
+            if (guided)
+                launch_nn_infer(s->dev, s->pb, cur, s->d_ctr, s->d_nnjob, params, s->num_sms, st,
+                                s->nn_cfg.encoding == PT_NN_ENC_ONEBLOB);
             launch_nn_shade(s->dev, s->pb, cur, P, s->d_ctr, s->film, params, PD, guided, s->d_job, st);
             launch_nn_shadow(s->dev, s->pb, s->d_ctr, s->film, PD, s->d_job, s->num_sms, st);
             launch_nn_finish(PD, s->d_ctr, s->d_nnjob, P.max_depth, capacity, st);
@@ -1297,7 +1306,7 @@ pt_status pt_debug_nn_forward_ex(const float* weights, const float* lo, const fl
         hj.encoding = encoding;
         DevNNJob* dj = dalloc<DevNNJob>(c.owned, 1);
         ck(cudaMemcpyAsync(dj, &hj, sizeof(hj), cudaMemcpyHostToDevice, c.st), "copy");
-        launch_nn_forward_debug(dj, din, n, dout, dstat, c.sms, c.st);
+        launch_nn_forward_debug(dj, din, n, dout, dstat, c.sms, c.st, encoding == PT_NN_ENC_ONEBLOB);
         ck(cudaMemcpyAsync(out, dout, sizeof(float) * 41 * n, cudaMemcpyDeviceToHost, c.st), "copy");
         uint32_t hstat = 0;
         ck(cudaMemcpyAsync(&hstat, dstat, sizeof(uint32_t), cudaMemcpyDeviceToHost, c.st), "copy");
@@ -1415,7 +1424,7 @@ void nn_grad_debug(const float* weights, const float* lo, const float* hi, const
     task.grad = grad;
     NNTrainTask* dtask = dalloc<NNTrainTask>(c.owned, 1);
     ck(cudaMemcpyAsync(dtask, &task, sizeof(task), cudaMemcpyHostToDevice, c.st), "copy");
-    launch_nn_train_tasks(dtask, 1, n, c.sms, c.st, prep, false);
+    launch_nn_train_tasks(dtask, 1, n, c.sms, c.st, prep, false, encoding == PT_NN_ENC_ONEBLOB);
     ck(cudaMemcpyAsync(out_grad, grad, sizeof(float) * kNNWeightCount, cudaMemcpyDeviceToHost, c.st), "copy");
     float sc[4] = {0.f, 0.f, 0.f, 0.f};
     ck(cudaMemcpyAsync(sc, scal, sizeof(sc), cudaMemcpyDeviceToHost, c.st), "copy");

@@ -160,7 +160,7 @@ __device__ __forceinline__ void tc_stage_wt(const __nv_bfloat16* wt, unsigned ch
 // threads of the CTA must call it.  status: kStatusTensorTimeout when a
 // completion wait runs out (the CTA then stops, frees its tensor memory and
 // returns).
-template <class GetIn, class Put>
+template <bool ONEBLOB, class GetIn, class Put>
 __device__ __forceinline__ void tc_infer_loop(int n, unsigned char* smem, const DevNNJob* __restrict__ nnj,
                                               uint32_t* status, GetIn get_in, Put put) {
     unsigned char* s_w = smem;
@@ -200,7 +200,7 @@ __device__ __forceinline__ void tc_infer_loop(int n, unsigned char* smem, const 
             float v[64];
             const f3 pn = mk((in.pn.x - nj.lo[0]) * nj.inv_ext[0], (in.pn.y - nj.lo[1]) * nj.inv_ext[1],
                              (in.pn.z - nj.lo[2]) * nj.inv_ext[2]);
-            nn_features(v, pn, in.n, in.wo, nj.encoding);
+            nn_features<ONEBLOB>(v, pn, in.n, in.wo, nj.encoding);
             if (!mine)
 #pragma unroll
                 for (int k = 0; k < 64; k++) v[k] = 0.f;
@@ -225,11 +225,12 @@ __device__ __forceinline__ void tc_infer_loop(int n, unsigned char* smem, const 
     tc_end(ok, tmem, bar, phase, status);
 }
 
+template <bool ONEBLOB>
 __global__ void __launch_bounds__(kTcInferThreads) k_nn_forward_debug(const DevNNJob* __restrict__ nnj,
                                                                       const float* __restrict__ in, int n,
                                                                       float* __restrict__ out, uint32_t* status) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    tc_infer_loop(
+    tc_infer_loop<ONEBLOB>(
         n, smem, nnj, status,
         [&](int i, NNIn& v, int& job) {
             const float* p = in + 9 * (size_t)i;
@@ -246,13 +247,14 @@ __global__ void __launch_bounds__(kTcInferThreads) k_nn_forward_debug(const DevN
 
 // Guide parameters for every live path's hit (run between extend and shade),
 // each path with its job's network.
+template <bool ONEBLOB>
 __global__ void __launch_bounds__(kTcInferThreads) k_nn_infer(DevScene S, PathBuffers B, int cur, WaveCounters* ctr,
                                                               const DevNNJob* __restrict__ nnj,
                                                               float4* __restrict__ params) {
     extern __shared__ __align__(1024) unsigned char smem[];
     const int n = ctr->n_cur;
     if (n == 0) return;
-    tc_infer_loop(
+    tc_infer_loop<ONEBLOB>(
         n, smem, nnj, &ctr->status,
         [&](int i, NNIn& v, int& job) {
             const float4 H = B.hit[i];
@@ -366,6 +368,7 @@ __device__ __forceinline__ void store_row_bf16(__nv_bfloat16* dst, const float* 
 constexpr int kNNThreads = 128;
 
 // blockIdx.y: the network (task) of a fused multi-network step.
+template <bool ONEBLOB>
 __global__ void __launch_bounds__(kTcRows) k_nn_train_fb(const NNTrainTask* __restrict__ tasks) {
     extern __shared__ __align__(1024) unsigned char smem[];
     const NNTrainTask& task = tasks[blockIdx.y];
@@ -411,7 +414,7 @@ __global__ void __launch_bounds__(kTcRows) k_nn_train_fb(const NNTrainTask* __re
             T = r3.y * inv_tsum;
         }
         float v[64];
-        nn_features(v, in.pn, in.n, in.wo, N.encoding);
+        nn_features<ONEBLOB>(v, in.pn, in.n, in.wo, N.encoding);
         if (!valid)
 #pragma unroll
             for (int j = 0; j < 64; j++) v[j] = 0.f;
@@ -601,28 +604,31 @@ cudaError_t nn_shadow_smem_limit();  // after k_shadow_nn below
 cudaError_t nn_set_smem_limits() {
     cudaError_t es = nn_shadow_smem_limit();
     if (es != cudaSuccess) return es;
-    cudaError_t e = cudaFuncSetAttribute(k_nn_forward_debug, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)nn_smem_infer());
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_nn_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nn_smem_infer());
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_nn_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWGSmem);
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_nn_train_fb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nn_smem_train());
+    const int si = (int)nn_smem_infer(), stn = (int)nn_smem_train();
+    cudaError_t e = cudaFuncSetAttribute(k_nn_forward_debug<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, si);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_nn_forward_debug<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, si);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_nn_infer<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, si);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_nn_infer<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, si);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_nn_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWGSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_nn_train_fb<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, stn);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_nn_train_fb<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, stn);
+    return e;
 }
 
 void launch_nn_pack(const NNWeights& W, cudaStream_t st) {
     k_nn_pack<<<(kNNWeights + 255) / 256, 256, 0, st>>>(W);
 }
 void launch_nn_forward_debug(const DevNNJob* nnj, const float* in, int n, float* out, uint32_t* status, int num_sms,
-                             cudaStream_t st) {
+                             cudaStream_t st, bool oneblob) {
     const int blocks = std::max(1, std::min(num_sms * 4, (n + kTcInferThreads - 1) / kTcInferThreads));
-    k_nn_forward_debug<<<blocks, kTcInferThreads, nn_smem_infer(), st>>>(nnj, in, n, out, status);
+    if (oneblob) k_nn_forward_debug<true><<<blocks, kTcInferThreads, nn_smem_infer(), st>>>(nnj, in, n, out, status);
+    else k_nn_forward_debug<false><<<blocks, kTcInferThreads, nn_smem_infer(), st>>>(nnj, in, n, out, status);
 }
 void launch_nn_infer(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, const DevNNJob* nnj,
-                     float4* params, int num_sms, cudaStream_t st) {
+                     float4* params, int num_sms, cudaStream_t st, bool oneblob) {
     // four CTAs of 128 threads per SM fit in shared memory (48 KB each)
-    k_nn_infer<<<num_sms * 4, kTcInferThreads, nn_smem_infer(), st>>>(S, B, cur, ctr, nnj, params);
+    if (oneblob) k_nn_infer<true><<<num_sms * 4, kTcInferThreads, nn_smem_infer(), st>>>(S, B, cur, ctr, nnj, params);
+    else k_nn_infer<false><<<num_sms * 4, kTcInferThreads, nn_smem_infer(), st>>>(S, B, cur, ctr, nnj, params);
 }
 // Zeroes each task's gradient and loss (and, with prep, its T sum).
 __global__ void k_nn_task_zero(const NNTrainTask* __restrict__ tasks, int prep) {
@@ -654,7 +660,7 @@ __global__ void k_nn_task_T(const NNTrainTask* __restrict__ tasks) {
 }
 
 void launch_nn_train_tasks(const NNTrainTask* tasks, int n_tasks, int max_n, int num_sms, cudaStream_t st, bool prep,
-                           bool apply) {
+                           bool apply, bool oneblob) {
     if (n_tasks < 1) return;
     const NNAdam opt;
     const dim3 gz((kNNWeights + 255) / 256, n_tasks);
@@ -666,7 +672,8 @@ void launch_nn_train_tasks(const NNTrainTask* tasks, int n_tasks, int max_n, int
     // two CTAs per SM fit (80 KB of shared memory each), shared by the tasks
     const int per_task = std::max(1, (num_sms * 2 + n_tasks - 1) / n_tasks);
     const dim3 gf(std::max(1, std::min(per_task, (max_n + kTcRows - 1) / kTcRows)), n_tasks);
-    k_nn_train_fb<<<gf, kTcRows, nn_smem_train(), st>>>(tasks);
+    if (oneblob) k_nn_train_fb<true><<<gf, kTcRows, nn_smem_train(), st>>>(tasks);
+    else k_nn_train_fb<false><<<gf, kTcRows, nn_smem_train(), st>>>(tasks);
     const int per_task_w = std::max(1, (num_sms + n_tasks - 1) / n_tasks);
     const dim3 gw(std::max(1, std::min(per_task_w, (max_n + kWGK - 1) / kWGK)), kNNLayers, n_tasks);
     k_nn_wgrad<<<gw, kTcRows, kWGSmem, st>>>(tasks);

@@ -93,11 +93,11 @@ __device__ __forceinline__ float nn_feature(int j, f3 pn, f3 n, f3 wo, int encod
 // All 64 input features of a sample under encoding (the values of
 // nn_feature, with the branch on the encoding taken once and the one-blob
 // angles computed once per sample).
-#ifndef CPPPT_NN_ONEBLOB
-#define CPPPT_NN_ONEBLOB 1
-#endif
+// ONEBLOB = false: a kernel instance for networks that all use the
+// frequency encoding (the branch and the one-blob code compiled out).
+template <bool ONEBLOB>
 __device__ __forceinline__ void nn_features(float v[64], f3 pn, f3 n, f3 wo, int encoding) {
-    if (CPPPT_NN_ONEBLOB && encoding == 1) {
+    if (ONEBLOB && encoding == 1) {
 #pragma unroll
         for (int j = 0; j < 36; j++) v[j] = nn_feature_oneblob(j, pn, n, wo);
         const float s4[4] = {0.5f * (n.z + 1.0f), atan2f(n.y, n.x) * (0.5f * kInvPi) + 0.5f, 0.5f * (wo.z + 1.0f),

@@ -71,10 +71,12 @@ size_t nn_wcopy_elems();  // bf16 elements of one padded weight copy
 cudaError_t nn_set_smem_limits();
 void launch_nn_pack(const NNWeights& W, cudaStream_t st);
 // status: one zeroed word; receives kStatusTensorTimeout if a wait ran out.
+// oneblob: some network of the table uses PT_NN_ENC_ONEBLOB (else the kernel
+// instance with the frequency encoding alone runs).
 void launch_nn_forward_debug(const DevNNJob* nnj, const float* in, int n, float* out, uint32_t* status, int num_sms,
-                             cudaStream_t st);
+                             cudaStream_t st, bool oneblob);
 void launch_nn_infer(const DevScene& S, const PathBuffers& B, int cur, WaveCounters* ctr, const DevNNJob* nnj,
-                     float4* params, int num_sms, cudaStream_t st);
+                     float4* params, int num_sms, cudaStream_t st, bool oneblob);
 // One network's part of a fused training step (device table; one launch
 // per stage covers every task: several scenes' guides train together).
 struct NNTrainTask {
@@ -95,7 +97,7 @@ struct NNTrainTask {
 // for chi-square); otherwise scal[1] holds it already.  apply: take the
 // Adam step (else only the gradient).
 void launch_nn_train_tasks(const NNTrainTask* tasks, int n_tasks, int max_n, int num_sms, cudaStream_t st, bool prep,
-                           bool apply);
+                           bool apply, bool oneblob);
 // One CTA that waits on a completion barrier nothing arrives on (bounded)
 // and sets kStatusTensorTimeout in *status: the tensor-core kernels' timeout
 // path, exercised without a tensor-core instruction.
