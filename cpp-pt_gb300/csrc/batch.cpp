@@ -94,7 +94,8 @@ struct pt_batch {
 
 namespace {
 
-constexpr int kMaxBatchCapacity = 1 << 22;
+constexpr int kMaxBatchCapacity = 1 << 24;
+constexpr int kMaxSlotCapacity = 1 << 22;  // learned-guide batches: vertex records per path and bounce
 constexpr unsigned long long kMaxBatchPixels = 1ull << 30;  // film pixel index travels as a 32-bit word
 
 template <class T>
@@ -238,7 +239,7 @@ void create_batch(pt_scene* const* scenes, int n, pt_batch* b) {
 
 void check_tuning(const pt_batch_tuning& t) {
     if (t.capacity < 1024 || t.capacity > kMaxBatchCapacity || t.capacity % 1024)
-        throw std::invalid_argument("capacity must be a multiple of 1024 in [1024, 4194304]");
+        throw std::invalid_argument("capacity must be a multiple of 1024 in [1024, 16777216]");
     if (t.iters_per_graph < 2 || t.iters_per_graph > 256 || t.iters_per_graph % 2)
         throw std::invalid_argument("iters_per_graph must be even, in [2, 256]");
     if (t.tile_w < 1 || t.tile_h < 1 || t.tile_w * t.tile_h > 1024)
@@ -443,7 +444,7 @@ void render_batch_slot(pt_batch* b, const pt_batch_job* jobs, int n_jobs, float*
     build_jobs(b, jobs, n_jobs, t, kIntegratorMIS, table, &total, &pixels);
     int max_depth = 1;
     for (const DevBatchJob& j : table) max_depth = std::max(max_depth, j.max_depth);
-    const int capacity = (int)std::min<unsigned long long>(t.capacity, (total + 1023) / 1024 * 1024);
+    const int capacity = (int)std::min<unsigned long long>(std::min(t.capacity, kMaxSlotCapacity), (total + 1023) / 1024 * 1024);
     ensure_buffers(b, capacity, 3 * pixels, n_jobs);
     cudaStream_t st = b->stream;
     const int n_members = (int)b->members.size();
@@ -723,7 +724,7 @@ pt_status pt_batch_stats(pt_batch* b, pt_render_stats* out) {
 
 // Autotuner: renders a reduced copy of the job list (spp divided by
 // spp_divisor, at least 1) once per candidate setting and keeps the one with
-// the highest paths per second.  Candidates: wavefront capacity 2^21 or 2^22
+// the highest paths per second.  Candidates: wavefront capacity 2^22 or 2^24
 // (scanline order), then scanline or 8x4 / 4x8 / 16x2 pixel tiles at the
 // better capacity: five settings.  The render loop runs on the device
 // (build_render_graph), so the iterations per loop body only set how often
@@ -737,7 +738,7 @@ pt_status pt_batch_autotune(pt_batch* b, const pt_batch_job* jobs, int32_t n_job
         if (spp_divisor < 1) throw std::invalid_argument("spp_divisor must be >= 1");
         std::vector<pt_batch_job> sample(jobs, jobs + n_jobs);
         for (pt_batch_job& j : sample) j.spp = std::max(1, j.spp / spp_divisor);
-        const int caps[] = {1 << 21, 1 << 22};
+        const int caps[] = {1 << 22, 1 << 24};
         const int tiles[][2] = {{1, 1}, {8, 4}, {4, 8}, {16, 2}};
         const int iters = b->tuning.iters_per_graph;
         pt_batch_tuning best = b->tuning;

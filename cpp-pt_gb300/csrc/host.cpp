@@ -286,14 +286,23 @@ void trace_host(pt_scene* s, const pt_ray* rays, int n, void* out, bool any) {
     check_status(s, status);
 }
 
+// Paths in flight of a single render.  Each traversal launch ends with a
+// tail in which a few long rays hold their SMs, so larger wavefronts
+// amortise it over more rays.  Measured on the 1M-triangle soup at 1080p,
+// 64 spp: 2^20 279.5 Mpaths/s, 2^21 310.6, 2^22 328.5, 2^23 337.3, 2^24
+// 342.6, 2^25 334.2 (2^24 paths hold 3.2 GB of path state).
 #ifndef CPPPT_MAX_WAVE_LOG2
-#define CPPPT_MAX_WAVE_LOG2 21
+#define CPPPT_MAX_WAVE_LOG2 24
 #endif
 constexpr int kMaxCapacity = 1 << CPPPT_MAX_WAVE_LOG2;
-// paths in flight of the learned-guide (slot) wavefront, each with a vertex
-// record per bounce for training
+// Paths in flight of the learned-guide (slot) wavefront, each with a vertex
+// record per bounce for training (112 B x depth per path: 5.6 GB at 2^22 and
+// depth 12).  Measured on the 200k-triangle slit room at 1280x720, depth 12
+// (8 spp per call): 2^20 plain 228.5, guided and training 157.5, frozen
+// 194 Mpaths/s; 2^21 251.5, 185.6, 220; 2^22 249.0, 204, 223 -- fewer
+// rounds, so fewer host steps between them.
 #ifndef CPPPT_NN_WAVE_LOG2
-#define CPPPT_NN_WAVE_LOG2 20
+#define CPPPT_NN_WAVE_LOG2 22
 #endif
 constexpr int kItersPerGraph = 16;  // even: buffers alternate
 

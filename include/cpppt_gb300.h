@@ -231,7 +231,8 @@ typedef struct pt_batch_job {
     int32_t rr_start;
     uint32_t seed;
 } pt_batch_job;
-/* Launch shape of a batch: paths in flight (multiple of 1024, <= 2^22),
+/* Launch shape of a batch: paths in flight (multiple of 1024, <= 2^24; a
+ * learned-guide batch uses at most 2^22),
  * wavefront iterations per CUDA graph launch (even), pixel tile of the
  * path order (1 x 1 = scanline; used where it divides the resolution).
  * None of them changes the images. */
