@@ -14,7 +14,7 @@
 
 Each case renders once to warm up (graph capture, allocation), then once
 more: the second render is the one to capture.  Device memory stays at a
-few GB.  The path state (about 400 MB at 2^21 paths in flight) exceeds the
+few GB.  The path state (about 180 MB for the extend case's 921,600 paths in flight) exceeds the
 129 MB L2; the soup's traversal data (about 70 MB) fits in it.
 """
 from __future__ import annotations
@@ -40,7 +40,7 @@ def case_extend():
 
 def case_raycounts():
     """Extension rays per bounce of the extend case.  All 921,600 paths start
-    in the first iteration (the wavefront holds 2^21), and a path's random
+    in the first iteration (the wavefront holds them all), and a path's random
     numbers depend only on its pixel, sample and bounce, so a render limited
     to depth b traces exactly the first b bounces of the depth-10 render:
     rays of bounce b = closest rays at depth b+1 minus those at depth b."""
