@@ -306,23 +306,40 @@ constexpr int kMaxCapacity = 1 << CPPPT_MAX_WAVE_LOG2;
 #endif
 constexpr int kItersPerGraph = 16;  // even: buffers alternate
 
-void ensure_wave(pt_scene* s, int capacity, int film_n) {
+// The scene's wavefront buffers for `capacity` paths in flight (192 B per
+// path, kept for later renders).  Returns the paths in flight the render
+// uses: `capacity`, or fewer when the device cannot hold that many (the
+// request halved down to 2^20 paths; the images do not depend on it).
+int ensure_wave(pt_scene* s, int capacity, int film_n) {
     if (s->pb.capacity < capacity) {
-        for (void* p : s->pb_owned) cudaFree(p);
-        s->pb_owned.clear();
         PathBuffers& B = s->pb;
-        for (int k = 0; k < 2; k++) {
-            B.o[k] = dalloc<float4>(s->pb_owned, capacity);
-            B.d[k] = dalloc<float4>(s->pb_owned, capacity);
-            B.thr[k] = dalloc<float4>(s->pb_owned, capacity);
-            B.info[k] = dalloc<int4>(s->pb_owned, capacity);
-        }
-        B.hit = dalloc<float4>(s->pb_owned, capacity);
-        B.sh_o = dalloc<float4>(s->pb_owned, capacity);
-        B.sh_d = dalloc<float4>(s->pb_owned, capacity);
-        B.sh_c = dalloc<float4>(s->pb_owned, capacity);
-        B.capacity = capacity;
+        auto release = [&] {
+            for (void* p : s->pb_owned) cudaFree(p);
+            s->pb_owned.clear();
+            B.capacity = 0;
+        };
+        release();
         if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
+        for (int c = capacity;; c = std::max(1 << 20, c / 2)) {
+            try {
+                for (int k = 0; k < 2; k++) {
+                    B.o[k] = dalloc<float4>(s->pb_owned, c);
+                    B.d[k] = dalloc<float4>(s->pb_owned, c);
+                    B.thr[k] = dalloc<float4>(s->pb_owned, c);
+                    B.info[k] = dalloc<int4>(s->pb_owned, c);
+                }
+                B.hit = dalloc<float4>(s->pb_owned, c);
+                B.sh_o = dalloc<float4>(s->pb_owned, c);
+                B.sh_d = dalloc<float4>(s->pb_owned, c);
+                B.sh_c = dalloc<float4>(s->pb_owned, c);
+                B.capacity = c;
+                break;
+            } catch (...) {
+                release();
+                cudaGetLastError();  // an allocation failure is not sticky
+                if (c <= (1 << 20)) throw;
+            }
+        }
     }
     if (s->film_n != film_n) {
         if (s->film) cudaFree(s->film);
@@ -333,6 +350,7 @@ void ensure_wave(pt_scene* s, int capacity, int film_n) {
         s->film_n = film_n;
         if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
     }
+    return std::min(capacity, s->pb.capacity);
 }
 
 // PPG::render (src/renderer/ppg.h:149-215): passes of 1, 2, 4, ... spp while
@@ -348,8 +366,8 @@ void render_ppg(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
     const int film_n = 3 * s->width * s->height;
     const int D = desc->max_depth;
     const unsigned long long max_pass = (unsigned long long)s->width * s->height * (unsigned long long)passes.back();
-    const int capacity = (int)std::min<unsigned long long>(1 << 20, (max_pass + 1023) / 1024 * 1024);
-    ensure_wave(s, capacity, film_n);
+    const int capacity =
+        ensure_wave(s, (int)std::min<unsigned long long>(1 << 20, (max_pass + 1023) / 1024 * 1024), film_n);
     std::vector<void*> tmp;  // per-render buffers
     struct Free {
         std::vector<void*>& v;
@@ -679,9 +697,9 @@ void render_nn(pt_scene* s, const pt_render_desc* desc, float* d_dst, bool guide
     P.height = s->height;
     P.flags = desc->flags;
     const unsigned long long total = (unsigned long long)s->width * s->height * (unsigned long long)desc->spp;
-    const int capacity = (int)std::min<unsigned long long>(1 << CPPPT_NN_WAVE_LOG2, (total + 1023) / 1024 * 1024);
     const int film_n = 3 * s->width * s->height;
-    ensure_wave(s, capacity, film_n);
+    const int capacity =
+        ensure_wave(s, (int)std::min<unsigned long long>(1 << CPPPT_NN_WAVE_LOG2, (total + 1023) / 1024 * 1024), film_n);
     NNPathData PD = nn_path_buffers(s, capacity, train ? P.max_depth : 0);
     const int batch = s->nn_cfg.batch;
     const int rec_cap = std::min(kNNRecordCap, s->nn_cfg.steps_per_round * batch);
@@ -807,9 +825,9 @@ void render_impl(pt_scene* s, const pt_render_desc* desc, float* d_dst) {
     P.width = s->width;
     P.height = s->height;
     const unsigned long long total = (unsigned long long)s->width * s->height * (unsigned long long)desc->spp;
-    int capacity = (int)std::min<unsigned long long>(kMaxCapacity, (total + 1023) / 1024 * 1024);
     const int film_n = 3 * s->width * s->height;
-    ensure_wave(s, capacity, film_n);
+    const int capacity =
+        ensure_wave(s, (int)std::min<unsigned long long>(kMaxCapacity, (total + 1023) / 1024 * 1024), film_n);
     cudaStream_t st = s->stream;
     const bool timed = (desc->flags & PT_FLAG_TIME_KERNELS) != 0;
     const bool count = (desc->flags & PT_FLAG_COUNT) != 0;
