@@ -296,13 +296,16 @@ void trace_host(pt_scene* s, const pt_ray* rays, int n, void* out, bool any) {
 #endif
 constexpr int kMaxCapacity = 1 << CPPPT_MAX_WAVE_LOG2;
 // Paths in flight of the learned-guide (slot) wavefront, each with a vertex
-// record per bounce for training (112 B x depth per path: 5.6 GB at 2^22 and
-// depth 12).  Measured on the 200k-triangle slit room at 1280x720, depth 12
-// (8 spp per call): 2^20 plain 228.5, guided and training 157.5, frozen
-// 194 Mpaths/s; 2^21 251.5, 185.6, 220; 2^22 249.0, 204, 223 -- fewer
-// rounds, so fewer host steps between them.
+// record per bounce for training (112 B x depth per path).  Larger
+// wavefronts render faster (on the 200k-triangle slit room at 1280x720,
+// depth 12, 8 spp per call: 2^20 guided and training 157.5 Mpaths/s, 2^22
+// 204) but train far worse guides: a round keeps at most steps_per_round x
+// batch records, and with 2^22 paths in flight that quota fills with the
+// records of the paths that finish first, the short ones; the guide then
+// rarely sees the long paths that carry the light through the slit
+// (config 4 at 60 s: relMSE 3.3e-3 against 4.7e-4 at 2^20).  So 2^20.
 #ifndef CPPPT_NN_WAVE_LOG2
-#define CPPPT_NN_WAVE_LOG2 22
+#define CPPPT_NN_WAVE_LOG2 20
 #endif
 constexpr int kItersPerGraph = 16;  // even: buffers alternate
 
