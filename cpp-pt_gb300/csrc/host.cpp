@@ -721,6 +721,7 @@ void render_nn(pt_scene* s, const pt_render_desc* desc, float* d_dst, bool guide
     nj.rec = train ? s->nn_rec : nullptr;
     nj.rec_cap = train ? rec_cap : 0;
     nj.n_rec = &s->d_ctr->n_rec;
+    nj.keep = s->nn_keep;
     ck(cudaMemcpyAsync(s->d_job, s->h_job, sizeof(DevBatchJob), cudaMemcpyHostToDevice, st), "job table");
     ck(cudaMemcpyAsync(s->d_nnjob, s->h_nnjob, sizeof(DevNNJob), cudaMemcpyHostToDevice, st), "guide job table");
     ck(cudaEventRecord(s->ev0, st), "event");
@@ -739,6 +740,7 @@ void render_nn(pt_scene* s, const pt_render_desc* desc, float* d_dst, bool guide
         64 + (total / (unsigned long long)capacity + 2) * (unsigned long long)(desc->max_depth + 2) * 4 / kItersPerGraph;
     double records = 0;
     int rec_left = -1;  // records kept after the last round's training (-1: that round did not train)
+    int n0 = init.n_rec;  // records held when the round started
     NNTrainPending pending;
     for (unsigned long long round = 0;; round++) {
         for (int k = 0; k < kItersPerGraph; k++) {
@@ -757,6 +759,15 @@ void render_nn(pt_scene* s, const pt_render_desc* desc, float* d_dst, bool guide
         ck(cudaStreamSynchronize(st), "render");
         check_status(s, s->h_ctr->status);
         rec_left = -1;
+        if (train) {
+            // the paths' share that leaves records, set so that a round's
+            // records (sampled evenly over its paths) fill about 80 % of
+            // the round's quota
+            const int got = s->h_ctr->n_rec - n0;
+            const double q = (double)s->nn_keep * 0.8 * rec_cap / std::max(1, got);
+            s->nn_keep = (float)std::min(1.0, std::max(1.0 / 1024.0, q));
+            nj.keep = s->nn_keep;
+        }
         if (train && s->h_ctr->n_rec >= batch) {
             // this round's full batches train on the training stream while
             // the next round fills the other record buffer
@@ -765,9 +776,11 @@ void render_nn(pt_scene* s, const pt_render_desc* desc, float* d_dst, bool guide
                           s->nn_tst, s->nn_ev_records, &launches, &rec_left, pending);
             records += (double)(std::min(s->h_ctr->n_rec, rec_cap) - rec_left);
             nj.rec = s->nn_rec;
+        }
+        if (train)
             ck(cudaMemcpyAsync(s->d_nnjob, s->h_nnjob, sizeof(DevNNJob), cudaMemcpyHostToDevice, st),
                "guide job table");
-        }
+        n0 = rec_left >= 0 ? rec_left : s->h_ctr->n_rec;
         if (s->h_ctr->n_cur == 0 && s->h_ctr->work_next >= s->h_ctr->work_total) break;
         if (round > max_rounds) throw Fail(PT_ERR_LIMIT, "render did not converge within the iteration bound");
     }
@@ -1228,6 +1241,7 @@ pt_status pt_nn_reset(pt_scene* s, uint32_t seed) {
         s->nn_last_loss = 0;
         s->nn_records = 0;
         s->nn_rec_count = 0;
+        s->nn_keep = 1.0f;
     });
 }
 
@@ -1263,6 +1277,7 @@ pt_status pt_nn_configure(pt_scene* s, const pt_nn_config* c) {
     }
     s->nn_cfg = *c;
     s->nn_rec_count = 0;  // records of the previous batch size are dropped
+    s->nn_keep = 1.0f;
     return PT_OK;
 }
 

@@ -180,6 +180,7 @@ struct pt_scene {
     cudaEvent_t nn_read_done[2] = {nullptr, nullptr};  // last training that read nn_rec_buf[k] completed
     cudaEvent_t nn_ev_records = nullptr;             // a round's records are complete (render stream)
     int nn_rec_count = 0;
+    float nn_keep = 1.0f;  // probability that a finished path leaves training records (adapted per round)
     int* h_rec_left = nullptr;  // pinned staging word for the kept-record count
     NNPathData nnpd{};          // per-path buffers of the slot-based wavefront (grown on demand)
     float4* nn_params = nullptr;

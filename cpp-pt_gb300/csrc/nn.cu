@@ -930,8 +930,22 @@ __global__ void __launch_bounds__(256) k_finish_nn(NNPathData PD, WaveCounters* 
     const bool release = i < n;
     int4 f = make_int4(0, 0, 0, 0);
     if (release) f = PD.fin[i];
-    const bool records = release && PD.rec_cap > 0;
+    bool records = release && PD.rec_cap > 0;
     const int job = records ? PD.slot_job[f.x] : -1;
+    if (records) {
+        // a path keeps its records with the job's probability, decided by a
+        // hash of its slot and the iteration, never by its length: the
+        // records of a round then sample its paths evenly (a quota filled in
+        // finishing order would hold the short paths)
+        const float keep = nnj[job].keep;
+        if (keep < 1.0f) {
+            uint32_t h = (uint32_t)f.x * 0x9E3779B1u ^ (uint32_t)ctr->stat_iters * 0x85EBCA77u;
+            h ^= h >> 15;
+            h *= 0x2C1B3C6Du;
+            h ^= h >> 12;
+            records = (float)(h >> 8) * (1.0f / 16777216.0f) < keep;
+        }
+    }
     int count = 0;
     if (records) visit_records(PD, f, max_depth, [&](const float4*, f3, float, float) { count++; });
     // one job for the whole warp (the usual case: jobs are rendered in order)?

@@ -54,6 +54,7 @@ struct DevNNJob {
     float4* rec;              // training records of the job's scene (4 float4 each)
     int32_t rec_cap;          // capacity of rec (0: no records)
     int32_t* n_rec;           // record counter of the job's scene
+    float keep = 1.0f;        // probability that a finished path leaves its records
 };
 
 // Path info word z of the slot wavefront: bounce (bits 0-15), sampled delta
