@@ -299,11 +299,11 @@ constexpr int kMaxCapacity = 1 << CPPPT_MAX_WAVE_LOG2;
 // record per bounce for training (112 B x depth per path).  Larger
 // wavefronts render faster (on the 200k-triangle slit room at 1280x720,
 // depth 12, 8 spp per call: 2^20 guided and training 157.5 Mpaths/s, 2^22
-// 204) but train far worse guides: a round keeps at most steps_per_round x
-// batch records, and with 2^22 paths in flight that quota fills with the
-// records of the paths that finish first, the short ones; the guide then
-// rarely sees the long paths that carry the light through the slit
-// (config 4 at 60 s: relMSE 3.3e-3 against 4.7e-4 at 2^20).  So 2^20.
+// 204) but gave far worse images: with the record quota filled in finishing
+// order the guide learned from short paths only (config 4 at 60 s: relMSE
+// 3.3e-3 against 4.7e-4 at 2^20); with records sampled evenly (the keep
+// probability) it learned faster but then took very bright samples
+// (relMSE 8.8e-3 at 10 s).  So 2^20.
 #ifndef CPPPT_NN_WAVE_LOG2
 #define CPPPT_NN_WAVE_LOG2 20
 #endif
