@@ -96,3 +96,30 @@ def test_wide_bvh_host_build_is_thread_independent():
     assert count.sum() == sc.n_triangles
     for s, c in zip(start[:5000], count[:5000]):
         assert np.all(np.diff(o1[s:s + c]) > 0)
+
+
+def test_wide_bvh_debug_entry_checks_its_arguments():
+    """pt_debug_wide_bvh (host build, no CUDA call): a leaf size outside
+    [1, 16] is refused, an empty list gives an empty tree, and a node buffer
+    that is too small gives PT_ERR_LIMIT with the node count set."""
+    import ctypes as C
+    from cpppt import lib, scenes
+    L = lib.load()
+    sc = scenes.cornell(8, 8)
+    tv = np.ascontiguousarray(sc.vertices[sc.triangles].reshape(-1), np.float32)
+    n = sc.n_triangles
+    order = np.zeros(n, np.int32)
+    nodes = np.zeros((64, 16), np.uint32)
+    nn, depth, infl = C.c_int32(), C.c_int32(), C.c_float()
+    args = lambda leaf, cap: (tv.ctypes.data, n, leaf, 0, 1, nodes.ctypes.data, cap, C.byref(nn),
+                              order.ctypes.data, C.byref(depth), C.byref(infl))
+    assert L.pt_debug_wide_bvh(*args(0, 64)) == 1 and L.pt_debug_wide_bvh(*args(17, 64)) == 1
+    assert L.pt_debug_wide_bvh(*args(4, 64)) == 0
+    full = nn.value
+    assert full >= 2 and depth.value >= 2 and infl.value > 0
+    assert np.array_equal(np.sort(order), np.arange(n))
+    assert L.pt_debug_wide_bvh(*args(4, full - 1)) == 4  # PT_ERR_LIMIT
+    assert nn.value == full
+    assert L.pt_debug_wide_bvh(None, 0, 4, 0, 1, nodes.ctypes.data, 64, C.byref(nn), None, C.byref(depth),
+                               None) == 0
+    assert nn.value == 1  # a root with no children
