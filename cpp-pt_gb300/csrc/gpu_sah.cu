@@ -184,7 +184,8 @@ __device__ __forceinline__ void warp_scan(uint32_t& cnt, uint32_t k[12], bool su
 // The host's split decision from the bins (SahBuilder::build): warp w < 3
 // evaluates axis w; the first strict minimum over (axis, bin) wins.  Writes
 // *out (leaf, axis or fallback) from thread 0; the caller synchronises.
-// bb / cb: the node's box and centroid bounds.
+// The node's box and centroid bounds come from s.key.  All threads of the
+// CTA call it (it synchronises once).
 __device__ void decide(const uint32_t* bins, const Seg& s, int max_leaf, Split* out, float* s_cost, int* s_bin) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float lo[3], hi[3], clo[3], chi[3];
