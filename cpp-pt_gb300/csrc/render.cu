@@ -168,7 +168,14 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceBlocksPerSM) k_shadow(Dev
 // the scene's light list inside the arena and the job's film offset.  A
 // single-scene render is a table of one job (so batched and single renders
 // run the same instructions and give bit-identical images).
-__global__ void __launch_bounds__(256, 3) k_shade(DevScene S, PathBuffers B, int cur, WaveCounters* ctr,
+// Resident CTAs of 256 threads per SM for the shading kernel.  Measured on
+// the 1M-triangle soup at 1080p, 64 spp, 2^24 paths in flight: 2 (128
+// registers) 333.4 Mpaths/s, 3 (80 registers) 341.5, 4 (64 registers, some
+// spilling) 345.1.
+#ifndef CPPPT_SHADE_BLOCKS
+#define CPPPT_SHADE_BLOCKS 4
+#endif
+__global__ void __launch_bounds__(256, CPPPT_SHADE_BLOCKS) k_shade(DevScene S, PathBuffers B, int cur, WaveCounters* ctr,
                                                unsigned long long* __restrict__ film,
                                                const DevBatchJob* __restrict__ jobs) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
